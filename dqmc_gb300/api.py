@@ -1,0 +1,360 @@
+"""Python host binding of the C ABI (include/dqmc_gpu.h) through ctypes.
+
+`DQMC` mirrors the reference's hot-path API on `AbstractDQMC`
+(src/QMC.jl, src/dqmc_framework.jl, src/stack.jl, src/local_updates.jl):
+`init`, `propagate`, `wrap_greens`, `calculate_greens`, `calc_greens`,
+`local_updates`, `update`, `multiply_B_left` & co., `calc_boson_action`.
+Every call goes to the CUDA library; there is no CPU fallback: if the
+library is missing or no GPU is visible the constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libdqmc_gpu.so")
+
+DQMC_OK = 0
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "non-finite value", -4: "singular M",
+          -5: "device wait timed out", -6: "invalid state"}
+
+B_LEFT, B_RIGHT, B_INV_LEFT, B_INV_RIGHT, B_DAG_LEFT = 0, 1, 2, 3, 4
+
+
+class DQMCError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class CParams(ctypes.Structure):
+    _fields_ = [("L", ctypes.c_int32), ("slices", ctypes.c_int32), ("safe_mult", ctypes.c_int32),
+                ("opdim", ctypes.c_int32), ("delta_tau", ctypes.c_double), ("lambda_", ctypes.c_double),
+                ("r", ctypes.c_double), ("c", ctypes.c_double), ("u", ctypes.c_double),
+                ("mu1", ctypes.c_double), ("mu2", ctypes.c_double), ("hoppings", ctypes.c_double * 4),
+                ("all_checks", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 6)]
+
+
+class CStats(ctypes.Structure):
+    _fields_ = [("proposals", ctypes.c_int64), ("accepted", ctypes.c_int64), ("acc_rate", ctypes.c_double),
+                ("max_instability", ctypes.c_double), ("device_ms", ctypes.c_double)]
+
+
+class CTiming(ctypes.Structure):
+    _fields_ = [("ms_wrap", ctypes.c_double), ("ms_stack", ctypes.c_double), ("ms_greens", ctypes.c_double),
+                ("ms_local", ctypes.c_double), ("n_wrap", ctypes.c_int64), ("n_stack", ctypes.c_int64),
+                ("n_greens", ctypes.c_int64), ("n_local", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
+
+
+# every symbol the header declares, with its argument types
+_P = ctypes.c_void_p
+_D = ctypes.POINTER(ctypes.c_double)
+_I32 = ctypes.c_int32
+SIGNATURES = {
+    "dqmc_version": ([], ctypes.c_char_p),
+    "dqmc_create": ([ctypes.POINTER(CParams), ctypes.POINTER(_P)], ctypes.c_int),
+    "dqmc_destroy": ([_P], ctypes.c_int),
+    "dqmc_last_error": ([_P], ctypes.c_char_p),
+    "dqmc_set_field": ([_P, _D], ctypes.c_int),
+    "dqmc_get_field": ([_P, _D], ctypes.c_int),
+    "dqmc_init": ([_P], ctypes.c_int),
+    "dqmc_propagate": ([_P], ctypes.c_int),
+    "dqmc_get_state": ([_P, ctypes.POINTER(_I32), ctypes.POINTER(_I32)], ctypes.c_int),
+    "dqmc_local_updates": ([_P, _D, _D, ctypes.c_void_p, _D, _D, _D], ctypes.c_int),
+    "dqmc_update": ([_P, _D, _D, ctypes.c_void_p, _D, _D, _D], ctypes.c_int),
+    "dqmc_sweep": ([_P, _I32, _D, _D, ctypes.c_void_p, ctypes.POINTER(CStats)], ctypes.c_int),
+    "dqmc_sweep_device": ([_P, _I32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                           ctypes.POINTER(CStats)], ctypes.c_int),
+    "dqmc_get_greens": ([_P, _D, ctypes.POINTER(_I32), ctypes.POINTER(_I32)], ctypes.c_int),
+    "dqmc_set_greens": ([_P, _D], ctypes.c_int),
+    "dqmc_calc_greens": ([_P, _I32, _D, _D], ctypes.c_int),
+    "dqmc_wrap_greens": ([_P, _D, _I32, _I32], ctypes.c_int),
+    "dqmc_calculate_greens_udt": ([_P, _D, _D, _D, _D, _D, _D, _D, _D], ctypes.c_int),
+    "dqmc_decompose_udt": ([_P, _D, _D, _D, _D], ctypes.c_int),
+    "dqmc_logdet": ([_P, _D], ctypes.c_int),
+    "dqmc_multiply_B": ([_P, _I32, _I32, _D], ctypes.c_int),
+    "dqmc_boson_action": ([_P, _D], ctypes.c_int),
+    "dqmc_calc_boson_action": ([_P, _D], ctypes.c_int),
+    "dqmc_measure": ([_P, _D, _D, _D], ctypes.c_int),
+    "dqmc_get_timing": ([_P, ctypes.POINTER(CTiming)], ctypes.c_int),
+    "dqmc_reset_timing": ([_P, _I32], ctypes.c_int),
+}
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -m dqmc_gb300.build` "
+                          "(or __graft_entry__.build())")
+    lib = ctypes.CDLL(path)
+    for name, (args, res) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+@dataclasses.dataclass
+class ModelParams:
+    """Subset of the reference's `Params` (src/parameters.jl:4-80)."""
+    L: int = 4
+    slices: int = 40
+    safe_mult: int = 10
+    delta_tau: float = 0.1
+    lambda_: float = 1.0
+    r: float = 1.0
+    c: float = 1.0
+    u: float = 1.0
+    mu1: float = -0.5
+    mu2: float = -0.5
+    hoppings: tuple = (1.0, 0.5, -0.5, -1.0)
+    box: float = 0.2
+    all_checks: bool = True
+
+    @property
+    def N(self):
+        return self.L * self.L
+
+    @property
+    def n(self):
+        return 4 * self.L * self.L
+
+    def to_c(self) -> CParams:
+        p = CParams()
+        p.L, p.slices, p.safe_mult, p.opdim = self.L, self.slices, self.safe_mult, 3
+        p.delta_tau, p.lambda_, p.r, p.c, p.u = self.delta_tau, self.lambda_, self.r, self.c, self.u
+        p.mu1, p.mu2 = self.mu1, self.mu2
+        for k in range(4):
+            p.hoppings[k] = self.hoppings[k]
+        p.all_checks = 1 if self.all_checks else 0
+        p.precision = 0
+        return p
+
+
+def _dptr(a):
+    return a.ctypes.data_as(_D)
+
+
+def _cplx_in(a, n):
+    a = np.asarray(a, dtype=np.complex128)
+    assert a.shape == (n, n)
+    return np.asfortranarray(a)
+
+
+class DQMC:
+    """One Markov chain on the GPU.  Method names follow the reference."""
+
+    def __init__(self, params: ModelParams, phi=None):
+        self.lib = load_library()
+        self.p = params
+        self.N, self.n, self.M = params.N, params.n, params.slices
+        h = ctypes.c_void_p()
+        rc = self.lib.dqmc_create(ctypes.byref(params.to_c()), ctypes.byref(h))
+        if rc != DQMC_OK:
+            raise DQMCError(rc, "dqmc_create failed (unsupported parameters or no usable GPU)")
+        self.h = h
+        if phi is not None:
+            self.set_field(phi)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dqmc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != DQMC_OK:
+            raise DQMCError(rc, self.lib.dqmc_last_error(self.h).decode())
+
+    # ---- field / state --------------------------------------------------
+    def set_field(self, phi):
+        phi = np.asfortranarray(np.asarray(phi, dtype=np.float64))
+        assert phi.shape == (3, self.N, self.M)
+        self._check(self.lib.dqmc_set_field(self.h, _dptr(phi)))
+
+    def get_field(self):
+        out = np.zeros((3, self.N, self.M), order="F")
+        self._check(self.lib.dqmc_get_field(self.h, _dptr(out)))
+        return out
+
+    def init(self, phi=None):
+        """init!(mc, start_conf) (src/dqmc_framework.jl:156-177)."""
+        if phi is not None:
+            self.set_field(phi)
+        self._check(self.lib.dqmc_init(self.h))
+
+    def propagate(self):
+        self._check(self.lib.dqmc_propagate(self.h))
+
+    @property
+    def state(self):
+        s, d = _I32(), _I32()
+        self._check(self.lib.dqmc_get_state(self.h, ctypes.byref(s), ctypes.byref(d)))
+        return s.value, d.value
+
+    @property
+    def current_slice(self):
+        return self.state[0]
+
+    @property
+    def direction(self):
+        return self.state[1]
+
+    # ---- Green's functions ------------------------------------------------
+    @property
+    def greens(self):
+        out = np.zeros((self.n, self.n), dtype=np.complex128, order="F")
+        self._check(self.lib.dqmc_get_greens(self.h, out.ctypes.data_as(_D), None, None))
+        return out
+
+    @greens.setter
+    def greens(self, G):
+        G = _cplx_in(G, self.n)
+        self._check(self.lib.dqmc_set_greens(self.h, G.ctypes.data_as(_D)))
+
+    def calc_greens_and_logdet(self, slice1):
+        out = np.zeros((self.n, self.n), dtype=np.complex128, order="F")
+        ld = ctypes.c_double()
+        self._check(self.lib.dqmc_calc_greens(self.h, int(slice1), out.ctypes.data_as(_D), ctypes.byref(ld)))
+        return out, ld.value
+
+    def calc_greens(self, slice1):
+        return self.calc_greens_and_logdet(slice1)[0]
+
+    def wrap_greens(self, G, slice1, direction):
+        out = np.array(_cplx_in(G, self.n), order="F", copy=True)
+        self._check(self.lib.dqmc_wrap_greens(self.h, out.ctypes.data_as(_D), int(slice1), int(direction)))
+        return out
+
+    def calculate_greens_udt(self, Ul, Dl, Tl, Ur, Dr, Tr):
+        n = self.n
+        args = [_cplx_in(x, n) for x in (Ul, Tl, Ur, Tr)]
+        Dl = np.ascontiguousarray(Dl, dtype=np.float64)
+        Dr = np.ascontiguousarray(Dr, dtype=np.float64)
+        G = np.zeros((n, n), dtype=np.complex128, order="F")
+        ld = ctypes.c_double()
+        self._check(self.lib.dqmc_calculate_greens_udt(
+            self.h, args[0].ctypes.data_as(_D), _dptr(Dl), args[1].ctypes.data_as(_D),
+            args[2].ctypes.data_as(_D), _dptr(Dr), args[3].ctypes.data_as(_D), G.ctypes.data_as(_D),
+            ctypes.byref(ld)))
+        return G, ld.value
+
+    def decompose_udt(self, A):
+        n = self.n
+        A = _cplx_in(A, n)
+        U = np.zeros((n, n), dtype=np.complex128, order="F")
+        T = np.zeros((n, n), dtype=np.complex128, order="F")
+        D = np.zeros(n)
+        self._check(self.lib.dqmc_decompose_udt(self.h, A.ctypes.data_as(_D), U.ctypes.data_as(_D), _dptr(D),
+                                                T.ctypes.data_as(_D)))
+        return U, D, T
+
+    @property
+    def log_det(self):
+        ld = ctypes.c_double()
+        self._check(self.lib.dqmc_logdet(self.h, ctypes.byref(ld)))
+        return ld.value
+
+    # ---- slice matrices ---------------------------------------------------
+    def _mulB(self, which, slice1, A):
+        out = np.array(_cplx_in(A, self.n), order="F", copy=True)
+        self._check(self.lib.dqmc_multiply_B(self.h, which, int(slice1), out.ctypes.data_as(_D)))
+        return out
+
+    def multiply_B_left(self, slice1, A):
+        return self._mulB(B_LEFT, slice1, A)
+
+    def multiply_B_right(self, slice1, A):
+        return self._mulB(B_RIGHT, slice1, A)
+
+    def multiply_B_inv_left(self, slice1, A):
+        return self._mulB(B_INV_LEFT, slice1, A)
+
+    def multiply_B_inv_right(self, slice1, A):
+        return self._mulB(B_INV_RIGHT, slice1, A)
+
+    def multiply_daggered_B_left(self, slice1, A):
+        return self._mulB(B_DAG_LEFT, slice1, A)
+
+    def slice_matrix(self, slice1, power=1.0):
+        eye = np.eye(self.n, dtype=np.complex128)
+        return self.multiply_B_left(slice1, eye) if power > 0 else self.multiply_B_inv_left(slice1, eye)
+
+    # ---- updates ----------------------------------------------------------
+    def local_updates(self, delta, unif, return_details=False):
+        """local_updates (src/local_updates.jl:1-38) with fixed-slot streams
+        delta (3, N) and unif (N,); returns the acceptance rate."""
+        delta = np.asfortranarray(np.asarray(delta, dtype=np.float64).reshape(3, self.N))
+        unif = np.ascontiguousarray(unif, dtype=np.float64).reshape(self.N)
+        acc = np.zeros(self.N, dtype=np.uint8)
+        det = np.zeros(self.N, dtype=np.complex128)
+        pacc = np.zeros(self.N)
+        rate = ctypes.c_double()
+        self._check(self.lib.dqmc_local_updates(self.h, _dptr(delta), _dptr(unif), acc.ctypes.data_as(ctypes.c_void_p),
+                                                det.ctypes.data_as(_D), _dptr(pacc), ctypes.byref(rate)))
+        if return_details:
+            return rate.value, acc.astype(bool), det, pacc
+        return rate.value
+
+    def update(self, delta, unif, return_details=False):
+        """update (src/dqmc_framework.jl:500-517), global updates off."""
+        self.propagate()
+        return self.local_updates(delta, unif, return_details)
+
+    def sweep(self, n_calls, delta_stream, unif_stream, return_accepted=False):
+        delta_stream = np.ascontiguousarray(np.asarray(delta_stream, dtype=np.float64).reshape(n_calls, 3, self.N))
+        # per call the (3, N) block is column-major: component fastest
+        d = np.ascontiguousarray(np.transpose(delta_stream, (0, 2, 1)))
+        u = np.ascontiguousarray(unif_stream, dtype=np.float64).reshape(n_calls, self.N)
+        acc = np.zeros((n_calls, self.N), dtype=np.uint8) if return_accepted else None
+        st = CStats()
+        self._check(self.lib.dqmc_sweep(self.h, int(n_calls), _dptr(d), _dptr(u),
+                                        acc.ctypes.data_as(ctypes.c_void_p) if acc is not None else None,
+                                        ctypes.byref(st)))
+        res = dict(proposals=st.proposals, accepted=st.accepted, acc_rate=st.acc_rate,
+                   max_instability=st.max_instability, device_ms=st.device_ms)
+        if return_accepted:
+            res["accepted_mask"] = acc.astype(bool)
+        return res
+
+    # ---- action / measurements --------------------------------------------
+    @property
+    def boson_action(self):
+        s = ctypes.c_double()
+        self._check(self.lib.dqmc_boson_action(self.h, ctypes.byref(s)))
+        return s.value
+
+    def calc_boson_action(self):
+        s = ctypes.c_double()
+        self._check(self.lib.dqmc_calc_boson_action(self.h, ctypes.byref(s)))
+        return s.value
+
+    def measure(self):
+        G = np.zeros((self.n, self.n), dtype=np.complex128, order="F")
+        occ, ek = ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.dqmc_measure(self.h, G.ctypes.data_as(_D), ctypes.byref(occ), ctypes.byref(ek)))
+        return dict(greens=G, occupation=occ.value, e_kin=ek.value)
+
+    def timing(self):
+        t = CTiming()
+        self._check(self.lib.dqmc_get_timing(self.h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in CTiming._fields_}
+
+    def reset_timing(self, enable=True):
+        self._check(self.lib.dqmc_reset_timing(self.h, 1 if enable else 0))

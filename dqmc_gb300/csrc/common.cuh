@@ -1,0 +1,101 @@
+// Shared device helpers for the DQMC sweep kernels (sm_103a).
+//
+// Complex numbers are stored as double2 {re, im}, layout-compatible with
+// Julia's ComplexF64 and C's double _Complex.  Every matrix is column-major
+// with leading dimension n (element (r, c) at c*n + r), exactly the layout
+// of the reference's `Matrix{ComplexF64}`.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define DQMC_HD __host__ __device__ __forceinline__
+
+typedef double2 cplx;
+
+DQMC_HD cplx cmake(double r, double i) { return make_double2(r, i); }
+DQMC_HD cplx cadd(cplx a, cplx b) { return cmake(a.x + b.x, a.y + b.y); }
+DQMC_HD cplx csub(cplx a, cplx b) { return cmake(a.x - b.x, a.y - b.y); }
+DQMC_HD cplx cmul(cplx a, cplx b) { return cmake(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+DQMC_HD cplx cconj(cplx a) { return cmake(a.x, -a.y); }
+DQMC_HD cplx cscale(cplx a, double s) { return cmake(a.x * s, a.y * s); }
+// acc + a*b
+DQMC_HD cplx cfma(cplx a, cplx b, cplx acc) {
+  return cmake(fma(a.x, b.x, fma(-a.y, b.y, acc.x)), fma(a.x, b.y, fma(a.y, b.x, acc.y)));
+}
+// acc + conj(a)*b
+DQMC_HD cplx cfma_conj(cplx a, cplx b, cplx acc) {
+  return cmake(fma(a.x, b.x, fma(a.y, b.y, acc.x)), fma(a.x, b.y, fma(-a.y, b.x, acc.y)));
+}
+DQMC_HD double cabs2(cplx a) { return a.x * a.x + a.y * a.y; }
+DQMC_HD cplx cdiv(cplx a, cplx b) {
+  // Smith's algorithm (robust complex division)
+  if (fabs(b.x) >= fabs(b.y)) {
+    double r = b.y / b.x, d = b.x + b.y * r;
+    return cmake((a.x + a.y * r) / d, (a.y - a.x * r) / d);
+  } else {
+    double r = b.x / b.y, d = b.x * r + b.y;
+    return cmake((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+  }
+}
+
+// Model constants needed on the device.  Filled once per handle.
+struct ModelConst {
+  int L, N, n, M;
+  double dtau, lambda, r, c, u;
+  double mu[2];          // band x, band y
+  // hyperbolic rotation factors of the plaquette layers, per band b (0 = x, 1 = y):
+  //   full step (prefactor 1):  ch_f[b] (horizontal), sh_f[b]; cv_f[b] (vertical), sv_f[b]
+  //   half step (prefactor 1/2): ch_h, sh_h, cv_h, sv_h
+  double ch_f[2], sh_f[2], cv_f[2], sv_f[2];
+  double ch_h[2], sh_h[2], cv_h[2], sv_h[2];
+  double emu[2], emu_inv[2];  // exp(dtau*mu), exp(-dtau*mu) per band
+};
+
+// Per-site interaction entries of one slice: (C, Re S, Im S, R) for power +1
+// (src/interactions.jl:52-64).  Power -1 flips the sign of S and R.
+struct EvEntry { double C, Sr, Si, R; };
+
+// Cross-CTA barrier for cooperative (co-resident) grids, with a bounded spin.
+// On timeout it sets *err (bit 1) and returns false: the kernel must then
+// leave its loop and return; it never hangs the device.
+struct GridBarrier {
+  unsigned int count;
+  unsigned int gen;
+};
+
+__device__ __forceinline__ bool grid_barrier(GridBarrier* b, int* err) {
+  __syncthreads();
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    volatile unsigned int* vgen = &b->gen;
+    unsigned int g = *vgen;
+    __threadfence();
+    unsigned int arrived = atomicAdd(&b->count, 1u);
+    int ok = 1;
+    if (arrived == gridDim.x - 1) {
+      atomicExch(&b->count, 0u);
+      __threadfence();
+      atomicAdd(&b->gen, 1u);
+    } else {
+      long long spins = 0;
+      while (*vgen == g) {
+        if (++spins > (1ll << 26)) { atomicOr(err, 2); ok = 0; break; }
+        if (*(volatile int*)err & 2) { ok = 0; break; }
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Error bits reported by kernels through a device int.
+enum {
+  DQMC_KERR_BARRIER_TIMEOUT = 2,
+  DQMC_KERR_NONFINITE = 4,
+  DQMC_KERR_SINGULAR = 8,
+  DQMC_KERR_BAD_SHAPE = 16,
+};
+
+__device__ __forceinline__ cplx ldcg_c(const cplx* p) { return __ldcg(p); }

@@ -1,0 +1,965 @@
+// Host engine and C ABI of the GB300 DQMC sweep library.
+//
+// The engine keeps the reference's state machine on the host (which slice,
+// which direction, when to stabilise: src/stack.jl:391-499) and runs every
+// matrix operation on the device, on one CUDA stream per handle.  All device
+// memory is allocated once in dqmc_create.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/dqmc_gpu.h"
+#include "common.cuh"
+#include "kernels.h"
+
+#define DQMC_VERSION_STRING "dqmc_gb300 0.1 (sm_103a, FP64)"
+
+struct TimedSpan {
+  cudaEvent_t a, b;
+  int group;
+};
+
+struct dqmc_handle {
+  dqmc_params p{};
+  ModelConst mc{};
+  int L = 0, N = 0, n = 0, M = 0, s = 0, ne = 0;
+  cudaStream_t st = nullptr;
+  int sm_count = 0;
+  int device = 0;
+  // ---- device state ----
+  double* phi = nullptr;       // (3, N, M)
+  void* evtab = nullptr;       // (N, M) EvEntry
+  cplx* G = nullptr;
+  cplx* Gtmp = nullptr;        // greens_temp
+  cplx* u_stack = nullptr;     // ne x (n x n)
+  double* d_stack = nullptr;   // ne x n
+  cplx* t_stack = nullptr;     // ne x (n x n)
+  cplx *Ul = nullptr, *Ur = nullptr, *Tl = nullptr, *Tr = nullptr;
+  double *Dl = nullptr, *Dr = nullptr;
+  cplx *W1 = nullptr, *W2 = nullptr, *W3 = nullptr, *W4 = nullptr;
+  double *D1 = nullptr, *d2 = nullptr;
+  int* ord1 = nullptr;
+  QRWork qr{};
+  // local updates
+  double* delta_d = nullptr;
+  double* unif_d = nullptr;
+  int stream_cap = 0;          // update calls the stream buffers hold
+  uint8_t* acc_d = nullptr;
+  cplx* det_d = nullptr;
+  double* pacc_d = nullptr;
+  int out_cap = 0;
+  double* action_d = nullptr;
+  int* nacc_d = nullptr;
+  cplx* Acol = nullptr;
+  cplx* Brow = nullptr;
+  GridBarrier* bar = nullptr;
+  int* err_d = nullptr;
+  double* scal_d = nullptr;    // scratch scalars: [0] logdet sum, [1] absdiff
+  // ---- host state ----
+  int current_slice = 0;
+  int direction = 1;
+  bool initialized = false;
+  double max_instability = 0.0;
+  std::string last_error;
+  // timing
+  bool timing = false;
+  std::vector<TimedSpan> spans;
+  std::vector<cudaEvent_t> event_pool;
+  size_t event_next = 0;
+  double ms[4] = {0, 0, 0, 0};
+  int64_t cnt[4] = {0, 0, 0, 0};
+  int64_t launches = 0;
+};
+
+namespace {
+
+enum { GRP_WRAP = 0, GRP_STACK = 1, GRP_GREENS = 2, GRP_LOCAL = 3 };
+
+int set_err(dqmc_handle* h, int code, const std::string& msg) {
+  if (h) h->last_error = msg;
+  return code;
+}
+
+#define CU(call)                                                                               \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess)                                                                     \
+      return set_err(h, DQMC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+  } while (0)
+
+#define CHK(expr)                 \
+  do {                            \
+    int r_ = (expr);              \
+    if (r_ != DQMC_OK) return r_; \
+  } while (0)
+
+cudaEvent_t next_event(dqmc_handle* h) {
+  if (h->event_next >= h->event_pool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    h->event_pool.push_back(e);
+  }
+  return h->event_pool[h->event_next++];
+}
+
+struct Span {
+  dqmc_handle* h;
+  int group;
+  cudaEvent_t a = nullptr;
+  Span(dqmc_handle* hh, int g) : h(hh), group(g) {
+    if (h->timing) {
+      a = next_event(h);
+      cudaEventRecord(a, h->st);
+    }
+  }
+  ~Span() {
+    if (h->timing) {
+      cudaEvent_t b = next_event(h);
+      cudaEventRecord(b, h->st);
+      h->spans.push_back({a, b, group});
+    }
+    h->cnt[group]++;
+  }
+};
+
+// Resolves recorded spans into accumulated milliseconds (stream must be idle).
+void resolve_spans(dqmc_handle* h) {
+  for (auto& sp : h->spans) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, sp.a, sp.b) == cudaSuccess) h->ms[sp.group] += t;
+  }
+  h->spans.clear();
+  h->event_next = 0;
+}
+
+int check_device_error(dqmc_handle* h) {
+  int e = 0;
+  CU(cudaMemcpyAsync(&e, h->err_d, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaStreamSynchronize(h->st));
+  if (e == 0) return DQMC_OK;
+  CU(cudaMemsetAsync(h->err_d, 0, sizeof(int), h->st));
+  if (e & DQMC_KERR_BARRIER_TIMEOUT) return set_err(h, DQMC_ERR_TIMEOUT, "device barrier timed out");
+  if (e & DQMC_KERR_SINGULAR) return set_err(h, DQMC_ERR_SINGULAR, "singular 4x4 M in a local update");
+  if (e & DQMC_KERR_NONFINITE) return set_err(h, DQMC_ERR_NONFINITE, "non-finite determinant ratio");
+  return set_err(h, DQMC_ERR_CUDA, "device error flag " + std::to_string(e));
+}
+
+int sync(dqmc_handle* h) {
+  CU(cudaStreamSynchronize(h->st));
+  if (h->timing) resolve_spans(h);
+  return check_device_error(h);
+}
+
+size_t nn_bytes(const dqmc_handle* h) { return (size_t)h->n * h->n * sizeof(cplx); }
+cplx* ustk(dqmc_handle* h, int k) { return h->u_stack + (size_t)k * h->n * h->n; }
+cplx* tstk(dqmc_handle* h, int k) { return h->t_stack + (size_t)k * h->n * h->n; }
+double* dstk(dqmc_handle* h, int k) { return h->d_stack + (size_t)k * h->n; }
+
+int copy_nn(dqmc_handle* h, cplx* dst, const cplx* src) {
+  CU(cudaMemcpyAsync(dst, src, nn_bytes(h), cudaMemcpyDeviceToDevice, h->st));
+  return DQMC_OK;
+}
+
+int set_identity(dqmc_handle* h, cplx* A) {
+  CU(launch_set_identity(A, h->n, h->st));
+  h->launches++;
+  return DQMC_OK;
+}
+
+int set_ones(dqmc_handle* h, double* d) {
+  std::vector<double> ones(h->n, 1.0);
+  CU(cudaMemcpyAsync(d, ones.data(), h->n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CU(cudaStreamSynchronize(h->st));
+  return DQMC_OK;
+}
+
+// ---- slice matrices ---------------------------------------------------------
+int apply_cols(dqmc_handle* h, cplx* A, int first0, int count, int step, int mode, const double* colscale) {
+  CU(launch_apply_cols(A, h->n, h->mc, h->evtab, first0, count, step, mode, colscale, h->st));
+  h->launches++;
+  return DQMC_OK;
+}
+int apply_rows(dqmc_handle* h, cplx* A, int first0, int count, int step, int mode) {
+  CU(launch_apply_rows(A, h->n, h->mc, h->evtab, first0, count, step, mode, h->st));
+  h->launches++;
+  return DQMC_OK;
+}
+
+// wrap_greens! (src/stack.jl:316-325); slice is 1-based.
+int wrap_greens(dqmc_handle* h, cplx* gf, int slice, int direction) {
+  Span sp(h, GRP_WRAP);
+  if (direction == -1) {
+    CHK(apply_cols(h, gf, slice - 2, 1, 1, SLICE_LEFT_BINV, nullptr));
+    CHK(apply_rows(h, gf, slice - 2, 1, 1, SLICE_RIGHT_B));
+  } else {
+    CHK(apply_cols(h, gf, slice - 1, 1, 1, SLICE_LEFT_B, nullptr));
+    CHK(apply_rows(h, gf, slice - 1, 1, 1, SLICE_RIGHT_BINV));
+  }
+  return DQMC_OK;
+}
+
+// ---- UDT ------------------------------------------------------------------
+// decompose_udt! (src/linalg.jl:20-39) of A (destroyed): U (explicit), D, T.
+int decompose_udt(dqmc_handle* h, cplx* A, cplx* U, double* D, cplx* T) {
+  CU(launch_qrp(A, h->n, h->qr, h->sm_count, h->st));
+  CU(launch_qrp_finalize(A, T, D, h->n, h->qr, h->st));
+  CHK(set_identity(h, U));
+  CU(launch_apply_q_right(U, h->n, h->n, h->qr, false, h->st));
+  h->launches += 3;
+  return DQMC_OK;
+}
+
+// add_slice_sequence_left (src/stack.jl:278-293); idx 1-based.
+int add_slice_sequence_left(dqmc_handle* h, int idx) {
+  Span sp(h, GRP_STACK);
+  const int k = idx - 1;
+  CHK(copy_nn(h, h->W1, ustk(h, k)));
+  CHK(apply_cols(h, h->W1, (idx - 1) * h->s, h->s, 1, SLICE_LEFT_B, dstk(h, k)));
+  CHK(decompose_udt(h, h->W1, ustk(h, k + 1), dstk(h, k + 1), h->W2));
+  CU(launch_zgemm(h->n, h->n, h->n, 'N', 'N', cmake(1, 0), h->W2, h->n, tstk(h, k), h->n, cmake(0, 0),
+                  tstk(h, k + 1), h->n, nullptr, nullptr, h->st));
+  h->launches++;
+  return DQMC_OK;
+}
+
+// add_slice_sequence_right (src/stack.jl:299-313); idx 1-based.
+int add_slice_sequence_right(dqmc_handle* h, int idx) {
+  Span sp(h, GRP_STACK);
+  const int k = idx - 1;
+  CHK(copy_nn(h, h->W1, ustk(h, k + 1)));
+  CHK(apply_cols(h, h->W1, idx * h->s - 1, h->s, -1, SLICE_LEFT_BDAG, dstk(h, k + 1)));
+  CHK(decompose_udt(h, h->W1, ustk(h, k), dstk(h, k), h->W2));
+  CU(launch_zgemm(h->n, h->n, h->n, 'N', 'N', cmake(1, 0), h->W2, h->n, tstk(h, k + 1), h->n, cmake(0, 0),
+                  tstk(h, k), h->n, nullptr, nullptr, h->st));
+  h->launches++;
+  return DQMC_OK;
+}
+
+// calculate_greens + calculate_logdet (src/stack.jl:338-385) on the device
+// copies Ul, Dl, Tl, Ur, Dr, Tr, written into `out`; log|det G| left in
+// scal_d[0].
+//
+// Same decomposition steps as the reference (two pivoted QRs), but every
+// inverse is taken through the triangular factors instead of LU:
+//   T1 = That1 P1^T  =>  T1^-1 = P1 That1^-1,   (T1 Ur^dag)^-1 = Ur T1^-1,
+// so  tmp = U^dag (T1 Ur^dag)^-1 + D1 = (U^dag Ur) P1 That1^-1 + D1  and
+//   G = (t2 T1 Ur^dag)^-1 diag(1/d2) (U u)^dag
+//     = Ur P1 That1^-1 P2 That2^-1 diag(1/d2) (U Q2)^dag.
+// log|det G| = -sum log d2 (|det| of the unitary and unit-triangular
+// factors is 1).
+int calculate_greens_into(dqmc_handle* h, cplx* out) {
+  Span sp(h, GRP_GREENS);
+  const int n = h->n;
+  const cplx one = cmake(1, 0), zero = cmake(0, 0);
+  // 1. X = Dl (Tl Tr^dag) Dr
+  CU(launch_zgemm(n, n, n, 'N', 'C', one, h->Tl, n, h->Tr, n, zero, h->W1, n, h->Dl, h->Dr, h->st));
+  // 2. X = Q1 D1 T1
+  CU(launch_qrp(h->W1, n, h->qr, h->sm_count, h->st));
+  CU(launch_qrp_finalize(h->W1, h->W2, h->D1, n, h->qr, h->st));
+  CU(cudaMemcpyAsync(h->ord1, h->qr.order, n * sizeof(int), cudaMemcpyDeviceToDevice, h->st));
+  // 3. U = Ul Q1
+  CHK(copy_nn(h, h->W3, h->Ul));
+  CU(launch_apply_q_right(h->W3, n, n, h->qr, false, h->st));
+  // 4. tmp = (U^dag Ur) P1 That1^-1 + diag(D1)
+  CU(launch_zgemm(n, n, n, 'C', 'N', one, h->W3, n, h->Ur, n, zero, h->W4, n, nullptr, nullptr, h->st));
+  CU(launch_permute(h->W4, h->W1, n, n, h->ord1, false, false, h->st));
+  CU(launch_trsm_right_upper(h->W2, h->ord1, h->W1, n, n, h->st));
+  CU(launch_add_diag(h->W1, n, h->D1, h->st));
+  // 5. tmp = Q2 d2 t2
+  CU(launch_qrp(h->W1, n, h->qr, h->sm_count, h->st));
+  CU(launch_qrp_finalize(h->W1, h->W4, h->d2, n, h->qr, h->st));
+  // 6. U Q2
+  CU(launch_apply_q_right(h->W3, n, n, h->qr, false, h->st));
+  // 7. G = Ur P1 That1^-1 P2 That2^-1 diag(1/d2) (U Q2)^dag
+  CU(launch_conj_transpose(h->W3, h->W1, n, h->st));
+  CU(launch_scale(h->W1, n, n, h->d2, true, nullptr, false, h->st));
+  CU(launch_trsm_left_upper(h->W4, h->qr.order, h->W1, n, n, h->st));
+  CU(launch_permute(h->W1, h->W3, n, n, h->qr.order, true, true, h->st));
+  CU(launch_trsm_left_upper(h->W2, h->ord1, h->W3, n, n, h->st));
+  CU(launch_permute(h->W3, h->W1, n, n, h->ord1, true, true, h->st));
+  CU(launch_zgemm(n, n, n, 'N', 'N', one, h->Ur, n, h->W1, n, zero, out, n, nullptr, nullptr, h->st));
+  CU(launch_sum_log(h->d2, n, h->scal_d, h->st));
+  h->launches += 19;
+  return DQMC_OK;
+}
+
+int calculate_greens(dqmc_handle* h) { return calculate_greens_into(h, h->G); }
+
+int save_logdet(dqmc_handle* h) {
+  // scal_d[0] = sum log d2  ->  scal_d[2] = log_det = -sum log d2
+  CU(cudaMemcpyAsync(h->scal_d + 2, h->scal_d, sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  return DQMC_OK;
+}
+
+int set_l(dqmc_handle* h, int k) {
+  CHK(copy_nn(h, h->Ul, ustk(h, k)));
+  CHK(copy_nn(h, h->Tl, tstk(h, k)));
+  CU(cudaMemcpyAsync(h->Dl, dstk(h, k), h->n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  return DQMC_OK;
+}
+int set_r(dqmc_handle* h, int k) {
+  CHK(copy_nn(h, h->Ur, ustk(h, k)));
+  CHK(copy_nn(h, h->Tr, tstk(h, k)));
+  CU(cudaMemcpyAsync(h->Dr, dstk(h, k), h->n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  return DQMC_OK;
+}
+int stack_identity(dqmc_handle* h, int k) {
+  CHK(set_identity(h, ustk(h, k)));
+  CHK(set_identity(h, tstk(h, k)));
+  CHK(set_ones(h, dstk(h, k)));
+  return DQMC_OK;
+}
+
+int instability_check(dqmc_handle* h) {
+  CU(launch_max_absdiff(h->Gtmp, h->G, (size_t)h->n * h->n, h->scal_d + 1, h->st));
+  h->launches++;
+  double d = 0.0;
+  CU(cudaMemcpyAsync(&d, h->scal_d + 1, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaStreamSynchronize(h->st));
+  if (!(d <= h->max_instability)) h->max_instability = d;
+  if (!std::isfinite(d)) return set_err(h, DQMC_ERR_NONFINITE, "non-finite Green's function");
+  return DQMC_OK;
+}
+
+// build_stack (src/stack.jl:251-272)
+int build_stack(dqmc_handle* h) {
+  CHK(stack_identity(h, 0));
+  for (int i = 1; i <= h->ne - 1; ++i) CHK(add_slice_sequence_left(h, i));
+  h->current_slice = h->M + 1;
+  h->direction = -1;
+  return DQMC_OK;
+}
+
+// propagate (src/stack.jl:391-499)
+int propagate(dqmc_handle* h) {
+  const int s = h->s, M = h->M;
+  if (h->direction == 1) {
+    if (h->current_slice % s == 0) {
+      h->current_slice += 1;
+      if (h->current_slice == 1) {
+        CHK(set_r(h, 0));
+        CHK(stack_identity(h, 0));
+        CHK(set_l(h, 0));
+        CHK(calculate_greens(h));
+        CHK(save_logdet(h));
+      } else if (h->current_slice > 1 && h->current_slice <= M) {
+        int idx = (h->current_slice - 1) / s;
+        CHK(set_r(h, idx));
+        CHK(add_slice_sequence_left(h, idx));
+        CHK(set_l(h, idx));
+        if (h->p.all_checks) {
+          CHK(copy_nn(h, h->Gtmp, h->G));
+          CHK(wrap_greens(h, h->Gtmp, h->current_slice - 1, 1));
+        }
+        CHK(calculate_greens(h));
+        if (h->p.all_checks) CHK(instability_check(h));
+      } else {
+        CHK(add_slice_sequence_left(h, h->ne - 1));
+        h->direction = -1;
+        h->current_slice = M + 1;
+        return propagate(h);
+      }
+    } else {
+      CHK(wrap_greens(h, h->G, h->current_slice, 1));
+      h->current_slice += 1;
+    }
+  } else {
+    if ((h->current_slice - 1) % s == 0) {
+      h->current_slice -= 1;
+      if (h->current_slice == M) {
+        const int e = h->ne - 1;
+        CHK(set_l(h, e));
+        CHK(stack_identity(h, e));
+        CHK(set_r(h, e));
+        CHK(calculate_greens(h));
+        CHK(save_logdet(h));
+        CHK(wrap_greens(h, h->G, h->current_slice + 1, -1));
+      } else if (h->current_slice > 0 && h->current_slice < M) {
+        int idx = h->current_slice / s + 1;
+        CHK(set_l(h, idx - 1));
+        CHK(add_slice_sequence_right(h, idx));
+        CHK(set_r(h, idx - 1));
+        if (h->p.all_checks) CHK(copy_nn(h, h->Gtmp, h->G));
+        CHK(calculate_greens(h));
+        if (h->p.all_checks) CHK(instability_check(h));
+        CHK(wrap_greens(h, h->G, h->current_slice + 1, -1));
+      } else {
+        CHK(add_slice_sequence_right(h, 1));
+        h->direction = 1;
+        h->current_slice = 0;
+        return propagate(h);
+      }
+    } else {
+      CHK(wrap_greens(h, h->G, h->current_slice, -1));
+      h->current_slice -= 1;
+    }
+  }
+  return DQMC_OK;
+}
+
+// calc_boson_action (src/action.jl:1-52) on a host copy of the field.
+double boson_action_host(const dqmc_handle* h, const std::vector<double>& phi) {
+  const int L = h->L, N = h->N, M = h->M;
+  const double dt = h->p.delta_tau, c = h->p.c, r = h->p.r, u = h->p.u;
+  auto at = [&](int a, int site, int sl) { return phi[(size_t)3 * ((size_t)N * sl + site) + a]; };
+  double S = 0.0, St = 0.0, Ss = 0.0, Sm = 0.0;
+  for (int sl = 0; sl < M; ++sl)
+    for (int x = 0; x < L; ++x)
+      for (int y = 0; y < L; ++y) {
+        int site = y + L * x;
+        int up = (y + 1) % L + L * x, right = y + L * ((x + 1) % L);
+        int later = (sl + 1) % M;
+        double sq = 0.0;
+        for (int a = 0; a < 3; ++a) {
+          double v = at(a, site, sl);
+          double dtm = v - at(a, site, later);
+          double dy = v - at(a, up, sl);
+          double dx = v - at(a, right, sl);
+          St += dtm * dtm;
+          Ss += dy * dy + dx * dx;
+          sq += v * v;
+        }
+        Sm += dt * r / 2.0 * sq + dt * u / 4.0 * sq * sq;
+      }
+  S = 0.5 / dt * 1.0 / (c * c) * St + dt * 0.5 * Ss + Sm;
+  return S;
+}
+
+int ensure_stream_capacity(dqmc_handle* h, int calls) {
+  if (calls <= h->stream_cap) return DQMC_OK;
+  if (h->delta_d) cudaFree(h->delta_d);
+  if (h->unif_d) cudaFree(h->unif_d);
+  h->delta_d = nullptr;
+  h->unif_d = nullptr;
+  h->stream_cap = 0;
+  CU(cudaMalloc(&h->delta_d, (size_t)calls * 3 * h->N * sizeof(double)));
+  CU(cudaMalloc(&h->unif_d, (size_t)calls * h->N * sizeof(double)));
+  h->stream_cap = calls;
+  return DQMC_OK;
+}
+
+int ensure_out_capacity(dqmc_handle* h, int calls) {
+  if (calls <= h->out_cap) return DQMC_OK;
+  if (h->acc_d) cudaFree(h->acc_d);
+  if (h->det_d) cudaFree(h->det_d);
+  if (h->pacc_d) cudaFree(h->pacc_d);
+  h->acc_d = nullptr; h->det_d = nullptr; h->pacc_d = nullptr;
+  h->out_cap = 0;
+  CU(cudaMalloc(&h->acc_d, (size_t)calls * h->N));
+  CU(cudaMalloc(&h->det_d, (size_t)calls * h->N * sizeof(cplx)));
+  CU(cudaMalloc(&h->pacc_d, (size_t)calls * h->N * sizeof(double)));
+  h->out_cap = calls;
+  return DQMC_OK;
+}
+
+// local_updates (src/local_updates.jl:1-38) on device streams; outputs to
+// device arrays (may be null).
+int local_updates_dev(dqmc_handle* h, const double* delta_dev, const double* unif_dev, uint8_t* acc_dev,
+                      cplx* det_dev, double* pacc_dev) {
+  if (h->current_slice < 1 || h->current_slice > h->M)
+    return set_err(h, DQMC_ERR_STATE, "local_updates needs 1 <= current_slice <= M (call dqmc_init)");
+  Span sp(h, GRP_LOCAL);
+  LocalUpdateArgs a{};
+  a.G = h->G;
+  a.phi = h->phi;
+  a.evtab = h->evtab;
+  a.slice0 = h->current_slice - 1;
+  a.delta = delta_dev;
+  a.unif = unif_dev;
+  a.acc_out = acc_dev;
+  a.det_out = det_dev;
+  a.pacc_out = pacc_dev;
+  a.action = h->action_d;
+  a.n_acc = h->nacc_d;
+  a.Acol = h->Acol;
+  a.Brow = h->Brow;
+  a.bar = h->bar;
+  a.err = h->err_d;
+  a.mc = h->mc;
+  CU(launch_local_updates(a, h->sm_count, h->st));
+  h->launches++;
+  return DQMC_OK;
+}
+
+int read_nacc(dqmc_handle* h, int* out) {
+  CU(cudaMemcpyAsync(out, h->nacc_d, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaStreamSynchronize(h->st));
+  return DQMC_OK;
+}
+
+void host_model_constants(dqmc_handle* h) {
+  ModelConst& m = h->mc;
+  const dqmc_params& p = h->p;
+  m.L = h->L; m.N = h->N; m.n = h->n; m.M = h->M;
+  m.dtau = p.delta_tau; m.lambda = p.lambda; m.r = p.r; m.c = p.c; m.u = p.u;
+  m.mu[0] = p.mu1; m.mu[1] = p.mu2;
+  // t[bond dir, band] = reshape(hoppings, 2, 2): t[0][b] horizontal, t[1][b] vertical
+  const double th[2] = {p.hoppings[0], p.hoppings[2]};
+  const double tv[2] = {p.hoppings[1], p.hoppings[3]};
+  for (int b = 0; b < 2; ++b) {
+    // cosh(fac * -t), sinh(fac * -t) with fac = -prefac * dtau (src/hoppings_checkerboard.jl:46-51)
+    double ff = -1.0 * p.delta_tau, fh = -0.5 * p.delta_tau;
+    m.ch_f[b] = std::cosh(ff * -th[b]); m.sh_f[b] = std::sinh(ff * -th[b]);
+    m.cv_f[b] = std::cosh(ff * -tv[b]); m.sv_f[b] = std::sinh(ff * -tv[b]);
+    m.ch_h[b] = std::cosh(fh * -th[b]); m.sh_h[b] = std::sinh(fh * -th[b]);
+    m.cv_h[b] = std::cosh(fh * -tv[b]); m.sv_h[b] = std::sinh(fh * -tv[b]);
+    // chkr_mu = exp(-dtau * -mu), chkr_mu_inv = exp(dtau * -mu) (src/hoppings_checkerboard.jl:122-127)
+    double mu = b == 0 ? p.mu1 : p.mu2;
+    m.emu[b] = std::exp(-p.delta_tau * -mu);
+    m.emu_inv[b] = std::exp(p.delta_tau * -mu);
+  }
+}
+
+void free_all(dqmc_handle* h) {
+  void* ptrs[] = {h->phi, h->evtab, h->G, h->Gtmp, h->u_stack, h->d_stack, h->t_stack, h->Ul, h->Ur, h->Tl,
+                  h->Tr, h->Dl, h->Dr, h->W1, h->W2, h->W3, h->W4, h->D1, h->d2, h->ord1, h->qr.vn1,
+                  h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->delta_d, h->unif_d,
+                  h->acc_d, h->det_d, h->pacc_d, h->action_d, h->nacc_d, h->Acol, h->Brow, h->bar, h->err_d,
+                  h->scal_d};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  for (auto e : h->event_pool) cudaEventDestroy(e);
+  if (h->st) cudaStreamDestroy(h->st);
+}
+
+int upload_nn(dqmc_handle* h, cplx* dst, const double* src) {
+  CU(cudaMemcpyAsync(dst, src, nn_bytes(h), cudaMemcpyHostToDevice, h->st));
+  return DQMC_OK;
+}
+int download_nn(dqmc_handle* h, double* dst, const cplx* src) {
+  CU(cudaMemcpyAsync(dst, src, nn_bytes(h), cudaMemcpyDeviceToHost, h->st));
+  return DQMC_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* dqmc_version(void) { return DQMC_VERSION_STRING; }
+
+const char* dqmc_last_error(const dqmc_handle* h) { return h ? h->last_error.c_str() : "null handle"; }
+
+int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
+  if (!p || !out) return DQMC_ERR_ARG;
+  *out = nullptr;
+  if (p->L < 2 || p->L % 2 != 0) return DQMC_ERR_ARG;                 // CBAssaad needs even L
+  if (p->slices < 1 || p->safe_mult < 1 || p->slices % p->safe_mult != 0) return DQMC_ERR_ARG;
+  if (p->opdim != 3) return DQMC_ERR_ARG;
+  if (p->precision != DQMC_PREC_FP64) return DQMC_ERR_ARG;
+  if (4 * p->L * p->L > 1024) return DQMC_ERR_ARG;                     // register-resident QR columns
+  dqmc_handle* h = new dqmc_handle();
+  h->p = *p;
+  h->L = p->L; h->N = p->L * p->L; h->n = 4 * h->N; h->M = p->slices; h->s = p->safe_mult;
+  h->ne = h->M / h->s + 1;
+  host_model_constants(h);
+  auto fail = [&](int code) { free_all(h); delete h; return code; };
+  if (cudaGetDevice(&h->device) != cudaSuccess) return fail(DQMC_ERR_CUDA);
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess) return fail(DQMC_ERR_CUDA);
+  h->sm_count = prop.multiProcessorCount;
+  if (!prop.cooperativeLaunch) return fail(DQMC_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) return fail(DQMC_ERR_CUDA);
+  const size_t n = h->n, N = h->N, M = h->M, ne = h->ne;
+  const size_t nn = n * n * sizeof(cplx);
+  bool ok = true;
+  auto A = [&](void** ptr, size_t bytes) {
+    if (ok && cudaMalloc(ptr, bytes) != cudaSuccess) ok = false;
+    if (ok) cudaMemset(*ptr, 0, bytes);
+  };
+  A((void**)&h->phi, 3 * N * M * sizeof(double));
+  A(&h->evtab, N * M * evtab_entry_bytes());
+  A((void**)&h->G, nn); A((void**)&h->Gtmp, nn);
+  A((void**)&h->u_stack, ne * nn); A((void**)&h->t_stack, ne * nn);
+  A((void**)&h->d_stack, ne * n * sizeof(double));
+  A((void**)&h->Ul, nn); A((void**)&h->Ur, nn); A((void**)&h->Tl, nn); A((void**)&h->Tr, nn);
+  A((void**)&h->Dl, n * sizeof(double)); A((void**)&h->Dr, n * sizeof(double));
+  A((void**)&h->W1, nn); A((void**)&h->W2, nn); A((void**)&h->W3, nn); A((void**)&h->W4, nn);
+  A((void**)&h->D1, n * sizeof(double)); A((void**)&h->d2, n * sizeof(double));
+  A((void**)&h->ord1, n * sizeof(int));
+  A((void**)&h->qr.vn1, n * sizeof(double)); A((void**)&h->qr.vn2, n * sizeof(double));
+  A((void**)&h->qr.order, n * sizeof(int)); A((void**)&h->qr.tau, n * sizeof(cplx));
+  A((void**)&h->qr.beta, n * sizeof(double)); A((void**)&h->qr.V, nn);
+  A((void**)&h->qr.bar, sizeof(GridBarrier));
+  A((void**)&h->action_d, sizeof(double)); A((void**)&h->nacc_d, sizeof(int));
+  A((void**)&h->Acol, 4 * n * sizeof(cplx)); A((void**)&h->Brow, 4 * n * sizeof(cplx));
+  A((void**)&h->bar, sizeof(GridBarrier)); A((void**)&h->err_d, sizeof(int));
+  A((void**)&h->scal_d, 8 * sizeof(double));
+  if (!ok) return fail(DQMC_ERR_CUDA);
+  h->qr.err = h->err_d;
+  if (cudaDeviceSynchronize() != cudaSuccess) return fail(DQMC_ERR_CUDA);
+  *out = h;
+  return DQMC_OK;
+}
+
+int dqmc_destroy(dqmc_handle* h) {
+  if (!h) return DQMC_ERR_ARG;
+  cudaStreamSynchronize(h->st);
+  free_all(h);
+  delete h;
+  return DQMC_OK;
+}
+
+int dqmc_set_field(dqmc_handle* h, const double* phi) {
+  if (!h || !phi) return DQMC_ERR_ARG;
+  CU(cudaMemcpyAsync(h->phi, phi, (size_t)3 * h->N * h->M * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CU(launch_build_evtab(h->phi, h->evtab, h->N, h->M, h->p.lambda * h->p.delta_tau, h->st));
+  h->launches++;
+  h->initialized = false;
+  return sync(h);
+}
+
+int dqmc_get_field(dqmc_handle* h, double* phi) {
+  if (!h || !phi) return DQMC_ERR_ARG;
+  CU(cudaMemcpyAsync(phi, h->phi, (size_t)3 * h->N * h->M * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  return sync(h);
+}
+
+int dqmc_init(dqmc_handle* h) {
+  if (!h) return DQMC_ERR_ARG;
+  std::vector<double> phi((size_t)3 * h->N * h->M);
+  CU(cudaMemcpyAsync(phi.data(), h->phi, phi.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaStreamSynchronize(h->st));
+  double S = boson_action_host(h, phi);
+  CU(cudaMemcpyAsync(h->action_d, &S, sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CU(cudaMemsetAsync(h->nacc_d, 0, sizeof(int), h->st));
+  h->max_instability = 0.0;
+  CHK(build_stack(h));
+  CHK(propagate(h));
+  h->initialized = true;
+  return sync(h);
+}
+
+int dqmc_propagate(dqmc_handle* h) {
+  if (!h) return DQMC_ERR_ARG;
+  if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
+  CHK(propagate(h));
+  return sync(h);
+}
+
+int dqmc_get_state(dqmc_handle* h, int32_t* slice, int32_t* direction) {
+  if (!h) return DQMC_ERR_ARG;
+  if (slice) *slice = h->current_slice;
+  if (direction) *direction = h->direction;
+  return DQMC_OK;
+}
+
+static int local_updates_host(dqmc_handle* h, const double* delta, const double* unif, uint8_t* accepted,
+                              double* detratio, double* p_acc, double* acc_rate) {
+  if (!delta || !unif) return set_err(h, DQMC_ERR_ARG, "delta and unif are required");
+  CHK(ensure_stream_capacity(h, 1));
+  CHK(ensure_out_capacity(h, 1));
+  CU(cudaMemcpyAsync(h->delta_d, delta, (size_t)3 * h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CU(cudaMemcpyAsync(h->unif_d, unif, (size_t)h->N * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  int before = 0;
+  CHK(read_nacc(h, &before));
+  CHK(local_updates_dev(h, h->delta_d, h->unif_d, h->acc_d, h->det_d, h->pacc_d));
+  if (accepted) CU(cudaMemcpyAsync(accepted, h->acc_d, h->N, cudaMemcpyDeviceToHost, h->st));
+  if (detratio) CU(cudaMemcpyAsync(detratio, h->det_d, h->N * sizeof(cplx), cudaMemcpyDeviceToHost, h->st));
+  if (p_acc) CU(cudaMemcpyAsync(p_acc, h->pacc_d, h->N * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CHK(sync(h));
+  if (acc_rate) {
+    int after = 0;
+    CHK(read_nacc(h, &after));
+    *acc_rate = (double)(after - before) / h->N;
+  }
+  return DQMC_OK;
+}
+
+int dqmc_local_updates(dqmc_handle* h, const double* delta, const double* unif, uint8_t* accepted,
+                       double* detratio, double* p_acc, double* acc_rate) {
+  if (!h) return DQMC_ERR_ARG;
+  if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
+  return local_updates_host(h, delta, unif, accepted, detratio, p_acc, acc_rate);
+}
+
+int dqmc_update(dqmc_handle* h, const double* delta, const double* unif, uint8_t* accepted, double* detratio,
+                double* p_acc, double* acc_rate) {
+  if (!h) return DQMC_ERR_ARG;
+  if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
+  CHK(propagate(h));
+  return local_updates_host(h, delta, unif, accepted, detratio, p_acc, acc_rate);
+}
+
+static int sweep_impl(dqmc_handle* h, int n_calls, const double* delta_dev, const double* unif_dev,
+                      uint8_t* acc_dev, dqmc_stats* stats) {
+  int before = 0;
+  CHK(read_nacc(h, &before));
+  h->max_instability = 0.0;
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  CU(cudaEventRecord(e0, h->st));
+  const size_t N = h->N;
+  for (int c = 0; c < n_calls; ++c) {
+    CHK(propagate(h));
+    CHK(local_updates_dev(h, delta_dev + (size_t)c * 3 * N, unif_dev + (size_t)c * N,
+                          acc_dev ? acc_dev + (size_t)c * N : nullptr, nullptr, nullptr));
+  }
+  CU(cudaEventRecord(e1, h->st));
+  CHK(sync(h));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  int after = 0;
+  CHK(read_nacc(h, &after));
+  if (stats) {
+    stats->proposals = (int64_t)n_calls * h->N;
+    stats->accepted = after - before;
+    stats->acc_rate = stats->proposals ? (double)stats->accepted / stats->proposals : 0.0;
+    stats->max_instability = h->max_instability;
+    stats->device_ms = ms;
+  }
+  return DQMC_OK;
+}
+
+int dqmc_sweep(dqmc_handle* h, int32_t n_calls, const double* delta_stream, const double* unif_stream,
+               uint8_t* accepted, dqmc_stats* stats) {
+  if (!h || n_calls < 0 || !delta_stream || !unif_stream) return DQMC_ERR_ARG;
+  if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
+  if (n_calls == 0) return DQMC_OK;
+  CHK(ensure_stream_capacity(h, n_calls));
+  CHK(ensure_out_capacity(h, n_calls));
+  CU(cudaMemcpyAsync(h->delta_d, delta_stream, (size_t)n_calls * 3 * h->N * sizeof(double),
+                     cudaMemcpyHostToDevice, h->st));
+  CU(cudaMemcpyAsync(h->unif_d, unif_stream, (size_t)n_calls * h->N * sizeof(double), cudaMemcpyHostToDevice,
+                     h->st));
+  CHK(sweep_impl(h, n_calls, h->delta_d, h->unif_d, accepted ? h->acc_d : nullptr, stats));
+  if (accepted) {
+    CU(cudaMemcpyAsync(accepted, h->acc_d, (size_t)n_calls * h->N, cudaMemcpyDeviceToHost, h->st));
+    return sync(h);
+  }
+  return DQMC_OK;
+}
+
+int dqmc_sweep_device(dqmc_handle* h, int32_t n_calls, const double* delta_stream_dev,
+                      const double* unif_stream_dev, uint8_t* accepted_dev, dqmc_stats* stats) {
+  if (!h || n_calls < 0 || !delta_stream_dev || !unif_stream_dev) return DQMC_ERR_ARG;
+  if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
+  if (n_calls == 0) return DQMC_OK;
+  return sweep_impl(h, n_calls, delta_stream_dev, unif_stream_dev, accepted_dev, stats);
+}
+
+int dqmc_get_greens(dqmc_handle* h, double* out, int32_t* slice, int32_t* direction) {
+  if (!h || !out) return DQMC_ERR_ARG;
+  CHK(download_nn(h, out, h->G));
+  if (slice) *slice = h->current_slice;
+  if (direction) *direction = h->direction;
+  return sync(h);
+}
+
+int dqmc_set_greens(dqmc_handle* h, const double* in) {
+  if (!h || !in) return DQMC_ERR_ARG;
+  CHK(upload_nn(h, h->G, in));
+  return sync(h);
+}
+
+int dqmc_wrap_greens(dqmc_handle* h, double* inout, int32_t slice, int32_t direction) {
+  if (!h || !inout || (direction != 1 && direction != -1)) return DQMC_ERR_ARG;
+  int sl0 = direction == 1 ? slice : slice - 1;
+  if (sl0 < 1 || sl0 > h->M) return set_err(h, DQMC_ERR_ARG, "slice out of range");
+  CHK(upload_nn(h, h->Gtmp, inout));
+  CHK(wrap_greens(h, h->Gtmp, slice, direction));
+  CHK(download_nn(h, inout, h->Gtmp));
+  return sync(h);
+}
+
+int dqmc_multiply_B(dqmc_handle* h, int32_t which, int32_t slice, double* inout) {
+  if (!h || !inout || which < 0 || which > 4) return DQMC_ERR_ARG;
+  if (slice < 1 || slice > h->M) return set_err(h, DQMC_ERR_ARG, "slice out of range");
+  CHK(upload_nn(h, h->Gtmp, inout));
+  if (which == DQMC_B_RIGHT || which == DQMC_B_INV_RIGHT)
+    CHK(apply_rows(h, h->Gtmp, slice - 1, 1, 1, which));
+  else
+    CHK(apply_cols(h, h->Gtmp, slice - 1, 1, 1, which, nullptr));
+  CHK(download_nn(h, inout, h->Gtmp));
+  return sync(h);
+}
+
+int dqmc_calculate_greens_udt(dqmc_handle* h, const double* Ul, const double* Dl, const double* Tl,
+                              const double* Ur, const double* Dr, const double* Tr, double* G, double* logdet) {
+  if (!h || !Ul || !Dl || !Tl || !Ur || !Dr || !Tr || !G) return DQMC_ERR_ARG;
+  const size_t dn = h->n * sizeof(double);
+  CHK(upload_nn(h, h->Ul, Ul));
+  CHK(upload_nn(h, h->Tl, Tl));
+  CHK(upload_nn(h, h->Ur, Ur));
+  CHK(upload_nn(h, h->Tr, Tr));
+  CU(cudaMemcpyAsync(h->Dl, Dl, dn, cudaMemcpyHostToDevice, h->st));
+  CU(cudaMemcpyAsync(h->Dr, Dr, dn, cudaMemcpyHostToDevice, h->st));
+  CHK(calculate_greens_into(h, h->Gtmp));
+  CHK(download_nn(h, G, h->Gtmp));
+  double sl = 0.0;
+  CU(cudaMemcpyAsync(&sl, h->scal_d, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CHK(sync(h));
+  if (logdet) *logdet = -sl;
+  return DQMC_OK;
+}
+
+int dqmc_decompose_udt(dqmc_handle* h, const double* A, double* U, double* D, double* T) {
+  if (!h || !A || !U || !D || !T) return DQMC_ERR_ARG;
+  CHK(upload_nn(h, h->W1, A));
+  CHK(decompose_udt(h, h->W1, h->W3, h->D1, h->W2));
+  CHK(download_nn(h, U, h->W3));
+  CHK(download_nn(h, T, h->W2));
+  CU(cudaMemcpyAsync(D, h->D1, h->n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  return sync(h);
+}
+
+int dqmc_logdet(dqmc_handle* h, double* logdet) {
+  if (!h || !logdet) return DQMC_ERR_ARG;
+  double sl = 0.0;
+  CU(cudaMemcpyAsync(&sl, h->scal_d + 2, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CHK(sync(h));
+  *logdet = -sl;
+  return DQMC_OK;
+}
+
+// calc_greens_and_logdet (src/fermion_measurements.jl:1061-1101): the B chains
+// B(slice)^dag ... B(M)^dag and B(slice-1) ... B(1) as UDTs, stabilised every
+// safe_mult slices (calc_Bchain_dagger / calc_Bchain, :964-1058).
+int dqmc_calc_greens(dqmc_handle* h, int32_t slice, double* out, double* logdet) {
+  if (!h || !out) return DQMC_ERR_ARG;
+  if (slice < 1 || slice > h->M) return set_err(h, DQMC_ERR_ARG, "slice out of range");
+  const int n = h->n, s = h->s;
+  const cplx one = cmake(1, 0), zero = cmake(0, 0);
+  // chain helper: U, D, T accumulate into (Ux, Dx, Tx) buffers
+  auto chain = [&](int start, int stop, bool dagger, cplx* Ux, double* Dx, cplx* Tx) -> int {
+    CHK(set_identity(h, Ux));
+    CHK(set_identity(h, Tx));
+    CHK(set_ones(h, Dx));
+    bool pending_scale = false;   // columns of Ux still need scaling by Dx before the next QR
+    auto flush = [&]() -> int {
+      CU(launch_scale(Ux, n, n, nullptr, false, Dx, false, h->st));
+      CHK(copy_nn(h, h->W1, Ux));
+      CHK(decompose_udt(h, h->W1, Ux, Dx, h->W2));
+      CU(launch_zgemm(n, n, n, 'N', 'N', one, h->W2, n, Tx, n, zero, h->W4, n, nullptr, nullptr, h->st));
+      CHK(copy_nn(h, Tx, h->W4));
+      h->launches += 2;
+      return DQMC_OK;
+    };
+    (void)pending_scale;
+    if (!dagger) {
+      for (int k = start; k <= stop; ++k) {
+        CHK(apply_cols(h, Ux, k - 1, 1, 1, SLICE_LEFT_B, nullptr));
+        if (k % s == 0 || k == stop) CHK(flush());
+      }
+    } else {
+      for (int k = stop; k >= start; --k) {
+        CHK(apply_cols(h, Ux, k - 1, 1, 1, SLICE_LEFT_BDAG, nullptr));
+        if (k % s == 0 || k == start) CHK(flush());
+      }
+    }
+    return DQMC_OK;
+  };
+  // Ur, Dr, Tr = B(slice)^dag ... B(M)^dag ; Ul, Dl, Tl = B(slice-1) ... B(1)
+  CHK(chain(slice, h->M, true, h->Ur, h->Dr, h->Tr));
+  if (slice - 1 >= 1) {
+    CHK(chain(1, slice - 1, false, h->Ul, h->Dl, h->Tl));
+  } else {
+    CHK(set_identity(h, h->Ul));
+    CHK(set_identity(h, h->Tl));
+    CHK(set_ones(h, h->Dl));
+  }
+  CHK(calculate_greens_into(h, h->Gtmp));
+  CHK(download_nn(h, out, h->Gtmp));
+  double sl = 0.0;
+  CU(cudaMemcpyAsync(&sl, h->scal_d, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CHK(sync(h));
+  if (logdet) *logdet = -sl;
+  // the stack copies Ul..Tr were overwritten: restore nothing (propagate re-reads them from the stack)
+  return DQMC_OK;
+}
+
+int dqmc_boson_action(dqmc_handle* h, double* S) {
+  if (!h || !S) return DQMC_ERR_ARG;
+  CU(cudaMemcpyAsync(S, h->action_d, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  return sync(h);
+}
+
+int dqmc_calc_boson_action(dqmc_handle* h, double* S) {
+  if (!h || !S) return DQMC_ERR_ARG;
+  std::vector<double> phi((size_t)3 * h->N * h->M);
+  CU(cudaMemcpyAsync(phi.data(), h->phi, phi.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CHK(sync(h));
+  *S = boson_action_host(h, phi);
+  return DQMC_OK;
+}
+
+int dqmc_measure(dqmc_handle* h, double* greens_out, double* occupation, double* e_kin) {
+  if (!h) return DQMC_ERR_ARG;
+  if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
+  const int n = h->n, N = h->N, L = h->L;
+  if (h->current_slice < 1 || h->current_slice > h->M) return set_err(h, DQMC_ERR_STATE, "no current slice");
+  // g = wrap_greens(G, current_slice, +1); effective -> true G
+  CHK(copy_nn(h, h->Gtmp, h->G));
+  CHK(wrap_greens(h, h->Gtmp, h->current_slice, 1));
+  CHK(apply_rows(h, h->Gtmp, 0, 1, 1, 5));   // G Hb_half Ha_half
+  CHK(apply_cols(h, h->Gtmp, 0, 1, 1, 6, nullptr));   // Ha_half^-1 Hb_half^-1 G
+  std::vector<double> g((size_t)2 * n * n);
+  CHK(download_nn(h, g.data(), h->Gtmp));
+  CHK(sync(h));
+  if (greens_out) std::memcpy(greens_out, g.data(), g.size() * sizeof(double));
+  auto Gre = [&](int r, int c) { return g[2 * ((size_t)c * n + r)]; };
+  if (occupation) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += 1.0 - Gre(i, i);
+    *occupation = s / n;
+  }
+  if (e_kin) {
+    // T = -mu on the diagonal, -t on nearest-neighbour bonds (src/hoppings.jl:23-43);
+    // E = sum_ij T_ij (delta_ij - G_ji)
+    const double th[2] = {h->p.hoppings[0], h->p.hoppings[2]};
+    const double tv[2] = {h->p.hoppings[1], h->p.hoppings[3]};
+    double E = 0.0;
+    for (int f = 0; f < 4; ++f) {
+      int b = f & 1;
+      double mu = b == 0 ? h->p.mu1 : h->p.mu2;
+      for (int x = 0; x < L; ++x)
+        for (int y = 0; y < L; ++y) {
+          int src = y + L * x;
+          int i = f * N + src;
+          E += -mu * (1.0 - Gre(i, i));
+          int nbs[4] = {(y + 1) % L + L * x, y + L * ((x + 1) % L), (y - 1 + L) % L + L * x,
+                        y + L * ((x - 1 + L) % L)};
+          double tt[4] = {tv[b], th[b], tv[b], th[b]};
+          for (int q = 0; q < 4; ++q) {
+            int j = f * N + nbs[q];   // T[j, i] = -t   ->  term T_ji (delta_ji - G_ij)
+            E += -tt[q] * (-(Gre(i, j)));
+          }
+        }
+    }
+    *e_kin = E;
+  }
+  return DQMC_OK;
+}
+
+int dqmc_get_timing(dqmc_handle* h, dqmc_timing* t) {
+  if (!h || !t) return DQMC_ERR_ARG;
+  CHK(sync(h));
+  t->ms_wrap = h->ms[GRP_WRAP];
+  t->ms_stack = h->ms[GRP_STACK];
+  t->ms_greens = h->ms[GRP_GREENS];
+  t->ms_local = h->ms[GRP_LOCAL];
+  t->n_wrap = h->cnt[GRP_WRAP];
+  t->n_stack = h->cnt[GRP_STACK];
+  t->n_greens = h->cnt[GRP_GREENS];
+  t->n_local = h->cnt[GRP_LOCAL];
+  t->kernel_launches = h->launches;
+  return DQMC_OK;
+}
+
+int dqmc_reset_timing(dqmc_handle* h, int32_t enable) {
+  if (!h) return DQMC_ERR_ARG;
+  CHK(sync(h));
+  for (int i = 0; i < 4; ++i) { h->ms[i] = 0; h->cnt[i] = 0; }
+  h->launches = 0;
+  h->timing = enable != 0;
+  return DQMC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,556 @@
+// Dense complex FP64 linear algebra for the UDT stabilisation.
+//
+// Reference: src/linalg.jl:20-39 (decompose_udt! = LAPACK zgeqp3 + zungqr),
+// src/stack.jl:338-369 (calculate_greens) and src/stack.jl:278-313
+// (add_slice_sequence_*).  The column-pivoted Householder QR restates the
+// published LAPACK algorithm (zgeqp3/zlaqp2: pivot = first column of maximal
+// partial norm, zlarfg reflector, column-norm downdating with the
+// sqrt(eps) recomputation guard).  Columns are never moved: a logical ->
+// physical order array replaces LAPACK's column swaps, so the triangular
+// factor comes out directly in the un-permuted ("T = R[:, invperm(p)]")
+// layout that the UDT decomposition needs.
+#include <cfloat>
+#include "common.cuh"
+#include "kernels.h"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// GEMM: C = alpha * diag(rs) * op(A) * op(B) * diag(cs) + beta * C
+// ---------------------------------------------------------------------------
+constexpr int GB_M = 64, GB_N = 64, GB_K = 8;
+
+__device__ __forceinline__ cplx load_op(const cplx* X, int ld, int r, int c, int rows, int cols, char op) {
+  // element (r, c) of op(X); op(X) has shape rows x cols
+  if (r >= rows || c >= cols) return cmake(0.0, 0.0);
+  if (op == 'N') return X[(size_t)c * ld + r];
+  cplx v = X[(size_t)r * ld + c];
+  return op == 'C' ? cconj(v) : v;
+}
+
+__global__ void __launch_bounds__(256) k_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha,
+                                              const cplx* __restrict__ A, int lda, const cplx* __restrict__ B,
+                                              int ldb, cplx beta, cplx* __restrict__ C, int ldc,
+                                              const double* __restrict__ rs, const double* __restrict__ cs) {
+  __shared__ cplx sA[GB_K][GB_M + 1];
+  __shared__ cplx sB[GB_K][GB_N + 1];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int i0 = blockIdx.y * GB_M, j0 = blockIdx.x * GB_N;
+  cplx acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = cmake(0.0, 0.0);
+  for (int k0 = 0; k0 < k; k0 += GB_K) {
+    for (int e = threadIdx.x; e < GB_M * GB_K; e += 256) {
+      int kk, ii;
+      if (opA == 'N') { ii = e % GB_M; kk = e / GB_M; } else { kk = e % GB_K; ii = e / GB_K; }
+      sA[kk][ii] = load_op(A, lda, i0 + ii, k0 + kk, m, k, opA);
+      int jj, kb;
+      if (opB == 'N') { kb = e % GB_K; jj = e / GB_K; } else { jj = e % GB_N; kb = e / GB_N; }
+      sB[kb][jj] = load_op(B, ldb, k0 + kb, j0 + jj, k, nn, opB);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GB_K; ++kk) {
+      cplx av[4], bv[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) av[a] = sA[kk][ty + 16 * a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) bv[b] = sB[kk][tx + 16 * b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = cfma(av[a], bv[b], acc[a][b]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    int i = i0 + ty + 16 * a;
+    if (i >= m) continue;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      int j = j0 + tx + 16 * b;
+      if (j >= nn) continue;
+      cplx v = acc[a][b];
+      if (rs) v = cscale(v, rs[i]);
+      if (cs) v = cscale(v, cs[j]);
+      v = cmul(alpha, v);
+      cplx* cp = &C[(size_t)j * ldc + i];
+      if (beta.x != 0.0 || beta.y != 0.0) v = cfma(beta, *cp, v);
+      *cp = v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// warp / block reductions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ cplx warp_sum(cplx v) { return cmake(warp_sum(v.x), warp_sum(v.y)); }
+
+// block-wide sum, deterministic (fixed tree); all threads get the result.
+__device__ double block_sum(double v, double* scratch) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) scratch[wid] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int q = 0; q < nw; ++q) t += scratch[q];
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// column-pivoted QR (cooperative, one grid barrier per column step)
+// ---------------------------------------------------------------------------
+constexpr int QR_THREADS = 256;
+constexpr int QR_MAXT = 32;   // elements per lane of one column (n <= 1024)
+
+__global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n, QRWork w) {
+  extern __shared__ double smem_qr[];
+  cplx* v = reinterpret_cast<cplx*>(smem_qr);         // (n) current reflector
+  int* order = reinterpret_cast<int*>(v + n);         // (n) logical -> physical
+  __shared__ double red[32];
+  __shared__ int redi[32];
+  __shared__ double s_tau_re, s_tau_im;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int warps = QR_THREADS / 32;
+  const int gwarp = blockIdx.x * warps + wid, nwarps = gridDim.x * warps;
+  const double tol3z = sqrt(DBL_EPSILON);
+
+  for (int q = threadIdx.x; q < n; q += blockDim.x) order[q] = q;
+  // initial column norms (zgeqp3: vn1 = vn2 = ||A(:, j)||)
+  for (int j = gwarp; j < n; j += nwarps) {
+    double s = 0.0;
+    for (int r = lane; r < n; r += 32) s += cabs2(A[(size_t)j * n + r]);
+    s = warp_sum(s);
+    if (lane == 0) { w.vn1[j] = sqrt(s); w.vn2[j] = sqrt(s); }
+  }
+  if (!grid_barrier(w.bar, w.err)) return;
+
+  for (int k = 0; k < n; ++k) {
+    // ---- pivot: first logical position of maximal partial norm ----
+    double best = -1.0;
+    int bestq = n;
+    for (int q = k + threadIdx.x; q < n; q += blockDim.x) {
+      double val = __ldcg(&w.vn1[order[q]]);
+      if (val > best) { best = val; bestq = q; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      int oq = __shfl_xor_sync(0xffffffffu, bestq, o);
+      if (ob > best || (ob == best && oq < bestq)) { best = ob; bestq = oq; }
+    }
+    if (lane == 0) { red[wid] = best; redi[wid] = bestq; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double b = red[0]; int bq = redi[0];
+      for (int q = 1; q < warps; ++q)
+        if (red[q] > b || (red[q] == b && redi[q] < bq)) { b = red[q]; bq = redi[q]; }
+      int t = order[k]; order[k] = order[bq]; order[bq] = t;
+    }
+    __syncthreads();
+    const int p = order[k];
+    // ---- reflector from A[k:n, p] (zlarfg) ----
+    double xn2 = 0.0;
+    for (int r = k + threadIdx.x; r < n; r += blockDim.x) {
+      cplx x = ldcg_c(&A[(size_t)p * n + r]);
+      v[r] = x;
+      if (r > k) xn2 += cabs2(x);
+    }
+    xn2 = block_sum(xn2, red);   // includes __syncthreads
+    const cplx alpha = v[k];
+    const double xnorm = sqrt(xn2);
+    double beta;
+    cplx tau;
+    if (xnorm == 0.0 && alpha.y == 0.0) {
+      tau = cmake(0.0, 0.0);
+      beta = alpha.x;
+    } else {
+      double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2);
+      beta = alpha.x >= 0.0 ? -nrm : nrm;
+      tau = cmake((beta - alpha.x) / beta, -alpha.y / beta);
+      cplx scal = cdiv(cmake(1.0, 0.0), csub(alpha, cmake(beta, 0.0)));
+      for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) v[r] = cmul(v[r], scal);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) v[k] = cmake(1.0, 0.0);
+    __syncthreads();
+    if (blockIdx.x == 0) {
+      if (threadIdx.x == 0) { w.tau[k] = tau; w.beta[k] = beta; }
+      for (int r = threadIdx.x; r < n; r += blockDim.x) w.V[(size_t)k * n + r] = r < k ? cmake(0.0, 0.0) : v[r];
+    }
+    // ---- apply H_k^H to the remaining columns, downdate their norms ----
+    const cplx ctau = cconj(tau);
+    for (int q = k + 1 + gwarp; q < n; q += nwarps) {
+      const int j = order[q];
+      cplx* col = A + (size_t)j * n;
+      cplx x[QR_MAXT];
+      cplx s = cmake(0.0, 0.0);
+#pragma unroll
+      for (int t = 0; t < QR_MAXT; ++t) {
+        int r = k + lane + 32 * t;
+        if (r < n) { x[t] = ldcg_c(&col[r]); s = cfma_conj(v[r], x[t], s); }
+      }
+      s = warp_sum(s);
+      cplx f = cmul(ctau, s);
+      double tail = 0.0;
+      cplx xk = cmake(0.0, 0.0);
+#pragma unroll
+      for (int t = 0; t < QR_MAXT; ++t) {
+        int r = k + lane + 32 * t;
+        if (r < n) {
+          x[t] = csub(x[t], cmul(f, v[r]));
+          col[r] = x[t];
+          if (r == k) xk = x[t];
+          else tail += cabs2(x[t]);
+        }
+      }
+      xk = cmake(__shfl_sync(0xffffffffu, xk.x, 0), __shfl_sync(0xffffffffu, xk.y, 0));
+      tail = warp_sum(tail);
+      if (lane == 0) {
+        double vn1 = __ldcg(&w.vn1[j]);
+        if (vn1 != 0.0) {
+          double vn2 = __ldcg(&w.vn2[j]);
+          double ratio = sqrt(cabs2(xk)) / vn1;
+          double temp = 1.0 - ratio * ratio;
+          temp = temp > 0.0 ? temp : 0.0;
+          double r2 = vn1 / vn2;
+          double temp2 = temp * r2 * r2;
+          if (temp2 <= tol3z) {
+            double nv = (k < n - 1) ? sqrt(tail) : 0.0;
+            w.vn1[j] = nv;
+            w.vn2[j] = nv;
+          } else {
+            w.vn1[j] = vn1 * sqrt(temp);
+          }
+        }
+      }
+    }
+    if (!grid_barrier(w.bar, w.err)) return;
+  }
+  if (blockIdx.x == 0)
+    for (int q = threadIdx.x; q < n; q += blockDim.x) w.order[q] = order[q];
+}
+
+// T (physical layout) = D^-1 R, zero below the logical diagonal; D = |beta|.
+__global__ void k_qrp_finalize(const cplx* __restrict__ A, cplx* __restrict__ T, double* __restrict__ D, int n,
+                               const int* __restrict__ order, const double* __restrict__ beta) {
+  extern __shared__ int pos[];   // physical -> logical
+  for (int q = threadIdx.x; q < n; q += blockDim.x) pos[order[q]] = q;
+  __syncthreads();
+  const size_t total = (size_t)n * n;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    int j = (int)(e / n), r = (int)(e - (size_t)j * n);
+    int q = pos[j];
+    double d = fabs(beta[r]);
+    cplx val;
+    if (r < q) val = cscale(A[e], 1.0 / d);
+    else if (r == q) val = cmake(beta[r] / d, 0.0);
+    else val = cmake(0.0, 0.0);
+    T[e] = val;
+  }
+  if (blockIdx.x == 0)
+    for (int q = threadIdx.x; q < n; q += blockDim.x) D[q] = fabs(beta[q]);
+}
+
+// X (m x n) <- X * Q (or X * Q^H), one warp per row, row held in registers.
+__global__ void __launch_bounds__(256) k_apply_q_right(cplx* __restrict__ X, int m, int n,
+                                                      const cplx* __restrict__ V, const cplx* __restrict__ tau,
+                                                      int conj_q) {
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (row >= m) return;
+  cplx x[QR_MAXT];
+#pragma unroll
+  for (int t = 0; t < QR_MAXT; ++t) {
+    int c = lane + 32 * t;
+    x[t] = c < n ? X[(size_t)c * m + row] : cmake(0.0, 0.0);
+  }
+  for (int s = 0; s < n; ++s) {
+    const int k = conj_q ? (n - 1 - s) : s;
+    const cplx* vk = V + (size_t)k * n;
+    cplx tk = tau[k];
+    if (tk.x == 0.0 && tk.y == 0.0) continue;
+    if (conj_q) tk = cconj(tk);
+    // X H = X - tau (X v) v^H
+    cplx d = cmake(0.0, 0.0);
+#pragma unroll
+    for (int t = 0; t < QR_MAXT; ++t) {
+      int c = lane + 32 * t;
+      if (c >= k && c < n) d = cfma(x[t], __ldg(&vk[c]), d);
+    }
+    d = warp_sum(d);
+    cplx f = cmul(tk, d);
+#pragma unroll
+    for (int t = 0; t < QR_MAXT; ++t) {
+      int c = lane + 32 * t;
+      if (c >= k && c < n) {
+        cplx vc = __ldg(&vk[c]);
+        // x_c -= f * conj(v_c)
+        x[t] = cmake(x[t].x - (f.x * vc.x + f.y * vc.y), x[t].y - (f.y * vc.x - f.x * vc.y));
+      }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < QR_MAXT; ++t) {
+    int c = lane + 32 * t;
+    if (c < n) X[(size_t)c * m + row] = x[t];
+  }
+}
+
+// Y <- That^-1 Y, That[r, q] = T[r, order[q]] upper triangular (logical order).
+// One warp per column of Y (column staged in shared memory).
+__global__ void __launch_bounds__(128) k_trsm_left_upper(const cplx* __restrict__ T, const int* __restrict__ order,
+                                                        cplx* __restrict__ Y, int n, int m) {
+  extern __shared__ double smem_t[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int col = blockIdx.x * (blockDim.x / 32) + wid;
+  if (col >= m) return;
+  cplx* y = reinterpret_cast<cplx*>(smem_t) + (size_t)wid * n;
+  cplx* yg = Y + (size_t)col * n;
+  for (int r = lane; r < n; r += 32) y[r] = yg[r];
+  __syncwarp();
+  for (int q = n - 1; q >= 0; --q) {
+    const cplx* tq = T + (size_t)__ldg(&order[q]) * n;
+    cplx yq = cdiv(y[q], __ldg(&tq[q]));
+    __syncwarp();
+    if (lane == 0) y[q] = yq;
+    for (int r = lane; r < q; r += 32) y[r] = csub(y[r], cmul(yq, __ldg(&tq[r])));
+    __syncwarp();
+  }
+  for (int r = lane; r < n; r += 32) yg[r] = y[r];
+}
+
+// Y <- Y That^-1 (Y is m x n), one warp per row: z That = y, forward over columns.
+__global__ void __launch_bounds__(128) k_trsm_right_upper(const cplx* __restrict__ T, const int* __restrict__ order,
+                                                         cplx* __restrict__ Y, int m, int n) {
+  extern __shared__ double smem_t[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int row = blockIdx.x * (blockDim.x / 32) + wid;
+  if (row >= m) return;
+  cplx* z = reinterpret_cast<cplx*>(smem_t) + (size_t)wid * n;
+  for (int c = lane; c < n; c += 32) z[c] = Y[(size_t)c * m + row];
+  __syncwarp();
+  for (int q = 0; q < n; ++q) {
+    const cplx* tq = T + (size_t)__ldg(&order[q]) * n;
+    cplx s = cmake(0.0, 0.0);
+    for (int r = lane; r < q; r += 32) s = cfma(z[r], __ldg(&tq[r]), s);
+    s = warp_sum(s);
+    if (lane == 0) z[q] = cdiv(csub(z[q], s), __ldg(&tq[q]));
+    __syncwarp();
+  }
+  for (int c = lane; c < n; c += 32) Y[(size_t)c * m + row] = z[c];
+}
+
+__global__ void k_permute(const cplx* __restrict__ src, cplx* __restrict__ dst, int rows, int cols,
+                          const int* __restrict__ order, int by_rows, int scatter) {
+  const size_t total = (size_t)rows * cols;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    int c = (int)(e / rows), r = (int)(e - (size_t)c * rows);
+    if (by_rows) {
+      if (scatter) dst[(size_t)c * rows + order[r]] = src[e];
+      else dst[e] = src[(size_t)c * rows + order[r]];
+    } else {
+      if (scatter) dst[(size_t)order[c] * rows + r] = src[e];
+      else dst[e] = src[(size_t)order[c] * rows + r];
+    }
+  }
+}
+
+__global__ void k_add_diag(cplx* A, int n, const double* d) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) A[(size_t)i * n + i].x += d[i];
+}
+
+__global__ void k_set_identity(cplx* A, int n) {
+  const size_t total = (size_t)n * n;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    int c = (int)(e / n), r = (int)(e - (size_t)c * n);
+    A[e] = cmake(r == c ? 1.0 : 0.0, 0.0);
+  }
+}
+
+__global__ void k_scale(cplx* A, int rows, int cols, const double* rs, int inv_r, const double* cs, int inv_c) {
+  const size_t total = (size_t)rows * cols;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    int c = (int)(e / rows), r = (int)(e - (size_t)c * rows);
+    double f = 1.0;
+    if (rs) f = inv_r ? f / rs[r] : f * rs[r];
+    if (cs) f = inv_c ? f / cs[c] : f * cs[c];
+    A[e] = cscale(A[e], f);
+  }
+}
+
+__global__ void k_conj_transpose(const cplx* __restrict__ A, cplx* __restrict__ B, int n) {
+  __shared__ cplx tile[32][33];
+  int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+    int c = bx + yy, r = by + threadIdx.x;
+    if (c < n && r < n) tile[yy][threadIdx.x] = A[(size_t)c * n + r];
+  }
+  __syncthreads();
+  for (int yy = threadIdx.y; yy < 32; yy += blockDim.y) {
+    int c = by + yy, r = bx + threadIdx.x;   // B[r, c] = conj(A[c, r])
+    if (c < n && r < n) B[(size_t)c * n + r] = cconj(tile[threadIdx.x][yy]);
+  }
+}
+
+// out[0] = sum log(x)  (single CTA, deterministic)
+__global__ void k_sum_log(const double* x, int n, double* out) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += log(x[i]);
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) out[0] = s;
+}
+
+__global__ void k_max_absdiff(const cplx* A, const cplx* B, size_t count, double* out) {
+  __shared__ double red[32];
+  double m = 0.0;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x) {
+    cplx d = csub(A[e], B[e]);
+    double a = sqrt(cabs2(d));
+    if (!(a <= m)) m = a;   // propagates NaN
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double q = __shfl_xor_sync(0xffffffffu, m, o);
+    if (!(q <= m)) m = q;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q)
+      if (!(red[q] <= t)) t = red[q];
+    // combine across CTAs: non-negative doubles order like their bit patterns
+    unsigned long long bits = __double_as_longlong(t);
+    if (t != t) bits = 0x7ff8000000000000ull;
+    atomicMax(reinterpret_cast<unsigned long long*>(out), bits);
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static inline int grid_for(size_t total, int threads = 256, int cap = 4096) {
+  size_t g = (total + threads - 1) / threads;
+  if (g < 1) g = 1;
+  if (g > (size_t)cap) g = cap;
+  return (int)g;
+}
+
+cudaError_t launch_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
+                         const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
+                         const double* colscale, cudaStream_t st) {
+  dim3 grid((nn + GB_N - 1) / GB_N, (m + GB_M - 1) / GB_M);
+  k_zgemm<<<grid, 256, 0, st>>>(m, nn, k, opA, opB, alpha, A, lda, B, ldb, beta, C, ldc, rowscale, colscale);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_qrp(cplx* A, int n, QRWork& w, int sm_count, cudaStream_t st) {
+  if (n > 32 * QR_MAXT) return cudaErrorInvalidValue;
+  size_t smem = (size_t)n * (sizeof(cplx) + sizeof(int));
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_qrp, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+    attr = true;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_qrp, QR_THREADS, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int grid = sm_count;   // one CTA per SM: 8 warps each, one column per warp per step
+  int need = (n + 7) / 8;
+  if (grid > need) grid = need < 1 ? 1 : need;
+  QRWork copy = w;
+  void* args[] = {&A, &n, &copy};
+  return cudaLaunchCooperativeKernel((void*)k_qrp, dim3(grid), dim3(QR_THREADS), args, smem, st);
+}
+
+cudaError_t launch_qrp_finalize(cplx* A, cplx* T, double* D, int n, const QRWork& w, cudaStream_t st) {
+  k_qrp_finalize<<<grid_for((size_t)n * n), 256, n * sizeof(int), st>>>(A, T, D, n, w.order, w.beta);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_apply_q_right(cplx* X, int m, int n, const QRWork& w, bool conj_transpose_q, cudaStream_t st) {
+  if (n > 32 * QR_MAXT) return cudaErrorInvalidValue;
+  int rows_per_cta = 8;
+  k_apply_q_right<<<(m + rows_per_cta - 1) / rows_per_cta, 256, 0, st>>>(X, m, n, w.V, w.tau,
+                                                                        conj_transpose_q ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trsm_left_upper(const cplx* T, const int* order, cplx* Y, int n, int m, cudaStream_t st) {
+  size_t smem = (size_t)4 * n * sizeof(cplx);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_trsm_left_upper, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  k_trsm_left_upper<<<(m + 3) / 4, 128, smem, st>>>(T, order, Y, n, m);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trsm_right_upper(const cplx* T, const int* order, cplx* Y, int m, int n, cudaStream_t st) {
+  size_t smem = (size_t)4 * n * sizeof(cplx);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_trsm_right_upper, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  k_trsm_right_upper<<<(m + 3) / 4, 128, smem, st>>>(T, order, Y, m, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_permute(const cplx* src, cplx* dst, int rows, int cols, const int* order, bool by_rows,
+                           bool scatter, cudaStream_t st) {
+  k_permute<<<grid_for((size_t)rows * cols), 256, 0, st>>>(src, dst, rows, cols, order, by_rows, scatter);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_add_diag(cplx* A, int n, const double* d, cudaStream_t st) {
+  k_add_diag<<<(n + 255) / 256, 256, 0, st>>>(A, n, d);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_identity(cplx* A, int n, cudaStream_t st) {
+  k_set_identity<<<grid_for((size_t)n * n), 256, 0, st>>>(A, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scale(cplx* A, int rows, int cols, const double* rowscale, bool invert_rows,
+                         const double* colscale, bool invert_cols, cudaStream_t st) {
+  k_scale<<<grid_for((size_t)rows * cols), 256, 0, st>>>(A, rows, cols, rowscale, invert_rows, colscale,
+                                                         invert_cols);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_conj_transpose(const cplx* A, cplx* B, int n, cudaStream_t st) {
+  dim3 grid((n + 31) / 32, (n + 31) / 32);
+  k_conj_transpose<<<grid, dim3(32, 8), 0, st>>>(A, B, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sum_log(const double* x, int n, double* out, cudaStream_t st) {
+  k_sum_log<<<1, 256, 0, st>>>(x, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_max_absdiff(const cplx* A, const cplx* B, size_t count, double* out, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), st);
+  if (e != cudaSuccess) return e;
+  k_max_absdiff<<<grid_for(count, 256, 1024), 256, 0, st>>>(A, B, count, out);
+  return cudaGetLastError();
+}

@@ -1,0 +1,98 @@
+// Host-side launch interface of the device kernels (internal to the library).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "common.cuh"
+
+enum SliceMode : int {
+  SLICE_LEFT_B = 0,      // M <- B_l M        (multiply_B_left!)
+  SLICE_RIGHT_B = 1,     // M <- M B_l        (multiply_B_right!)
+  SLICE_LEFT_BINV = 2,   // M <- B_l^-1 M     (multiply_B_inv_left!)
+  SLICE_RIGHT_BINV = 3,  // M <- M B_l^-1     (multiply_B_inv_right!)
+  SLICE_LEFT_BDAG = 4,   // M <- B_l^dag M    (multiply_daggered_B_left!)
+  SLICE_EFF_RIGHT = 5,   // M <- M Hb_half Ha_half           (effective_greens2greens!, right part)
+  SLICE_EFF_LEFT_INV = 6 // M <- Ha_half^-1 Hb_half^-1 M     (effective_greens2greens!, left part)
+};
+
+// ---- slice matrices (k_slice.cu) ----
+size_t evtab_entry_bytes();
+cudaError_t launch_build_evtab(const double* phi, void* evtab, int N, int M, double lambda_dtau, cudaStream_t st);
+// Applies `count` slices (0-based first, stepping by `step`) to the columns
+// of A (left modes), then scales column c by colscale[c] when colscale != 0.
+cudaError_t launch_apply_cols(cplx* A, int n, const ModelConst& mc, const void* evtab, int first_slice0,
+                              int count, int step, int mode, const double* colscale, cudaStream_t st);
+// Applies `count` slices to the rows of A (right modes).
+cudaError_t launch_apply_rows(cplx* A, int n, const ModelConst& mc, const void* evtab, int first_slice0,
+                              int count, int step, int mode, cudaStream_t st);
+
+// ---- local updates (k_local.cu) ----
+struct LocalUpdateArgs {
+  cplx* G;
+  double* phi;             // (3, N, M)
+  void* evtab;             // (N, M) interaction entries, kept in sync with phi
+  int slice0;              // 0-based slice
+  const double* delta;     // (3, N) proposal shifts of this call
+  const double* unif;      // (N) Metropolis uniforms of this call
+  uint8_t* acc_out;        // (N) or null
+  cplx* det_out;           // (N) or null
+  double* pacc_out;        // (N) or null
+  double* action;          // running boson action (device scalar)
+  int* n_acc;              // running accepted count (device scalar)
+  cplx* Acol;              // scratch (n, 4)
+  cplx* Brow;              // scratch (4, n)
+  GridBarrier* bar;
+  int* err;
+  ModelConst mc;
+};
+cudaError_t launch_local_updates(const LocalUpdateArgs& a, int sm_count, cudaStream_t st);
+
+// ---- dense linear algebra (k_linalg.cu) ----
+// C = alpha * op(A) * op(B) + beta * C, all n x n column-major; op: 'N', 'C' (conjugate transpose)
+// optional diagonal scalings: rowscale (applied to rows of op(A)), colscale (to columns of op(B)).
+cudaError_t launch_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
+                         const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
+                         const double* colscale, cudaStream_t st);
+
+struct QRWork {
+  double* vn1;       // (n)
+  double* vn2;       // (n)
+  int* order;        // (n) logical position -> physical column
+  cplx* tau;         // (n)
+  double* beta;      // (n) real diagonal of R in logical order
+  cplx* V;           // (n, n) Householder vectors, column k = v_k (v_k[k] = 1, zero above)
+  GridBarrier* bar;
+  int* err;
+};
+// Column-pivoted Householder QR of A (n x n) in place (LAPACK geqp3 semantics
+// without physical column swaps).  On return the upper part of A (rows <=
+// logical position of each physical column) holds R in physical column
+// order; V/tau hold the reflectors; order/beta the pivots and diag(R).
+cudaError_t launch_qrp(cplx* A, int n, QRWork& w, int sm_count, cudaStream_t st);
+// After launch_qrp: D[k] = |beta[k]|, T (physical layout) = D^-1 R with zeros below.
+cudaError_t launch_qrp_finalize(cplx* A, cplx* T, double* D, int n, const QRWork& w, cudaStream_t st);
+// X (m x n) <- X * Q  with Q = H_0 ... H_{n-1} (reflectors in w).  Also used
+// with X = I to form Q explicitly.  conj_transpose_q: X <- X * Q^H.
+cudaError_t launch_apply_q_right(cplx* X, int m, int n, const QRWork& w, bool conj_transpose_q, cudaStream_t st);
+// Upper-triangular solves with the logical-order factor Rhat of a QR (unit
+// scaled: That = D^-1 R), using the physical-layout T from launch_qrp_finalize:
+//   left:  Y <- That^-1 Y       (Y is n x m)
+//   right: Y <- Y That^-1       (Y is m x n)
+// Row/column permutation by the pivot order is applied by the caller with
+// launch_permute.
+cudaError_t launch_trsm_left_upper(const cplx* T, const int* order, cplx* Y, int n, int m, cudaStream_t st);
+cudaError_t launch_trsm_right_upper(const cplx* T, const int* order, cplx* Y, int m, int n, cudaStream_t st);
+// dst = src with rows (by_rows) or columns permuted: dst[order[k]] = src[k] (scatter) when scatter, else gather.
+cudaError_t launch_permute(const cplx* src, cplx* dst, int rows, int cols, const int* order, bool by_rows,
+                           bool scatter, cudaStream_t st);
+// A += diag(d) (d real)
+cudaError_t launch_add_diag(cplx* A, int n, const double* d, cudaStream_t st);
+// A <- I
+cudaError_t launch_set_identity(cplx* A, int n, cudaStream_t st);
+// out[0] = sum_k log(x[k]) computed as one deterministic reduction, out[1] = sum_k log(|x[k]|) with sign flags ...
+cudaError_t launch_sum_log(const double* x, int n, double* out, cudaStream_t st);
+// max |A - B| over n*n entries -> out
+cudaError_t launch_max_absdiff(const cplx* A, const cplx* B, size_t count, double* out, cudaStream_t st);
+// A (rows x cols) scaled: A[r,c] *= rowscale[r] (if non-null) * colscale[c] (if non-null); rowscale may be inverted
+cudaError_t launch_scale(cplx* A, int rows, int cols, const double* rowscale, bool invert_rows,
+                         const double* colscale, bool invert_cols, cudaStream_t st);
+cudaError_t launch_conj_transpose(const cplx* A, cplx* B, int n, cudaStream_t st);

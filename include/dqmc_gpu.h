@@ -1,0 +1,176 @@
+/*
+ * dqmc_gpu.h -- C ABI of the GB300 (sm_103a) DQMC sweep library.
+ *
+ * This is the drop-in boundary for the hot path of carstenbauer/dqmc (the
+ * O(3) spin-fermion model, Assaad checkerboard, no B-field): a Julia host
+ * binds these symbols with `ccall`, a Python host with ctypes.  Every entry
+ * point is `extern "C"`, takes plain pointers and sizes, returns an int
+ * status (0 = ok, < 0 = error; see DQMC_ERR_*) and never throws.  The
+ * message of the last error of a handle is returned by dqmc_last_error().
+ *
+ * Conventions shared with the reference:
+ *   - G is n x n complex128, column-major (Julia Matrix{ComplexF64}),
+ *     n = 4 N, N = L^2, index = flavour * N + site, site = y + L * x;
+ *   - the boson field phi is double[3 * N * M], column-major (3, N, M)
+ *     (src/parameters.jl:19);
+ *   - slice numbers at this boundary are 1-based, as in the reference;
+ *   - complex arrays are passed as double* with interleaved (re, im).
+ *
+ * A handle owns all device memory and one CUDA stream; it is not
+ * thread-safe (one host thread drives it), distinct handles are independent.
+ */
+#ifndef DQMC_GPU_H
+#define DQMC_GPU_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define DQMC_API __attribute__((visibility("default")))
+#else
+#define DQMC_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DQMC_OK 0
+#define DQMC_ERR_ARG (-1)        /* invalid argument / unsupported configuration */
+#define DQMC_ERR_CUDA (-2)       /* CUDA runtime error (message has the details) */
+#define DQMC_ERR_NONFINITE (-3)  /* NaN/Inf met in G or a determinant ratio */
+#define DQMC_ERR_SINGULAR (-4)   /* singular 4x4 M in a local update */
+#define DQMC_ERR_TIMEOUT (-5)    /* a device-side wait gave up (bounded spin) */
+#define DQMC_ERR_STATE (-6)      /* call not valid in the current state */
+
+#define DQMC_PREC_FP64 0         /* plain FP64 everywhere */
+
+/* Parameters of the O(3) model; the subset of `Params` (src/parameters.jl:4-80)
+ * that the sweep needs.  hoppings[] is the HOPPINGS string
+ * "tx_x,ty_x,tx_y,ty_y" (src/lattice.jl:59). */
+typedef struct dqmc_params {
+  int32_t L;           /* linear lattice size (even, >= 2) */
+  int32_t slices;      /* M = beta / delta_tau */
+  int32_t safe_mult;   /* stabilisation interval; must divide slices */
+  int32_t opdim;       /* must be 3 (O(3) model, 4 flavours) */
+  double delta_tau;
+  double lambda;       /* Yukawa coupling */
+  double r, c, u;      /* boson action couplings */
+  double mu1, mu2;     /* chemical potentials of band x and band y */
+  double hoppings[4];  /* tx_x, ty_x, tx_y, ty_y */
+  int32_t all_checks;  /* compare wrapped and fresh G at each stabilisation (src/stack.jl:416-429) */
+  int32_t precision;   /* DQMC_PREC_FP64 */
+  int32_t reserved[6];
+} dqmc_params;
+
+typedef struct dqmc_stats {
+  int64_t proposals;        /* site proposals made */
+  int64_t accepted;         /* accepted proposals */
+  double acc_rate;          /* accepted / proposals */
+  double max_instability;   /* max |G_wrapped - G_fresh| seen at stabilisations */
+  double device_ms;         /* device time of the call (CUDA events on the handle's stream) */
+} dqmc_stats;
+
+typedef struct dqmc_timing {
+  double ms_wrap;           /* slice application kernels of wrap_greens */
+  double ms_stack;          /* add_slice_sequence_* (B chain + QR + products) */
+  double ms_greens;         /* calculate_greens */
+  double ms_local;          /* local update kernels */
+  int64_t n_wrap, n_stack, n_greens, n_local;
+  int64_t kernel_launches;  /* kernels launched by the library since the last reset */
+} dqmc_timing;
+
+typedef struct dqmc_handle dqmc_handle;
+
+/* ---- lifetime ------------------------------------------------------------ */
+/* DQMC(p) (src/dqmc_framework.jl:105-135) + load_lattice / checkerboard setup
+ * (src/hoppings_checkerboard.jl:65-136).  Allocates the device state. */
+DQMC_API int dqmc_create(const dqmc_params* p, dqmc_handle** out);
+DQMC_API int dqmc_destroy(dqmc_handle* h);
+DQMC_API const char* dqmc_last_error(const dqmc_handle* h);
+/* Library version string. */
+DQMC_API const char* dqmc_version(void);
+
+/* ---- field and state ------------------------------------------------------- */
+/* p.hsfield = phi (init!(mc, start_conf), src/dqmc_framework.jl:156-163). */
+DQMC_API int dqmc_set_field(dqmc_handle* h, const double* phi);
+DQMC_API int dqmc_get_field(dqmc_handle* h, double* phi);
+/* init! (src/dqmc_framework.jl:156-177): boson action, initialize_stack,
+ * build_stack, first propagate.  Leaves the state at (slice M, direction -1). */
+DQMC_API int dqmc_init(dqmc_handle* h);
+/* propagate (src/stack.jl:391-499). */
+DQMC_API int dqmc_propagate(dqmc_handle* h);
+/* Current slice / direction (s.current_slice, s.direction). */
+DQMC_API int dqmc_get_state(dqmc_handle* h, int32_t* slice, int32_t* direction);
+
+/* ---- local updates ------------------------------------------------------- */
+/* local_updates (src/local_updates.jl:1-38) at the current slice with
+ * fixed-slot streams: delta[3*N] (proposal shifts phi' = phi + delta, already
+ * in [-box, box]) and unif[N] (Metropolis uniforms, used only when p <= 1).
+ * Optional outputs (may be NULL): accepted[N], detratio[2*N] (complex),
+ * p_acc[N], acc_rate[1]. */
+DQMC_API int dqmc_local_updates(dqmc_handle* h, const double* delta, const double* unif, uint8_t* accepted,
+                       double* detratio, double* p_acc, double* acc_rate);
+/* update (src/dqmc_framework.jl:500-517, global updates off): propagate, then
+ * local_updates. */
+DQMC_API int dqmc_update(dqmc_handle* h, const double* delta, const double* unif, uint8_t* accepted,
+                double* detratio, double* p_acc, double* acc_rate);
+/* n_calls consecutive update() calls (one sweep = M calls; the reference's
+ * ud-sweep loop `for u in 1:2*p.slices update(mc, i) end`,
+ * src/dqmc_framework.jl:259-261).  delta_stream[n_calls*3*N],
+ * unif_stream[n_calls*N]; accepted[n_calls*N] may be NULL. */
+DQMC_API int dqmc_sweep(dqmc_handle* h, int32_t n_calls, const double* delta_stream, const double* unif_stream,
+               uint8_t* accepted, dqmc_stats* stats);
+/* Same as dqmc_sweep but reads the streams from device memory (no host
+ * copies); device pointers as returned by the caller's allocator. */
+DQMC_API int dqmc_sweep_device(dqmc_handle* h, int32_t n_calls, const double* delta_stream_dev,
+                      const double* unif_stream_dev, uint8_t* accepted_dev, dqmc_stats* stats);
+
+/* ---- Green's functions ------------------------------------------------------ */
+/* s.greens (effective G at the current slice). out: double[2*n*n]. */
+DQMC_API int dqmc_get_greens(dqmc_handle* h, double* out, int32_t* slice, int32_t* direction);
+/* Overwrite s.greens (testing and restart). */
+DQMC_API int dqmc_set_greens(dqmc_handle* h, const double* in);
+/* calc_greens_and_logdet (src/fermion_measurements.jl:1061-1101): G of
+ * `slice` computed from scratch with the B chains, plus log|det G|. */
+DQMC_API int dqmc_calc_greens(dqmc_handle* h, int32_t slice, double* out, double* logdet);
+/* wrap_greens (src/stack.jl:316-332) of a host matrix: inout <- B G B^-1
+ * (direction +1) or B^-1 G B (direction -1) at `slice`. */
+DQMC_API int dqmc_wrap_greens(dqmc_handle* h, double* inout, int32_t slice, int32_t direction);
+/* calculate_greens + calculate_logdet (src/stack.jl:338-385) on given UDTs:
+ * G = [1 + Ul Dl Tl (Ur Dr Tr)^dag]^-1.  Matrices n x n complex, D real[n]. */
+DQMC_API int dqmc_calculate_greens_udt(dqmc_handle* h, const double* Ul, const double* Dl, const double* Tl,
+                              const double* Ur, const double* Dr, const double* Tr, double* G,
+                              double* logdet);
+/* decompose_udt! (src/linalg.jl:20-39): A = U diag(D) T with pivoted QR. */
+DQMC_API int dqmc_decompose_udt(dqmc_handle* h, const double* A, double* U, double* D, double* T);
+/* s.log_det after the last fresh G (src/stack.jl:377-385). */
+DQMC_API int dqmc_logdet(dqmc_handle* h, double* logdet);
+
+/* ---- slice matrices ---------------------------------------------------------- */
+#define DQMC_B_LEFT 0        /* multiply_B_left!       (src/slice_matrices.jl:101) */
+#define DQMC_B_RIGHT 1       /* multiply_B_right!      (src/slice_matrices.jl:131) */
+#define DQMC_B_INV_LEFT 2    /* multiply_B_inv_left!   (src/slice_matrices.jl:155) */
+#define DQMC_B_INV_RIGHT 3   /* multiply_B_inv_right!  (src/slice_matrices.jl:179) */
+#define DQMC_B_DAG_LEFT 4    /* multiply_daggered_B_left! (src/slice_matrices.jl:203) */
+DQMC_API int dqmc_multiply_B(dqmc_handle* h, int32_t which, int32_t slice, double* inout);
+
+/* ---- boson action and measurements ---------------------------------------- */
+/* p.boson_action as maintained by the updates (src/local_updates.jl:34). */
+DQMC_API int dqmc_boson_action(dqmc_handle* h, double* S);
+/* calc_boson_action (src/action.jl:1-52) recomputed from the current field. */
+DQMC_API int dqmc_calc_boson_action(dqmc_handle* h, double* S);
+/* Measurement hook _measure_observables! (src/dqmc_framework.jl:371-384):
+ * true G = effective_greens2greens!(wrap_greens(G, slice, +1))
+ * (src/fermion_measurements.jl:1125-1142) written to greens_out (may be NULL);
+ * occupation (src/fermion_measurements.jl:322) and kinetic energy
+ * E_kin = sum_ij T_ij <c_i^dag c_j> (not an observable of the reference). */
+DQMC_API int dqmc_measure(dqmc_handle* h, double* greens_out, double* occupation, double* e_kin);
+
+/* ---- diagnostics ------------------------------------------------------------- */
+DQMC_API int dqmc_get_timing(dqmc_handle* h, dqmc_timing* t);
+DQMC_API int dqmc_reset_timing(dqmc_handle* h, int32_t enable);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DQMC_GPU_H */

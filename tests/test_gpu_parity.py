@@ -1,0 +1,205 @@
+"""Parity of the CUDA library (through the C ABI) with the CPU oracle.
+
+Tolerances: FP64 results must agree with the oracle within 1e-10 relative
+(max-norm, relative to max |G| = O(1)); accept/reject sequences and the final
+field must be identical wherever the acceptance margin |p_acc - u| exceeds
+1e-9 (both codes compute p_acc in FP64 with different summation orders).
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from oracle import dqmc_ref as R
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def relerr(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(1.0, float(np.max(np.abs(b)))))
+
+
+def api_params(p: R.Params, all_checks=True):
+    from dqmc_gb300.api import ModelParams
+    return ModelParams(L=p.L, slices=p.slices, safe_mult=p.safe_mult, delta_tau=p.delta_tau, lambda_=p.lambda_,
+                       r=p.r, c=p.c, u=p.u, mu1=p.mu1, mu2=p.mu2, hoppings=tuple(p.hoppings), box=p.box,
+                       all_checks=all_checks)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from dqmc_gb300 import build
+    build.build()
+    from dqmc_gb300 import api
+    return api
+
+
+# config 0 of the workload list: L=4, beta=4 (M=40), lambda=1, r=c=u=1, box 0.2
+C0 = R.Params(L=4, slices=40, delta_tau=0.1, safe_mult=10, lambda_=1.0, r=1.0, c=1.0, u=1.0, mu1=-0.5, mu2=-0.5,
+              box=0.2)
+
+
+def test_multiply_B_all_modes(lib, golden, small_params):
+    p = small_params
+    ref = R.DQMCRef(p, golden["randconf"])
+    gpu = lib.DQMC(api_params(p), golden["randconf"])
+    rng = np.random.default_rng(1)
+    A = rng.standard_normal((p.n, p.n)) + 1j * rng.standard_normal((p.n, p.n))
+    for sl in (1, 3, 10):
+        for name in ("multiply_B_left", "multiply_B_right", "multiply_B_inv_left", "multiply_B_inv_right",
+                     "multiply_daggered_B_left"):
+            want = getattr(ref, name)(sl, A.copy())
+            got = getattr(gpu, name)(sl, A)
+            assert relerr(got, want) < 1e-13, (sl, name, relerr(got, want))
+
+
+def test_calculate_greens_kat(lib, golden, small_params):
+    # tests_O3.jl:217-227 through the C ABI
+    gpu = lib.DQMC(api_params(small_params), golden["randconf"])
+    G, ld = gpu.calculate_greens_udt(golden["Ul"], golden["Dl"], golden["Tl"], golden["Ur"], golden["Dr"],
+                                     golden["Tr"])
+    assert relerr(G, golden["greens"]) < TOL
+    _, ld_ref = R.greens_from_udts(golden["Ul"], golden["Dl"], golden["Tl"], golden["Ur"], golden["Dr"],
+                                   golden["Tr"])
+    assert abs(ld - ld_ref) < 1e-9 * max(1.0, abs(ld_ref))
+
+
+def test_decompose_udt(lib, small_params):
+    gpu = lib.DQMC(api_params(small_params), R.synthetic_field(16, 10, 0))
+    rng = np.random.default_rng(3)
+    n = small_params.n
+    A = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * np.logspace(0, 12, n)[None, :]
+    U, D, T = gpu.decompose_udt(A)
+    Ur, Dr, Tr = R.decompose_udt(A)
+    assert np.allclose(U.conj().T @ U, np.eye(n), atol=1e-13)
+    assert np.allclose((U * D[None, :]) @ T, A, rtol=0, atol=1e-12 * np.max(np.abs(A)))
+    assert np.allclose(D, Dr, rtol=1e-10)
+    assert np.allclose(np.abs(T), np.abs(Tr), atol=1e-10)
+
+
+@pytest.mark.parametrize("cfg", ["small", "c0"])
+def test_init_and_full_propagation(lib, golden, small_params, cfg):
+    p = small_params if cfg == "small" else C0
+    phi = golden["randconf"] if cfg == "small" else R.synthetic_field(p.N, p.slices, 100)
+    ref = R.DQMCRef(p, phi)
+    ref.init()
+    gpu = lib.DQMC(api_params(p), phi)
+    gpu.init()
+    assert gpu.state == (ref.current_slice, ref.direction)
+    assert relerr(gpu.greens, ref.greens) < TOL
+    assert abs(gpu.log_det - ref.log_det) < 1e-9 * max(1.0, abs(ref.log_det))
+    # one full down + up pass, G compared at every slice (tests_O3.jl:252-263)
+    for _ in range(2 * p.slices):
+        ref.propagate()
+        gpu.propagate()
+        assert gpu.state == (ref.current_slice, ref.direction)
+        assert relerr(gpu.greens, ref.greens) < TOL, gpu.state
+
+
+def test_calc_greens_from_scratch(lib, golden, small_params):
+    p = C0
+    phi = R.synthetic_field(p.N, p.slices, 5)
+    ref = R.DQMCRef(p, phi)
+    gpu = lib.DQMC(api_params(p), phi)
+    gpu.init()
+    for sl in (1, 7, 20, 40):
+        G, ld = gpu.calc_greens_and_logdet(sl)
+        Gr, ldr = ref.calc_greens_and_logdet(sl)
+        assert relerr(G, Gr) < TOL
+        assert abs(ld - ldr) < 1e-9 * max(1.0, abs(ldr))
+
+
+def test_wrap_greens(lib, small_params):
+    p = C0
+    phi = R.synthetic_field(p.N, p.slices, 6)
+    ref = R.DQMCRef(p, phi)
+    gpu = lib.DQMC(api_params(p), phi)
+    gpu.init()
+    g = ref.calc_greens(12)
+    for d in (1, -1):
+        assert relerr(gpu.wrap_greens(g, 12, d), ref.wrap_greens(g, 12, d)) < 1e-13
+
+
+def _compare_updates(ref, gpu, delta, u, margin=1e-9):
+    rate_g, acc_g, det_g, pacc_g = gpu.local_updates(delta, u, return_details=True)
+    rec = []
+    rate_r = ref.local_updates(delta, u, record=rec)
+    acc_r = np.array([r[2] for r in rec])
+    det_r = np.array([r[3] for r in rec])
+    pacc_r = np.array([r[4] for r in rec])
+    safe = np.abs(pacc_r - u) > margin
+    assert np.array_equal(acc_g[safe], acc_r[safe])
+    assert np.allclose(det_g, det_r, rtol=1e-10, atol=0)
+    return rate_g, rate_r
+
+
+def test_local_updates_one_slice(lib, golden, small_params):
+    p = dataclasses.replace(C0)
+    phi = R.synthetic_field(p.N, p.slices, 7)
+    ref = R.DQMCRef(p, phi)
+    ref.init()
+    gpu = lib.DQMC(api_params(p), phi)
+    gpu.init()
+    delta, u = R.synthetic_streams(p.N, 1, p.box, 8)
+    _compare_updates(ref, gpu, delta[0], u[0])
+    assert relerr(gpu.greens, ref.greens) < TOL
+    assert np.array_equal(gpu.get_field(), ref.phi)
+    assert abs(gpu.boson_action - ref.boson_action_value) < 1e-10 * abs(ref.boson_action_value)
+
+
+def test_sweep_config0_accept_sequence(lib):
+    """Config 0: one full sweep (M update calls) on shared streams."""
+    p = C0
+    phi = R.synthetic_field(p.N, p.slices, 2024)
+    delta, u = R.synthetic_streams(p.N, p.slices, p.box, 2025)
+    ref = R.DQMCRef(p, phi)
+    ref.init()
+    rec = []
+    ref.sweep(p.slices, delta, u, record=rec)
+    gpu = lib.DQMC(api_params(p), phi)
+    gpu.init()
+    res = gpu.sweep(p.slices, delta, u, return_accepted=True)
+    acc_r = np.array([r[2] for r in rec]).reshape(p.slices, p.N)
+    margin = np.abs(np.array([r[4] - r[5] for r in rec])).reshape(p.slices, p.N)
+    assert np.array_equal(res["accepted_mask"], acc_r), f"min margin {margin.min():.3e}"
+    assert np.array_equal(gpu.get_field(), ref.phi)
+    assert relerr(gpu.greens, ref.greens) < TOL
+    assert gpu.state == (ref.current_slice, ref.direction)
+    assert res["max_instability"] < 1e-7
+    assert abs(gpu.boson_action - ref.boson_action_value) < 1e-10 * abs(ref.boson_action_value)
+
+
+def test_sweep_config1_shapes(lib):
+    """Config 1 shapes (L=10, M=100): 15 update calls crossing a stabilisation."""
+    p = R.Params(L=10, slices=100, delta_tau=0.1, safe_mult=10, lambda_=1.0, r=1.0, c=1.0, u=1.0, mu1=-0.5,
+                 mu2=-0.5, box=0.2)
+    calls = 15
+    phi = R.synthetic_field(p.N, p.slices, 31)
+    delta, u = R.synthetic_streams(p.N, calls, p.box, 32)
+    ref = R.DQMCRef(p, phi)
+    ref.init()
+    rec = []
+    ref.sweep(calls, delta, u, record=rec)
+    gpu = lib.DQMC(api_params(p), phi)
+    gpu.init()
+    res = gpu.sweep(calls, delta, u, return_accepted=True)
+    acc_r = np.array([r[2] for r in rec]).reshape(calls, p.N)
+    assert np.array_equal(res["accepted_mask"], acc_r)
+    assert np.array_equal(gpu.get_field(), ref.phi)
+    assert relerr(gpu.greens, ref.greens) < TOL
+
+
+def test_measurement_hook(lib):
+    p = C0
+    phi = R.synthetic_field(p.N, p.slices, 77)
+    ref = R.DQMCRef(p, phi)
+    ref.init()
+    gpu = lib.DQMC(api_params(p), phi)
+    gpu.init()
+    m = gpu.measure()
+    Gt = ref.measured_greens()
+    assert relerr(m["greens"], Gt) < TOL
+    assert abs(m["occupation"] - float(np.mean(1 - np.diag(Gt)).real)) < 1e-12
+    assert abs(m["e_kin"] - ref.kinetic_energy(Gt)) < 1e-10 * max(1.0, abs(ref.kinetic_energy(Gt)))

@@ -1,0 +1,102 @@
+"""Structural invariants of the CPU oracle, restated from the reference's
+tests (test/tests_O3.jl:211-263, 283-332; test/tests_linalg.jl:37-60) plus
+the free-fermion limit (test/tests_freefermions.jl:71-98 checks it against
+ED; here against the closed form G = (1 + B_M ... B_1)^-1)."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from oracle import dqmc_ref as R
+
+
+@pytest.fixture(scope="module")
+def mc(golden, small_params):
+    m = R.DQMCRef(small_params, golden["randconf"])
+    m.init()
+    return m
+
+
+def test_udt_properties():
+    rng = np.random.default_rng(1234)
+    x = rng.random((10, 10))
+    u, d, t = R.decompose_udt(x.astype(np.complex128))
+    assert np.allclose(u @ u.conj().T, np.eye(10))
+    assert sorted(int(np.sum(np.abs(t[:, j]) == 0)) for j in range(10)) == list(range(10))
+    assert np.allclose(u @ np.diag(d) @ t, x)
+    assert np.all(np.diff(d) <= 1e-12 * d[0])   # pivoting orders |R_kk|
+
+
+def test_slice_matrix_inverses(mc):
+    n = mc.n
+    rng = np.random.default_rng(7)
+    A = rng.random((n, n)) + 1j * rng.random((n, n))
+    B = mc.slice_matrix(3, 1.0)
+    Binv = mc.slice_matrix(3, -1.0)
+    assert np.allclose(B @ Binv, np.eye(n), atol=1e-12)
+    Ares = B.conj().T @ A
+    assert np.allclose(mc.multiply_daggered_B_left(3, A.copy()), Ares, atol=1e-12)
+    X = A.copy()
+    mc.multiply_B_left(3, X)
+    mc.multiply_B_inv_left(3, X)
+    assert np.allclose(X, A, atol=1e-12)
+    mc.multiply_B_right(3, X)
+    mc.multiply_B_inv_right(3, X)
+    assert np.allclose(X, A, atol=1e-12)
+    assert np.allclose(mc.multiply_B_right(3, np.eye(n, dtype=complex)), B, atol=1e-14)
+    assert np.allclose(mc.multiply_B_inv_right(3, np.eye(n, dtype=complex)), Binv, atol=1e-14)
+
+
+def test_init_greens_matches_fresh(mc):
+    # tests_O3.jl:212-213
+    assert mc.current_slice == mc.M and mc.direction == -1
+    assert np.max(np.abs(mc.greens - mc.calc_greens(mc.current_slice))) < 1e-12
+
+
+def test_wrapping(mc):
+    # tests_O3.jl:232-238
+    g = mc.calc_greens(2)
+    assert np.allclose(mc.wrap_greens(g, 2, 1), mc.calc_greens(3), atol=1e-12)
+    assert np.allclose(mc.wrap_greens(g, 2, -1), mc.calc_greens(1), atol=1e-12)
+
+
+def test_propagation_within_bounds(golden, small_params):
+    # tests_O3.jl:252-263, for two directions and a stabilisation inside the chain
+    p = dataclasses.replace(small_params, slices=20, safe_mult=5)
+    phi = R.synthetic_field(p.N, p.slices, 11)
+    m = R.DQMCRef(p, phi)
+    m.init()
+    m.propagate()
+    steps = 0
+    while not (m.current_slice == m.M and m.direction == -1):
+        assert np.max(np.abs(m.calc_greens(m.current_slice) - m.greens)) < 1e-12
+        m.propagate()
+        steps += 1
+    assert steps == 2 * m.M - 1
+    assert max(d for _, _, d in m.instability) < 1e-10
+
+
+def test_free_fermions_closed_form(small_params):
+    p = dataclasses.replace(small_params, lambda_=0.0, slices=20)
+    m = R.DQMCRef(p, R.synthetic_field(p.N, p.slices, 3))
+    m.init()
+    Bchain = np.eye(m.n, dtype=complex)
+    for sl in range(1, m.M + 1):
+        Bchain = m.slice_matrix(sl) @ Bchain
+    # G(slice M) = [1 + B_{M-1}...B_1 B_M]^-1
+    BM = m.slice_matrix(m.M)
+    G_exact = np.linalg.inv(np.eye(m.n) + np.linalg.inv(BM) @ Bchain @ BM)
+    assert np.allclose(m.greens, G_exact, atol=1e-10)
+
+
+def test_local_update_consistency(mc):
+    """update_greens! yields the fresh G of the updated field (Sherman-Morrison)."""
+    rng = np.random.default_rng(5)
+    N = mc.N
+    m = R.DQMCRef(mc.p, mc.phi.copy())
+    m.init()
+    delta = rng.uniform(-0.2, 0.2, size=(3, N))
+    rate = m.local_updates(delta, rng.uniform(size=N))
+    assert 0 < rate <= 1
+    assert np.max(np.abs(m.greens - m.calc_greens(m.current_slice))) < 1e-10
+    assert np.isclose(m.boson_action_value, R.boson_action(m.p, m.phi), rtol=1e-12)
