@@ -1,0 +1,360 @@
+"""Benchmark of the GPU DQMC sweep (one JSON line on rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c3] [--impl ours|reference]
+
+A step is one sweep = M `update` calls (propagate + local updates of one
+slice) of the O(3) spin-fermion model on seeded synthetic fields and
+pre-generated proposal streams.  The default workload is the headline
+configuration: L=16 (n=1024), beta=20 (M=200), dtau=0.1, safe_mult=10,
+plain FP64.
+
+value  : sweeps/s with the streams resident on the device (dqmc_sweep_device),
+         summed CUDA-event time of the K timed sweeps on the library's stream.
+e2e    : sweeps/s through dqmc_sweep with host (pinned) buffers: the H2D copy
+         of each sweep's streams and the D2H copy of its accept flags are
+         inside the timed region (wall clock, synchronised).
+The working set (the UDT stack alone is 2 * 21 * 16.8 MB) is larger than the
+129 MB L2, and L2 is additionally flushed (256 MB write) before each timed
+sweep.
+
+Multi-GPU: independent replicas (one chain per rank, no collective on the
+data path); value = sweeps of all ranks / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    # name: (L, M, description)
+    "c0": (4, 40, "O(3) L=4 beta=4 (M=40) dtau=0.1 safe_mult=10 FP64"),
+    "c1": (10, 100, "O(3) L=10 beta=10 (M=100) dtau=0.1 safe_mult=10 FP64"),
+    "c3": (16, 200, "O(3) L=16 beta=20 (M=200) dtau=0.1 safe_mult=10 FP64"),
+    "c4": (12, 100, "O(3) L=12 beta=10 (M=100) dtau=0.1 safe_mult=10 FP64"),
+}
+METRIC = "O(3) L=16 sweeps/s: mixed vs FP64 at G err≤1e-8; batched chain-sweeps/s"
+
+
+def model_params(L, M):
+    from oracle.dqmc_ref import Params
+    return Params(L=L, slices=M, delta_tau=0.1, safe_mult=10, lambda_=1.0, r=1.0, c=1.0, u=1.0,
+                  mu1=-0.5, mu2=-0.5, hoppings=(1.0, 0.5, -0.5, -1.0), box=0.2)
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def flops_model(kind, t, n, accepted):
+    k = t["kinds"][kind]
+    if kind == "local_updates":
+        return 32.0 * n * n * accepted, 32.0 * n * n * accepted
+    return k["flops"], k["bytes"]
+
+
+def cpu_baseline(p, phi, n_calls, seed, threads):
+    """Oracle (numpy/scipy restatement of the reference) on the host cores:
+    n_calls update() calls of the same workload, extrapolated to sweeps/s."""
+    from oracle import dqmc_ref as R
+    ref = R.DQMCRef(p, phi)
+    ref.init()
+    delta, u = R.synthetic_streams(p.N, n_calls, p.box, seed)
+    t0 = time.perf_counter()
+    for c in range(n_calls):
+        ref.update(delta[c], u[c])
+    dt = time.perf_counter() - t0
+    return (n_calls / p.slices) / dt, dt
+
+
+def run_reference(args, world, rank):
+    """The reference's own CPU implementation is Julia (not installed on
+    either machine); its CPU restatement (the oracle) is timed instead."""
+    if rank != 0:
+        return
+    L, M, desc = CONFIGS[args.config]
+    p = model_params(L, M)
+    from oracle import dqmc_ref as R
+    threads = os.cpu_count() or 1
+    phi = R.synthetic_field(p.N, p.slices, 1000)
+    ref = R.DQMCRef(p, phi)
+    ref.init()
+    calls_per_step = max(1, args.ref_calls)
+    delta, u = R.synthetic_streams(p.N, calls_per_step * (args.warmup + args.steps), p.box, 1001)
+    c = 0
+    for _ in range(args.warmup):
+        for _ in range(calls_per_step):
+            ref.update(delta[c], u[c]); c += 1
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        for _ in range(calls_per_step):
+            ref.update(delta[c], u[c]); c += 1
+        times.append(time.perf_counter() - t0)
+    per_call = sum(times) / (args.steps * calls_per_step)
+    value = 1.0 / (per_call * p.slices)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform fields/streams)",
+        "config": {"workload": desc, "L": L, "slices": M, "sample": f"{calls_per_step} update calls per step"},
+        "cpu_baseline": {"value": value, "unit": "sweeps/s", "cores": threads, "kind": "port",
+                         "sample": f"{calls_per_step} of {M} update calls per step, extrapolated; "
+                                   "Julia reference unavailable (no Julia toolchain)"},
+        "e2e": {"value": value, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    from dqmc_gb300 import api
+    from oracle.dqmc_ref import synthetic_field, synthetic_streams
+
+    L, M, desc = CONFIGS[args.config]
+    rp = model_params(L, M)
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    mp = api.ModelParams(L=L, slices=M, safe_mult=rp.safe_mult, delta_tau=rp.delta_tau, lambda_=rp.lambda_,
+                         r=rp.r, c=rp.c, u=rp.u, mu1=rp.mu1, mu2=rp.mu2, hoppings=rp.hoppings, box=rp.box,
+                         all_checks=not args.no_checks, device=dev)
+    N, n = rp.N, rp.n
+    phi = synthetic_field(N, M, 1000 + rank)
+    sweeps = args.warmup + args.steps
+    delta, unif = synthetic_streams(N, sweeps * M, rp.box, 1001 + rank)
+    # (calls, 3, N) -> per call component-fastest layout of the C ABI
+    d_host = np.ascontiguousarray(np.transpose(delta, (0, 2, 1)))
+    chain = api.DQMC(mp, phi)
+    chain.init()
+
+    # device-resident streams for `value`
+    d_dev = torch.from_numpy(d_host).to(f"cuda:{dev}")
+    u_dev = torch.from_numpy(np.ascontiguousarray(unif)).to(f"cuda:{dev}")
+    acc_dev = torch.zeros(sweeps * M * N, dtype=torch.uint8, device=f"cuda:{dev}")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    st = api.CStats()
+    import ctypes
+
+    def sweep_dev(s):
+        off = s * M
+        rc = chain.lib.dqmc_sweep_device(chain.h, M, ctypes.c_void_p(d_dev.data_ptr() + off * 3 * N * 8),
+                                         ctypes.c_void_p(u_dev.data_ptr() + off * N * 8),
+                                         ctypes.c_void_p(acc_dev.data_ptr() + off * N), ctypes.byref(st))
+        chain._check(rc)
+        return st.device_ms, st.accepted, st.max_instability
+
+    for s in range(args.warmup):
+        sweep_dev(s)
+    torch.cuda.synchronize()
+    barrier(world)
+    chain.reset_timing(True)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    torch.cuda.synchronize()
+    barrier(world)
+    t_wall0 = time.perf_counter()
+    dev_ms, accepted, instab = 0.0, 0, 0.0
+    for s in range(args.warmup, sweeps):
+        flush.fill_(float(s))
+        torch.cuda.synchronize()
+        ms, acc, ins = sweep_dev(s)
+        dev_ms += ms
+        accepted += acc
+        instab = max(instab, ins)
+    torch.cuda.synchronize()
+    barrier(world)
+    t_wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    tim = chain.timing()
+    dev_s = allreduce_max(dev_ms / 1000.0, world)
+    value = world * args.steps / dev_s
+
+    # ---- e2e through the public host-buffer API ----
+    d_pin = torch.from_numpy(d_host).pin_memory().numpy()
+    u_pin = torch.from_numpy(np.ascontiguousarray(unif)).pin_memory().numpy()
+    acc_pin = torch.zeros(M * N, dtype=torch.uint8).pin_memory().numpy()
+    chain.reset_timing(False)
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for s in range(e2e_steps):
+        off = ((args.warmup + s) % sweeps) * M
+        rc = chain.lib.dqmc_sweep(chain.h, M, d_pin[off:off + M].ctypes.data_as(api._D),
+                                  u_pin[off:off + M].ctypes.data_as(api._D),
+                                  acc_pin.ctypes.data_as(ctypes.c_void_p), ctypes.byref(st))
+        chain._check(rc)
+    torch.cuda.synchronize()
+    barrier(world)
+    e2e_s = allreduce_max(time.perf_counter() - t0, world)
+    e2e_value = world * e2e_steps / e2e_s
+
+    # ---- roofline of the dominant kernel ----
+    kinds = tim["kinds"]
+    top = max(kinds, key=lambda k: kinds[k]["ms"])
+    fl, by = flops_model(top, tim, n, accepted)
+    ms_top = kinds[top]["ms"]
+    launches_top = max(1, kinds[top]["launches"])
+    peak_fp64 = api.peak_fp64_tflops(dev)
+    achieved = fl / launches_top / (ms_top / launches_top / 1000.0) / 1e12
+    peaks, peak_kind = measured_peaks()
+    breakdown = {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
+                     "share": round(v["ms"] / max(1e-9, sum(x["ms"] for x in kinds.values())), 4)}
+                 for k, v in kinds.items()}
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu:
+            threads = os.cpu_count() or 1
+            val, secs = cpu_baseline(rp, phi, args.cpu_calls, 1002, threads)
+            cpu = {"value": val, "unit": "sweeps/s", "cores": threads, "kind": "port",
+                   "sample": f"{args.cpu_calls} of {M} update calls (numpy/scipy oracle, OpenBLAS "
+                             f"{threads} threads), {secs:.1f} s, extrapolated to one sweep"}
+        line = {
+            "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_s * 1000.0 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded uniform[-1,1] fields, uniform proposal/Metropolis streams)",
+            "config": {"workload": desc, "L": L, "slices": M, "n": n, "safe_mult": 10, "chains_per_gpu": 1,
+                       "precision": "fp64", "parallelism": f"replicas x{world}",
+                       "l2": "working set > L2 (stack 2x21x16.8 MB) and 256 MB L2 flush before each sweep"},
+            "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": int(M * 4 * N * 8),
+                    "d2h_bytes_per_step": int(M * N), "steps": e2e_steps},
+            "gpu_launches": int(tim["kernel_launches"]),
+            "roofline": {"bound": "fp64", "kernel": top, "achieved": achieved, "peak": peak_fp64,
+                         "unit": "TFLOP/s", "frac": achieved / peak_fp64, "traffic": None,
+                         "peak_source": "FP64 FMA peak measured live on this GPU (dqmc_peak_fp64)",
+                         "hbm_peak_gbs": peaks.get("hbm_gbs"), "bf16_peak_tflops": peaks.get("bf16_tflops"),
+                         "peaks_file": peak_kind},
+            "kernel_breakdown": breakdown,
+            "acc_rate": accepted / (args.steps * M * N),
+            "max_instability": instab,
+            "wall_s_timed": t_wall,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    chain.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c3", choices=sorted(CONFIGS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-checks", action="store_true", help="all_checks off")
+    ap.add_argument("--cpu-calls", type=int, default=10)
+    ap.add_argument("--ref-calls", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -36,8 +36,8 @@ class CParams(ctypes.Structure):
                 ("opdim", ctypes.c_int32), ("delta_tau", ctypes.c_double), ("lambda_", ctypes.c_double),
                 ("r", ctypes.c_double), ("c", ctypes.c_double), ("u", ctypes.c_double),
                 ("mu1", ctypes.c_double), ("mu2", ctypes.c_double), ("hoppings", ctypes.c_double * 4),
-                ("all_checks", ctypes.c_int32), ("precision", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 6)]
+                ("all_checks", ctypes.c_int32), ("precision", ctypes.c_int32), ("device", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 5)]
 
 
 class CStats(ctypes.Structure):
@@ -45,10 +45,12 @@ class CStats(ctypes.Structure):
                 ("max_instability", ctypes.c_double), ("device_ms", ctypes.c_double)]
 
 
+KERNEL_KINDS = ["slice_cols", "slice_rows", "local_updates", "zgemm", "qrp", "apply_q", "trsm", "misc"]
+
+
 class CTiming(ctypes.Structure):
-    _fields_ = [("ms_wrap", ctypes.c_double), ("ms_stack", ctypes.c_double), ("ms_greens", ctypes.c_double),
-                ("ms_local", ctypes.c_double), ("n_wrap", ctypes.c_int64), ("n_stack", ctypes.c_int64),
-                ("n_greens", ctypes.c_int64), ("n_local", ctypes.c_int64), ("kernel_launches", ctypes.c_int64)]
+    _fields_ = [("ms", ctypes.c_double * 8), ("launches", ctypes.c_int64 * 8), ("flops", ctypes.c_double * 8),
+                ("bytes", ctypes.c_double * 8), ("kernel_launches", ctypes.c_int64)]
 
 
 # every symbol the header declares, with its argument types
@@ -83,6 +85,7 @@ SIGNATURES = {
     "dqmc_measure": ([_P, _D, _D, _D], ctypes.c_int),
     "dqmc_get_timing": ([_P, ctypes.POINTER(CTiming)], ctypes.c_int),
     "dqmc_reset_timing": ([_P, _I32], ctypes.c_int),
+    "dqmc_peak_fp64": ([_I32, _D], ctypes.c_int),
 }
 
 _lib = None
@@ -121,6 +124,7 @@ class ModelParams:
     hoppings: tuple = (1.0, 0.5, -0.5, -1.0)
     box: float = 0.2
     all_checks: bool = True
+    device: int = -1
 
     @property
     def N(self):
@@ -139,6 +143,7 @@ class ModelParams:
             p.hoppings[k] = self.hoppings[k]
         p.all_checks = 1 if self.all_checks else 0
         p.precision = 0
+        p.device = self.device
         return p
 
 
@@ -150,6 +155,16 @@ def _cplx_in(a, n):
     a = np.asarray(a, dtype=np.complex128)
     assert a.shape == (n, n)
     return np.asfortranarray(a)
+
+
+def peak_fp64_tflops(device=0):
+    """Measured FP64 FMA throughput of `device` in TFLOP/s."""
+    lib = load_library()
+    out = ctypes.c_double()
+    rc = lib.dqmc_peak_fp64(int(device), ctypes.byref(out))
+    if rc != DQMC_OK:
+        raise DQMCError(rc, "dqmc_peak_fp64 failed")
+    return out.value
 
 
 class DQMC:
@@ -352,9 +367,12 @@ class DQMC:
         return dict(greens=G, occupation=occ.value, e_kin=ek.value)
 
     def timing(self):
+        """Per kernel kind: device ms, launches, algorithmic flops and bytes."""
         t = CTiming()
         self._check(self.lib.dqmc_get_timing(self.h, ctypes.byref(t)))
-        return {k: getattr(t, k) for k, _ in CTiming._fields_}
+        kinds = {k: dict(ms=t.ms[i], launches=t.launches[i], flops=t.flops[i], bytes=t.bytes[i])
+                 for i, k in enumerate(KERNEL_KINDS)}
+        return dict(kinds=kinds, kernel_launches=t.kernel_launches)
 
     def reset_timing(self, enable=True):
         self._check(self.lib.dqmc_reset_timing(self.h, 1 if enable else 0))

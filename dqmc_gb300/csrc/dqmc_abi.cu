@@ -18,7 +18,7 @@
 
 struct TimedSpan {
   cudaEvent_t a, b;
-  int group;
+  int kind;
 };
 
 struct dqmc_handle {
@@ -68,14 +68,14 @@ struct dqmc_handle {
   std::vector<TimedSpan> spans;
   std::vector<cudaEvent_t> event_pool;
   size_t event_next = 0;
-  double ms[4] = {0, 0, 0, 0};
-  int64_t cnt[4] = {0, 0, 0, 0};
+  double ms[DQMC_NKINDS] = {};
+  int64_t cnt[DQMC_NKINDS] = {};
+  double flops[DQMC_NKINDS] = {};
+  double bytes[DQMC_NKINDS] = {};
   int64_t launches = 0;
 };
 
 namespace {
-
-enum { GRP_WRAP = 0, GRP_STACK = 1, GRP_GREENS = 2, GRP_LOCAL = 3 };
 
 int set_err(dqmc_handle* h, int code, const std::string& msg) {
   if (h) h->last_error = msg;
@@ -104,31 +104,42 @@ cudaEvent_t next_event(dqmc_handle* h) {
   return h->event_pool[h->event_next++];
 }
 
-struct Span {
+// One kernel launch: counted, its algorithmic work accumulated, and bracketed
+// by CUDA events on the handle's stream when timing is enabled.
+struct KSpan {
   dqmc_handle* h;
-  int group;
+  int kind;
   cudaEvent_t a = nullptr;
-  Span(dqmc_handle* hh, int g) : h(hh), group(g) {
+  KSpan(dqmc_handle* hh, int k, double fl, double by) : h(hh), kind(k) {
     if (h->timing) {
       a = next_event(h);
       cudaEventRecord(a, h->st);
     }
+    h->cnt[kind]++;
+    h->flops[kind] += fl;
+    h->bytes[kind] += by;
+    h->launches++;
   }
-  ~Span() {
+  ~KSpan() {
     if (h->timing) {
       cudaEvent_t b = next_event(h);
       cudaEventRecord(b, h->st);
-      h->spans.push_back({a, b, group});
+      h->spans.push_back({a, b, kind});
     }
-    h->cnt[group]++;
   }
 };
+
+#define LAUNCH(kind, fl, by, call)      \
+  do {                                  \
+    KSpan ks_(h, kind, (fl), (by));     \
+    CU(call);                           \
+  } while (0)
 
 // Resolves recorded spans into accumulated milliseconds (stream must be idle).
 void resolve_spans(dqmc_handle* h) {
   for (auto& sp : h->spans) {
     float t = 0.f;
-    if (cudaEventElapsedTime(&t, sp.a, sp.b) == cudaSuccess) h->ms[sp.group] += t;
+    if (cudaEventElapsedTime(&t, sp.a, sp.b) == cudaSuccess) h->ms[sp.kind] += t;
   }
   h->spans.clear();
   h->event_next = 0;
@@ -153,6 +164,11 @@ int sync(dqmc_handle* h) {
 }
 
 size_t nn_bytes(const dqmc_handle* h) { return (size_t)h->n * h->n * sizeof(cplx); }
+// algorithmic work models (real FP64 flops; bytes of one pass over the operands)
+double n2(const dqmc_handle* h) { return (double)h->n * h->n; }
+double n3(const dqmc_handle* h) { return (double)h->n * h->n * h->n; }
+double gemm_flops(double m, double nn, double k) { return 8.0 * m * nn * k; }
+double gemm_bytes(double m, double nn, double k) { return 16.0 * (m * k + k * nn + 2.0 * m * nn); }
 cplx* ustk(dqmc_handle* h, int k) { return h->u_stack + (size_t)k * h->n * h->n; }
 cplx* tstk(dqmc_handle* h, int k) { return h->t_stack + (size_t)k * h->n * h->n; }
 double* dstk(dqmc_handle* h, int k) { return h->d_stack + (size_t)k * h->n; }
@@ -163,8 +179,7 @@ int copy_nn(dqmc_handle* h, cplx* dst, const cplx* src) {
 }
 
 int set_identity(dqmc_handle* h, cplx* A) {
-  CU(launch_set_identity(A, h->n, h->st));
-  h->launches++;
+  LAUNCH(DQMC_K_MISC, 0.0, 16.0 * n2(h), launch_set_identity(A, h->n, h->st));
   return DQMC_OK;
 }
 
@@ -177,19 +192,20 @@ int set_ones(dqmc_handle* h, double* d) {
 
 // ---- slice matrices ---------------------------------------------------------
 int apply_cols(dqmc_handle* h, cplx* A, int first0, int count, int step, int mode, const double* colscale) {
-  CU(launch_apply_cols(A, h->n, h->mc, h->evtab, first0, count, step, mode, colscale, h->st));
-  h->launches++;
+  const double per = (mode == SLICE_EFF_LEFT_INV) ? 32.0 : 74.0;
+  LAUNCH(DQMC_K_SLICE_COLS, per * n2(h) * count, 32.0 * n2(h),
+         launch_apply_cols(A, h->n, h->mc, h->evtab, first0, count, step, mode, colscale, h->st));
   return DQMC_OK;
 }
 int apply_rows(dqmc_handle* h, cplx* A, int first0, int count, int step, int mode) {
-  CU(launch_apply_rows(A, h->n, h->mc, h->evtab, first0, count, step, mode, h->st));
-  h->launches++;
+  const double per = (mode == SLICE_EFF_RIGHT) ? 32.0 : 74.0;
+  LAUNCH(DQMC_K_SLICE_ROWS, per * n2(h) * count, 32.0 * n2(h),
+         launch_apply_rows(A, h->n, h->mc, h->evtab, first0, count, step, mode, h->st));
   return DQMC_OK;
 }
 
 // wrap_greens! (src/stack.jl:316-325); slice is 1-based.
 int wrap_greens(dqmc_handle* h, cplx* gf, int slice, int direction) {
-  Span sp(h, GRP_WRAP);
   if (direction == -1) {
     CHK(apply_cols(h, gf, slice - 2, 1, 1, SLICE_LEFT_BINV, nullptr));
     CHK(apply_rows(h, gf, slice - 2, 1, 1, SLICE_RIGHT_B));
@@ -200,40 +216,64 @@ int wrap_greens(dqmc_handle* h, cplx* gf, int slice, int direction) {
   return DQMC_OK;
 }
 
+// ---- dense kernels with their work models ----------------------------------
+int gemm(dqmc_handle* h, char opA, char opB, const cplx* A, const cplx* B, cplx* C, const double* rs = nullptr,
+         const double* cs = nullptr) {
+  const int n = h->n;
+  LAUNCH(DQMC_K_GEMM, gemm_flops(n, n, n), gemm_bytes(n, n, n),
+         launch_zgemm(n, n, n, opA, opB, cmake(1, 0), A, n, B, n, cmake(0, 0), C, n, rs, cs, h->st));
+  return DQMC_OK;
+}
+// pivoted QR of A (destroyed) -> T (physical layout), D; reflectors in h->qr
+int qrp(dqmc_handle* h, cplx* A, cplx* T, double* D) {
+  LAUNCH(DQMC_K_QRP, 16.0 / 3.0 * n3(h), 32.0 * n2(h), launch_qrp(A, h->n, h->qr, h->sm_count, h->st));
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_qrp_finalize(A, T, D, h->n, h->qr, h->st));
+  return DQMC_OK;
+}
+// X <- X Q with the reflectors of the last qrp
+int apply_q(dqmc_handle* h, cplx* X) {
+  LAUNCH(DQMC_K_APPLYQ, 8.0 * n3(h), 40.0 * n2(h), launch_apply_q_right(X, h->n, h->n, h->qr, false, h->st));
+  return DQMC_OK;
+}
+int trsm_left(dqmc_handle* h, const cplx* T, const int* order, cplx* Y) {
+  LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_upper(T, order, Y, h->n, h->n, h->st));
+  return DQMC_OK;
+}
+int trsm_right(dqmc_handle* h, const cplx* T, const int* order, cplx* Y) {
+  LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_right_upper(T, order, Y, h->n, h->n, h->st));
+  return DQMC_OK;
+}
+int permute(dqmc_handle* h, const cplx* src, cplx* dst, const int* order, bool by_rows, bool scatter) {
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_permute(src, dst, h->n, h->n, order, by_rows, scatter, h->st));
+  return DQMC_OK;
+}
+
 // ---- UDT ------------------------------------------------------------------
 // decompose_udt! (src/linalg.jl:20-39) of A (destroyed): U (explicit), D, T.
 int decompose_udt(dqmc_handle* h, cplx* A, cplx* U, double* D, cplx* T) {
-  CU(launch_qrp(A, h->n, h->qr, h->sm_count, h->st));
-  CU(launch_qrp_finalize(A, T, D, h->n, h->qr, h->st));
+  CHK(qrp(h, A, T, D));
   CHK(set_identity(h, U));
-  CU(launch_apply_q_right(U, h->n, h->n, h->qr, false, h->st));
-  h->launches += 3;
+  CHK(apply_q(h, U));
   return DQMC_OK;
 }
 
 // add_slice_sequence_left (src/stack.jl:278-293); idx 1-based.
 int add_slice_sequence_left(dqmc_handle* h, int idx) {
-  Span sp(h, GRP_STACK);
   const int k = idx - 1;
   CHK(copy_nn(h, h->W1, ustk(h, k)));
   CHK(apply_cols(h, h->W1, (idx - 1) * h->s, h->s, 1, SLICE_LEFT_B, dstk(h, k)));
   CHK(decompose_udt(h, h->W1, ustk(h, k + 1), dstk(h, k + 1), h->W2));
-  CU(launch_zgemm(h->n, h->n, h->n, 'N', 'N', cmake(1, 0), h->W2, h->n, tstk(h, k), h->n, cmake(0, 0),
-                  tstk(h, k + 1), h->n, nullptr, nullptr, h->st));
-  h->launches++;
+  CHK(gemm(h, 'N', 'N', h->W2, tstk(h, k), tstk(h, k + 1)));
   return DQMC_OK;
 }
 
 // add_slice_sequence_right (src/stack.jl:299-313); idx 1-based.
 int add_slice_sequence_right(dqmc_handle* h, int idx) {
-  Span sp(h, GRP_STACK);
   const int k = idx - 1;
   CHK(copy_nn(h, h->W1, ustk(h, k + 1)));
   CHK(apply_cols(h, h->W1, idx * h->s - 1, h->s, -1, SLICE_LEFT_BDAG, dstk(h, k + 1)));
   CHK(decompose_udt(h, h->W1, ustk(h, k), dstk(h, k), h->W2));
-  CU(launch_zgemm(h->n, h->n, h->n, 'N', 'N', cmake(1, 0), h->W2, h->n, tstk(h, k + 1), h->n, cmake(0, 0),
-                  tstk(h, k), h->n, nullptr, nullptr, h->st));
-  h->launches++;
+  CHK(gemm(h, 'N', 'N', h->W2, tstk(h, k + 1), tstk(h, k)));
   return DQMC_OK;
 }
 
@@ -250,38 +290,33 @@ int add_slice_sequence_right(dqmc_handle* h, int idx) {
 // log|det G| = -sum log d2 (|det| of the unitary and unit-triangular
 // factors is 1).
 int calculate_greens_into(dqmc_handle* h, cplx* out) {
-  Span sp(h, GRP_GREENS);
   const int n = h->n;
-  const cplx one = cmake(1, 0), zero = cmake(0, 0);
   // 1. X = Dl (Tl Tr^dag) Dr
-  CU(launch_zgemm(n, n, n, 'N', 'C', one, h->Tl, n, h->Tr, n, zero, h->W1, n, h->Dl, h->Dr, h->st));
+  CHK(gemm(h, 'N', 'C', h->Tl, h->Tr, h->W1, h->Dl, h->Dr));
   // 2. X = Q1 D1 T1
-  CU(launch_qrp(h->W1, n, h->qr, h->sm_count, h->st));
-  CU(launch_qrp_finalize(h->W1, h->W2, h->D1, n, h->qr, h->st));
+  CHK(qrp(h, h->W1, h->W2, h->D1));
   CU(cudaMemcpyAsync(h->ord1, h->qr.order, n * sizeof(int), cudaMemcpyDeviceToDevice, h->st));
   // 3. U = Ul Q1
   CHK(copy_nn(h, h->W3, h->Ul));
-  CU(launch_apply_q_right(h->W3, n, n, h->qr, false, h->st));
+  CHK(apply_q(h, h->W3));
   // 4. tmp = (U^dag Ur) P1 That1^-1 + diag(D1)
-  CU(launch_zgemm(n, n, n, 'C', 'N', one, h->W3, n, h->Ur, n, zero, h->W4, n, nullptr, nullptr, h->st));
-  CU(launch_permute(h->W4, h->W1, n, n, h->ord1, false, false, h->st));
-  CU(launch_trsm_right_upper(h->W2, h->ord1, h->W1, n, n, h->st));
-  CU(launch_add_diag(h->W1, n, h->D1, h->st));
+  CHK(gemm(h, 'C', 'N', h->W3, h->Ur, h->W4));
+  CHK(permute(h, h->W4, h->W1, h->ord1, false, false));
+  CHK(trsm_right(h, h->W2, h->ord1, h->W1));
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n, launch_add_diag(h->W1, n, h->D1, h->st));
   // 5. tmp = Q2 d2 t2
-  CU(launch_qrp(h->W1, n, h->qr, h->sm_count, h->st));
-  CU(launch_qrp_finalize(h->W1, h->W4, h->d2, n, h->qr, h->st));
+  CHK(qrp(h, h->W1, h->W4, h->d2));
   // 6. U Q2
-  CU(launch_apply_q_right(h->W3, n, n, h->qr, false, h->st));
+  CHK(apply_q(h, h->W3));
   // 7. G = Ur P1 That1^-1 P2 That2^-1 diag(1/d2) (U Q2)^dag
-  CU(launch_conj_transpose(h->W3, h->W1, n, h->st));
-  CU(launch_scale(h->W1, n, n, h->d2, true, nullptr, false, h->st));
-  CU(launch_trsm_left_upper(h->W4, h->qr.order, h->W1, n, n, h->st));
-  CU(launch_permute(h->W1, h->W3, n, n, h->qr.order, true, true, h->st));
-  CU(launch_trsm_left_upper(h->W2, h->ord1, h->W3, n, n, h->st));
-  CU(launch_permute(h->W3, h->W1, n, n, h->ord1, true, true, h->st));
-  CU(launch_zgemm(n, n, n, 'N', 'N', one, h->Ur, n, h->W1, n, zero, out, n, nullptr, nullptr, h->st));
-  CU(launch_sum_log(h->d2, n, h->scal_d, h->st));
-  h->launches += 19;
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_conj_transpose(h->W3, h->W1, n, h->st));
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_scale(h->W1, n, n, h->d2, true, nullptr, false, h->st));
+  CHK(trsm_left(h, h->W4, h->qr.order, h->W1));
+  CHK(permute(h, h->W1, h->W3, h->qr.order, true, true));
+  CHK(trsm_left(h, h->W2, h->ord1, h->W3));
+  CHK(permute(h, h->W3, h->W1, h->ord1, true, true));
+  CHK(gemm(h, 'N', 'N', h->Ur, h->W1, out));
+  LAUNCH(DQMC_K_MISC, 0.0, 8.0 * n, launch_sum_log(h->d2, n, h->scal_d, h->st));
   return DQMC_OK;
 }
 
@@ -313,8 +348,7 @@ int stack_identity(dqmc_handle* h, int k) {
 }
 
 int instability_check(dqmc_handle* h) {
-  CU(launch_max_absdiff(h->Gtmp, h->G, (size_t)h->n * h->n, h->scal_d + 1, h->st));
-  h->launches++;
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_max_absdiff(h->Gtmp, h->G, (size_t)h->n * h->n, h->scal_d + 1, h->st));
   double d = 0.0;
   CU(cudaMemcpyAsync(&d, h->scal_d + 1, sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CU(cudaStreamSynchronize(h->st));
@@ -460,7 +494,6 @@ int local_updates_dev(dqmc_handle* h, const double* delta_dev, const double* uni
                       cplx* det_dev, double* pacc_dev) {
   if (h->current_slice < 1 || h->current_slice > h->M)
     return set_err(h, DQMC_ERR_STATE, "local_updates needs 1 <= current_slice <= M (call dqmc_init)");
-  Span sp(h, GRP_LOCAL);
   LocalUpdateArgs a{};
   a.G = h->G;
   a.phi = h->phi;
@@ -478,8 +511,9 @@ int local_updates_dev(dqmc_handle* h, const double* delta_dev, const double* uni
   a.bar = h->bar;
   a.err = h->err_d;
   a.mc = h->mc;
-  CU(launch_local_updates(a, h->sm_count, h->st));
-  h->launches++;
+  // flops/bytes of the local updates depend on the acceptances; the caller
+  // derives them from the accepted count (32 n^2 flops and bytes per accept)
+  LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_updates(a, h->sm_count, h->st));
   return DQMC_OK;
 }
 
@@ -552,6 +586,7 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
   if (p->opdim != 3) return DQMC_ERR_ARG;
   if (p->precision != DQMC_PREC_FP64) return DQMC_ERR_ARG;
   if (4 * p->L * p->L > 1024) return DQMC_ERR_ARG;                     // register-resident QR columns
+  if (p->device >= 0 && cudaSetDevice(p->device) != cudaSuccess) return DQMC_ERR_CUDA;
   dqmc_handle* h = new dqmc_handle();
   h->p = *p;
   h->L = p->L; h->N = p->L * p->L; h->n = 4 * h->N; h->M = p->slices; h->s = p->safe_mult;
@@ -597,6 +632,7 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
 }
 
 int dqmc_destroy(dqmc_handle* h) {
+  if (h) cudaSetDevice(h->device);
   if (!h) return DQMC_ERR_ARG;
   cudaStreamSynchronize(h->st);
   free_all(h);
@@ -605,21 +641,24 @@ int dqmc_destroy(dqmc_handle* h) {
 }
 
 int dqmc_set_field(dqmc_handle* h, const double* phi) {
+  if (h) cudaSetDevice(h->device);
   if (!h || !phi) return DQMC_ERR_ARG;
   CU(cudaMemcpyAsync(h->phi, phi, (size_t)3 * h->N * h->M * sizeof(double), cudaMemcpyHostToDevice, h->st));
-  CU(launch_build_evtab(h->phi, h->evtab, h->N, h->M, h->p.lambda * h->p.delta_tau, h->st));
-  h->launches++;
+  LAUNCH(DQMC_K_MISC, 0.0, 56.0 * h->N * h->M,
+         launch_build_evtab(h->phi, h->evtab, h->N, h->M, h->p.lambda * h->p.delta_tau, h->st));
   h->initialized = false;
   return sync(h);
 }
 
 int dqmc_get_field(dqmc_handle* h, double* phi) {
+  if (h) cudaSetDevice(h->device);
   if (!h || !phi) return DQMC_ERR_ARG;
   CU(cudaMemcpyAsync(phi, h->phi, (size_t)3 * h->N * h->M * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   return sync(h);
 }
 
 int dqmc_init(dqmc_handle* h) {
+  if (h) cudaSetDevice(h->device);
   if (!h) return DQMC_ERR_ARG;
   std::vector<double> phi((size_t)3 * h->N * h->M);
   CU(cudaMemcpyAsync(phi.data(), h->phi, phi.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -635,6 +674,7 @@ int dqmc_init(dqmc_handle* h) {
 }
 
 int dqmc_propagate(dqmc_handle* h) {
+  if (h) cudaSetDevice(h->device);
   if (!h) return DQMC_ERR_ARG;
   if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
   CHK(propagate(h));
@@ -642,6 +682,7 @@ int dqmc_propagate(dqmc_handle* h) {
 }
 
 int dqmc_get_state(dqmc_handle* h, int32_t* slice, int32_t* direction) {
+  if (h) cudaSetDevice(h->device);
   if (!h) return DQMC_ERR_ARG;
   if (slice) *slice = h->current_slice;
   if (direction) *direction = h->direction;
@@ -672,6 +713,7 @@ static int local_updates_host(dqmc_handle* h, const double* delta, const double*
 
 int dqmc_local_updates(dqmc_handle* h, const double* delta, const double* unif, uint8_t* accepted,
                        double* detratio, double* p_acc, double* acc_rate) {
+  if (h) cudaSetDevice(h->device);
   if (!h) return DQMC_ERR_ARG;
   if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
   return local_updates_host(h, delta, unif, accepted, detratio, p_acc, acc_rate);
@@ -679,6 +721,7 @@ int dqmc_local_updates(dqmc_handle* h, const double* delta, const double* unif, 
 
 int dqmc_update(dqmc_handle* h, const double* delta, const double* unif, uint8_t* accepted, double* detratio,
                 double* p_acc, double* acc_rate) {
+  if (h) cudaSetDevice(h->device);
   if (!h) return DQMC_ERR_ARG;
   if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
   CHK(propagate(h));
@@ -720,6 +763,7 @@ static int sweep_impl(dqmc_handle* h, int n_calls, const double* delta_dev, cons
 
 int dqmc_sweep(dqmc_handle* h, int32_t n_calls, const double* delta_stream, const double* unif_stream,
                uint8_t* accepted, dqmc_stats* stats) {
+  if (h) cudaSetDevice(h->device);
   if (!h || n_calls < 0 || !delta_stream || !unif_stream) return DQMC_ERR_ARG;
   if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
   if (n_calls == 0) return DQMC_OK;
@@ -739,6 +783,7 @@ int dqmc_sweep(dqmc_handle* h, int32_t n_calls, const double* delta_stream, cons
 
 int dqmc_sweep_device(dqmc_handle* h, int32_t n_calls, const double* delta_stream_dev,
                       const double* unif_stream_dev, uint8_t* accepted_dev, dqmc_stats* stats) {
+  if (h) cudaSetDevice(h->device);
   if (!h || n_calls < 0 || !delta_stream_dev || !unif_stream_dev) return DQMC_ERR_ARG;
   if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
   if (n_calls == 0) return DQMC_OK;
@@ -746,6 +791,7 @@ int dqmc_sweep_device(dqmc_handle* h, int32_t n_calls, const double* delta_strea
 }
 
 int dqmc_get_greens(dqmc_handle* h, double* out, int32_t* slice, int32_t* direction) {
+  if (h) cudaSetDevice(h->device);
   if (!h || !out) return DQMC_ERR_ARG;
   CHK(download_nn(h, out, h->G));
   if (slice) *slice = h->current_slice;
@@ -754,12 +800,14 @@ int dqmc_get_greens(dqmc_handle* h, double* out, int32_t* slice, int32_t* direct
 }
 
 int dqmc_set_greens(dqmc_handle* h, const double* in) {
+  if (h) cudaSetDevice(h->device);
   if (!h || !in) return DQMC_ERR_ARG;
   CHK(upload_nn(h, h->G, in));
   return sync(h);
 }
 
 int dqmc_wrap_greens(dqmc_handle* h, double* inout, int32_t slice, int32_t direction) {
+  if (h) cudaSetDevice(h->device);
   if (!h || !inout || (direction != 1 && direction != -1)) return DQMC_ERR_ARG;
   int sl0 = direction == 1 ? slice : slice - 1;
   if (sl0 < 1 || sl0 > h->M) return set_err(h, DQMC_ERR_ARG, "slice out of range");
@@ -770,6 +818,7 @@ int dqmc_wrap_greens(dqmc_handle* h, double* inout, int32_t slice, int32_t direc
 }
 
 int dqmc_multiply_B(dqmc_handle* h, int32_t which, int32_t slice, double* inout) {
+  if (h) cudaSetDevice(h->device);
   if (!h || !inout || which < 0 || which > 4) return DQMC_ERR_ARG;
   if (slice < 1 || slice > h->M) return set_err(h, DQMC_ERR_ARG, "slice out of range");
   CHK(upload_nn(h, h->Gtmp, inout));
@@ -783,6 +832,7 @@ int dqmc_multiply_B(dqmc_handle* h, int32_t which, int32_t slice, double* inout)
 
 int dqmc_calculate_greens_udt(dqmc_handle* h, const double* Ul, const double* Dl, const double* Tl,
                               const double* Ur, const double* Dr, const double* Tr, double* G, double* logdet) {
+  if (h) cudaSetDevice(h->device);
   if (!h || !Ul || !Dl || !Tl || !Ur || !Dr || !Tr || !G) return DQMC_ERR_ARG;
   const size_t dn = h->n * sizeof(double);
   CHK(upload_nn(h, h->Ul, Ul));
@@ -801,6 +851,7 @@ int dqmc_calculate_greens_udt(dqmc_handle* h, const double* Ul, const double* Dl
 }
 
 int dqmc_decompose_udt(dqmc_handle* h, const double* A, double* U, double* D, double* T) {
+  if (h) cudaSetDevice(h->device);
   if (!h || !A || !U || !D || !T) return DQMC_ERR_ARG;
   CHK(upload_nn(h, h->W1, A));
   CHK(decompose_udt(h, h->W1, h->W3, h->D1, h->W2));
@@ -811,6 +862,7 @@ int dqmc_decompose_udt(dqmc_handle* h, const double* A, double* U, double* D, do
 }
 
 int dqmc_logdet(dqmc_handle* h, double* logdet) {
+  if (h) cudaSetDevice(h->device);
   if (!h || !logdet) return DQMC_ERR_ARG;
   double sl = 0.0;
   CU(cudaMemcpyAsync(&sl, h->scal_d + 2, sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -823,26 +875,23 @@ int dqmc_logdet(dqmc_handle* h, double* logdet) {
 // B(slice)^dag ... B(M)^dag and B(slice-1) ... B(1) as UDTs, stabilised every
 // safe_mult slices (calc_Bchain_dagger / calc_Bchain, :964-1058).
 int dqmc_calc_greens(dqmc_handle* h, int32_t slice, double* out, double* logdet) {
+  if (h) cudaSetDevice(h->device);
   if (!h || !out) return DQMC_ERR_ARG;
   if (slice < 1 || slice > h->M) return set_err(h, DQMC_ERR_ARG, "slice out of range");
   const int n = h->n, s = h->s;
-  const cplx one = cmake(1, 0), zero = cmake(0, 0);
   // chain helper: U, D, T accumulate into (Ux, Dx, Tx) buffers
   auto chain = [&](int start, int stop, bool dagger, cplx* Ux, double* Dx, cplx* Tx) -> int {
     CHK(set_identity(h, Ux));
     CHK(set_identity(h, Tx));
     CHK(set_ones(h, Dx));
-    bool pending_scale = false;   // columns of Ux still need scaling by Dx before the next QR
     auto flush = [&]() -> int {
-      CU(launch_scale(Ux, n, n, nullptr, false, Dx, false, h->st));
+      LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_scale(Ux, n, n, nullptr, false, Dx, false, h->st));
       CHK(copy_nn(h, h->W1, Ux));
       CHK(decompose_udt(h, h->W1, Ux, Dx, h->W2));
-      CU(launch_zgemm(n, n, n, 'N', 'N', one, h->W2, n, Tx, n, zero, h->W4, n, nullptr, nullptr, h->st));
+      CHK(gemm(h, 'N', 'N', h->W2, Tx, h->W4));
       CHK(copy_nn(h, Tx, h->W4));
-      h->launches += 2;
       return DQMC_OK;
     };
-    (void)pending_scale;
     if (!dagger) {
       for (int k = start; k <= stop; ++k) {
         CHK(apply_cols(h, Ux, k - 1, 1, 1, SLICE_LEFT_B, nullptr));
@@ -876,12 +925,14 @@ int dqmc_calc_greens(dqmc_handle* h, int32_t slice, double* out, double* logdet)
 }
 
 int dqmc_boson_action(dqmc_handle* h, double* S) {
+  if (h) cudaSetDevice(h->device);
   if (!h || !S) return DQMC_ERR_ARG;
   CU(cudaMemcpyAsync(S, h->action_d, sizeof(double), cudaMemcpyDeviceToHost, h->st));
   return sync(h);
 }
 
 int dqmc_calc_boson_action(dqmc_handle* h, double* S) {
+  if (h) cudaSetDevice(h->device);
   if (!h || !S) return DQMC_ERR_ARG;
   std::vector<double> phi((size_t)3 * h->N * h->M);
   CU(cudaMemcpyAsync(phi.data(), h->phi, phi.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -891,6 +942,7 @@ int dqmc_calc_boson_action(dqmc_handle* h, double* S) {
 }
 
 int dqmc_measure(dqmc_handle* h, double* greens_out, double* occupation, double* e_kin) {
+  if (h) cudaSetDevice(h->device);
   if (!h) return DQMC_ERR_ARG;
   if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
   const int n = h->n, N = h->N, L = h->L;
@@ -939,24 +991,29 @@ int dqmc_measure(dqmc_handle* h, double* greens_out, double* occupation, double*
 }
 
 int dqmc_get_timing(dqmc_handle* h, dqmc_timing* t) {
+  if (h) cudaSetDevice(h->device);
   if (!h || !t) return DQMC_ERR_ARG;
   CHK(sync(h));
-  t->ms_wrap = h->ms[GRP_WRAP];
-  t->ms_stack = h->ms[GRP_STACK];
-  t->ms_greens = h->ms[GRP_GREENS];
-  t->ms_local = h->ms[GRP_LOCAL];
-  t->n_wrap = h->cnt[GRP_WRAP];
-  t->n_stack = h->cnt[GRP_STACK];
-  t->n_greens = h->cnt[GRP_GREENS];
-  t->n_local = h->cnt[GRP_LOCAL];
+  for (int k = 0; k < DQMC_NKINDS; ++k) {
+    t->ms[k] = h->ms[k];
+    t->launches[k] = h->cnt[k];
+    t->flops[k] = h->flops[k];
+    t->bytes[k] = h->bytes[k];
+  }
   t->kernel_launches = h->launches;
   return DQMC_OK;
 }
 
+int dqmc_peak_fp64(int32_t device, double* tflops) {
+  if (!tflops || device < 0) return DQMC_ERR_ARG;
+  return measure_peak_fp64(device, tflops) == cudaSuccess ? DQMC_OK : DQMC_ERR_CUDA;
+}
+
 int dqmc_reset_timing(dqmc_handle* h, int32_t enable) {
+  if (h) cudaSetDevice(h->device);
   if (!h) return DQMC_ERR_ARG;
   CHK(sync(h));
-  for (int i = 0; i < 4; ++i) { h->ms[i] = 0; h->cnt[i] = 0; }
+  for (int i = 0; i < DQMC_NKINDS; ++i) { h->ms[i] = 0; h->cnt[i] = 0; h->flops[i] = 0; h->bytes[i] = 0; }
   h->launches = 0;
   h->timing = enable != 0;
   return DQMC_OK;

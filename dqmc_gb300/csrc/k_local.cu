@@ -195,7 +195,10 @@ __global__ void __launch_bounds__(256) k_local_updates(LocalUpdateArgs a) {
       }
     }
     __syncthreads();
-    if (!dec.accepted) continue;
+    const int accepted = dec.accepted;
+    // every thread has read the decision before thread 0 may overwrite it
+    __syncthreads();
+    if (!accepted) continue;
 
     // ---- phase 1: A = (G[:, cols] - I[:, cols]) M^-1, B = Delta G[rows, :] ----
     for (size_t t = gtid; t < (size_t)2 * n; t += gthreads) {

@@ -88,7 +88,7 @@ cudaError_t launch_permute(const cplx* src, cplx* dst, int rows, int cols, const
 cudaError_t launch_add_diag(cplx* A, int n, const double* d, cudaStream_t st);
 // A <- I
 cudaError_t launch_set_identity(cplx* A, int n, cudaStream_t st);
-// out[0] = sum_k log(x[k]) computed as one deterministic reduction, out[1] = sum_k log(|x[k]|) with sign flags ...
+// out[0] = sum_k log(x[k]) (one deterministic single-CTA reduction)
 cudaError_t launch_sum_log(const double* x, int n, double* out, cudaStream_t st);
 // max |A - B| over n*n entries -> out
 cudaError_t launch_max_absdiff(const cplx* A, const cplx* B, size_t count, double* out, cudaStream_t st);
@@ -96,3 +96,6 @@ cudaError_t launch_max_absdiff(const cplx* A, const cplx* B, size_t count, doubl
 cudaError_t launch_scale(cplx* A, int rows, int cols, const double* rowscale, bool invert_rows,
                          const double* colscale, bool invert_cols, cudaStream_t st);
 cudaError_t launch_conj_transpose(const cplx* A, cplx* B, int n, cudaStream_t st);
+
+// ---- diagnostics (k_diag.cu) ----
+cudaError_t measure_peak_fp64(int device, double* tflops);

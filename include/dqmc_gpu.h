@@ -59,7 +59,8 @@ typedef struct dqmc_params {
   double hoppings[4];  /* tx_x, ty_x, tx_y, ty_y */
   int32_t all_checks;  /* compare wrapped and fresh G at each stabilisation (src/stack.jl:416-429) */
   int32_t precision;   /* DQMC_PREC_FP64 */
-  int32_t reserved[6];
+  int32_t device;      /* CUDA device ordinal; -1 = the calling thread's current device */
+  int32_t reserved[5];
 } dqmc_params;
 
 typedef struct dqmc_stats {
@@ -70,13 +71,23 @@ typedef struct dqmc_stats {
   double device_ms;         /* device time of the call (CUDA events on the handle's stream) */
 } dqmc_stats;
 
+/* Kernel kinds of dqmc_timing (one CUDA-event pair per launch when timing is on). */
+#define DQMC_K_SLICE_COLS 0   /* B / B^-1 / B^dag applied to columns (left products) */
+#define DQMC_K_SLICE_ROWS 1   /* B / B^-1 applied to rows (right products) */
+#define DQMC_K_LOCAL 2        /* local updates of one slice (detratio + rank-4 updates) */
+#define DQMC_K_GEMM 3         /* complex FP64 GEMM */
+#define DQMC_K_QRP 4          /* column-pivoted Householder QR */
+#define DQMC_K_APPLYQ 5       /* X <- X Q (reflector application / explicit Q) */
+#define DQMC_K_TRSM 6         /* triangular solves with the QR factors */
+#define DQMC_K_MISC 7         /* permutations, scalings, reductions, fills */
+#define DQMC_NKINDS 8
+
 typedef struct dqmc_timing {
-  double ms_wrap;           /* slice application kernels of wrap_greens */
-  double ms_stack;          /* add_slice_sequence_* (B chain + QR + products) */
-  double ms_greens;         /* calculate_greens */
-  double ms_local;          /* local update kernels */
-  int64_t n_wrap, n_stack, n_greens, n_local;
-  int64_t kernel_launches;  /* kernels launched by the library since the last reset */
+  double ms[DQMC_NKINDS];           /* accumulated device time per kernel kind */
+  int64_t launches[DQMC_NKINDS];    /* launches per kernel kind */
+  double flops[DQMC_NKINDS];        /* algorithmic FP64 flops per kernel kind */
+  double bytes[DQMC_NKINDS];        /* algorithmic DRAM/L2 bytes per kernel kind */
+  int64_t kernel_launches;          /* all kernels launched by the library since the last reset */
 } dqmc_timing;
 
 typedef struct dqmc_handle dqmc_handle;
@@ -167,8 +178,14 @@ DQMC_API int dqmc_calc_boson_action(dqmc_handle* h, double* S);
 DQMC_API int dqmc_measure(dqmc_handle* h, double* greens_out, double* occupation, double* e_kin);
 
 /* ---- diagnostics ------------------------------------------------------------- */
+/* Per-group device times (CUDA events on the handle's stream) and the number
+ * of kernels launched since the last reset; enable != 0 turns event timing on. */
 DQMC_API int dqmc_get_timing(dqmc_handle* h, dqmc_timing* t);
 DQMC_API int dqmc_reset_timing(dqmc_handle* h, int32_t enable);
+/* Measures the FP64 FMA throughput of `device` (TFLOP/s, 2 flops per FMA) with
+ * a register-resident DFMA kernel: the roofline denominator of the FP64
+ * kernels.  No counterpart in the reference (a diagnostic of this library). */
+DQMC_API int dqmc_peak_fp64(int32_t device, double* tflops);
 
 #ifdef __cplusplus
 }
