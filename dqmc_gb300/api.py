@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(_HERE, "libdqmc_gpu.so")
 
 DQMC_OK = 0
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "non-finite value", -4: "singular M",
-          -5: "device wait timed out", -6: "invalid state"}
+          -5: "device wait timed out", -6: "invalid state", -7: "size exceeds the static scratch (n > 1024)"}
 
 B_LEFT, B_RIGHT, B_INV_LEFT, B_INV_RIGHT, B_DAG_LEFT = 0, 1, 2, 3, 4
 
@@ -86,6 +86,9 @@ SIGNATURES = {
     "dqmc_get_timing": ([_P, ctypes.POINTER(CTiming)], ctypes.c_int),
     "dqmc_reset_timing": ([_P, _I32], ctypes.c_int),
     "dqmc_peak_fp64": ([_I32, _D], ctypes.c_int),
+    "dqmc_local_updates_noalloc": ([ctypes.POINTER(CParams), ctypes.c_void_p, ctypes.c_void_p, _I32,
+                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p], ctypes.c_int),
 }
 
 _lib = None

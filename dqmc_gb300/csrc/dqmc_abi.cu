@@ -75,6 +75,8 @@ struct dqmc_handle {
   int64_t launches = 0;
 };
 
+void fill_model_const(const dqmc_params& p, ModelConst& m);
+
 namespace {
 
 int set_err(dqmc_handle* h, int code, const std::string& msg) {
@@ -523,28 +525,7 @@ int read_nacc(dqmc_handle* h, int* out) {
   return DQMC_OK;
 }
 
-void host_model_constants(dqmc_handle* h) {
-  ModelConst& m = h->mc;
-  const dqmc_params& p = h->p;
-  m.L = h->L; m.N = h->N; m.n = h->n; m.M = h->M;
-  m.dtau = p.delta_tau; m.lambda = p.lambda; m.r = p.r; m.c = p.c; m.u = p.u;
-  m.mu[0] = p.mu1; m.mu[1] = p.mu2;
-  // t[bond dir, band] = reshape(hoppings, 2, 2): t[0][b] horizontal, t[1][b] vertical
-  const double th[2] = {p.hoppings[0], p.hoppings[2]};
-  const double tv[2] = {p.hoppings[1], p.hoppings[3]};
-  for (int b = 0; b < 2; ++b) {
-    // cosh(fac * -t), sinh(fac * -t) with fac = -prefac * dtau (src/hoppings_checkerboard.jl:46-51)
-    double ff = -1.0 * p.delta_tau, fh = -0.5 * p.delta_tau;
-    m.ch_f[b] = std::cosh(ff * -th[b]); m.sh_f[b] = std::sinh(ff * -th[b]);
-    m.cv_f[b] = std::cosh(ff * -tv[b]); m.sv_f[b] = std::sinh(ff * -tv[b]);
-    m.ch_h[b] = std::cosh(fh * -th[b]); m.sh_h[b] = std::sinh(fh * -th[b]);
-    m.cv_h[b] = std::cosh(fh * -tv[b]); m.sv_h[b] = std::sinh(fh * -tv[b]);
-    // chkr_mu = exp(-dtau * -mu), chkr_mu_inv = exp(dtau * -mu) (src/hoppings_checkerboard.jl:122-127)
-    double mu = b == 0 ? p.mu1 : p.mu2;
-    m.emu[b] = std::exp(-p.delta_tau * -mu);
-    m.emu_inv[b] = std::exp(p.delta_tau * -mu);
-  }
-}
+void host_model_constants(dqmc_handle* h) { fill_model_const(h->p, h->mc); }
 
 void free_all(dqmc_handle* h) {
   void* ptrs[] = {h->phi, h->evtab, h->G, h->Gtmp, h->u_stack, h->d_stack, h->t_stack, h->Ul, h->Ur, h->Tl,
@@ -568,6 +549,29 @@ int download_nn(dqmc_handle* h, double* dst, const cplx* src) {
 }
 
 }  // namespace
+
+// Device constants of the model from the ABI parameters (also used by the
+// handle-free entry point).
+void fill_model_const(const dqmc_params& p, ModelConst& m) {
+  m.L = p.L; m.N = p.L * p.L; m.n = 4 * m.N; m.M = p.slices;
+  m.dtau = p.delta_tau; m.lambda = p.lambda; m.r = p.r; m.c = p.c; m.u = p.u;
+  m.mu[0] = p.mu1; m.mu[1] = p.mu2;
+  // t[bond dir, band] = reshape(hoppings, 2, 2): t[0][b] horizontal, t[1][b] vertical
+  const double th[2] = {p.hoppings[0], p.hoppings[2]};
+  const double tv[2] = {p.hoppings[1], p.hoppings[3]};
+  for (int b = 0; b < 2; ++b) {
+    // cosh(fac * -t), sinh(fac * -t) with fac = -prefac * dtau (src/hoppings_checkerboard.jl:46-51)
+    double ff = -1.0 * p.delta_tau, fh = -0.5 * p.delta_tau;
+    m.ch_f[b] = std::cosh(ff * -th[b]); m.sh_f[b] = std::sinh(ff * -th[b]);
+    m.cv_f[b] = std::cosh(ff * -tv[b]); m.sv_f[b] = std::sinh(ff * -tv[b]);
+    m.ch_h[b] = std::cosh(fh * -th[b]); m.sh_h[b] = std::sinh(fh * -th[b]);
+    m.cv_h[b] = std::cosh(fh * -tv[b]); m.sv_h[b] = std::sinh(fh * -tv[b]);
+    // chkr_mu = exp(-dtau * -mu), chkr_mu_inv = exp(dtau * -mu) (src/hoppings_checkerboard.jl:122-127)
+    double mu = b == 0 ? p.mu1 : p.mu2;
+    m.emu[b] = std::exp(-p.delta_tau * -mu);
+    m.emu_inv[b] = std::exp(p.delta_tau * -mu);
+  }
+}
 
 // ===========================================================================
 // C ABI

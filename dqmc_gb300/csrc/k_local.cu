@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(256) k_local_updates(LocalUpdateArgs a) {
         if (acc) {
           double* pg = &a.phi[((size_t)N * l + i) * 3];
           pg[0] = nw[0]; pg[1] = nw[1]; pg[2] = nw[2];
-          reinterpret_cast<EvEntry*>(a.evtab)[(size_t)N * l + i] = evn;
+          if (a.evtab) reinterpret_cast<EvEntry*>(a.evtab)[(size_t)N * l + i] = evn;
           *a.action += -log(exp_dS);
           *a.n_acc += 1;
         }

@@ -29,7 +29,7 @@ cudaError_t launch_apply_rows(cplx* A, int n, const ModelConst& mc, const void* 
 struct LocalUpdateArgs {
   cplx* G;
   double* phi;             // (3, N, M)
-  void* evtab;             // (N, M) interaction entries, kept in sync with phi
+  void* evtab;             // (N, M) interaction entries, kept in sync with phi (may be null)
   int slice0;              // 0-based slice
   const double* delta;     // (3, N) proposal shifts of this call
   const double* unif;      // (N) Metropolis uniforms of this call

@@ -41,6 +41,7 @@ extern "C" {
 #define DQMC_ERR_SINGULAR (-4)   /* singular 4x4 M in a local update */
 #define DQMC_ERR_TIMEOUT (-5)    /* a device-side wait gave up (bounded spin) */
 #define DQMC_ERR_STATE (-6)      /* call not valid in the current state */
+#define DQMC_ERR_TOO_LARGE (-7)  /* n = 4 L^2 exceeds the static scratch of dqmc_local_updates_noalloc (1024) */
 
 #define DQMC_PREC_FP64 0         /* plain FP64 everywhere */
 
@@ -135,6 +136,27 @@ DQMC_API int dqmc_sweep(dqmc_handle* h, int32_t n_calls, const double* delta_str
  * copies); device pointers as returned by the caller's allocator. */
 DQMC_API int dqmc_sweep_device(dqmc_handle* h, int32_t n_calls, const double* delta_stream_dev,
                       const double* unif_stream_dev, uint8_t* accepted_dev, dqmc_stats* stats);
+
+/* Local updates of one slice for callers that cannot let the library allocate
+ * device memory (their allocator owns all GPU memory, or they must stay inside
+ * a fixed pre-reserved budget).  No counterpart in the reference: it is the
+ * handle-free form of dqmc_local_updates, on buffers the caller owns, all of
+ * them DEVICE pointers: greens (n x n complex, updated in place), phi
+ * (3 x N x M, updated in place), delta[3*N], unif[N], accepted[N] (may be
+ * NULL) and action (one double, incremented by each accepted Delta S).
+ * `stream` is a cudaStream_t (NULL = legacy default stream); the call returns
+ * after the stream has finished the update.
+ *   - It allocates nothing: its scratch (the rank-4 factors, a grid barrier
+ *     and an error flag; 128 KB) is one static device array that every GPU
+ *     which loads the library holds until exit.  Limit: n = 4 L^2 <= 1024
+ *     (L <= 16); larger sizes return DQMC_ERR_TOO_LARGE.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - All calls share the array: calls that overlap on the GPU (other host
+ *     threads, other streams) race and must be serialised by the caller. */
+DQMC_API int dqmc_local_updates_noalloc(const dqmc_params* p, double* greens, double* phi, int32_t slice,
+                                        const double* delta, const double* unif, uint8_t* accepted,
+                                        double* action, void* stream);
 
 /* ---- Green's functions ------------------------------------------------------ */
 /* s.greens (effective G at the current slice). out: double[2*n*n]. */
