@@ -118,7 +118,6 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
   int* order = reinterpret_cast<int*>(v + n);         // (n) logical -> physical
   __shared__ double red[32];
   __shared__ int redi[32];
-  __shared__ double s_tau_re, s_tau_im;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int warps = QR_THREADS / 32;
   const int gwarp = blockIdx.x * warps + wid, nwarps = gridDim.x * warps;
@@ -188,33 +187,38 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
       for (int r = threadIdx.x; r < n; r += blockDim.x) w.V[(size_t)k * n + r] = r < k ? cmake(0.0, 0.0) : v[r];
     }
     // ---- apply H_k^H to the remaining columns, downdate their norms ----
+    // remaining logical positions k+1..n-1 are dealt round-robin over the CTAs
+    // first, so every SM keeps an equal share of the columns as k grows
     const cplx ctau = cconj(tau);
-    for (int q = k + 1 + gwarp; q < n; q += nwarps) {
-      const int j = order[q];
+    const int rem = n - k - 1;
+    for (int t = blockIdx.x + gridDim.x * wid; t < rem; t += gridDim.x * warps) {
+      const int j = order[k + 1 + t];
       cplx* col = A + (size_t)j * n;
       cplx x[QR_MAXT];
-      cplx s = cmake(0.0, 0.0);
+      cplx sp[4] = {cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0)};
 #pragma unroll
-      for (int t = 0; t < QR_MAXT; ++t) {
-        int r = k + lane + 32 * t;
-        if (r < n) { x[t] = ldcg_c(&col[r]); s = cfma_conj(v[r], x[t], s); }
+      for (int q = 0; q < QR_MAXT; ++q) {
+        int r = k + lane + 32 * q;
+        x[q] = cmake(0.0, 0.0);
+        if (r < n) { x[q] = ldcg_c(&col[r]); sp[q & 3] = cfma_conj(v[r], x[q], sp[q & 3]); }
       }
+      cplx s = cadd(cadd(sp[0], sp[1]), cadd(sp[2], sp[3]));
       s = warp_sum(s);
       cplx f = cmul(ctau, s);
-      double tail = 0.0;
+      double tp[4] = {0.0, 0.0, 0.0, 0.0};
       cplx xk = cmake(0.0, 0.0);
 #pragma unroll
-      for (int t = 0; t < QR_MAXT; ++t) {
-        int r = k + lane + 32 * t;
+      for (int q = 0; q < QR_MAXT; ++q) {
+        int r = k + lane + 32 * q;
         if (r < n) {
-          x[t] = csub(x[t], cmul(f, v[r]));
-          col[r] = x[t];
-          if (r == k) xk = x[t];
-          else tail += cabs2(x[t]);
+          x[q] = csub(x[q], cmul(f, v[r]));
+          col[r] = x[q];
+          if (q == 0 && lane == 0) xk = x[q];
+          else tp[q & 3] += cabs2(x[q]);
         }
       }
       xk = cmake(__shfl_sync(0xffffffffu, xk.x, 0), __shfl_sync(0xffffffffu, xk.y, 0));
-      tail = warp_sum(tail);
+      double tail = warp_sum((tp[0] + tp[1]) + (tp[2] + tp[3]));
       if (lane == 0) {
         double vn1 = __ldcg(&w.vn1[j]);
         if (vn1 != 0.0) {
@@ -281,13 +285,13 @@ __global__ void __launch_bounds__(256) k_apply_q_right(cplx* __restrict__ X, int
     if (tk.x == 0.0 && tk.y == 0.0) continue;
     if (conj_q) tk = cconj(tk);
     // X H = X - tau (X v) v^H
-    cplx d = cmake(0.0, 0.0);
+    cplx dp[4] = {cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0)};
 #pragma unroll
     for (int t = 0; t < QR_MAXT; ++t) {
       int c = lane + 32 * t;
-      if (c >= k && c < n) d = cfma(x[t], __ldg(&vk[c]), d);
+      if (c >= k && c < n) dp[t & 3] = cfma(x[t], __ldg(&vk[c]), dp[t & 3]);
     }
-    d = warp_sum(d);
+    cplx d = warp_sum(cadd(cadd(dp[0], dp[1]), cadd(dp[2], dp[3])));
     cplx f = cmul(tk, d);
 #pragma unroll
     for (int t = 0; t < QR_MAXT; ++t) {

@@ -5,13 +5,20 @@
 // src/interactions.jl:102-141 (interaction_matrix_exp_op!).
 //
 // One cooperative (co-resident) launch visits all N sites of the slice in
-// order.  Every CTA evaluates the 4x4 determinant ratio of the current site
-// redundantly from the same 16 entries of G, so all CTAs take the same
-// accept/reject decision without communicating.  On acceptance the rank-4
-// update G += A B, A = (G[:,c] - I[:,c]) M^-1 (n x 4), B = Delta G[r,:]
-// (4 x n), is split over the whole grid in two phases separated by grid
-// barriers (phase 1 forms A and B from the unmodified G, phase 2 writes G).
-// Rejected sites cost no barrier.
+// order.  Structure:
+//   * prologue: every CTA builds, for all sites in parallel, the 4x4 block
+//     Delta_i = e^{+dtau V(phi_i)} e^{-dtau V(phi_i + delta_i)} - I into shared
+//     memory (the old field of a site cannot change before its own visit);
+//   * per site, warp 0 of every CTA evaluates the ratio redundantly and
+//     identically from the same 16 entries of G: lanes build
+//     M = I + Delta (I - G_ii) entry-wise, 24 lanes form the permutation
+//     expansion of det M, and on acceptance 16 lanes form M^-1 = adj(M)/det;
+//     all CTAs therefore take the same decision without communicating;
+//   * on acceptance the rank-4 update G += A B, A = (G[:,c] - I[:,c]) M^-1
+//     (n x 4), B = Delta G[r,:] (4 x n), runs over the whole grid in two phases
+//     separated by grid barriers: phase 1 forms A and B from the unmodified G,
+//     phase 2 applies them with warp tiles of 128 rows x 4 columns (A held in
+//     registers, B broadcast).  Rejected sites cost no barrier.
 //
 // Proposal streams use fixed slots: delta[:, i] and unif[i] belong to site
 // i of this call; unif[i] decides only when p_acc <= 1, exactly as
@@ -21,218 +28,259 @@
 
 namespace {
 
-struct C4 { cplx a[4][4]; };
+// The 24 permutations of (0,1,2,3) and their signs, for det M.
+__constant__ unsigned char c_perm[24][4] = {
+    {0, 1, 2, 3}, {0, 1, 3, 2}, {0, 2, 1, 3}, {0, 2, 3, 1}, {0, 3, 1, 2}, {0, 3, 2, 1},
+    {1, 0, 2, 3}, {1, 0, 3, 2}, {1, 2, 0, 3}, {1, 2, 3, 0}, {1, 3, 0, 2}, {1, 3, 2, 0},
+    {2, 0, 1, 3}, {2, 0, 3, 1}, {2, 1, 0, 3}, {2, 1, 3, 0}, {2, 3, 0, 1}, {2, 3, 1, 0},
+    {3, 0, 1, 2}, {3, 0, 2, 1}, {3, 1, 0, 2}, {3, 1, 2, 0}, {3, 2, 0, 1}, {3, 2, 1, 0}};
+__constant__ signed char c_psign[24] = {1, -1, -1, 1, 1, -1, -1, 1, 1, -1, -1, 1,
+                                         1, -1, -1, 1, 1, -1, -1, 1, 1, -1, -1, 1};
 
-// exp(-power*dtau*V(op)) for one site (src/interactions.jl:102-141).
-__device__ void ev_block(const ModelConst& mc, const double op[3], double power, C4& e, EvEntry* entry) {
+// Interaction block parameters of exp(-power*dtau*V(op)) for one site
+// (src/interactions.jl:102-141): C, S, R with S, R scaled by `power`.
+__device__ __forceinline__ void ev_params(const ModelConst& mc, const double op[3], double power, double& C,
+                                          cplx& S, double& R, double& shn) {
   double nrm = sqrt(op[0] * op[0] + op[1] * op[1] + op[2] * op[2]);
   double a = mc.lambda * mc.dtau * nrm;
-  double shn = sinh(a) / nrm;
-  double C = cosh(a);
+  shn = sinh(a) / nrm;
+  C = cosh(a);
   double sh = power * shn;
-  cplx S = cmake(-op[0] * sh, op[1] * sh);
-  double R = -op[2] * sh;
-  cplx z = cmake(0.0, 0.0);
-  e.a[0][0] = cmake(C, 0); e.a[0][1] = S;         e.a[0][2] = z;              e.a[0][3] = cmake(R, 0);
-  e.a[1][0] = cconj(S);    e.a[1][1] = cmake(C, 0); e.a[1][2] = cmake(-R, 0); e.a[1][3] = z;
-  e.a[2][0] = z;           e.a[2][1] = cmake(-R, 0); e.a[2][2] = cmake(C, 0); e.a[2][3] = cconj(S);
-  e.a[3][0] = cmake(R, 0); e.a[3][1] = z;           e.a[3][2] = S;            e.a[3][3] = cmake(C, 0);
-  if (entry) { entry->C = C; entry->Sr = -op[0] * shn; entry->Si = op[1] * shn; entry->R = -op[2] * shn; }
+  S = cmake(-op[0] * sh, op[1] * sh);
+  R = -op[2] * sh;
 }
 
-__device__ void mat4_mul(const C4& A, const C4& B, C4& Cm) {
-  for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 4; ++j) {
-      cplx s = cmake(0, 0);
-      for (int k = 0; k < 4; ++k) s = cfma(A.a[i][k], B.a[k][j], s);
-      Cm.a[i][j] = s;
-    }
+// Entry (r, c) of the block [[C,S,0,R],[S*,C,-R,0],[0,-R,C,S*],[R,0,S,C]].
+__device__ __forceinline__ cplx ev_entry(int r, int c, double C, cplx S, double R) {
+  const int code = r * 4 + c;
+  switch (code) {
+    case 0: case 5: case 10: case 15: return cmake(C, 0.0);
+    case 1: case 14: return S;
+    case 4: case 11: return cconj(S);
+    case 3: case 12: return cmake(R, 0.0);
+    case 6: case 9: return cmake(-R, 0.0);
+    default: return cmake(0.0, 0.0);
+  }
 }
 
-// LU with partial pivoting: determinant and (optionally) inverse of a 4x4.
-__device__ cplx mat4_det_inv(const C4& Min, C4* inv, bool* singular) {
-  C4 A = Min;
-  int piv[4] = {0, 1, 2, 3};
-  cplx det = cmake(1.0, 0.0);
-  *singular = false;
-  for (int k = 0; k < 4; ++k) {
-    int p = k;
-    double best = cabs2(A.a[k][k]);
-    for (int r = k + 1; r < 4; ++r) {
-      double v = cabs2(A.a[r][k]);
-      if (v > best) { best = v; p = r; }
-    }
-    if (best == 0.0) { *singular = true; return cmake(0, 0); }
-    if (p != k) {
-      for (int c = 0; c < 4; ++c) { cplx t = A.a[k][c]; A.a[k][c] = A.a[p][c]; A.a[p][c] = t; }
-      int t = piv[k]; piv[k] = piv[p]; piv[p] = t;
-      det = cmake(-det.x, -det.y);
-    }
-    det = cmul(det, A.a[k][k]);
-    for (int r = k + 1; r < 4; ++r) {
-      cplx l = cdiv(A.a[r][k], A.a[k][k]);
-      A.a[r][k] = l;
-      for (int c = k + 1; c < 4; ++c) A.a[r][c] = csub(A.a[r][c], cmul(l, A.a[k][c]));
-    }
-  }
-  if (inv) {
-    // solve A X = P I column by column
-    for (int col = 0; col < 4; ++col) {
-      cplx y[4];
-      for (int r = 0; r < 4; ++r) y[r] = cmake(piv[r] == col ? 1.0 : 0.0, 0.0);
-      for (int r = 0; r < 4; ++r)
-        for (int c = 0; c < r; ++c) y[r] = csub(y[r], cmul(A.a[r][c], y[c]));
-      for (int r = 3; r >= 0; --r) {
-        for (int c = r + 1; c < 4; ++c) y[r] = csub(y[r], cmul(A.a[r][c], y[c]));
-        y[r] = cdiv(y[r], A.a[r][r]);
-      }
-      for (int r = 0; r < 4; ++r) inv->a[r][col] = y[r];
-    }
-  }
-  return det;
+__device__ __forceinline__ cplx shfl_c(cplx v, int src) {
+  return cmake(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
 
 struct SiteDecision {
   int accepted;
-  double newop[3];
-  double dS;
-  double exp_dS;
-  cplx det;
-  double pacc;
-  EvEntry ev_new;
-  C4 delta;
-  C4 minv;
+  cplx minv[4][4];
 };
 
-__global__ void __launch_bounds__(256) k_local_updates(LocalUpdateArgs a) {
+constexpr int LU_THREADS = 256;
+
+__global__ void __launch_bounds__(LU_THREADS, 2) k_local_updates(LocalUpdateArgs a) {
   const ModelConst& mc = a.mc;
   const int N = mc.N, n = mc.n, M = mc.M, L = mc.L;
   const int l = a.slice0;
-  extern __shared__ double smem_local[];
-  double* phis = smem_local;  // (3, N): this CTA's copy of phi[:, :, l]
+  extern __shared__ double4_16a smem_local[];
+  cplx* delta_all = reinterpret_cast<cplx*>(smem_local);           // (N, 16): Delta_i row-major
+  EvEntry* evnew = reinterpret_cast<EvEntry*>(delta_all + 16 * N);  // (N): entries of the proposed field
+  double* phis = reinterpret_cast<double*>(evnew + N);              // (3, N): this CTA's copy of phi[:, :, l]
   __shared__ SiteDecision dec;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 
+  // ---- prologue: field copy and Delta_i for every site ----
   for (int k = threadIdx.x; k < 3 * N; k += blockDim.x) phis[k] = a.phi[(size_t)3 * N * l + k];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const double* po = &a.phi[((size_t)N * l + i) * 3];
+    double old[3] = {po[0], po[1], po[2]};
+    double nw[3] = {old[0] + a.delta[3 * i], old[1] + a.delta[3 * i + 1], old[2] + a.delta[3 * i + 2]};
+    double C1, R1, s1, C2, R2, s2;
+    cplx S1, S2;
+    ev_params(mc, old, -1.0, C1, S1, R1, s1);
+    ev_params(mc, nw, 1.0, C2, S2, R2, s2);
+    EvEntry e;
+    e.C = C2; e.Sr = -nw[0] * s2; e.Si = nw[1] * s2; e.R = -nw[2] * s2;
+    evnew[i] = e;
+    for (int r = 0; r < 4; ++r)
+      for (int c = 0; c < 4; ++c) {
+        cplx s = cmake(0.0, 0.0);
+        for (int k = 0; k < 4; ++k) s = cfma(ev_entry(r, k, C1, S1, R1), ev_entry(k, c, C2, S2, R2), s);
+        if (r == c) s.x -= 1.0;
+        delta_all[16 * i + 4 * r + c] = s;
+      }
+  }
   __syncthreads();
   const int lt_later = (l + 1) % M, lt_earlier = (l - 1 + M) % M;
-  const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const size_t gthreads = (size_t)gridDim.x * blockDim.x;
+  const int gwarp = blockIdx.x * (LU_THREADS / 32) + wid;
+  const int nwarps = gridDim.x * (LU_THREADS / 32);
 
   for (int i = 0; i < N; ++i) {
-    if (threadIdx.x == 0) {
-      // ---- boson action difference (src/action.jl:57-100) ----
-      double old[3] = {phis[3 * i], phis[3 * i + 1], phis[3 * i + 2]};
-      double nw[3];
-      for (int c = 0; c < 3; ++c) nw[c] = old[c] + a.delta[3 * i + c];
-      double diff[3] = {nw[0] - old[0], nw[1] - old[1], nw[2] - old[2]};
-      double old_sq = old[0] * old[0] + old[1] * old[1] + old[2] * old[2];
-      double new_sq = nw[0] * nw[0] + nw[1] * nw[1] + nw[2] * nw[2];
-      double sq_diff = new_sq - old_sq;
-      double pow4_diff = new_sq * new_sq - old_sq * old_sq;
-      const double* pe = (lt_earlier == l) ? &phis[3 * i] : &a.phi[((size_t)N * lt_earlier + i) * 3];
-      const double* pl = (lt_later == l) ? &phis[3 * i] : &a.phi[((size_t)N * lt_later + i) * 3];
-      int y = i % L, x = i / L;
-      int nbs[4] = {(y + 1) % L + L * x, y + L * ((x + 1) % L), (y - 1 + L) % L + L * x,
-                    y + L * ((x - 1 + L) % L)};
-      double tdot = 0.0, sdot = 0.0;
-      for (int c = 0; c < 3; ++c) {
-        double ot = pl[c] + pe[c];
-        double os = 0.0;
-        for (int q = 0; q < 4; ++q) os = os + phis[3 * nbs[q] + c];
-        tdot += ot * diff[c];
-        sdot += os * diff[c];
-      }
+    if (wid == 0) {
+      // ---- boson action difference (src/action.jl:57-100), lane 0 ----
       double dS = 0.0;
-      dS += 1.0 / (mc.dtau * mc.c * mc.c) * (sq_diff - tdot);
-      dS += 0.5 * mc.dtau * (4 * sq_diff - 2.0 * sdot);
-      dS += mc.dtau * (0.5 * mc.r * sq_diff + 0.25 * mc.u * pow4_diff);
-      double exp_dS = exp(-dS);
-      // ---- determinant ratio (src/local_updates.jl:42-59) ----
-      C4 e1, e2, d, Gii, Mm;
-      ev_block(mc, old, -1.0, e1, nullptr);
-      EvEntry evn;
-      ev_block(mc, nw, 1.0, e2, &evn);
-      mat4_mul(e1, e2, d);
-      for (int r = 0; r < 4; ++r) d.a[r][r] = csub(d.a[r][r], cmake(1.0, 0.0));
-      for (int r = 0; r < 4; ++r)
-        for (int c = 0; c < 4; ++c) {
-          cplx g = ldcg_c(&a.G[(size_t)(i + c * N) * n + i + r * N]);
-          Gii.a[r][c] = cmake((r == c ? 1.0 : 0.0) - g.x, -g.y);   // I - G_ii
+      if (lane == 0) {
+        double old[3] = {phis[3 * i], phis[3 * i + 1], phis[3 * i + 2]};
+        double nw[3];
+        for (int c = 0; c < 3; ++c) nw[c] = old[c] + a.delta[3 * i + c];
+        double diff[3] = {nw[0] - old[0], nw[1] - old[1], nw[2] - old[2]};
+        double old_sq = old[0] * old[0] + old[1] * old[1] + old[2] * old[2];
+        double new_sq = nw[0] * nw[0] + nw[1] * nw[1] + nw[2] * nw[2];
+        double sq_diff = new_sq - old_sq;
+        double pow4_diff = new_sq * new_sq - old_sq * old_sq;
+        const double* pe = (lt_earlier == l) ? &phis[3 * i] : &a.phi[((size_t)N * lt_earlier + i) * 3];
+        const double* pl = (lt_later == l) ? &phis[3 * i] : &a.phi[((size_t)N * lt_later + i) * 3];
+        int y = i % L, x = i / L;
+        int nbs[4] = {(y + 1) % L + L * x, y + L * ((x + 1) % L), (y - 1 + L) % L + L * x,
+                      y + L * ((x - 1 + L) % L)};
+        double tdot = 0.0, sdot = 0.0;
+        for (int c = 0; c < 3; ++c) {
+          double ot = pl[c] + pe[c];
+          double os = 0.0;
+          for (int q = 0; q < 4; ++q) os = os + phis[3 * nbs[q] + c];
+          tdot += ot * diff[c];
+          sdot += os * diff[c];
         }
-      mat4_mul(d, Gii, Mm);
-      for (int r = 0; r < 4; ++r) Mm.a[r][r] = cadd(Mm.a[r][r], cmake(1.0, 0.0));
-      bool singular;
-      C4 minv;
-      cplx det = mat4_det_inv(Mm, &minv, &singular);
-      double pacc = exp_dS * det.x;
-      double u = a.unif[i];
-      int acc = (pacc > 1.0 || u < pacc) ? 1 : 0;
-      if (singular || !isfinite(det.x) || !isfinite(det.y)) {
-        acc = 0;
-        if (blockIdx.x == 0) atomicOr(a.err, singular ? DQMC_KERR_SINGULAR : DQMC_KERR_NONFINITE);
+        dS += 1.0 / (mc.dtau * mc.c * mc.c) * (sq_diff - tdot);
+        dS += 0.5 * mc.dtau * (4 * sq_diff - 2.0 * sdot);
+        dS += mc.dtau * (0.5 * mc.r * sq_diff + 0.25 * mc.u * pow4_diff);
       }
-      dec.accepted = acc;
-      for (int c = 0; c < 3; ++c) dec.newop[c] = nw[c];
-      dec.dS = dS;
-      dec.exp_dS = exp_dS;
-      dec.det = det;
-      dec.pacc = pacc;
-      dec.ev_new = evn;
-      dec.delta = d;
-      dec.minv = minv;
-      if (acc) { phis[3 * i] = nw[0]; phis[3 * i + 1] = nw[1]; phis[3 * i + 2] = nw[2]; }
-      if (blockIdx.x == 0) {
-        if (a.acc_out) a.acc_out[i] = (uint8_t)acc;
-        if (a.det_out) a.det_out[i] = det;
-        if (a.pacc_out) a.pacc_out[i] = pacc;
+      dS = __shfl_sync(0xffffffffu, dS, 0);
+      // ---- M = I + Delta (I - G_ii), lane 4r+c holds M[r][c] (src/local_updates.jl:49-55) ----
+      const int r = (lane >> 2) & 3, c = lane & 3;
+      cplx g = cmake(0.0, 0.0);
+      if (lane < 16) g = ldcg_c(&a.G[(size_t)(i + c * N) * n + i + r * N]);
+      cplx mt = cmake((r == c ? 1.0 : 0.0) - g.x, -g.y);   // (I - G_ii)[r][c]
+      cplx m = cmake(r == c ? 1.0 : 0.0, 0.0);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        cplx mtk = shfl_c(mt, 4 * k + c);                  // (I - G_ii)[k][c]
+        m = cfma(delta_all[16 * i + 4 * r + k], mtk, m);
+      }
+      // ---- det M by the permutation expansion (24 lanes) ----
+      cplx term = cmake(0.0, 0.0);
+      {
+        const int j = lane < 24 ? lane : 0;
+        cplx p = cmake(1.0, 0.0);
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr) p = cmul(p, shfl_c(m, 4 * rr + c_perm[j][rr]));
+        if (lane < 24) term = cscale(p, (double)c_psign[j]);
+      }
+      cplx det = term;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) det = cadd(det, shfl_c(det, lane ^ o));
+      // lanes associate the sum differently; lane 0's value (the same in every
+      // CTA) is the one every lane uses, so all decisions agree bit for bit
+      det = shfl_c(det, 0);
+      const double exp_dS = exp(-dS);
+      const double pacc = exp_dS * det.x;
+      const double u = a.unif[i];
+      int acc = (pacc > 1.0 || u < pacc) ? 1 : 0;
+      const bool bad = !isfinite(det.x) || !isfinite(det.y) || (det.x == 0.0 && det.y == 0.0);
+      if (bad) acc = 0;
+      // ---- M^-1 = adj(M) / det (lanes 4r+c: entry [r][c] = cofactor C[c][r] / det) ----
+      if (acc) {
+        // minor of M without row c and column r
+        int rows[3], cols[3];
+        for (int t = 0, q = 0; t < 4; ++t) if (t != c) rows[q++] = t;
+        for (int t = 0, q = 0; t < 4; ++t) if (t != r) cols[q++] = t;
+        cplx e[3][3];
+#pragma unroll
+        for (int u3 = 0; u3 < 3; ++u3)
+#pragma unroll
+          for (int v3 = 0; v3 < 3; ++v3) e[u3][v3] = shfl_c(m, (4 * rows[u3] + cols[v3]) & 31);
+        cplx d3 = csub(cmul(e[0][0], csub(cmul(e[1][1], e[2][2]), cmul(e[1][2], e[2][1]))),
+                       cmul(e[0][1], csub(cmul(e[1][0], e[2][2]), cmul(e[1][2], e[2][0]))));
+        d3 = cadd(d3, cmul(e[0][2], csub(cmul(e[1][0], e[2][1]), cmul(e[1][1], e[2][0]))));
+        if ((r + c) & 1) d3 = cmake(-d3.x, -d3.y);
+        if (lane < 16) dec.minv[r][c] = cdiv(d3, det);
+      }
+      if (lane == 0) {
+        dec.accepted = acc;
         if (acc) {
-          double* pg = &a.phi[((size_t)N * l + i) * 3];
-          pg[0] = nw[0]; pg[1] = nw[1]; pg[2] = nw[2];
-          if (a.evtab) reinterpret_cast<EvEntry*>(a.evtab)[(size_t)N * l + i] = evn;
-          *a.action += -log(exp_dS);
-          *a.n_acc += 1;
+          for (int q = 0; q < 3; ++q) phis[3 * i + q] += a.delta[3 * i + q];
+        }
+        if (blockIdx.x == 0) {
+          if (bad) atomicOr(a.err, DQMC_KERR_NONFINITE);
+          if (a.acc_out) a.acc_out[i] = (uint8_t)acc;
+          if (a.det_out) a.det_out[i] = det;
+          if (a.pacc_out) a.pacc_out[i] = pacc;
+          if (acc) {
+            double* pg = &a.phi[((size_t)N * l + i) * 3];
+            pg[0] = phis[3 * i]; pg[1] = phis[3 * i + 1]; pg[2] = phis[3 * i + 2];
+            if (a.evtab) reinterpret_cast<EvEntry*>(a.evtab)[(size_t)N * l + i] = evnew[i];
+            *a.action += -log(exp_dS);
+            *a.n_acc += 1;
+          }
         }
       }
     }
     __syncthreads();
     const int accepted = dec.accepted;
-    // every thread has read the decision before thread 0 may overwrite it
-    __syncthreads();
-    if (!accepted) continue;
-
+    if (!accepted) {
+      __syncthreads();   // every thread has read the decision before warp 0 overwrites it
+      continue;
+    }
     // ---- phase 1: A = (G[:, cols] - I[:, cols]) M^-1, B = Delta G[rows, :] ----
-    for (size_t t = gtid; t < (size_t)2 * n; t += gthreads) {
-      if (t < (size_t)n) {
-        int r = (int)t;
+    const cplx* Dl = &delta_all[16 * i];
+    for (int t = blockIdx.x * LU_THREADS + threadIdx.x; t < 2 * n; t += gridDim.x * LU_THREADS) {
+      if (t < n) {
+        const int row = t;
         cplx g[4];
+#pragma unroll
         for (int k = 0; k < 4; ++k) {
-          g[k] = ldcg_c(&a.G[(size_t)(i + k * N) * n + r]);
-          if (r == i + k * N) g[k].x -= 1.0;
+          g[k] = ldcg_c(&a.G[(size_t)(i + k * N) * n + row]);
+          if (row == i + k * N) g[k].x -= 1.0;
         }
+#pragma unroll
         for (int c = 0; c < 4; ++c) {
           cplx s = cmake(0, 0);
-          for (int k = 0; k < 4; ++k) s = cfma(g[k], dec.minv.a[k][c], s);
-          a.Acol[(size_t)c * n + r] = s;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) s = cfma(g[k], dec.minv[k][c], s);
+          a.Acol[(size_t)c * n + row] = s;
         }
       } else {
-        int col = (int)(t - n);
+        const int col = t - n;
         cplx g[4];
+#pragma unroll
         for (int k = 0; k < 4; ++k) g[k] = ldcg_c(&a.G[(size_t)col * n + i + k * N]);
+#pragma unroll
         for (int r = 0; r < 4; ++r) {
           cplx s = cmake(0, 0);
-          for (int k = 0; k < 4; ++k) s = cfma(dec.delta.a[r][k], g[k], s);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) s = cfma(Dl[4 * r + k], g[k], s);
           a.Brow[(size_t)r * n + col] = s;
         }
       }
     }
     if (!grid_barrier(a.bar, a.err)) return;
-    // ---- phase 2: G += A B (src/local_updates.jl:86-91) ----
-    const size_t total = (size_t)n * n;
-    for (size_t e = gtid; e < total; e += gthreads) {
-      int col = (int)(e / n), r = (int)(e - (size_t)col * n);
-      cplx acc = ldcg_c(&a.G[e]);
-      for (int k = 0; k < 4; ++k) acc = cfma(ldcg_c(&a.Acol[(size_t)k * n + r]), ldcg_c(&a.Brow[(size_t)k * n + col]), acc);
-      a.G[e] = acc;
+    // ---- phase 2: G += A B over warp tiles of 128 rows x 4 columns ----
+    const int tiles_r = (n + 127) / 128, tiles_c = (n + 3) / 4;
+    for (int tile = gwarp; tile < tiles_r * tiles_c; tile += nwarps) {
+      const int tr = tile % tiles_r, tc = tile / tiles_r;
+      const int r0 = tr * 128 + lane, c0 = tc * 4;
+      cplx Av[4][4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int row = r0 + 32 * q;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) Av[q][k] = row < n ? ldcg_c(&a.Acol[(size_t)k * n + row]) : cmake(0, 0);
+      }
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) {
+        const int col = c0 + cc;
+        if (col >= n) break;
+        cplx Bv[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) Bv[k] = ldcg_c(&a.Brow[(size_t)k * n + col]);
+        cplx* gcol = a.G + (size_t)col * n;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int row = r0 + 32 * q;
+          if (row < n) {
+            cplx v = ldcg_c(&gcol[row]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) v = cfma(Av[q][k], Bv[k], v);
+            gcol[row] = v;
+          }
+        }
+      }
     }
     if (!grid_barrier(a.bar, a.err)) return;
   }
@@ -241,16 +289,26 @@ __global__ void __launch_bounds__(256) k_local_updates(LocalUpdateArgs a) {
 }  // namespace
 
 cudaError_t launch_local_updates(const LocalUpdateArgs& a, int sm_count, cudaStream_t st) {
-  size_t smem = (size_t)3 * a.mc.N * sizeof(double);
+  const size_t smem = (size_t)a.mc.N * (16 * sizeof(cplx) + sizeof(EvEntry)) + (size_t)3 * a.mc.N * sizeof(double);
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_local_updates, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  if (smem > 100 * 1024) return cudaErrorInvalidValue;
   int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local_updates, 256, smem);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local_updates, LU_THREADS, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   if (per_sm > 2) per_sm = 2;
   int grid = sm_count * per_sm;
-  size_t need = ((size_t)a.mc.n * a.mc.n + 255) / 256;
-  if ((size_t)grid > need) grid = (int)need < 1 ? 1 : (int)need;
+  // small matrices: no more CTAs than warp tiles of the update
+  const int n = a.mc.n;
+  const int tiles = ((n + 127) / 128) * ((n + 3) / 4);
+  const int need = (tiles + (LU_THREADS / 32) - 1) / (LU_THREADS / 32);
+  if (grid > need) grid = need < 1 ? 1 : need;
   LocalUpdateArgs copy = a;
   void* args[] = {&copy};
-  return cudaLaunchCooperativeKernel((void*)k_local_updates, dim3(grid), dim3(256), args, smem, st);
+  return cudaLaunchCooperativeKernel((void*)k_local_updates, dim3(grid), dim3(LU_THREADS), args, smem, st);
 }
