@@ -212,7 +212,7 @@ def run_ours(args, world, rank, local):
     torch.cuda.set_device(dev)
     mp = api.ModelParams(L=L, slices=M, safe_mult=rp.safe_mult, delta_tau=rp.delta_tau, lambda_=rp.lambda_,
                          r=rp.r, c=rp.c, u=rp.u, mu1=rp.mu1, mu2=rp.mu2, hoppings=rp.hoppings, box=rp.box,
-                         all_checks=not args.no_checks, device=dev)
+                         all_checks=not args.no_checks, device=dev, precision=args.precision, delay=args.delay)
     N, n = rp.N, rp.n
     phi = synthetic_field(N, M, 1000 + rank)
     sweeps = args.warmup + args.steps
@@ -309,10 +309,11 @@ def run_ours(args, world, rank, local):
         line = {
             "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_s * 1000.0 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f64 + split-bf16 tensor GEMMs",
             "data": "synthetic (seeded uniform[-1,1] fields, uniform proposal/Metropolis streams)",
             "config": {"workload": desc, "L": L, "slices": M, "n": n, "safe_mult": 10, "chains_per_gpu": 1,
-                       "precision": "fp64", "parallelism": f"replicas x{world}",
+                       "precision": args.precision, "delay": args.delay, "parallelism": f"replicas x{world}",
                        "l2": "working set > L2 (stack 2x21x16.8 MB) and 256 MB L2 flush before each sweep"},
             "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": int(M * 4 * N * 8),
                     "d2h_bytes_per_step": int(M * N), "steps": e2e_steps},
@@ -345,6 +346,8 @@ def main():
     ap.add_argument("--cpu-calls", type=int, default=10)
     ap.add_argument("--ref-calls", type=int, default=2)
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--delay", type=int, default=16, help="delayed-update depth k (1 = immediate rank-4)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

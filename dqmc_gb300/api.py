@@ -37,7 +37,7 @@ class CParams(ctypes.Structure):
                 ("r", ctypes.c_double), ("c", ctypes.c_double), ("u", ctypes.c_double),
                 ("mu1", ctypes.c_double), ("mu2", ctypes.c_double), ("hoppings", ctypes.c_double * 4),
                 ("all_checks", ctypes.c_int32), ("precision", ctypes.c_int32), ("device", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 5)]
+                ("ozaki_bits", ctypes.c_int32), ("delay", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
 
 class CStats(ctypes.Structure):
@@ -45,12 +45,14 @@ class CStats(ctypes.Structure):
                 ("max_instability", ctypes.c_double), ("device_ms", ctypes.c_double)]
 
 
-KERNEL_KINDS = ["slice_cols", "slice_rows", "local_updates", "zgemm", "qrp", "apply_q", "trsm", "misc"]
+KERNEL_KINDS = ["slice_cols", "slice_rows", "local_updates", "zgemm", "qrp", "apply_q", "trsm", "misc",
+                "ozaki_gemm", "flush"]
+NK = len(KERNEL_KINDS)
 
 
 class CTiming(ctypes.Structure):
-    _fields_ = [("ms", ctypes.c_double * 8), ("launches", ctypes.c_int64 * 8), ("flops", ctypes.c_double * 8),
-                ("bytes", ctypes.c_double * 8), ("kernel_launches", ctypes.c_int64)]
+    _fields_ = [("ms", ctypes.c_double * NK), ("launches", ctypes.c_int64 * NK), ("flops", ctypes.c_double * NK),
+                ("bytes", ctypes.c_double * NK), ("kernel_launches", ctypes.c_int64)]
 
 
 # every symbol the header declares, with its argument types
@@ -86,6 +88,7 @@ SIGNATURES = {
     "dqmc_get_timing": ([_P, ctypes.POINTER(CTiming)], ctypes.c_int),
     "dqmc_reset_timing": ([_P, _I32], ctypes.c_int),
     "dqmc_peak_fp64": ([_I32, _D], ctypes.c_int),
+    "dqmc_gemm_check": ([_P, _I32, _D, _D, _D], ctypes.c_int),
     "dqmc_local_updates_noalloc": ([ctypes.POINTER(CParams), ctypes.c_void_p, ctypes.c_void_p, _I32,
                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p], ctypes.c_int),
@@ -128,6 +131,9 @@ class ModelParams:
     box: float = 0.2
     all_checks: bool = True
     device: int = -1
+    precision: str = "fp64"        # "fp64" or "mixed"
+    ozaki_bits: int = 0            # mantissa bits per GEMM operand in the mixed form (0 = default 35)
+    delay: int = 0                 # delayed-update depth (0/1 = immediate rank-4)
 
     @property
     def N(self):
@@ -145,8 +151,10 @@ class ModelParams:
         for k in range(4):
             p.hoppings[k] = self.hoppings[k]
         p.all_checks = 1 if self.all_checks else 0
-        p.precision = 0
+        p.precision = {"fp64": 0, "mixed": 1}[self.precision]
         p.device = self.device
+        p.ozaki_bits = self.ozaki_bits
+        p.delay = self.delay
         return p
 
 
@@ -368,6 +376,15 @@ class DQMC:
         occ, ek = ctypes.c_double(), ctypes.c_double()
         self._check(self.lib.dqmc_measure(self.h, G.ctypes.data_as(_D), ctypes.byref(occ), ctypes.byref(ek)))
         return dict(greens=G, occupation=occ.value, e_kin=ek.value)
+
+    def gemm_check(self, A, B, mode):
+        """C = A B with the FP64 kernel (mode 0) or the split-BF16 GEMM (mode 1)."""
+        n = self.n
+        A, B = _cplx_in(A, n), _cplx_in(B, n)
+        C = np.zeros((n, n), dtype=np.complex128, order="F")
+        self._check(self.lib.dqmc_gemm_check(self.h, int(mode), A.ctypes.data_as(_D), B.ctypes.data_as(_D),
+                                             C.ctypes.data_as(_D)))
+        return C
 
     def timing(self):
         """Per kernel kind: device ms, launches, algorithmic flops and bytes."""

@@ -14,7 +14,7 @@
 #include "common.cuh"
 #include "kernels.h"
 
-#define DQMC_VERSION_STRING "dqmc_gb300 0.1 (sm_103a, FP64)"
+#define DQMC_VERSION_STRING "dqmc_gb300 0.2 (sm_103a, FP64 + split-BF16 tensor-core form)"
 
 struct TimedSpan {
   cudaEvent_t a, b;
@@ -42,6 +42,10 @@ struct dqmc_handle {
   double *D1 = nullptr, *d2 = nullptr;
   int* ord1 = nullptr;
   QRWork qr{};
+  // mixed form: split-BF16 GEMM scratch and slicing
+  void* oz_scratch = nullptr;
+  size_t oz_bytes = 0;
+  int oz_target = 35;   // mantissa bits kept per operand
   // local updates
   double* delta_d = nullptr;
   double* unif_d = nullptr;
@@ -54,6 +58,11 @@ struct dqmc_handle {
   int* nacc_d = nullptr;
   cplx* Acol = nullptr;
   cplx* Brow = nullptr;
+  // delayed updates: pending factors and {next site, pending count}
+  int delay = 1;
+  cplx* Xd = nullptr;
+  cplx* Yd = nullptr;
+  int* dstate = nullptr;
   GridBarrier* bar = nullptr;
   int* err_d = nullptr;
   double* scal_d = nullptr;    // scratch scalars: [0] logdet sum, [1] absdiff
@@ -219,12 +228,32 @@ int wrap_greens(dqmc_handle* h, cplx* gf, int slice, int direction) {
 }
 
 // ---- dense kernels with their work models ----------------------------------
+// tensor flops of one split-BF16 complex GEMM: S(S+1)/2 slice pairs x 2 real GEMMs with K' = 2K
+double ozaki_tensor_flops(double m, double nn, double k, int S) {
+  const double kp = 2.0 * std::ceil(k / 16.0) * 16.0;
+  return S * (S + 1) / 2.0 * 2.0 * 2.0 * m * nn * kp;
+}
+int zgemm_general(dqmc_handle* h, int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
+                  const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rs, const double* cs,
+                  bool allow_split, int kind = -1, const int* active = nullptr) {
+  if (allow_split && h->p.precision == DQMC_PREC_MIXED) {
+    int S = 0, bits = 0;
+    if (!ozaki_plan(k, h->oz_target, &S, &bits)) return set_err(h, DQMC_ERR_ARG, "no exact slicing for this K");
+    LAUNCH(kind >= 0 ? kind : DQMC_K_OZGEMM, ozaki_tensor_flops(m, nn, k, S), gemm_bytes(m, nn, k),
+           launch_ozaki_zgemm(m, nn, k, opA, opB, alpha, A, lda, B, ldb, beta, C, ldc, rs, cs, S, bits,
+                              h->oz_scratch, h->oz_bytes, h->st, active));
+    h->launches += 2;   // the two slicing kernels
+    return DQMC_OK;
+  }
+  LAUNCH(kind >= 0 ? kind : DQMC_K_GEMM, gemm_flops(m, nn, k), gemm_bytes(m, nn, k),
+         launch_zgemm(m, nn, k, opA, opB, alpha, A, lda, B, ldb, beta, C, ldc, rs, cs, h->st, active));
+  return DQMC_OK;
+}
+// n x n x n product of the stabilisation (split-BF16 in the mixed form)
 int gemm(dqmc_handle* h, char opA, char opB, const cplx* A, const cplx* B, cplx* C, const double* rs = nullptr,
          const double* cs = nullptr) {
   const int n = h->n;
-  LAUNCH(DQMC_K_GEMM, gemm_flops(n, n, n), gemm_bytes(n, n, n),
-         launch_zgemm(n, n, n, opA, opB, cmake(1, 0), A, n, B, n, cmake(0, 0), C, n, rs, cs, h->st));
-  return DQMC_OK;
+  return zgemm_general(h, n, n, n, opA, opB, cmake(1, 0), A, n, B, n, cmake(0, 0), C, n, rs, cs, true);
 }
 // pivoted QR of A (destroyed) -> T (physical layout), D; reflectors in h->qr
 int qrp(dqmc_handle* h, cplx* A, cplx* T, double* D) {
@@ -491,7 +520,11 @@ int ensure_out_capacity(dqmc_handle* h, int calls) {
 }
 
 // local_updates (src/local_updates.jl:1-38) on device streams; outputs to
-// device arrays (may be null).
+// device arrays (may be null).  delay <= 1: immediate rank-4 updates in one
+// cooperative launch.  delay = k > 1: rounds of [local kernel until k accepts
+// are pending, flush G += X Y (FP64 or split-BF16 GEMM), factor reset]; the
+// number of rounds is the bound ceil(N/k) + 1 and rounds with nothing left
+// return at once on a device-side flag, so the host never waits.
 int local_updates_dev(dqmc_handle* h, const double* delta_dev, const double* unif_dev, uint8_t* acc_dev,
                       cplx* det_dev, double* pacc_dev) {
   if (h->current_slice < 1 || h->current_slice > h->M)
@@ -513,9 +546,24 @@ int local_updates_dev(dqmc_handle* h, const double* delta_dev, const double* uni
   a.bar = h->bar;
   a.err = h->err_d;
   a.mc = h->mc;
-  // flops/bytes of the local updates depend on the acceptances; the caller
-  // derives them from the accepted count (32 n^2 flops and bytes per accept)
-  LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_updates(a, h->sm_count, h->st));
+  if (h->delay <= 1) {
+    // flops/bytes of the local updates depend on the acceptances; the caller
+    // derives them from the accepted count (32 n^2 flops and bytes per accept)
+    LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_updates(a, h->sm_count, h->st));
+    return DQMC_OK;
+  }
+  const int n = h->n, k = h->delay;
+  DelayedArgs d{h->Xd, h->Yd, h->dstate, k};
+  CU(cudaMemsetAsync(h->dstate, 0, 2 * sizeof(int), h->st));
+  const int rounds = (h->N + k - 1) / k + 1;
+  for (int r = 0; r < rounds; ++r) {
+    LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_delayed(a, d, h->sm_count, h->st));
+    // flush G += X Y, skipped on the device when no update is pending
+    CHK(zgemm_general(h, n, n, 4 * k, 'N', 'T', cmake(1, 0), h->Xd, n, h->Yd, n, cmake(1, 0), h->G, n, nullptr,
+                      nullptr, true, DQMC_K_FLUSH, h->dstate + 1));
+    LAUNCH(DQMC_K_MISC, 0.0, 0.0, launch_delayed_reset(d, n, h->st));
+    h->launches++;
+  }
   return DQMC_OK;
 }
 
@@ -532,7 +580,7 @@ void free_all(dqmc_handle* h) {
                   h->Tr, h->Dl, h->Dr, h->W1, h->W2, h->W3, h->W4, h->D1, h->d2, h->ord1, h->qr.vn1,
                   h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->delta_d, h->unif_d,
                   h->acc_d, h->det_d, h->pacc_d, h->action_d, h->nacc_d, h->Acol, h->Brow, h->bar, h->err_d,
-                  h->scal_d};
+                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   for (auto e : h->event_pool) cudaEventDestroy(e);
@@ -588,7 +636,8 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
   if (p->L < 2 || p->L % 2 != 0) return DQMC_ERR_ARG;                 // CBAssaad needs even L
   if (p->slices < 1 || p->safe_mult < 1 || p->slices % p->safe_mult != 0) return DQMC_ERR_ARG;
   if (p->opdim != 3) return DQMC_ERR_ARG;
-  if (p->precision != DQMC_PREC_FP64) return DQMC_ERR_ARG;
+  if (p->precision != DQMC_PREC_FP64 && p->precision != DQMC_PREC_MIXED) return DQMC_ERR_ARG;
+  if (p->ozaki_bits < 0 || p->ozaki_bits > 60 || p->delay < 0 || p->delay > 64) return DQMC_ERR_ARG;
   if (4 * p->L * p->L > 1024) return DQMC_ERR_ARG;                     // register-resident QR columns
   if (p->device >= 0 && cudaSetDevice(p->device) != cudaSuccess) return DQMC_ERR_CUDA;
   dqmc_handle* h = new dqmc_handle();
@@ -628,6 +677,25 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
   A((void**)&h->Acol, 4 * n * sizeof(cplx)); A((void**)&h->Brow, 4 * n * sizeof(cplx));
   A((void**)&h->bar, sizeof(GridBarrier)); A((void**)&h->err_d, sizeof(int));
   A((void**)&h->scal_d, 8 * sizeof(double));
+  h->delay = p->delay > 1 ? p->delay : 1;
+  if (h->delay > 1) {
+    A((void**)&h->Xd, (size_t)4 * h->delay * n * sizeof(cplx));
+    A((void**)&h->Yd, (size_t)4 * h->delay * n * sizeof(cplx));
+    A((void**)&h->dstate, 2 * sizeof(int));
+  }
+  if (p->precision == DQMC_PREC_MIXED) {
+    h->oz_target = p->ozaki_bits > 0 ? p->ozaki_bits : 35;
+    // the largest products are n x n x n; the flush (K = 4k) needs fewer slices
+    int S = 0, bits = 0;
+    if (!ozaki_plan((int)n, h->oz_target, &S, &bits)) return fail(DQMC_ERR_ARG);
+    size_t need = ozaki_scratch_bytes((int)n, (int)n, (int)n, S);
+    if (h->delay > 1 && ozaki_plan(4 * h->delay, h->oz_target, &S, &bits)) {
+      size_t f = ozaki_scratch_bytes((int)n, (int)n, 4 * h->delay, S);
+      if (f > need) need = f;
+    }
+    h->oz_bytes = need;
+    A(&h->oz_scratch, h->oz_bytes);
+  }
   if (!ok) return fail(DQMC_ERR_CUDA);
   h->qr.err = h->err_d;
   if (cudaDeviceSynchronize() != cudaSuccess) return fail(DQMC_ERR_CUDA);
@@ -1006,6 +1074,20 @@ int dqmc_get_timing(dqmc_handle* h, dqmc_timing* t) {
   }
   t->kernel_launches = h->launches;
   return DQMC_OK;
+}
+
+int dqmc_gemm_check(dqmc_handle* h, int32_t mode, const double* A, const double* B, double* C) {
+  if (h) cudaSetDevice(h->device);
+  if (!h || !A || !B || !C || (mode != 0 && mode != 1)) return DQMC_ERR_ARG;
+  if (mode == 1 && h->p.precision != DQMC_PREC_MIXED)
+    return set_err(h, DQMC_ERR_STATE, "mode 1 needs a handle created with DQMC_PREC_MIXED");
+  const int n = h->n;
+  CHK(upload_nn(h, h->W1, A));
+  CHK(upload_nn(h, h->W2, B));
+  CHK(zgemm_general(h, n, n, n, 'N', 'N', cmake(1, 0), h->W1, n, h->W2, n, cmake(0, 0), h->W3, n, nullptr, nullptr,
+                    mode == 1));
+  CHK(download_nn(h, C, h->W3));
+  return sync(h);
 }
 
 int dqmc_peak_fp64(int32_t device, double* tflops) {

@@ -31,7 +31,9 @@ __device__ __forceinline__ cplx load_op(const cplx* X, int ld, int r, int c, int
 __global__ void __launch_bounds__(256) k_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha,
                                               const cplx* __restrict__ A, int lda, const cplx* __restrict__ B,
                                               int ldb, cplx beta, cplx* __restrict__ C, int ldc,
-                                              const double* __restrict__ rs, const double* __restrict__ cs) {
+                                              const double* __restrict__ rs, const double* __restrict__ cs,
+                                              const int* __restrict__ active) {
+  if (active && *active == 0) return;
   __shared__ cplx sA[GB_K][GB_M + 1];
   __shared__ cplx sB[GB_K][GB_N + 1];
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
@@ -196,8 +198,10 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
       cplx* col = A + (size_t)j * n;
       cplx x[QR_MAXT];
       cplx sp[4] = {cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0)};
+      const int nq = (n - k + 31) >> 5;   // warp-uniform: no FP64 work on fully masked slots
 #pragma unroll
       for (int q = 0; q < QR_MAXT; ++q) {
+        if (q >= nq) break;
         int r = k + lane + 32 * q;
         x[q] = cmake(0.0, 0.0);
         if (r < n) { x[q] = ldcg_c(&col[r]); sp[q & 3] = cfma_conj(v[r], x[q], sp[q & 3]); }
@@ -209,12 +213,15 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
       cplx xk = cmake(0.0, 0.0);
 #pragma unroll
       for (int q = 0; q < QR_MAXT; ++q) {
+        if (q >= nq) break;
         int r = k + lane + 32 * q;
         if (r < n) {
-          x[q] = csub(x[q], cmul(f, v[r]));
+          // x -= f v with four fused multiply-adds
+          const cplx vr = v[r];
+          x[q] = cmake(fma(-f.x, vr.x, fma(f.y, vr.y, x[q].x)), fma(-f.x, vr.y, fma(-f.y, vr.x, x[q].y)));
           col[r] = x[q];
           if (q == 0 && lane == 0) xk = x[q];
-          else tp[q & 3] += cabs2(x[q]);
+          else tp[q & 3] = fma(x[q].x, x[q].x, fma(x[q].y, x[q].y, tp[q & 3]));
         }
       }
       xk = cmake(__shfl_sync(0xffffffffu, xk.x, 0), __shfl_sync(0xffffffffu, xk.y, 0));
@@ -266,7 +273,7 @@ __global__ void k_qrp_finalize(const cplx* __restrict__ A, cplx* __restrict__ T,
 }
 
 // X (m x n) <- X * Q (or X * Q^H), one warp per row, row held in registers.
-__global__ void __launch_bounds__(256) k_apply_q_right(cplx* __restrict__ X, int m, int n,
+__global__ void __launch_bounds__(128) k_apply_q_right(cplx* __restrict__ X, int m, int n,
                                                       const cplx* __restrict__ V, const cplx* __restrict__ tau,
                                                       int conj_q) {
   const int lane = threadIdx.x & 31;
@@ -286,8 +293,11 @@ __global__ void __launch_bounds__(256) k_apply_q_right(cplx* __restrict__ X, int
     if (conj_q) tk = cconj(tk);
     // X H = X - tau (X v) v^H
     cplx dp[4] = {cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0)};
+    const int t0 = k >> 5, t1 = (n + 31) >> 5;   // warp-uniform range of slots holding columns >= k
 #pragma unroll
     for (int t = 0; t < QR_MAXT; ++t) {
+      if (t < t0) continue;
+      if (t >= t1) break;
       int c = lane + 32 * t;
       if (c >= k && c < n) dp[t & 3] = cfma(x[t], __ldg(&vk[c]), dp[t & 3]);
     }
@@ -295,11 +305,13 @@ __global__ void __launch_bounds__(256) k_apply_q_right(cplx* __restrict__ X, int
     cplx f = cmul(tk, d);
 #pragma unroll
     for (int t = 0; t < QR_MAXT; ++t) {
+      if (t < t0) continue;
+      if (t >= t1) break;
       int c = lane + 32 * t;
       if (c >= k && c < n) {
         cplx vc = __ldg(&vk[c]);
-        // x_c -= f * conj(v_c)
-        x[t] = cmake(x[t].x - (f.x * vc.x + f.y * vc.y), x[t].y - (f.y * vc.x - f.x * vc.y));
+        // x_c -= f * conj(v_c) with four fused multiply-adds
+        x[t] = cmake(fma(-f.x, vc.x, fma(-f.y, vc.y, x[t].x)), fma(-f.y, vc.x, fma(f.x, vc.y, x[t].y)));
       }
     }
   }
@@ -457,9 +469,10 @@ static inline int grid_for(size_t total, int threads = 256, int cap = 4096) {
 
 cudaError_t launch_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
                          const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
-                         const double* colscale, cudaStream_t st) {
+                         const double* colscale, cudaStream_t st, const int* active) {
   dim3 grid((nn + GB_N - 1) / GB_N, (m + GB_M - 1) / GB_M);
-  k_zgemm<<<grid, 256, 0, st>>>(m, nn, k, opA, opB, alpha, A, lda, B, ldb, beta, C, ldc, rowscale, colscale);
+  k_zgemm<<<grid, 256, 0, st>>>(m, nn, k, opA, opB, alpha, A, lda, B, ldb, beta, C, ldc, rowscale, colscale,
+                                active);
   return cudaGetLastError();
 }
 
@@ -475,9 +488,7 @@ cudaError_t launch_qrp(cplx* A, int n, QRWork& w, int sm_count, cudaStream_t st)
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_qrp, QR_THREADS, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  int grid = sm_count;   // one CTA per SM: 8 warps each, one column per warp per step
-  int need = (n + 7) / 8;
-  if (grid > need) grid = need < 1 ? 1 : need;
+  int grid = sm_count;   // one CTA per SM; remaining columns are dealt round-robin over all CTAs
   QRWork copy = w;
   void* args[] = {&A, &n, &copy};
   return cudaLaunchCooperativeKernel((void*)k_qrp, dim3(grid), dim3(QR_THREADS), args, smem, st);
@@ -490,8 +501,9 @@ cudaError_t launch_qrp_finalize(cplx* A, cplx* T, double* D, int n, const QRWork
 
 cudaError_t launch_apply_q_right(cplx* X, int m, int n, const QRWork& w, bool conj_transpose_q, cudaStream_t st) {
   if (n > 32 * QR_MAXT) return cudaErrorInvalidValue;
-  int rows_per_cta = 8;
-  k_apply_q_right<<<(m + rows_per_cta - 1) / rows_per_cta, 256, 0, st>>>(X, m, n, w.V, w.tau,
+  // one row per warp, 4 warps per CTA: up to 2 CTAs per SM at 256 registers per thread
+  int rows_per_cta = 4;
+  k_apply_q_right<<<(m + rows_per_cta - 1) / rows_per_cta, 128, 0, st>>>(X, m, n, w.V, w.tau,
                                                                         conj_transpose_q ? 1 : 0);
   return cudaGetLastError();
 }

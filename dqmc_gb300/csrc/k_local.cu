@@ -74,20 +74,28 @@ struct SiteDecision {
 
 constexpr int LU_THREADS = 256;
 
-__global__ void __launch_bounds__(LU_THREADS, 2) k_local_updates(LocalUpdateArgs a) {
-  const ModelConst& mc = a.mc;
-  const int N = mc.N, n = mc.n, M = mc.M, L = mc.L;
-  const int l = a.slice0;
-  extern __shared__ double4_16a smem_local[];
-  cplx* delta_all = reinterpret_cast<cplx*>(smem_local);           // (N, 16): Delta_i row-major
-  EvEntry* evnew = reinterpret_cast<EvEntry*>(delta_all + 16 * N);  // (N): entries of the proposed field
-  double* phis = reinterpret_cast<double*>(evnew + N);              // (3, N): this CTA's copy of phi[:, :, l]
-  __shared__ SiteDecision dec;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+// Shared-memory layout of both local-update kernels.
+struct LocalSmem {
+  cplx* delta_all;   // (N, 16): Delta_i row-major
+  EvEntry* evnew;    // (N): interaction entries of the proposed field
+  double* phis;      // (3, N): this CTA's copy of phi[:, :, l]
+};
 
-  // ---- prologue: field copy and Delta_i for every site ----
-  for (int k = threadIdx.x; k < 3 * N; k += blockDim.x) phis[k] = a.phi[(size_t)3 * N * l + k];
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+__device__ LocalSmem local_smem(void* base, int N) {
+  LocalSmem s;
+  s.delta_all = reinterpret_cast<cplx*>(base);
+  s.evnew = reinterpret_cast<EvEntry*>(s.delta_all + 16 * N);
+  s.phis = reinterpret_cast<double*>(s.evnew + N);
+  return s;
+}
+
+// Field copy of slice l and Delta_i = e^{+dtau V(phi_i)} e^{-dtau V(phi_i + delta_i)} - I
+// for sites >= first (the old field of a site cannot change before its visit).
+__device__ void local_prologue(const LocalUpdateArgs& a, const LocalSmem& sm, int first) {
+  const ModelConst& mc = a.mc;
+  const int N = mc.N, l = a.slice0;
+  for (int k = threadIdx.x; k < 3 * N; k += blockDim.x) sm.phis[k] = a.phi[(size_t)3 * N * l + k];
+  for (int i = first + threadIdx.x; i < N; i += blockDim.x) {
     const double* po = &a.phi[((size_t)N * l + i) * 3];
     double old[3] = {po[0], po[1], po[2]};
     double nw[3] = {old[0] + a.delta[3 * i], old[1] + a.delta[3 * i + 1], old[2] + a.delta[3 * i + 2]};
@@ -97,119 +105,144 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_updates(LocalUpdateArgs
     ev_params(mc, nw, 1.0, C2, S2, R2, s2);
     EvEntry e;
     e.C = C2; e.Sr = -nw[0] * s2; e.Si = nw[1] * s2; e.R = -nw[2] * s2;
-    evnew[i] = e;
+    sm.evnew[i] = e;
     for (int r = 0; r < 4; ++r)
       for (int c = 0; c < 4; ++c) {
         cplx s = cmake(0.0, 0.0);
         for (int k = 0; k < 4; ++k) s = cfma(ev_entry(r, k, C1, S1, R1), ev_entry(k, c, C2, S2, R2), s);
         if (r == c) s.x -= 1.0;
-        delta_all[16 * i + 4 * r + c] = s;
+        sm.delta_all[16 * i + 4 * r + c] = s;
       }
   }
-  __syncthreads();
+}
+
+// Metropolis decision for site i, executed by warp 0 of every CTA.  g is
+// G_cur[i + rN, i + cN] in lane 4r + c (lanes < 16).  Writes dec (accepted
+// flag, M^-1), the CTA's field copy, and (CTA 0) the outputs, the field,
+// the interaction table, the action and the accepted count.
+__device__ void local_decide(const LocalUpdateArgs& a, const LocalSmem& sm, int i, cplx g, SiteDecision& dec) {
+  const ModelConst& mc = a.mc;
+  const int N = mc.N, M = mc.M, L = mc.L, l = a.slice0;
+  const int lane = threadIdx.x & 31;
   const int lt_later = (l + 1) % M, lt_earlier = (l - 1 + M) % M;
+  double* phis = sm.phis;
+  // ---- boson action difference (src/action.jl:57-100), lane 0 ----
+  double dS = 0.0;
+  if (lane == 0) {
+    double old[3] = {phis[3 * i], phis[3 * i + 1], phis[3 * i + 2]};
+    double nw[3];
+    for (int c = 0; c < 3; ++c) nw[c] = old[c] + a.delta[3 * i + c];
+    double diff[3] = {nw[0] - old[0], nw[1] - old[1], nw[2] - old[2]};
+    double old_sq = old[0] * old[0] + old[1] * old[1] + old[2] * old[2];
+    double new_sq = nw[0] * nw[0] + nw[1] * nw[1] + nw[2] * nw[2];
+    double sq_diff = new_sq - old_sq;
+    double pow4_diff = new_sq * new_sq - old_sq * old_sq;
+    const double* pe = (lt_earlier == l) ? &phis[3 * i] : &a.phi[((size_t)N * lt_earlier + i) * 3];
+    const double* pl = (lt_later == l) ? &phis[3 * i] : &a.phi[((size_t)N * lt_later + i) * 3];
+    int y = i % L, x = i / L;
+    int nbs[4] = {(y + 1) % L + L * x, y + L * ((x + 1) % L), (y - 1 + L) % L + L * x, y + L * ((x - 1 + L) % L)};
+    double tdot = 0.0, sdot = 0.0;
+    for (int c = 0; c < 3; ++c) {
+      double ot = pl[c] + pe[c];
+      double os = 0.0;
+      for (int q = 0; q < 4; ++q) os = os + phis[3 * nbs[q] + c];
+      tdot += ot * diff[c];
+      sdot += os * diff[c];
+    }
+    dS += 1.0 / (mc.dtau * mc.c * mc.c) * (sq_diff - tdot);
+    dS += 0.5 * mc.dtau * (4 * sq_diff - 2.0 * sdot);
+    dS += mc.dtau * (0.5 * mc.r * sq_diff + 0.25 * mc.u * pow4_diff);
+  }
+  dS = __shfl_sync(0xffffffffu, dS, 0);
+  // ---- M = I + Delta (I - G_ii), lane 4r+c holds M[r][c] (src/local_updates.jl:49-55) ----
+  const int r = (lane >> 2) & 3, c = lane & 3;
+  if (lane >= 16) g = cmake(0.0, 0.0);
+  cplx mt = cmake((r == c ? 1.0 : 0.0) - g.x, -g.y);   // (I - G_ii)[r][c]
+  cplx m = cmake(r == c ? 1.0 : 0.0, 0.0);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    cplx mtk = shfl_c(mt, 4 * k + c);                  // (I - G_ii)[k][c]
+    m = cfma(sm.delta_all[16 * i + 4 * r + k], mtk, m);
+  }
+  // ---- det M by the permutation expansion (24 lanes) ----
+  cplx term = cmake(0.0, 0.0);
+  {
+    const int j = lane < 24 ? lane : 0;
+    cplx p = cmake(1.0, 0.0);
+#pragma unroll
+    for (int rr = 0; rr < 4; ++rr) p = cmul(p, shfl_c(m, 4 * rr + c_perm[j][rr]));
+    if (lane < 24) term = cscale(p, (double)c_psign[j]);
+  }
+  cplx det = term;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) det = cadd(det, shfl_c(det, lane ^ o));
+  // lanes associate the sum differently; lane 0's value (the same in every
+  // CTA) is the one every lane uses, so all decisions agree bit for bit
+  det = shfl_c(det, 0);
+  const double exp_dS = exp(-dS);
+  const double pacc = exp_dS * det.x;
+  const double u = a.unif[i];
+  int acc = (pacc > 1.0 || u < pacc) ? 1 : 0;
+  const bool bad = !isfinite(det.x) || !isfinite(det.y) || (det.x == 0.0 && det.y == 0.0);
+  if (bad) acc = 0;
+  // ---- M^-1 = adj(M) / det (lane 4r+c: entry [r][c] = cofactor C[c][r] / det) ----
+  if (acc) {
+    int rows[3], cols[3];
+    for (int t = 0, q = 0; t < 4; ++t) if (t != c) rows[q++] = t;
+    for (int t = 0, q = 0; t < 4; ++t) if (t != r) cols[q++] = t;
+    cplx e[3][3];
+#pragma unroll
+    for (int u3 = 0; u3 < 3; ++u3)
+#pragma unroll
+      for (int v3 = 0; v3 < 3; ++v3) e[u3][v3] = shfl_c(m, (4 * rows[u3] + cols[v3]) & 31);
+    cplx d3 = csub(cmul(e[0][0], csub(cmul(e[1][1], e[2][2]), cmul(e[1][2], e[2][1]))),
+                   cmul(e[0][1], csub(cmul(e[1][0], e[2][2]), cmul(e[1][2], e[2][0]))));
+    d3 = cadd(d3, cmul(e[0][2], csub(cmul(e[1][0], e[2][1]), cmul(e[1][1], e[2][0]))));
+    if ((r + c) & 1) d3 = cmake(-d3.x, -d3.y);
+    if (lane < 16) dec.minv[r][c] = cdiv(d3, det);
+  }
+  if (lane == 0) {
+    dec.accepted = acc;
+    if (acc) {
+      for (int q = 0; q < 3; ++q) phis[3 * i + q] += a.delta[3 * i + q];
+    }
+    if (blockIdx.x == 0) {
+      if (bad) atomicOr(a.err, DQMC_KERR_NONFINITE);
+      if (a.acc_out) a.acc_out[i] = (uint8_t)acc;
+      if (a.det_out) a.det_out[i] = det;
+      if (a.pacc_out) a.pacc_out[i] = pacc;
+      if (acc) {
+        double* pg = &a.phi[((size_t)N * l + i) * 3];
+        pg[0] = phis[3 * i]; pg[1] = phis[3 * i + 1]; pg[2] = phis[3 * i + 2];
+        if (a.evtab) reinterpret_cast<EvEntry*>(a.evtab)[(size_t)N * l + i] = sm.evnew[i];
+        *a.action += -log(exp_dS);
+        *a.n_acc += 1;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// immediate rank-4 updates
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(LU_THREADS, 2) k_local_updates(LocalUpdateArgs a) {
+  const ModelConst& mc = a.mc;
+  const int N = mc.N, n = mc.n;
+  extern __shared__ double4_16a smem_local[];
+  const LocalSmem sm = local_smem(smem_local, N);
+  __shared__ SiteDecision dec;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  local_prologue(a, sm, 0);
+  __syncthreads();
   const int gwarp = blockIdx.x * (LU_THREADS / 32) + wid;
   const int nwarps = gridDim.x * (LU_THREADS / 32);
 
   for (int i = 0; i < N; ++i) {
     if (wid == 0) {
-      // ---- boson action difference (src/action.jl:57-100), lane 0 ----
-      double dS = 0.0;
-      if (lane == 0) {
-        double old[3] = {phis[3 * i], phis[3 * i + 1], phis[3 * i + 2]};
-        double nw[3];
-        for (int c = 0; c < 3; ++c) nw[c] = old[c] + a.delta[3 * i + c];
-        double diff[3] = {nw[0] - old[0], nw[1] - old[1], nw[2] - old[2]};
-        double old_sq = old[0] * old[0] + old[1] * old[1] + old[2] * old[2];
-        double new_sq = nw[0] * nw[0] + nw[1] * nw[1] + nw[2] * nw[2];
-        double sq_diff = new_sq - old_sq;
-        double pow4_diff = new_sq * new_sq - old_sq * old_sq;
-        const double* pe = (lt_earlier == l) ? &phis[3 * i] : &a.phi[((size_t)N * lt_earlier + i) * 3];
-        const double* pl = (lt_later == l) ? &phis[3 * i] : &a.phi[((size_t)N * lt_later + i) * 3];
-        int y = i % L, x = i / L;
-        int nbs[4] = {(y + 1) % L + L * x, y + L * ((x + 1) % L), (y - 1 + L) % L + L * x,
-                      y + L * ((x - 1 + L) % L)};
-        double tdot = 0.0, sdot = 0.0;
-        for (int c = 0; c < 3; ++c) {
-          double ot = pl[c] + pe[c];
-          double os = 0.0;
-          for (int q = 0; q < 4; ++q) os = os + phis[3 * nbs[q] + c];
-          tdot += ot * diff[c];
-          sdot += os * diff[c];
-        }
-        dS += 1.0 / (mc.dtau * mc.c * mc.c) * (sq_diff - tdot);
-        dS += 0.5 * mc.dtau * (4 * sq_diff - 2.0 * sdot);
-        dS += mc.dtau * (0.5 * mc.r * sq_diff + 0.25 * mc.u * pow4_diff);
-      }
-      dS = __shfl_sync(0xffffffffu, dS, 0);
-      // ---- M = I + Delta (I - G_ii), lane 4r+c holds M[r][c] (src/local_updates.jl:49-55) ----
       const int r = (lane >> 2) & 3, c = lane & 3;
       cplx g = cmake(0.0, 0.0);
       if (lane < 16) g = ldcg_c(&a.G[(size_t)(i + c * N) * n + i + r * N]);
-      cplx mt = cmake((r == c ? 1.0 : 0.0) - g.x, -g.y);   // (I - G_ii)[r][c]
-      cplx m = cmake(r == c ? 1.0 : 0.0, 0.0);
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        cplx mtk = shfl_c(mt, 4 * k + c);                  // (I - G_ii)[k][c]
-        m = cfma(delta_all[16 * i + 4 * r + k], mtk, m);
-      }
-      // ---- det M by the permutation expansion (24 lanes) ----
-      cplx term = cmake(0.0, 0.0);
-      {
-        const int j = lane < 24 ? lane : 0;
-        cplx p = cmake(1.0, 0.0);
-#pragma unroll
-        for (int rr = 0; rr < 4; ++rr) p = cmul(p, shfl_c(m, 4 * rr + c_perm[j][rr]));
-        if (lane < 24) term = cscale(p, (double)c_psign[j]);
-      }
-      cplx det = term;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) det = cadd(det, shfl_c(det, lane ^ o));
-      // lanes associate the sum differently; lane 0's value (the same in every
-      // CTA) is the one every lane uses, so all decisions agree bit for bit
-      det = shfl_c(det, 0);
-      const double exp_dS = exp(-dS);
-      const double pacc = exp_dS * det.x;
-      const double u = a.unif[i];
-      int acc = (pacc > 1.0 || u < pacc) ? 1 : 0;
-      const bool bad = !isfinite(det.x) || !isfinite(det.y) || (det.x == 0.0 && det.y == 0.0);
-      if (bad) acc = 0;
-      // ---- M^-1 = adj(M) / det (lanes 4r+c: entry [r][c] = cofactor C[c][r] / det) ----
-      if (acc) {
-        // minor of M without row c and column r
-        int rows[3], cols[3];
-        for (int t = 0, q = 0; t < 4; ++t) if (t != c) rows[q++] = t;
-        for (int t = 0, q = 0; t < 4; ++t) if (t != r) cols[q++] = t;
-        cplx e[3][3];
-#pragma unroll
-        for (int u3 = 0; u3 < 3; ++u3)
-#pragma unroll
-          for (int v3 = 0; v3 < 3; ++v3) e[u3][v3] = shfl_c(m, (4 * rows[u3] + cols[v3]) & 31);
-        cplx d3 = csub(cmul(e[0][0], csub(cmul(e[1][1], e[2][2]), cmul(e[1][2], e[2][1]))),
-                       cmul(e[0][1], csub(cmul(e[1][0], e[2][2]), cmul(e[1][2], e[2][0]))));
-        d3 = cadd(d3, cmul(e[0][2], csub(cmul(e[1][0], e[2][1]), cmul(e[1][1], e[2][0]))));
-        if ((r + c) & 1) d3 = cmake(-d3.x, -d3.y);
-        if (lane < 16) dec.minv[r][c] = cdiv(d3, det);
-      }
-      if (lane == 0) {
-        dec.accepted = acc;
-        if (acc) {
-          for (int q = 0; q < 3; ++q) phis[3 * i + q] += a.delta[3 * i + q];
-        }
-        if (blockIdx.x == 0) {
-          if (bad) atomicOr(a.err, DQMC_KERR_NONFINITE);
-          if (a.acc_out) a.acc_out[i] = (uint8_t)acc;
-          if (a.det_out) a.det_out[i] = det;
-          if (a.pacc_out) a.pacc_out[i] = pacc;
-          if (acc) {
-            double* pg = &a.phi[((size_t)N * l + i) * 3];
-            pg[0] = phis[3 * i]; pg[1] = phis[3 * i + 1]; pg[2] = phis[3 * i + 2];
-            if (a.evtab) reinterpret_cast<EvEntry*>(a.evtab)[(size_t)N * l + i] = evnew[i];
-            *a.action += -log(exp_dS);
-            *a.n_acc += 1;
-          }
-        }
-      }
+      local_decide(a, sm, i, g, dec);
     }
     __syncthreads();
     const int accepted = dec.accepted;
@@ -218,7 +251,7 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_updates(LocalUpdateArgs
       continue;
     }
     // ---- phase 1: A = (G[:, cols] - I[:, cols]) M^-1, B = Delta G[rows, :] ----
-    const cplx* Dl = &delta_all[16 * i];
+    const cplx* Dl = &sm.delta_all[16 * i];
     for (int t = blockIdx.x * LU_THREADS + threadIdx.x; t < 2 * n; t += gridDim.x * LU_THREADS) {
       if (t < n) {
         const int row = t;
@@ -286,10 +319,173 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_updates(LocalUpdateArgs
   }
 }
 
+// ---------------------------------------------------------------------------
+// delayed rank-k updates: G_cur = G + X Y with X (n x 4k), Y (4k x n)
+// ---------------------------------------------------------------------------
+// Processes sites state[0] .. N-1 until k accepted updates are pending
+// (state[1] == k) or the slice ends; state[0] is left at the next site.  The
+// flush G += X Y (a separate GEMM launch) resets state[1] to 0.
+__global__ void __launch_bounds__(LU_THREADS, 2) k_local_delayed(LocalUpdateArgs a, DelayedArgs d) {
+  const ModelConst& mc = a.mc;
+  const int N = mc.N, n = mc.n, K4 = 4 * d.k;
+  __shared__ int s_first, s_p;
+  if (threadIdx.x == 0) { s_first = __ldcg(&d.state[0]); s_p = __ldcg(&d.state[1]); }
+  __syncthreads();
+  const int first = s_first;
+  int p = s_p;
+  if (first >= N || p >= d.k) return;   // nothing to do in this round (uniform over the grid)
+  extern __shared__ double4_16a smem_local[];
+  const LocalSmem sm = local_smem(smem_local, N);
+  cplx* Ysm = reinterpret_cast<cplx*>(sm.phis + 3 * N);   // (4k x 4): Y[j, i + cN] of the current site
+  cplx* Xsm = Ysm + (size_t)K4 * 4;                        // (4 x 4k): X[i + rN, j]
+  __shared__ SiteDecision dec;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  local_prologue(a, sm, first);
+  __syncthreads();
+
+  for (int i = first; i < N; ++i) {
+    const int J = 4 * p;   // pending columns of X / rows of Y
+    // pending factor entries touching site i
+    for (int t = threadIdx.x; t < 4 * J; t += blockDim.x) {
+      const int j = t >> 2, c = t & 3;
+      Ysm[4 * j + c] = ldcg_c(&d.Y[(size_t)j * n + i + c * N]);
+      Xsm[(size_t)c * K4 + j] = ldcg_c(&d.X[(size_t)j * n + i + c * N]);
+    }
+    __syncthreads();
+    if (wid == 0) {
+      const int r = (lane >> 2) & 3, c = lane & 3;
+      cplx g = cmake(0.0, 0.0);
+      if (lane < 16) {
+        g = ldcg_c(&a.G[(size_t)(i + c * N) * n + i + r * N]);
+        for (int j = 0; j < J; ++j) g = cfma(Xsm[(size_t)r * K4 + j], Ysm[4 * j + c], g);
+      }
+      local_decide(a, sm, i, g, dec);
+    }
+    __syncthreads();
+    const int accepted = dec.accepted;
+    if (!accepted) {
+      __syncthreads();
+      continue;
+    }
+    // ---- A = (G_cur[:, cols] - I[:, cols]) M^-1 -> X[:, J..J+3]; B = Delta G_cur[rows, :] -> Y[J..J+3, :] ----
+    // 16 lanes per item (item < n: row of A, item >= n: column of B); lane
+    // (k, jc) sums the pending terms j = jc, jc+4, ... of output k.
+    const cplx* Dl = &sm.delta_all[16 * i];
+    {
+      const int sub = lane & 15, k = sub >> 2, jc = sub & 3;
+      const int half = lane >> 4;
+      const int gw = blockIdx.x * (LU_THREADS / 32) + wid;
+      const int nw = gridDim.x * (LU_THREADS / 32);
+      for (int base = 2 * gw; base < 2 * n; base += 2 * nw) {   // uniform trip count over the warp
+        const int it = base + half;
+        const bool valid = it < 2 * n;
+        cplx gsum = cmake(0.0, 0.0);
+        if (valid) {
+          if (it < n) {
+            const int row = it;
+            for (int j = jc; j < J; j += 4) gsum = cfma(ldcg_c(&d.X[(size_t)j * n + row]), Ysm[4 * j + k], gsum);
+          } else {
+            const int col = it - n;
+            for (int j = jc; j < J; j += 4) gsum = cfma(Xsm[(size_t)k * K4 + j], ldcg_c(&d.Y[(size_t)j * n + col]), gsum);
+          }
+        }
+        gsum = cadd(gsum, shfl_c(gsum, lane ^ 1));
+        gsum = cadd(gsum, shfl_c(gsum, lane ^ 2));
+        if (valid && jc == 0) {
+          if (it < n) {
+            const int row = it;
+            cplx g = cadd(ldcg_c(&a.G[(size_t)(i + k * N) * n + row]), gsum);
+            if (row == i + k * N) g.x -= 1.0;
+            gsum = g;
+          } else {
+            const int col = it - n;
+            gsum = cadd(ldcg_c(&a.G[(size_t)col * n + i + k * N]), gsum);
+          }
+        }
+        // gather g[0..3] of this item (lanes jc == 0 of the 4 k groups)
+        cplx gk[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) gk[q] = shfl_c(gsum, (half << 4) + 4 * q);
+        if (valid && jc == 0) {
+          if (it < n) {
+            cplx s2 = cmake(0, 0);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) s2 = cfma(gk[q], dec.minv[q][k], s2);
+            d.X[(size_t)(J + k) * n + it] = s2;
+          } else {
+            cplx s2 = cmake(0, 0);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) s2 = cfma(Dl[4 * k + q], gk[q], s2);
+            d.Y[(size_t)(J + k) * n + (it - n)] = s2;
+          }
+        }
+      }
+    }
+    ++p;
+    if (p == d.k || i == N - 1) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) { d.state[0] = i + 1; d.state[1] = p; }
+      return;   // the flush follows as its own launch
+    }
+    if (!grid_barrier(a.bar, a.err)) return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) { d.state[0] = N; d.state[1] = p; }
+}
+
+// After a flush: zero the used factor columns and clear the pending count.
+__global__ void k_delayed_reset(DelayedArgs d, int n) {
+  const int p = __ldcg(&d.state[1]);
+  if (p == 0) return;
+  const size_t used = (size_t)4 * p * n;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < used; e += (size_t)gridDim.x * blockDim.x) {
+    d.X[e] = cmake(0.0, 0.0);
+    d.Y[e] = cmake(0.0, 0.0);
+  }
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    __threadfence();
+  }
+}
+
+__global__ void k_delayed_clear_count(int* state) { state[1] = 0; }
+
 }  // namespace
 
+static size_t local_smem_bytes(int N) {
+  return (size_t)N * (16 * sizeof(cplx) + sizeof(EvEntry)) + (size_t)3 * N * sizeof(double);
+}
+
+cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d, int sm_count, cudaStream_t st) {
+  const size_t smem = local_smem_bytes(a.mc.N) + (size_t)2 * 4 * d.k * 4 * sizeof(cplx);
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_local_delayed, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  if (smem > 100 * 1024) return cudaErrorInvalidValue;
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local_delayed, LU_THREADS, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  if (per_sm > 2) per_sm = 2;
+  int grid = sm_count * per_sm;
+  // two items (rows of A / columns of B) per warp
+  const int need = (a.mc.n + (LU_THREADS / 32) - 1) / (LU_THREADS / 32);
+  if (grid > need) grid = need < 1 ? 1 : need;
+  LocalUpdateArgs ca = a;
+  DelayedArgs cd = d;
+  void* args[] = {&ca, &cd};
+  return cudaLaunchCooperativeKernel((void*)k_local_delayed, dim3(grid), dim3(LU_THREADS), args, smem, st);
+}
+
+cudaError_t launch_delayed_reset(const DelayedArgs& d, int n, cudaStream_t st) {
+  k_delayed_reset<<<256, 256, 0, st>>>(d, n);
+  k_delayed_clear_count<<<1, 1, 0, st>>>(d.state);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_local_updates(const LocalUpdateArgs& a, int sm_count, cudaStream_t st) {
-  const size_t smem = (size_t)a.mc.N * (16 * sizeof(cplx) + sizeof(EvEntry)) + (size_t)3 * a.mc.N * sizeof(double);
+  const size_t smem = local_smem_bytes(a.mc.N);
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_local_updates, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);

@@ -1,0 +1,362 @@
+// Split-precision complex GEMM on the BF16 tensor cores (Ozaki scheme).
+//
+//   C = alpha * diag(rs) * op(A) * op(B) * diag(cs) + beta * C     (complex FP64)
+//
+// GB300 runs FP64 at ~1/1500 of its BF16 tensor rate, so the mixed-precision
+// form computes the dense products of the UDT stabilisation and of the
+// delayed local-update flush as sums of exact BF16 x BF16 -> FP32 products:
+//
+//  * every row i of op(A) gets a power-of-two scale sigma_i >= max_k |op(A)_ik|
+//    (real and imaginary parts together), every column j of op(B) a scale
+//    tau_j; the scaled entries lie in [-1, 1];
+//  * each scaled entry x is cut into S slices of B_BITS bits,
+//    x ~ sum_p 2^{-B_BITS p} a_p with integers |a_p| <= 2^B_BITS, which BF16
+//    holds exactly;
+//  * the complex product is two real GEMMs with K' = 2K on stacked operands,
+//    A' = [Re A, Im A] and B'_re = [Re B; -Im B], B'_im = [Im B; Re B];
+//  * slice pairs (p, q) with p + q = t <= S + 1 are accumulated into one FP32
+//    accumulator per t; with K' * S * 2^{2 B_BITS} <= 2^24 every partial sum is
+//    an integer below 2^24, so the FP32 accumulation is exact; the groups are
+//    combined in FP64 with their weights 2^{-B_BITS t} and the scales.
+// The only error is the truncation of the slice expansion (~2^{-B_BITS S}
+// relative to sigma_i tau_j K).
+//
+// The tensor-core products use warp-level mma.sync m16n8k16 (BF16 in, FP32
+// accumulate) fed from shared memory with ldmatrix; operands are staged with
+// cp.async double buffering.
+#include <cuda_bf16.h>
+#include <cmath>
+#include "common.cuh"
+#include "kernels.h"
+
+namespace {
+
+constexpr int OZ_BM = 64, OZ_BN = 64, OZ_BK = 32;
+constexpr int OZ_THREADS = 256;
+constexpr int OZ_LDS = OZ_BK + 8;   // padded shared-memory row (bf16 elements): 80 B, conflict-free ldmatrix
+
+// ---------------------------------------------------------------------------
+// split: slices of op(X) scaled per row ("row" side = A) or per column (B side)
+// ---------------------------------------------------------------------------
+// element (r, c) of op(X) where X is column-major with leading dimension ld
+__device__ __forceinline__ cplx op_elem(const cplx* X, int ld, int r, int c, char op) {
+  if (op == 'N') return X[(size_t)c * ld + r];
+  cplx v = X[(size_t)r * ld + c];
+  return op == 'C' ? cconj(v) : v;
+}
+
+// Power-of-two scale >= m (1 for m == 0).
+__device__ __forceinline__ double pow2_ceil(double m) {
+  if (!(m > 0.0)) return 1.0;
+  int e;
+  double f = frexp(m, &e);   // m = f * 2^e, f in [0.5, 1)
+  (void)f;
+  return ldexp(1.0, e);      // 2^e >= m
+}
+
+// A side: op(A) is rows x K; writes S slices of A' (rows x Kp, row-major,
+// Kp = 2 * Kpad): row i = [Re op(A)_i,:  Im op(A)_i,:], zero padded.
+__global__ void k_oz_split_rows(const cplx* __restrict__ X, int ld, char op, int rows, int K, int Kpad, int S,
+                                int bits, __nv_bfloat16* __restrict__ out, double* __restrict__ scale,
+                                const int* __restrict__ active) {
+  const int i = blockIdx.x;
+  if (i >= rows || (active && *active == 0)) return;
+  __shared__ double red[32];
+  double m = 0.0;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    cplx v = op_elem(X, ld, i, k, op);
+    m = fmax(m, fmax(fabs(v.x), fabs(v.y)));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t = fmax(t, red[q]);
+    red[0] = pow2_ceil(t);
+  }
+  __syncthreads();
+  const double sc = red[0];
+  if (threadIdx.x == 0) scale[i] = sc;
+  const double inv = 1.0 / sc, step = ldexp(1.0, bits);
+  const size_t Kp = 2 * (size_t)Kpad;
+  for (int k = threadIdx.x; k < Kpad; k += blockDim.x) {
+    cplx v = k < K ? op_elem(X, ld, i, k, op) : cmake(0.0, 0.0);
+    double xr = v.x * inv, xi = v.y * inv;
+    for (int p = 0; p < S; ++p) {
+      double ar = rint(xr * step), ai = rint(xi * step);
+      xr = xr * step - ar;
+      xi = xi * step - ai;
+      __nv_bfloat16* o = out + (size_t)p * rows * Kp + (size_t)i * Kp;
+      o[k] = __double2bfloat16(ar);
+      o[Kpad + k] = __double2bfloat16(ai);
+    }
+  }
+}
+
+// B side: op(B) is K x cols; writes S slices of B'_re and B'_im (cols x Kp,
+// K contiguous per column): column j of B'_re = [Re op(B)_:,j ; -Im op(B)_:,j],
+// of B'_im = [Im op(B)_:,j ; Re op(B)_:,j].
+__global__ void k_oz_split_cols(const cplx* __restrict__ X, int ld, char op, int K, int cols, int Kpad, int S,
+                                int bits, __nv_bfloat16* __restrict__ out_re, __nv_bfloat16* __restrict__ out_im,
+                                double* __restrict__ scale, const int* __restrict__ active) {
+  const int j = blockIdx.x;
+  if (j >= cols || (active && *active == 0)) return;
+  __shared__ double red[32];
+  double m = 0.0;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    cplx v = op_elem(X, ld, k, j, op);
+    m = fmax(m, fmax(fabs(v.x), fabs(v.y)));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t = fmax(t, red[q]);
+    red[0] = pow2_ceil(t);
+  }
+  __syncthreads();
+  const double sc = red[0];
+  if (threadIdx.x == 0) scale[j] = sc;
+  const double inv = 1.0 / sc, step = ldexp(1.0, bits);
+  const size_t Kp = 2 * (size_t)Kpad;
+  for (int k = threadIdx.x; k < Kpad; k += blockDim.x) {
+    cplx v = k < K ? op_elem(X, ld, k, j, op) : cmake(0.0, 0.0);
+    double xr = v.x * inv, xi = v.y * inv;
+    for (int p = 0; p < S; ++p) {
+      double ar = rint(xr * step), ai = rint(xi * step);
+      xr = xr * step - ar;
+      xi = xi * step - ai;
+      size_t base = (size_t)p * cols * Kp + (size_t)j * Kp;
+      out_re[base + k] = __double2bfloat16(ar);
+      out_re[base + Kpad + k] = __double2bfloat16(-ai);
+      out_im[base + k] = __double2bfloat16(ai);
+      out_im[base + Kpad + k] = __double2bfloat16(ar);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// products
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+__device__ __forceinline__ void ldmatrix_x4(unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3, const void* p) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(s));
+}
+__device__ __forceinline__ void ldmatrix_x2(unsigned& r0, unsigned& r1, const void* p) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n" : "=r"(r0), "=r"(r1) : "r"(s));
+}
+__device__ __forceinline__ void mma_bf16(float* d, const unsigned* a, const unsigned* b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+struct OzArgs {
+  const __nv_bfloat16* As;   // S x (m x Kp), row-major
+  const __nv_bfloat16* Bre;  // S x (n x Kp), K contiguous per column
+  const __nv_bfloat16* Bim;
+  const double* sA;          // (m) row scales
+  const double* sB;          // (n) column scales
+  int m, n, Kp, S, bits;
+  cplx alpha, beta;
+  cplx* C;
+  int ldc;
+  const double* rs;          // optional extra row scaling
+  const double* cs;          // optional extra column scaling
+  const int* active;         // optional: nothing to do when *active == 0
+};
+
+// One CTA: 64 x 64 output tile; 8 warps in a 2 x 4 grid of 32 x 16 warp tiles.
+__global__ void __launch_bounds__(OZ_THREADS) k_oz_gemm(OzArgs a) {
+  if (a.active && *a.active == 0) return;
+  __shared__ __align__(16) __nv_bfloat16 sA[2][OZ_BM * OZ_LDS];
+  __shared__ __align__(16) __nv_bfloat16 sBr[2][OZ_BN * OZ_LDS];
+  __shared__ __align__(16) __nv_bfloat16 sBi[2][OZ_BN * OZ_LDS];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int wm = wid >> 2, wn = wid & 3;          // warp tile origin: rows 32*wm, cols 16*wn
+  const int i0 = blockIdx.y * OZ_BM, j0 = blockIdx.x * OZ_BN;
+  const size_t Kp = a.Kp;
+  const size_t sliceA = (size_t)a.m * Kp, sliceB = (size_t)a.n * Kp;
+
+  // FP64 accumulators: 2 (m16) x 2 (n8) mma tiles x 4 values, re and im
+  double accr[2][2][4], acci[2][2][4];
+#pragma unroll
+  for (int x = 0; x < 2; ++x)
+#pragma unroll
+    for (int y = 0; y < 2; ++y)
+#pragma unroll
+      for (int z = 0; z < 4; ++z) { accr[x][y][z] = 0.0; acci[x][y][z] = 0.0; }
+
+  // staging of one K step of pair (p, q) into buffer `buf`
+  auto stage = [&](int buf, int p, int q, int k0) {
+    // 64 rows x 32 bf16 = 4 chunks of 16 B per row; 256 threads -> 1 chunk each per operand
+    const int r = tid >> 2, ch = tid & 3;
+    {
+      int gi = i0 + r;
+      __nv_bfloat16* dst = &sA[buf][r * OZ_LDS + ch * 8];
+      if (gi < a.m) cp_async16(dst, a.As + (size_t)p * sliceA + (size_t)gi * Kp + k0 + ch * 8);
+      else *reinterpret_cast<uint4*>(dst) = make_uint4(0, 0, 0, 0);
+    }
+    {
+      int gj = j0 + r;
+      __nv_bfloat16* dr = &sBr[buf][r * OZ_LDS + ch * 8];
+      __nv_bfloat16* di = &sBi[buf][r * OZ_LDS + ch * 8];
+      if (gj < a.n) {
+        cp_async16(dr, a.Bre + (size_t)q * sliceB + (size_t)gj * Kp + k0 + ch * 8);
+        cp_async16(di, a.Bim + (size_t)q * sliceB + (size_t)gj * Kp + k0 + ch * 8);
+      } else {
+        *reinterpret_cast<uint4*>(dr) = make_uint4(0, 0, 0, 0);
+        *reinterpret_cast<uint4*>(di) = make_uint4(0, 0, 0, 0);
+      }
+    }
+    cp_async_commit();
+  };
+
+  const int ksteps = (int)(Kp / OZ_BK);
+  for (int t = 2; t <= a.S + 1; ++t) {
+    float fr[2][2][4], fi[2][2][4];
+#pragma unroll
+    for (int x = 0; x < 2; ++x)
+#pragma unroll
+      for (int y = 0; y < 2; ++y)
+#pragma unroll
+        for (int z = 0; z < 4; ++z) { fr[x][y][z] = 0.f; fi[x][y][z] = 0.f; }
+    const int pmin = t - a.S > 1 ? t - a.S : 1, pmax = t - 1 < a.S ? t - 1 : a.S;
+    for (int p = pmin; p <= pmax; ++p) {
+      const int q = t - p;
+      stage(0, p - 1, q - 1, 0);
+      for (int ks = 0; ks < ksteps; ++ks) {
+        const int buf = ks & 1;
+        cp_async_wait_all();
+        __syncthreads();
+        if (ks + 1 < ksteps) stage(buf ^ 1, p - 1, q - 1, (ks + 1) * OZ_BK);
+#pragma unroll
+        for (int kk = 0; kk < OZ_BK; kk += 16) {
+          unsigned af[2][4];
+#pragma unroll
+          for (int x = 0; x < 2; ++x) {
+            // rows 32*wm + 16*x + (lane % 16), k columns kk + 8*(lane / 16)
+            const __nv_bfloat16* pa = &sA[buf][(32 * wm + 16 * x + (lane & 15)) * OZ_LDS + kk + 8 * (lane >> 4)];
+            ldmatrix_x4(af[x][0], af[x][1], af[x][2], af[x][3], pa);
+          }
+          unsigned br[2][2], bi[2][2];
+#pragma unroll
+          for (int y = 0; y < 2; ++y) {
+            // columns 16*wn + 8*y + (lane % 8), k rows kk + 8*((lane / 8) % 2)
+            const int rowb = 16 * wn + 8 * y + (lane & 7);
+            const int kof = kk + 8 * ((lane >> 3) & 1);
+            ldmatrix_x2(br[y][0], br[y][1], &sBr[buf][rowb * OZ_LDS + kof]);
+            ldmatrix_x2(bi[y][0], bi[y][1], &sBi[buf][rowb * OZ_LDS + kof]);
+          }
+#pragma unroll
+          for (int x = 0; x < 2; ++x)
+#pragma unroll
+            for (int y = 0; y < 2; ++y) {
+              mma_bf16(fr[x][y], af[x], br[y]);
+              mma_bf16(fi[x][y], af[x], bi[y]);
+            }
+        }
+      }
+      __syncthreads();   // buffers free before the next pair stages into them
+    }
+    const double wgt = ldexp(1.0, -a.bits * t);
+#pragma unroll
+    for (int x = 0; x < 2; ++x)
+#pragma unroll
+      for (int y = 0; y < 2; ++y)
+#pragma unroll
+        for (int z = 0; z < 4; ++z) {
+          accr[x][y][z] = fma(wgt, (double)fr[x][y][z], accr[x][y][z]);
+          acci[x][y][z] = fma(wgt, (double)fi[x][y][z], acci[x][y][z]);
+        }
+  }
+  // epilogue: mma C fragment layout (m16n8): value z of lane -> row (lane/4) + 8*(z/2), col 2*(lane%4) + (z%2)
+#pragma unroll
+  for (int x = 0; x < 2; ++x)
+#pragma unroll
+    for (int y = 0; y < 2; ++y)
+#pragma unroll
+      for (int z = 0; z < 4; ++z) {
+        const int row = i0 + 32 * wm + 16 * x + (lane >> 2) + 8 * (z >> 1);
+        const int col = j0 + 16 * wn + 8 * y + 2 * (lane & 3) + (z & 1);
+        if (row < a.m && col < a.n) {
+          double f = a.sA[row] * a.sB[col];
+          if (a.rs) f *= a.rs[row];
+          if (a.cs) f *= a.cs[col];
+          cplx v = cmake(accr[x][y][z] * f, acci[x][y][z] * f);
+          v = cmul(a.alpha, v);
+          cplx* cp = &a.C[(size_t)col * a.ldc + row];
+          if (a.beta.x != 0.0 || a.beta.y != 0.0) v = cfma(a.beta, *cp, v);
+          *cp = v;
+        }
+      }
+}
+
+}  // namespace
+
+// Slice count S and width `bits` for a product with inner dimension K and a
+// target of `target_bits` mantissa bits: the smallest S whose widest exact
+// width bits = floor((24 - log2(K' S)) / 2) (at most 8, the BF16 integer range)
+// reaches the target.  Returns false when no S <= 12 does.
+bool ozaki_plan(int K, int target_bits, int* S_out, int* bits_out) {
+  const double kp = 2.0 * ((K + 15) / 16 * 16);
+  for (int S = 2; S <= 12; ++S) {
+    int bits = (int)std::floor((24.0 - std::log2(kp * S)) / 2.0);
+    if (bits > 8) bits = 8;
+    if (bits < 1) return false;
+    if (S * bits >= target_bits) {
+      *S_out = S;
+      *bits_out = bits;
+      return true;
+    }
+  }
+  return false;
+}
+
+// Scratch: As S*m*Kp, Bre/Bim S*n*Kp bf16, scales m + n doubles.
+size_t ozaki_scratch_bytes(int m, int n, int K, int S) {
+  const size_t Kpad = ((size_t)K + 15) / 16 * 16;
+  const size_t Kp = 2 * Kpad;
+  return (size_t)S * Kp * ((size_t)m + 2 * (size_t)n) * sizeof(__nv_bfloat16) + ((size_t)m + n) * sizeof(double) + 256;
+}
+
+cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
+                               const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
+                               const double* colscale, int S, int bits, void* scratch, size_t scratch_bytes,
+                               cudaStream_t st, const int* active) {
+  if (S < 1 || S > 12 || bits < 1 || bits > 8) return cudaErrorInvalidValue;
+  const int Kpad = (k + 15) / 16 * 16;
+  const size_t Kp = 2 * (size_t)Kpad;
+  // exactness of the FP32 group sums: Kp * S * 2^(2 bits) <= 2^24
+  if ((double)Kp * S * ldexp(1.0, 2 * bits) > 16777216.0) return cudaErrorInvalidValue;
+  if (ozaki_scratch_bytes(m, nn, k, S) > scratch_bytes) return cudaErrorInvalidValue;
+  char* base = static_cast<char*>(scratch);
+  __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(base);
+  __nv_bfloat16* Bre = As + (size_t)S * m * Kp;
+  __nv_bfloat16* Bim = Bre + (size_t)S * nn * Kp;
+  double* sA = reinterpret_cast<double*>(Bim + (size_t)S * nn * Kp);
+  double* sB = sA + m;
+  k_oz_split_rows<<<m, 128, 0, st>>>(A, lda, opA, m, k, Kpad, S, bits, As, sA, active);
+  k_oz_split_cols<<<nn, 128, 0, st>>>(B, ldb, opB, k, nn, Kpad, S, bits, Bre, Bim, sB, active);
+  OzArgs a;
+  a.As = As; a.Bre = Bre; a.Bim = Bim; a.sA = sA; a.sB = sB;
+  a.m = m; a.n = nn; a.Kp = (int)Kp; a.S = S; a.bits = bits;
+  a.alpha = alpha; a.beta = beta; a.C = C; a.ldc = ldc; a.rs = rowscale; a.cs = colscale; a.active = active;
+  dim3 grid((nn + OZ_BN - 1) / OZ_BN, (m + OZ_BM - 1) / OZ_BM);
+  k_oz_gemm<<<grid, OZ_THREADS, 0, st>>>(a);
+  return cudaGetLastError();
+}

@@ -45,13 +45,25 @@ struct LocalUpdateArgs {
   ModelConst mc;
 };
 cudaError_t launch_local_updates(const LocalUpdateArgs& a, int sm_count, cudaStream_t st);
+// delayed rank-k form: pending factors X (n x 4k, column-major) and Y (4k x n,
+// row j at Y + j*n); state[0] = next site of the slice, state[1] = pending accepts
+struct DelayedArgs {
+  cplx* X;
+  cplx* Y;
+  int* state;
+  int k;
+};
+cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d, int sm_count, cudaStream_t st);
+// zero the used factor columns and the pending count after a flush
+cudaError_t launch_delayed_reset(const DelayedArgs& d, int n, cudaStream_t st);
 
 // ---- dense linear algebra (k_linalg.cu) ----
 // C = alpha * op(A) * op(B) + beta * C, all n x n column-major; op: 'N', 'C' (conjugate transpose)
 // optional diagonal scalings: rowscale (applied to rows of op(A)), colscale (to columns of op(B)).
+// active: optional device flag; the launch does nothing when *active == 0.
 cudaError_t launch_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
                          const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
-                         const double* colscale, cudaStream_t st);
+                         const double* colscale, cudaStream_t st, const int* active = nullptr);
 
 struct QRWork {
   double* vn1;       // (n)
@@ -99,3 +111,11 @@ cudaError_t launch_conj_transpose(const cplx* A, cplx* B, int n, cudaStream_t st
 
 // ---- diagnostics (k_diag.cu) ----
 cudaError_t measure_peak_fp64(int device, double* tflops);
+
+// ---- split-precision complex GEMM (k_ozaki.cu) ----
+bool ozaki_plan(int K, int target_bits, int* S, int* bits);
+size_t ozaki_scratch_bytes(int m, int n, int K, int S);
+cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
+                               const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
+                               const double* colscale, int S, int bits, void* scratch, size_t scratch_bytes,
+                               cudaStream_t st, const int* active = nullptr);

@@ -44,6 +44,8 @@ extern "C" {
 #define DQMC_ERR_TOO_LARGE (-7)  /* n = 4 L^2 exceeds the static scratch of dqmc_local_updates_noalloc (1024) */
 
 #define DQMC_PREC_FP64 0         /* plain FP64 everywhere */
+#define DQMC_PREC_MIXED 1        /* dense products as split-BF16 tensor-core GEMMs (Ozaki); QR, D scales,
+                                    triangular solves, determinant ratios and the wrap stay FP64 */
 
 /* Parameters of the O(3) model; the subset of `Params` (src/parameters.jl:4-80)
  * that the sweep needs.  hoppings[] is the HOPPINGS string
@@ -59,9 +61,11 @@ typedef struct dqmc_params {
   double mu1, mu2;     /* chemical potentials of band x and band y */
   double hoppings[4];  /* tx_x, ty_x, tx_y, ty_y */
   int32_t all_checks;  /* compare wrapped and fresh G at each stabilisation (src/stack.jl:416-429) */
-  int32_t precision;   /* DQMC_PREC_FP64 */
+  int32_t precision;   /* DQMC_PREC_FP64 or DQMC_PREC_MIXED */
   int32_t device;      /* CUDA device ordinal; -1 = the calling thread's current device */
-  int32_t reserved[5];
+  int32_t ozaki_bits;  /* mixed form: mantissa bits kept per GEMM operand (0 = default 35, max 60) */
+  int32_t delay;       /* delayed-update depth k (0 or 1 = immediate rank-4 updates) */
+  int32_t reserved[3];
 } dqmc_params;
 
 typedef struct dqmc_stats {
@@ -81,7 +85,9 @@ typedef struct dqmc_stats {
 #define DQMC_K_APPLYQ 5       /* X <- X Q (reflector application / explicit Q) */
 #define DQMC_K_TRSM 6         /* triangular solves with the QR factors */
 #define DQMC_K_MISC 7         /* permutations, scalings, reductions, fills */
-#define DQMC_NKINDS 8
+#define DQMC_K_OZGEMM 8       /* split-BF16 tensor-core complex GEMM (mixed form); flops = tensor flops */
+#define DQMC_K_FLUSH 9        /* delayed-update flush G += X Y */
+#define DQMC_NKINDS 10
 
 typedef struct dqmc_timing {
   double ms[DQMC_NKINDS];           /* accumulated device time per kernel kind */
@@ -204,6 +210,10 @@ DQMC_API int dqmc_measure(dqmc_handle* h, double* greens_out, double* occupation
  * of kernels launched since the last reset; enable != 0 turns event timing on. */
 DQMC_API int dqmc_get_timing(dqmc_handle* h, dqmc_timing* t);
 DQMC_API int dqmc_reset_timing(dqmc_handle* h, int32_t enable);
+/* Diagnostic: C = A * B for n x n complex matrices (column-major, interleaved)
+ * with the handle's FP64 GEMM kernel (mode 0) or its split-BF16 tensor-core
+ * GEMM (mode 1).  No counterpart in the reference. */
+DQMC_API int dqmc_gemm_check(dqmc_handle* h, int32_t mode, const double* A, const double* B, double* C);
 /* Measures the FP64 FMA throughput of `device` (TFLOP/s, 2 flops per FMA) with
  * a register-resident DFMA kernel: the roofline denominator of the FP64
  * kernels.  No counterpart in the reference (a diagnostic of this library). */

@@ -50,5 +50,5 @@ def test_version_string_without_gpu(libpath):
 
 
 def test_params_struct_layout():
-    # dqmc_params: 4 int32, 7 doubles, 4 doubles, 3 int32, 5 int32 -> 112 bytes
-    assert ctypes.sizeof(api.CParams) == 4 * 4 + 7 * 8 + 4 * 8 + 3 * 4 + 5 * 4
+    # dqmc_params: 4 int32, 7 doubles, 4 doubles, 5 int32, 3 int32 -> 112 bytes
+    assert ctypes.sizeof(api.CParams) == 4 * 4 + 7 * 8 + 4 * 8 + 5 * 4 + 3 * 4

@@ -149,8 +149,10 @@ def test_local_updates_one_slice(lib, golden, small_params):
     assert abs(gpu.boson_action - ref.boson_action_value) < 1e-10 * abs(ref.boson_action_value)
 
 
-def test_sweep_config0_accept_sequence(lib):
-    """Config 0: one full sweep (M update calls) on shared streams."""
+@pytest.mark.parametrize("delay", [1, 4, 16])
+def test_sweep_config0_accept_sequence(lib, delay):
+    """Config 0: one full sweep (M update calls) on shared streams, with
+    immediate rank-4 updates (delay 1) and delayed rank-k updates."""
     p = C0
     phi = R.synthetic_field(p.N, p.slices, 2024)
     delta, u = R.synthetic_streams(p.N, p.slices, p.box, 2025)
@@ -158,7 +160,9 @@ def test_sweep_config0_accept_sequence(lib):
     ref.init()
     rec = []
     ref.sweep(p.slices, delta, u, record=rec)
-    gpu = lib.DQMC(api_params(p), phi)
+    mp = api_params(p)
+    mp.delay = delay
+    gpu = lib.DQMC(mp, phi)
     gpu.init()
     res = gpu.sweep(p.slices, delta, u, return_accepted=True)
     acc_r = np.array([r[2] for r in rec]).reshape(p.slices, p.N)
@@ -171,8 +175,10 @@ def test_sweep_config0_accept_sequence(lib):
     assert abs(gpu.boson_action - ref.boson_action_value) < 1e-10 * abs(ref.boson_action_value)
 
 
-def test_sweep_config1_shapes(lib):
-    """Config 1 shapes (L=10, M=100): 15 update calls crossing a stabilisation."""
+@pytest.mark.parametrize("delay", [1, 16])
+def test_sweep_config1_shapes(lib, delay):
+    """Config 1 shapes (L=10, M=100): 15 update calls crossing a stabilisation,
+    immediate and delayed (k = 16) updates."""
     p = R.Params(L=10, slices=100, delta_tau=0.1, safe_mult=10, lambda_=1.0, r=1.0, c=1.0, u=1.0, mu1=-0.5,
                  mu2=-0.5, box=0.2)
     calls = 15
@@ -182,7 +188,9 @@ def test_sweep_config1_shapes(lib):
     ref.init()
     rec = []
     ref.sweep(calls, delta, u, record=rec)
-    gpu = lib.DQMC(api_params(p), phi)
+    mp = api_params(p)
+    mp.delay = delay
+    gpu = lib.DQMC(mp, phi)
     gpu.init()
     res = gpu.sweep(calls, delta, u, return_accepted=True)
     acc_r = np.array([r[2] for r in rec]).reshape(calls, p.N)
@@ -203,3 +211,73 @@ def test_measurement_hook(lib):
     assert relerr(m["greens"], Gt) < TOL
     assert abs(m["occupation"] - float(np.mean(1 - np.diag(Gt)).real)) < 1e-12
     assert abs(m["e_kin"] - ref.kinetic_energy(Gt)) < 1e-10 * max(1.0, abs(ref.kinetic_energy(Gt)))
+
+
+# ---------------------------------------------------------------------------
+# mixed-precision form (split-BF16 tensor-core GEMMs)
+# ---------------------------------------------------------------------------
+MIXED_TOL = 1e-8   # max |G_mixed - G_FP64| target of the mixed form
+
+
+@pytest.mark.parametrize("L", [4, 16])
+def test_split_bf16_gemm_accuracy(lib, L):
+    from dqmc_gb300.api import ModelParams
+    p = ModelParams(L=L, slices=10, safe_mult=10, precision="mixed")
+    gpu = lib.DQMC(p, R.synthetic_field(p.N, p.slices, 9))
+    n = p.n
+    rng = np.random.default_rng(11)
+    # rows and columns over many decades, as in the UDT products
+    A = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * np.logspace(-8, 8, n)[:, None]
+    B = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * np.logspace(5, -5, n)[None, :]
+    C_ref = A @ B
+    C_fp64 = gpu.gemm_check(A, B, 0)
+    C_oz = gpu.gemm_check(A, B, 1)
+    scale = np.abs(A) @ np.abs(B)                       # elementwise error scale
+    assert np.max(np.abs(C_fp64 - C_ref) / scale) < 1e-14
+    assert np.max(np.abs(C_oz - C_ref) / scale) < 1e-8
+
+
+@pytest.mark.parametrize("delay", [1, 16])
+def test_mixed_sweep_matches_fp64(lib, delay):
+    p = C0
+    phi = R.synthetic_field(p.N, p.slices, 555)
+    delta, u = R.synthetic_streams(p.N, p.slices, p.box, 556)
+    ref = R.DQMCRef(p, phi)
+    ref.init()
+    rec = []
+    ref.sweep(p.slices, delta, u, record=rec)
+    mp = api_params(p)
+    mp.precision = "mixed"
+    mp.delay = delay
+    gpu = lib.DQMC(mp, phi)
+    gpu.init()
+    res = gpu.sweep(p.slices, delta, u, return_accepted=True)
+    acc_r = np.array([r[2] for r in rec]).reshape(p.slices, p.N)
+    margin = np.abs(np.array([r[4] - r[5] for r in rec])).reshape(p.slices, p.N)
+    safe = margin > 1e-6
+    assert np.array_equal(res["accepted_mask"][safe], acc_r[safe])
+    if np.array_equal(res["accepted_mask"], acc_r):
+        assert relerr(gpu.greens, ref.greens) < MIXED_TOL
+
+
+def test_mixed_config1_greens_error(lib):
+    """Mixed form at config 1 shapes: |G_mixed - G_FP64| after 15 update calls
+    (delayed k = 16) with the accept sequences compared where the margin is
+    above the mixed-form error."""
+    p = R.Params(L=10, slices=100, delta_tau=0.1, safe_mult=10, lambda_=1.0, r=1.0, c=1.0, u=1.0, mu1=-0.5,
+                 mu2=-0.5, box=0.2)
+    calls = 15
+    phi = R.synthetic_field(p.N, p.slices, 31)
+    delta, u = R.synthetic_streams(p.N, calls, p.box, 32)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        mp = api_params(p)
+        mp.precision = prec
+        mp.delay = 16
+        g = lib.DQMC(mp, phi)
+        g.init()
+        res = g.sweep(calls, delta, u, return_accepted=True)
+        out[prec] = (g.greens, res["accepted_mask"], g.get_field())
+        g.close()
+    assert np.array_equal(out["fp64"][1], out["mixed"][1])
+    assert relerr(out["mixed"][0], out["fp64"][0]) < MIXED_TOL
