@@ -132,7 +132,7 @@ class ModelParams:
     all_checks: bool = True
     device: int = -1
     precision: str = "fp64"        # "fp64" or "mixed"
-    ozaki_bits: int = 0            # mantissa bits per GEMM operand in the mixed form (0 = default 35)
+    ozaki_bits: int = 0            # mantissa bits per GEMM operand in the mixed form (0 = default 40)
     delay: int = 0                 # delayed-update depth (0/1 = immediate rank-4)
 
     @property

@@ -45,7 +45,7 @@ struct dqmc_handle {
   // mixed form: split-BF16 GEMM scratch and slicing
   void* oz_scratch = nullptr;
   size_t oz_bytes = 0;
-  int oz_target = 35;   // mantissa bits kept per operand
+  int oz_target = 40;   // mantissa bits kept per operand
   // local updates
   double* delta_d = nullptr;
   double* unif_d = nullptr;
@@ -261,7 +261,7 @@ int qrp(dqmc_handle* h, cplx* A, cplx* T, double* D) {
   LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_qrp_finalize(A, T, D, h->n, h->qr, h->st));
   return DQMC_OK;
 }
-// X <- X Q with the reflectors of the last qrp
+// X <- X Q with the reflectors of the last qrp (one register-resident pass per row)
 int apply_q(dqmc_handle* h, cplx* X) {
   LAUNCH(DQMC_K_APPLYQ, 8.0 * n3(h), 40.0 * n2(h), launch_apply_q_right(X, h->n, h->n, h->qr, false, h->st));
   return DQMC_OK;
@@ -578,7 +578,7 @@ void host_model_constants(dqmc_handle* h) { fill_model_const(h->p, h->mc); }
 void free_all(dqmc_handle* h) {
   void* ptrs[] = {h->phi, h->evtab, h->G, h->Gtmp, h->u_stack, h->d_stack, h->t_stack, h->Ul, h->Ur, h->Tl,
                   h->Tr, h->Dl, h->Dr, h->W1, h->W2, h->W3, h->W4, h->D1, h->d2, h->ord1, h->qr.vn1,
-                  h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->delta_d, h->unif_d,
+                  h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->qr.cand_v, h->qr.cand_q, h->delta_d, h->unif_d,
                   h->acc_d, h->det_d, h->pacc_d, h->action_d, h->nacc_d, h->Acol, h->Brow, h->bar, h->err_d,
                   h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate};
   for (void* q : ptrs)
@@ -673,6 +673,7 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
   A((void**)&h->qr.order, n * sizeof(int)); A((void**)&h->qr.tau, n * sizeof(cplx));
   A((void**)&h->qr.beta, n * sizeof(double)); A((void**)&h->qr.V, nn);
   A((void**)&h->qr.bar, sizeof(GridBarrier));
+  A((void**)&h->qr.cand_v, 1024 * sizeof(double)); A((void**)&h->qr.cand_q, 1024 * sizeof(int));
   A((void**)&h->action_d, sizeof(double)); A((void**)&h->nacc_d, sizeof(int));
   A((void**)&h->Acol, 4 * n * sizeof(cplx)); A((void**)&h->Brow, 4 * n * sizeof(cplx));
   A((void**)&h->bar, sizeof(GridBarrier)); A((void**)&h->err_d, sizeof(int));
@@ -684,7 +685,7 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
     A((void**)&h->dstate, 2 * sizeof(int));
   }
   if (p->precision == DQMC_PREC_MIXED) {
-    h->oz_target = p->ozaki_bits > 0 ? p->ozaki_bits : 35;
+    h->oz_target = p->ozaki_bits > 0 ? p->ozaki_bits : 40;
     // the largest products are n x n x n; the flush (K = 4k) needs fewer slices
     int S = 0, bits = 0;
     if (!ozaki_plan((int)n, h->oz_target, &S, &bits)) return fail(DQMC_ERR_ARG);

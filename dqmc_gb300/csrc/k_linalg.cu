@@ -114,6 +114,12 @@ __device__ double block_sum(double v, double* scratch) {
 constexpr int QR_THREADS = 256;
 constexpr int QR_MAXT = 32;   // elements per lane of one column (n <= 1024)
 
+// Candidate of the next pivot: the CTA-local maximum of the partial norms
+// and its logical position (ties: smaller position, as LAPACK's idamax).
+__device__ __forceinline__ bool cand_better(double v, int q, double bv, int bq) {
+  return v > bv || (v == bv && q < bq);
+}
+
 __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n, QRWork w) {
   extern __shared__ double smem_qr[];
   cplx* v = reinterpret_cast<cplx*>(smem_qr);         // (n) current reflector
@@ -126,45 +132,65 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
   const double tol3z = sqrt(DBL_EPSILON);
 
   for (int q = threadIdx.x; q < n; q += blockDim.x) order[q] = q;
-  // initial column norms (zgeqp3: vn1 = vn2 = ||A(:, j)||)
+  // initial column norms (zgeqp3: vn1 = vn2 = ||A(:, j)||) and the first candidates
+  double cb = -1.0;
+  int cq = n;
   for (int j = gwarp; j < n; j += nwarps) {
     double s = 0.0;
     for (int r = lane; r < n; r += 32) s += cabs2(A[(size_t)j * n + r]);
     s = warp_sum(s);
     if (lane == 0) { w.vn1[j] = sqrt(s); w.vn2[j] = sqrt(s); }
+    if (cand_better(sqrt(s), j, cb, cq)) { cb = sqrt(s); cq = j; }
+  }
+  if (lane == 0) { red[wid] = cb; redi[wid] = cq; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = red[0]; int bq = redi[0];
+    for (int q = 1; q < warps; ++q)
+      if (cand_better(red[q], redi[q], b, bq)) { b = red[q]; bq = redi[q]; }
+    w.cand_v[blockIdx.x] = b;
+    w.cand_q[blockIdx.x] = bq;
   }
   if (!grid_barrier(w.bar, w.err)) return;
 
   for (int k = 0; k < n; ++k) {
-    // ---- pivot: first logical position of maximal partial norm ----
-    double best = -1.0;
-    int bestq = n;
-    for (int q = k + threadIdx.x; q < n; q += blockDim.x) {
-      double val = __ldcg(&w.vn1[order[q]]);
-      if (val > best) { best = val; bestq = q; }
-    }
+    // ---- pivot: best of the per-CTA candidates (first position of maximal norm) ----
+    {
+      double best = -1.0;
+      int bestq = n;
+      for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x) {
+        double val = __ldcg(&w.cand_v[c]);
+        int q = __ldcg(&w.cand_q[c]);
+        if (cand_better(val, q, best, bestq)) { best = val; bestq = q; }
+      }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      double ob = __shfl_xor_sync(0xffffffffu, best, o);
-      int oq = __shfl_xor_sync(0xffffffffu, bestq, o);
-      if (ob > best || (ob == best && oq < bestq)) { best = ob; bestq = oq; }
+      for (int o = 16; o > 0; o >>= 1) {
+        double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        int oq = __shfl_xor_sync(0xffffffffu, bestq, o);
+        if (cand_better(ob, oq, best, bestq)) { best = ob; bestq = oq; }
+      }
+      if (lane == 0) { red[wid] = best; redi[wid] = bestq; }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double b = red[0]; int bq = redi[0];
+        for (int q = 1; q < warps; ++q)
+          if (cand_better(red[q], redi[q], b, bq)) { b = red[q]; bq = redi[q]; }
+        if (bq < k || bq >= n) bq = k;   // no candidate (all norms zero): keep the order
+        int t = order[k]; order[k] = order[bq]; order[bq] = t;
+      }
+      __syncthreads();
     }
-    if (lane == 0) { red[wid] = best; redi[wid] = bestq; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double b = red[0]; int bq = redi[0];
-      for (int q = 1; q < warps; ++q)
-        if (red[q] > b || (red[q] == b && redi[q] < bq)) { b = red[q]; bq = redi[q]; }
-      int t = order[k]; order[k] = order[bq]; order[bq] = t;
-    }
-    __syncthreads();
     const int p = order[k];
-    // ---- reflector from A[k:n, p] (zlarfg) ----
+    // ---- reflector from A[k:n, p] (zlarfg); independent loads, 4 per thread at n <= 1024 ----
     double xn2 = 0.0;
-    for (int r = k + threadIdx.x; r < n; r += blockDim.x) {
-      cplx x = ldcg_c(&A[(size_t)p * n + r]);
-      v[r] = x;
-      if (r > k) xn2 += cabs2(x);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int r = k + threadIdx.x + u * QR_THREADS;
+      if (r < n) {
+        cplx x = ldcg_c(&A[(size_t)p * n + r]);
+        v[r] = x;
+        if (r > k) xn2 += cabs2(x);
+      }
     }
     xn2 = block_sum(xn2, red);   // includes __syncthreads
     const cplx alpha = v[k];
@@ -193,9 +219,14 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
     // first, so every SM keeps an equal share of the columns as k grows
     const cplx ctau = cconj(tau);
     const int rem = n - k - 1;
+    double cbest = -1.0;
+    int cbq = n;
     for (int t = blockIdx.x + gridDim.x * wid; t < rem; t += gridDim.x * warps) {
-      const int j = order[k + 1 + t];
+      const int qpos = k + 1 + t;
+      const int j = order[qpos];
       cplx* col = A + (size_t)j * n;
+      double vn1 = 0.0, vn2 = 0.0;
+      if (lane == 0) { vn1 = __ldcg(&w.vn1[j]); vn2 = __ldcg(&w.vn2[j]); }   // in flight during the update
       cplx x[QR_MAXT];
       cplx sp[4] = {cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0)};
       const int nq = (n - k + 31) >> 5;   // warp-uniform: no FP64 work on fully masked slots
@@ -224,12 +255,9 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
           else tp[q & 3] = fma(x[q].x, x[q].x, fma(x[q].y, x[q].y, tp[q & 3]));
         }
       }
-      xk = cmake(__shfl_sync(0xffffffffu, xk.x, 0), __shfl_sync(0xffffffffu, xk.y, 0));
       double tail = warp_sum((tp[0] + tp[1]) + (tp[2] + tp[3]));
       if (lane == 0) {
-        double vn1 = __ldcg(&w.vn1[j]);
         if (vn1 != 0.0) {
-          double vn2 = __ldcg(&w.vn2[j]);
           double ratio = sqrt(cabs2(xk)) / vn1;
           double temp = 1.0 - ratio * ratio;
           temp = temp > 0.0 ? temp : 0.0;
@@ -237,13 +265,26 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
           double temp2 = temp * r2 * r2;
           if (temp2 <= tol3z) {
             double nv = (k < n - 1) ? sqrt(tail) : 0.0;
-            w.vn1[j] = nv;
+            vn1 = nv;
+            vn2 = nv;
             w.vn2[j] = nv;
           } else {
-            w.vn1[j] = vn1 * sqrt(temp);
+            vn1 = vn1 * sqrt(temp);
           }
+          w.vn1[j] = vn1;
         }
+        if (cand_better(vn1, qpos, cbest, cbq)) { cbest = vn1; cbq = qpos; }
       }
+    }
+    // this CTA's candidate for the next pivot (lane 0 of each warp holds its best)
+    if (lane == 0) { red[wid] = cbest; redi[wid] = cbq; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double b = red[0]; int bq = redi[0];
+      for (int q = 1; q < warps; ++q)
+        if (cand_better(red[q], redi[q], b, bq)) { b = red[q]; bq = redi[q]; }
+      w.cand_v[blockIdx.x] = b;
+      w.cand_q[blockIdx.x] = bq;
     }
     if (!grid_barrier(w.bar, w.err)) return;
   }

@@ -72,6 +72,8 @@ struct QRWork {
   cplx* tau;         // (n)
   double* beta;      // (n) real diagonal of R in logical order
   cplx* V;           // (n, n) Householder vectors, column k = v_k (v_k[k] = 1, zero above)
+  double* cand_v;    // (grid) per-CTA pivot candidates: norm
+  int* cand_q;       // (grid) and logical position
   GridBarrier* bar;
   int* err;
 };
