@@ -89,6 +89,7 @@ SIGNATURES = {
     "dqmc_reset_timing": ([_P, _I32], ctypes.c_int),
     "dqmc_peak_fp64": ([_I32, _D], ctypes.c_int),
     "dqmc_gemm_check": ([_P, _I32, _D, _D, _D], ctypes.c_int),
+    "dqmc_force": ([_P, _D, _D], ctypes.c_int),
     "dqmc_local_updates_noalloc": ([ctypes.POINTER(CParams), ctypes.c_void_p, ctypes.c_void_p, _I32,
                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p], ctypes.c_int),
@@ -376,6 +377,24 @@ class DQMC:
         occ, ek = ctypes.c_double(), ctypes.c_double()
         self._check(self.lib.dqmc_measure(self.h, G.ctypes.data_as(_D), ctypes.byref(occ), ctypes.byref(ek)))
         return dict(greens=G, occupation=occ.value, e_kin=ek.value)
+
+    def force(self):
+        """(d log|det M|/d phi, d S_boson/d phi), each (3, N, M); needs the
+        state (slice M, direction -1) and returns to it."""
+        gl = np.zeros((3, self.N, self.M), order="F")
+        gb = np.zeros((3, self.N, self.M), order="F")
+        self._check(self.lib.dqmc_force(self.h, _dptr(gl), _dptr(gb)))
+        return gl, gb
+
+    def langevin_step(self, eps, rng):
+        """One Langevin move on the effective action S_b - log|det M|:
+        phi <- phi - eps (dS_b - dlog|det M|) + sqrt(2 eps) eta, then the stack
+        is rebuilt (dqmc_init)."""
+        gl, gb = self.force()
+        phi = self.get_field()
+        phi = phi - eps * (gb - gl) + np.sqrt(2.0 * eps) * rng.standard_normal(phi.shape)
+        self.init(phi)
+        return phi
 
     def gemm_check(self, A, B, mode):
         """C = A B with the FP64 kernel (mode 0) or the split-BF16 GEMM (mode 1)."""

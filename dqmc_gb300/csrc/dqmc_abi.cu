@@ -63,6 +63,7 @@ struct dqmc_handle {
   cplx* Xd = nullptr;
   cplx* Yd = nullptr;
   int* dstate = nullptr;
+  double* force_d = nullptr;   // (3, N, M) d log|det M| / d phi
   GridBarrier* bar = nullptr;
   int* err_d = nullptr;
   double* scal_d = nullptr;    // scratch scalars: [0] logdet sum, [1] absdiff
@@ -492,6 +493,32 @@ double boson_action_host(const dqmc_handle* h, const std::vector<double>& phi) {
   return S;
 }
 
+// d S_boson / d phi (src/action.jl:1-52): temporal, spatial (4 neighbours),
+// mass and quartic terms.
+void boson_gradient_host(const dqmc_handle* h, const std::vector<double>& phi, double* out) {
+  const int L = h->L, N = h->N, M = h->M;
+  const double dt = h->p.delta_tau, c = h->p.c, r = h->p.r, u = h->p.u;
+  auto at = [&](int a, int site, int sl) { return phi[(size_t)3 * ((size_t)N * sl + site) + a]; };
+  for (int sl = 0; sl < M; ++sl)
+    for (int x = 0; x < L; ++x)
+      for (int y = 0; y < L; ++y) {
+        const int s = y + L * x;
+        const int nbs[4] = {(y + 1) % L + L * x, y + L * ((x + 1) % L), (y - 1 + L) % L + L * x,
+                            y + L * ((x - 1 + L) % L)};
+        double sq = 0.0;
+        for (int a = 0; a < 3; ++a) sq += at(a, s, sl) * at(a, s, sl);
+        for (int a = 0; a < 3; ++a) {
+          const double v = at(a, s, sl);
+          double g = (2 * v - at(a, s, (sl + 1) % M) - at(a, s, (sl - 1 + M) % M)) / (dt * c * c);
+          double nsum = 0.0;
+          for (int q = 0; q < 4; ++q) nsum += at(a, nbs[q], sl);
+          g += dt * (4 * v - nsum);
+          g += dt * (r * v + u * sq * v);
+          out[(size_t)3 * ((size_t)N * sl + s) + a] = g;
+        }
+      }
+}
+
 int ensure_stream_capacity(dqmc_handle* h, int calls) {
   if (calls <= h->stream_cap) return DQMC_OK;
   if (h->delta_d) cudaFree(h->delta_d);
@@ -580,7 +607,7 @@ void free_all(dqmc_handle* h) {
                   h->Tr, h->Dl, h->Dr, h->W1, h->W2, h->W3, h->W4, h->D1, h->d2, h->ord1, h->qr.vn1,
                   h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->qr.cand_v, h->qr.cand_q, h->delta_d, h->unif_d,
                   h->acc_d, h->det_d, h->pacc_d, h->action_d, h->nacc_d, h->Acol, h->Brow, h->bar, h->err_d,
-                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate};
+                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->force_d};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   for (auto e : h->event_pool) cudaEventDestroy(e);
@@ -994,6 +1021,33 @@ int dqmc_calc_greens(dqmc_handle* h, int32_t slice, double* out, double* logdet)
   CHK(sync(h));
   if (logdet) *logdet = -sl;
   // the stack copies Ul..Tr were overwritten: restore nothing (propagate re-reads them from the stack)
+  return DQMC_OK;
+}
+
+int dqmc_force(dqmc_handle* h, double* grad_logdet, double* grad_boson) {
+  if (h) cudaSetDevice(h->device);
+  if (!h) return DQMC_ERR_ARG;
+  if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
+  if (h->current_slice != h->M || h->direction != -1)
+    return set_err(h, DQMC_ERR_STATE, "dqmc_force needs the state (slice M, direction -1)");
+  const size_t cnt = (size_t)3 * h->N * h->M;
+  if (!h->force_d) CU(cudaMalloc(&h->force_d, cnt * sizeof(double)));
+  const double ld = h->p.lambda * h->p.delta_tau;
+  // down pass: slices M, M-1, ..., 1
+  for (int c = 0; c < h->M; ++c) {
+    if (c > 0) CHK(propagate(h));
+    LAUNCH(DQMC_K_MISC, 0.0, 0.0, launch_force_slice(h->G, h->phi, h->force_d, h->N, h->current_slice - 1, ld, h->st));
+  }
+  // back to (M, -1): turnaround at 0 and the up pass
+  while (!(h->current_slice == h->M && h->direction == -1)) CHK(propagate(h));
+  if (grad_logdet) CU(cudaMemcpyAsync(grad_logdet, h->force_d, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CHK(sync(h));
+  if (grad_boson) {
+    std::vector<double> phi(cnt);
+    CU(cudaMemcpyAsync(phi.data(), h->phi, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CHK(sync(h));
+    boson_gradient_host(h, phi, grad_boson);
+  }
   return DQMC_OK;
 }
 

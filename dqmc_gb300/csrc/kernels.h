@@ -121,3 +121,8 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
                                const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
                                const double* colscale, int S, int bits, void* scratch, size_t scratch_bytes,
                                cudaStream_t st, const int* active = nullptr);
+
+// ---- adjoint force (k_force.cu) ----
+// grad[:, :, slice0] = d log|det M| / d phi[:, :, slice0] from G of that slice
+cudaError_t launch_force_slice(const cplx* G, const double* phi, double* grad, int N, int slice0, double lambda_dtau,
+                               cudaStream_t st);

@@ -205,6 +205,18 @@ DQMC_API int dqmc_calc_boson_action(dqmc_handle* h, double* S);
  * E_kin = sum_ij T_ij <c_i^dag c_j> (not an observable of the reference). */
 DQMC_API int dqmc_measure(dqmc_handle* h, double* greens_out, double* occupation, double* e_kin);
 
+/* ---- adjoint force ----------------------------------------------------------- */
+/* Gradients of the log-weight parts with respect to every field component
+ * (double[3*N*M], layout of phi):
+ *   grad_logdet[a,i,l] = d log|det M| / d phi[a,i,l] = -Re tr(G_l[ii] E_i^-1 dE_i/dphi_a),
+ *   grad_boson[a,i,l]  = d S_boson / d phi[a,i,l]  (src/action.jl:1-52).
+ * M = 1 + B_M ... B_1; G_l is the equal-time G of slice l, taken from the
+ * stack (checkpointed UDTs every safe_mult slices, wrapped in between) during
+ * one down pass, after which the state returns to (slice M, direction -1).
+ * Needs the state (M, -1), i.e. right after dqmc_init or after 2M updates.
+ * No counterpart in the reference; either output may be NULL. */
+DQMC_API int dqmc_force(dqmc_handle* h, double* grad_logdet, double* grad_boson);
+
 /* ---- diagnostics ------------------------------------------------------------- */
 /* Per-group device times (CUDA events on the handle's stream) and the number
  * of kernels launched since the last reset; enable != 0 turns event timing on. */

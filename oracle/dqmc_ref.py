@@ -722,6 +722,70 @@ class DQMCRef:
 
 
 # ---------------------------------------------------------------------------
+# gradients of the log-weight (not in the reference; built from its pieces)
+# ---------------------------------------------------------------------------
+def interaction_op_derivs(p: Params, op):
+    """E = exp(-dtau V(op)) (power +1) of one site and dE/dop_a, a = 0..2,
+    from C = cosh(x), S = (i op2 - op1) sh, R = -op3 sh, sh = sinh(x)/|op|,
+    x = lambda dtau |op| (src/interactions.jl:102-141)."""
+    nrm = math.sqrt(op[0] ** 2 + op[1] ** 2 + op[2] ** 2)
+    x = p.lambda_ * p.delta_tau * nrm
+    sh = math.sinh(x) / nrm
+    C = math.cosh(x)
+    dsh = (p.lambda_ * p.delta_tau * C - sh) / nrm ** 2      # (d sh / d op_a) / op_a
+    out = []
+    for a in range(3):
+        dC = p.lambda_ * p.delta_tau * op[a] * sh
+        dS = (1j * op[1] - op[0]) * dsh * op[a] + ((1j if a == 1 else 0) - (1 if a == 0 else 0)) * sh
+        dR = -op[2] * dsh * op[a] - (sh if a == 2 else 0.0)
+        e = np.zeros((4, 4), dtype=np.complex128)
+        e[0, 0] = dC; e[0, 1] = dS; e[1, 0] = np.conj(dS); e[1, 1] = dC
+        e[0, 3] = dR; e[1, 2] = -dR; e[2, 1] = -dR; e[2, 2] = dC; e[2, 3] = np.conj(dS)
+        e[3, 0] = dR; e[3, 2] = dS; e[3, 3] = dC
+        out.append(e)
+    return out
+
+
+def force_logdetM(mc: "DQMCRef"):
+    """d log|det M| / d phi[a, i, l] = -Re tr(G_l[ii] E_i^-1 dE_i/dphi_a), with
+    M = 1 + B_M ... B_1 and G_l the equal-time G of slice l (computed from
+    scratch, src/fermion_measurements.jl:1061)."""
+    p, N, M = mc.p, mc.N, mc.M
+    grad = np.zeros((3, N, M))
+    for l in range(1, M + 1):
+        G = mc.calc_greens(l)
+        for i in range(N):
+            op = mc.phi[:, i, l - 1]
+            Einv = interaction_op(p, op, -1.0)
+            dE = interaction_op_derivs(p, op)
+            Gii = G[i::N, i::N]
+            for a in range(3):
+                grad[a, i, l - 1] = -np.real(np.trace(Gii @ Einv @ dE[a]))
+    return grad
+
+
+def force_boson(p: Params, phi):
+    """d S_boson / d phi (src/action.jl:1-52)."""
+    L, M = p.L, phi.shape[2]
+    h = phi.reshape((3, L, L, M), order="F")
+    g = (2 * h - np.roll(h, -1, axis=3) - np.roll(h, 1, axis=3)) / (p.delta_tau * p.c ** 2)
+    if not p.edrun:
+        nb = np.roll(h, -1, axis=1) + np.roll(h, 1, axis=1) + np.roll(h, -1, axis=2) + np.roll(h, 1, axis=2)
+        g = g + p.delta_tau * (4 * h - nb)
+    else:
+        g = np.zeros_like(h)
+    sq = np.sum(h * h, axis=0)[None]
+    g = g + p.delta_tau * (p.r * h + (0.0 if p.edrun else p.u) * sq * h)
+    return g.reshape((3, L * L, M), order="F")
+
+
+def log_weight_parts(mc: "DQMCRef"):
+    """(log|det M|, S_boson) of the current field; log|det M| = -log|det G|."""
+    _, ld = mc.calc_greens_and_logdet(1)
+    return -ld, boson_action(mc.p, mc.phi)
+
+
+# ---------------------------------------------------------------------------
 # boson measurements  (src/boson_measurements.jl:6-56)
 # ---------------------------------------------------------------------------
 def measure_chi_dynamic(conf, delta_tau=0.1):

@@ -100,3 +100,28 @@ def test_local_update_consistency(mc):
     assert 0 < rate <= 1
     assert np.max(np.abs(m.greens - m.calc_greens(m.current_slice))) < 1e-10
     assert np.isclose(m.boson_action_value, R.boson_action(m.p, m.phi), rtol=1e-12)
+
+
+def test_force_formula_matches_finite_differences(small_params):
+    """The adjoint force formula d log|det M|/d phi = -Re tr(G_ii E^-1 dE) and
+    the boson-action gradient against central differences (h = 1e-5) of the
+    log-weight parts on random entries."""
+    p = dataclasses.replace(small_params, slices=10, lambda_=1.0, r=1.0, c=1.0, u=1.0)
+    phi = R.synthetic_field(p.N, p.slices, 21)
+    m = R.DQMCRef(p, phi)
+    gl = R.force_logdetM(m)
+    gb = R.force_boson(p, phi)
+    rng = np.random.default_rng(22)
+    h = 1e-5
+    for _ in range(6):
+        a, i, l = rng.integers(3), rng.integers(p.N), rng.integers(p.slices)
+        vals = []
+        for sgn in (1, -1):
+            ph = phi.copy()
+            ph[a, i, l] += sgn * h
+            mm = R.DQMCRef(p, ph)
+            vals.append(R.log_weight_parts(mm))
+        fd_logdet = (vals[0][0] - vals[1][0]) / (2 * h)
+        fd_boson = (vals[0][1] - vals[1][1]) / (2 * h)
+        assert abs(gl[a, i, l] - fd_logdet) <= 1e-6 * max(1.0, abs(fd_logdet))
+        assert abs(gb[a, i, l] - fd_boson) <= 1e-6 * max(1.0, abs(fd_boson))
