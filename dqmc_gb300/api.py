@@ -90,6 +90,7 @@ SIGNATURES = {
     "dqmc_peak_fp64": ([_I32, _D], ctypes.c_int),
     "dqmc_gemm_check": ([_P, _I32, _D, _D, _D], ctypes.c_int),
     "dqmc_force": ([_P, _D, _D], ctypes.c_int),
+    "dqmc_global_update": ([_P, _D, ctypes.c_double, ctypes.POINTER(_I32), _D], ctypes.c_int),
     "dqmc_local_updates_noalloc": ([ctypes.POINTER(CParams), ctypes.c_void_p, ctypes.c_void_p, _I32,
                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p], ctypes.c_int),
@@ -377,6 +378,14 @@ class DQMC:
         occ, ek = ctypes.c_double(), ctypes.c_double()
         self._check(self.lib.dqmc_measure(self.h, G.ctypes.data_as(_D), ctypes.byref(occ), ctypes.byref(ek)))
         return dict(greens=G, occupation=occ.value, e_kin=ek.value)
+
+    def global_update(self, shift, u):
+        """global_update (src/global_updates.jl:18-58) with a fixed-slot shift
+        (3,) and uniform u; returns (accepted, p_acc)."""
+        sh = np.ascontiguousarray(shift, dtype=np.float64).reshape(3)
+        acc, pa = _I32(), ctypes.c_double()
+        self._check(self.lib.dqmc_global_update(self.h, _dptr(sh), float(u), ctypes.byref(acc), ctypes.byref(pa)))
+        return bool(acc.value), pa.value
 
     def force(self):
         """(d log|det M|/d phi, d S_boson/d phi), each (3, N, M); needs the

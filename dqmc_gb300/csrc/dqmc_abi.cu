@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <utility>
 #include <string>
 #include <vector>
 
@@ -64,6 +65,10 @@ struct dqmc_handle {
   cplx* Yd = nullptr;
   int* dstate = nullptr;
   double* force_d = nullptr;   // (3, N, M) d log|det M| / d phi
+  // global updates: backup of stack, G, field and interaction table (allocated on first use)
+  cplx *gb_u = nullptr, *gb_t = nullptr, *gb_G = nullptr;
+  double *gb_d = nullptr, *gb_phi = nullptr;
+  void* gb_evtab = nullptr;
   GridBarrier* bar = nullptr;
   int* err_d = nullptr;
   double* scal_d = nullptr;    // scratch scalars: [0] logdet sum, [1] absdiff
@@ -607,7 +612,7 @@ void free_all(dqmc_handle* h) {
                   h->Tr, h->Dl, h->Dr, h->W1, h->W2, h->W3, h->W4, h->D1, h->d2, h->ord1, h->qr.vn1,
                   h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->qr.cand_v, h->qr.cand_q, h->delta_d, h->unif_d,
                   h->acc_d, h->det_d, h->pacc_d, h->action_d, h->nacc_d, h->Acol, h->Brow, h->bar, h->err_d,
-                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->force_d};
+                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   for (auto e : h->event_pool) cudaEventDestroy(e);
@@ -1021,6 +1026,65 @@ int dqmc_calc_greens(dqmc_handle* h, int32_t slice, double* out, double* logdet)
   CHK(sync(h));
   if (logdet) *logdet = -sl;
   // the stack copies Ul..Tr were overwritten: restore nothing (propagate re-reads them from the stack)
+  return DQMC_OK;
+}
+
+int dqmc_global_update(dqmc_handle* h, const double* shift, double u, int32_t* accepted, double* p_acc) {
+  if (h) cudaSetDevice(h->device);
+  if (!h || !shift) return DQMC_ERR_ARG;
+  if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
+  if (h->current_slice != h->M || h->direction != -1)
+    return set_err(h, DQMC_ERR_STATE, "dqmc_global_update needs the state (slice M, direction -1)");
+  const size_t stack_c = (size_t)h->ne * h->n * h->n, NM = (size_t)h->N * h->M;
+  if (!h->gb_u) {
+    CU(cudaMalloc(&h->gb_u, stack_c * sizeof(cplx)));
+    CU(cudaMalloc(&h->gb_t, stack_c * sizeof(cplx)));
+    CU(cudaMalloc(&h->gb_d, (size_t)h->ne * h->n * sizeof(double)));
+    CU(cudaMalloc(&h->gb_G, nn_bytes(h)));
+    CU(cudaMalloc(&h->gb_phi, 3 * NM * sizeof(double)));
+    CU(cudaMalloc(&h->gb_evtab, NM * evtab_entry_bytes()));
+  }
+  double S_old = 0.0, ldsum_old = 0.0;
+  CU(cudaMemcpyAsync(&S_old, h->action_d, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaMemcpyAsync(&ldsum_old, h->scal_d + 2, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CHK(sync(h));
+  // back up (stack and G by pointer swap, field and table by copy), shift, rebuild
+  std::swap(h->u_stack, h->gb_u);
+  std::swap(h->t_stack, h->gb_t);
+  std::swap(h->d_stack, h->gb_d);
+  std::swap(h->G, h->gb_G);
+  CU(cudaMemcpyAsync(h->gb_phi, h->phi, 3 * NM * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  CU(cudaMemcpyAsync(h->gb_evtab, h->evtab, NM * evtab_entry_bytes(), cudaMemcpyDeviceToDevice, h->st));
+  LAUNCH(DQMC_K_MISC, 0.0, 0.0, launch_shift_field(h->phi, NM, shift[0], shift[1], shift[2], h->st));
+  LAUNCH(DQMC_K_MISC, 0.0, 0.0,
+         launch_build_evtab(h->phi, h->evtab, h->N, h->M, h->p.lambda * h->p.delta_tau, h->st));
+  CHK(build_stack(h));
+  CHK(propagate(h));
+  std::vector<double> phi(3 * NM);
+  double ldsum_new = 0.0;
+  CU(cudaMemcpyAsync(phi.data(), h->phi, phi.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaMemcpyAsync(&ldsum_new, h->scal_d + 2, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CHK(sync(h));
+  const double S_new = boson_action_host(h, phi);
+  // log det G = -sum log d2; p_fermion = exp(logdetG_old - logdetG_new)
+  const double p_boson = std::exp(-(S_new - S_old));
+  const double p_fermion = std::exp(-ldsum_old + ldsum_new);
+  const double p = p_boson * p_fermion;
+  const bool acc = p > 1.0 || u < p;
+  if (acc) {
+    CU(cudaMemcpyAsync(h->action_d, &S_new, sizeof(double), cudaMemcpyHostToDevice, h->st));
+  } else {
+    std::swap(h->u_stack, h->gb_u);
+    std::swap(h->t_stack, h->gb_t);
+    std::swap(h->d_stack, h->gb_d);
+    std::swap(h->G, h->gb_G);
+    CU(cudaMemcpyAsync(h->phi, h->gb_phi, 3 * NM * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    CU(cudaMemcpyAsync(h->evtab, h->gb_evtab, NM * evtab_entry_bytes(), cudaMemcpyDeviceToDevice, h->st));
+    CU(cudaMemcpyAsync(h->scal_d + 2, &ldsum_old, sizeof(double), cudaMemcpyHostToDevice, h->st));
+  }
+  CHK(sync(h));
+  if (accepted) *accepted = acc ? 1 : 0;
+  if (p_acc) *p_acc = p;
   return DQMC_OK;
 }
 

@@ -55,7 +55,22 @@ __global__ void k_force_slice(const cplx* __restrict__ G, const double* __restri
   }
 }
 
+__global__ void k_shift_field(double* phi, size_t NM, double s0, double s1, double s2) {
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < NM; e += (size_t)gridDim.x * blockDim.x) {
+    phi[3 * e] += s0;
+    phi[3 * e + 1] += s1;
+    phi[3 * e + 2] += s2;
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_shift_field(double* phi, size_t NM, double s0, double s1, double s2, cudaStream_t st) {
+  int grid = (int)((NM + 255) / 256);
+  if (grid > 4096) grid = 4096;
+  k_shift_field<<<grid, 256, 0, st>>>(phi, NM, s0, s1, s2);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_force_slice(const cplx* G, const double* phi, double* grad, int N, int slice0, double lambda_dtau,
                                cudaStream_t st) {

@@ -126,3 +126,5 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
 // grad[:, :, slice0] = d log|det M| / d phi[:, :, slice0] from G of that slice
 cudaError_t launch_force_slice(const cplx* G, const double* phi, double* grad, int N, int slice0, double lambda_dtau,
                                cudaStream_t st);
+// phi[a, :, :] += shift[a] for a = 0..2 (field of N sites x M slices)
+cudaError_t launch_shift_field(double* phi, size_t NM, double s0, double s1, double s2, cudaStream_t st);

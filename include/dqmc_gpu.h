@@ -205,6 +205,14 @@ DQMC_API int dqmc_calc_boson_action(dqmc_handle* h, double* S);
  * E_kin = sum_ij T_ij <c_i^dag c_j> (not an observable of the reference). */
 DQMC_API int dqmc_measure(dqmc_handle* h, double* greens_out, double* occupation, double* e_kin);
 
+/* global_update (src/global_updates.jl:18-58): shift every slice and site of
+ * field component k by shift[k] (fixed slot, already in [-box_global,
+ * box_global]), rebuild the stack, and accept with
+ * p = exp(-(S_new - S_old)) * exp(logdetG_old - logdetG_new) if p > 1 or
+ * u < p; a rejection restores field, stack, G and action.  Needs the state
+ * (M, -1).  accepted / p_acc may be NULL. */
+DQMC_API int dqmc_global_update(dqmc_handle* h, const double* shift, double u, int32_t* accepted, double* p_acc);
+
 /* ---- adjoint force ----------------------------------------------------------- */
 /* Gradients of the log-weight parts with respect to every field component
  * (double[3*N*M], layout of phi):

@@ -647,6 +647,28 @@ class DQMCRef:
                 self.update_greens(i)
         return acc / N
 
+    def global_update(self, shift, u):
+        """src/global_updates.jl:18-58 with a fixed-slot shift (3,) (already in
+        [-box_global, box_global]) and Metropolis uniform u.  Needs the state
+        (M, -1).  Returns (accepted, p_acc)."""
+        assert self.current_slice == self.M and self.direction == -1
+        S_old = self.boson_action_value
+        backup = (self.u_stack.copy(), self.d_stack.copy(), self.t_stack.copy(), self.greens.copy(),
+                  self.log_det, self.phi.copy())
+        for k in range(3):
+            self.phi[k, :, :] += shift[k]
+        self.build_stack()
+        self.propagate()
+        self.boson_action_value = boson_action(self.p, self.phi)
+        p_boson = math.exp(-(self.boson_action_value - S_old))
+        p_fermion = math.exp(backup[4] - self.log_det)
+        p_acc = p_boson * p_fermion
+        if p_acc > 1.0 or u < p_acc:
+            return True, p_acc
+        self.boson_action_value = S_old
+        self.u_stack, self.d_stack, self.t_stack, self.greens, self.log_det, self.phi = backup
+        return False, p_acc
+
     def update(self, delta, uniforms, record=None):
         """src/dqmc_framework.jl:500-517 with global updates off."""
         self.propagate()

@@ -336,3 +336,31 @@ def test_langevin_steps(lib):
         assert np.all(np.isfinite(phi))
     assert np.isfinite(gpu.log_det)
     assert abs(gpu.boson_action - R.boson_action(p, gpu.get_field())) < 1e-9 * abs(gpu.boson_action)
+
+
+# ---------------------------------------------------------------------------
+# global update (src/global_updates.jl:18-58)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("force_accept", [True, False])
+def test_global_update(lib, force_accept):
+    p = C0
+    phi = R.synthetic_field(p.N, p.slices, 91)
+    shift = np.array([0.05, -0.03, 0.02])
+    u = 0.0 if force_accept else 1.0 - 1e-15
+    ref = R.DQMCRef(p, phi)
+    ref.init()
+    acc_r, pacc_r = ref.global_update(shift, u)
+    gpu = lib.DQMC(api_params(p), phi)
+    gpu.init()
+    acc_g, pacc_g = gpu.global_update(shift, u)
+    assert abs(pacc_g - pacc_r) < 1e-9 * max(1.0, pacc_r)
+    if pacc_r < 1.0 - 1e-9:
+        assert acc_g == acc_r == force_accept
+    assert np.allclose(gpu.get_field(), ref.phi, rtol=0, atol=1e-15)
+    assert relerr(gpu.greens, ref.greens) < TOL
+    assert abs(gpu.boson_action - ref.boson_action_value) < 1e-10 * abs(ref.boson_action_value)
+    # the sweep continues from the (possibly restored) state
+    delta, uu = R.synthetic_streams(p.N, 3, p.box, 92)
+    ref.sweep(3, delta, uu)
+    gpu.sweep(3, delta, uu)
+    assert relerr(gpu.greens, ref.greens) < TOL
