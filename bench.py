@@ -40,6 +40,7 @@ if ROOT not in sys.path:
 CONFIGS = {
     # name: (L, M, description)
     "c0": (4, 40, "O(3) L=4 beta=4 (M=40) dtau=0.1 safe_mult=10 FP64"),
+    "c2": (0, 80, "64 independent O(3) chains, L uniform in {6,8,10,12}, beta=8 (M=80) dtau=0.1 safe_mult=10"),
     "c1": (10, 100, "O(3) L=10 beta=10 (M=100) dtau=0.1 safe_mult=10 FP64"),
     "c3": (16, 200, "O(3) L=16 beta=20 (M=200) dtau=0.1 safe_mult=10 FP64"),
     "c4": (12, 100, "O(3) L=12 beta=10 (M=100) dtau=0.1 safe_mult=10 FP64"),
@@ -201,6 +202,83 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args, world, rank, local):
+    """Config c2: 64 chains of uneven L swept concurrently (dqmc_batch_*);
+    value = chain-sweeps/s of all chains (wall clock around the batch sweep,
+    synchronised; the device streams are resident)."""
+    import torch
+    from dqmc_gb300 import api
+    from oracle.dqmc_ref import synthetic_field, synthetic_streams
+
+    _, M, desc = CONFIGS["c2"]
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(2000 + rank)
+    Ls = [int(x) for x in rng.choice([6, 8, 10, 12], size=args.chains)]
+    plist, fields = [], []
+    for k, L in enumerate(Ls):
+        rp = model_params(L, M)
+        plist.append(api.ModelParams(L=L, slices=M, safe_mult=10, delta_tau=rp.delta_tau, lambda_=rp.lambda_,
+                                     r=rp.r, c=rp.c, u=rp.u, mu1=rp.mu1, mu2=rp.mu2, hoppings=rp.hoppings,
+                                     box=rp.box, all_checks=not args.no_checks, device=dev,
+                                     precision=args.precision, delay=args.delay))
+        fields.append(synthetic_field(L * L, M, 3000 + 100 * rank + k))
+    batch = api.Batch(plist, fields)
+    batch.init()
+    sweeps = args.warmup + args.steps
+    d_dev, u_dev = [], []
+    for k, L in enumerate(Ls):
+        delta, unif = synthetic_streams(L * L, sweeps * M, 0.2, 4000 + 100 * rank + k)
+        d_dev.append(torch.from_numpy(np.ascontiguousarray(np.transpose(delta, (0, 2, 1)))).to(f"cuda:{dev}"))
+        u_dev.append(torch.from_numpy(np.ascontiguousarray(unif)).to(f"cuda:{dev}"))
+    torch.cuda.synchronize()
+
+    def run(s):
+        off = s * M
+        return batch.sweep_device(M, [t.data_ptr() + off * 3 * (L * L) * 8 for t, L in zip(d_dev, Ls)],
+                                  [t.data_ptr() + off * (L * L) * 8 for t, L in zip(u_dev, Ls)])
+
+    for s in range(args.warmup):
+        run(s)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    t0 = time.perf_counter()
+    acc = prop = 0
+    for s in range(args.warmup, sweeps):
+        st = run(s)
+        acc += sum(x["accepted"] for x in st)
+        prop += sum(x["proposals"] for x in st)
+    torch.cuda.synchronize()
+    barrier(world)
+    wall = allreduce_max(time.perf_counter() - t0, world)
+    clk = clocks.stop()
+    value = world * args.chains * args.steps / wall
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu:
+            from oracle import dqmc_ref as R
+            rp = model_params(8, M)
+            val, secs = cpu_baseline(rp, R.synthetic_field(rp.N, M, 5), args.cpu_calls, 6, os.cpu_count() or 1)
+            cpu = {"value": val, "unit": "chain-sweeps/s", "cores": os.cpu_count() or 1, "kind": "port",
+                   "sample": f"one L=8 chain, {args.cpu_calls} of {M} update calls (numpy/scipy oracle), "
+                             f"{secs:.1f} s, extrapolated; chains run one after another on the CPU"}
+        line = {
+            "metric": METRIC, "value": value, "unit": "chain-sweeps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall * 1000.0 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f64 + split-bf16 tensor GEMMs",
+            "data": "synthetic (seeded uniform[-1,1] fields, uniform proposal/Metropolis streams)",
+            "config": {"workload": desc, "chains": args.chains, "L_counts": {L: Ls.count(L) for L in (6, 8, 10, 12)},
+                       "slices": M, "precision": args.precision, "delay": args.delay,
+                       "parallelism": f"{args.chains} chains per GPU, replicas x{world}"},
+            "acc_rate": acc / max(1, prop), "clocks": clk, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    batch.close()
+
+
 def run_ours(args, world, rank, local):
     import torch
     from dqmc_gb300 import api
@@ -348,10 +426,13 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--delay", type=int, default=16, help="delayed-update depth k (1 = immediate rank-4)")
+    ap.add_argument("--chains", type=int, default=64, help="chains of the batched config c2")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.config == "c2":
+        run_batch(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)
     if world > 1:

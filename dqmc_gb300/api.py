@@ -91,6 +91,11 @@ SIGNATURES = {
     "dqmc_gemm_check": ([_P, _I32, _D, _D, _D], ctypes.c_int),
     "dqmc_force": ([_P, _D, _D], ctypes.c_int),
     "dqmc_global_update": ([_P, _D, ctypes.c_double, ctypes.POINTER(_I32), _D], ctypes.c_int),
+    "dqmc_batch_create": ([ctypes.POINTER(CParams), _I32, ctypes.POINTER(_P)], ctypes.c_int),
+    "dqmc_batch_destroy": ([_P], ctypes.c_int),
+    "dqmc_batch_handle": ([_P, _I32, ctypes.POINTER(_P)], ctypes.c_int),
+    "dqmc_batch_sweep": ([_P, _I32, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                          ctypes.POINTER(CStats)], ctypes.c_int),
     "dqmc_local_updates_noalloc": ([ctypes.POINTER(CParams), ctypes.c_void_p, ctypes.c_void_p, _I32,
                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p], ctypes.c_int),
@@ -196,9 +201,9 @@ class DQMC:
             self.set_field(phi)
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and getattr(self, "_owned", True):
             self.lib.dqmc_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -424,3 +429,57 @@ class DQMC:
 
     def reset_timing(self, enable=True):
         self._check(self.lib.dqmc_reset_timing(self.h, 1 if enable else 0))
+
+
+class Batch:
+    """Independent chains sharing one GPU (dqmc_batch_*).  `chains[i]` is a
+    DQMC view of chain i for the single-chain calls."""
+
+    def __init__(self, params_list, fields=None):
+        self.lib = load_library()
+        arr = (CParams * len(params_list))(*[p.to_c() for p in params_list])
+        b = ctypes.c_void_p()
+        rc = self.lib.dqmc_batch_create(arr, len(params_list), ctypes.byref(b))
+        if rc != DQMC_OK:
+            raise DQMCError(rc, "dqmc_batch_create failed")
+        self.b = b
+        self.params = list(params_list)
+        self.chains = []
+        for i, p in enumerate(params_list):
+            h = ctypes.c_void_p()
+            self.lib.dqmc_batch_handle(self.b, i, ctypes.byref(h))
+            c = DQMC.__new__(DQMC)
+            c.lib, c.p, c.N, c.n, c.M, c.h = self.lib, p, p.N, p.n, p.slices, h
+            c._owned = False
+            self.chains.append(c)
+        if fields is not None:
+            for c, f in zip(self.chains, fields):
+                c.set_field(f)
+
+    def init(self):
+        for c in self.chains:
+            c.init()
+
+    def sweep_device(self, n_calls, delta_ptrs, unif_ptrs):
+        """n_calls update() calls on every chain; *_ptrs are device addresses
+        (ints) of each chain's streams.  Returns a list of stats dicts."""
+        C = len(self.chains)
+        dp = (ctypes.c_void_p * C)(*delta_ptrs)
+        up = (ctypes.c_void_p * C)(*unif_ptrs)
+        st = (CStats * C)()
+        rc = self.lib.dqmc_batch_sweep(self.b, int(n_calls), dp, up, st)
+        if rc != DQMC_OK:
+            raise DQMCError(rc, "dqmc_batch_sweep failed")
+        return [dict(proposals=s.proposals, accepted=s.accepted, acc_rate=s.acc_rate,
+                     max_instability=s.max_instability, device_ms=s.device_ms) for s in st]
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.lib.dqmc_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

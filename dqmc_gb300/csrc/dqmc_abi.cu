@@ -6,7 +6,10 @@
 // memory is allocated once in dqmc_create.
 #include <cmath>
 #include <cstdio>
+#include <algorithm>
+#include <chrono>
 #include <cstring>
+#include <thread>
 #include <utility>
 #include <string>
 #include <vector>
@@ -29,6 +32,7 @@ struct dqmc_handle {
   cudaStream_t st = nullptr;
   int sm_count = 0;
   int device = 0;
+  int coop_cap = 0;            // > 0: cap of the cooperative grids (chains sharing the GPU)
   // ---- device state ----
   double* phi = nullptr;       // (3, N, M)
   void* evtab = nullptr;       // (N, M) EvEntry
@@ -71,7 +75,9 @@ struct dqmc_handle {
   void* gb_evtab = nullptr;
   GridBarrier* bar = nullptr;
   int* err_d = nullptr;
-  double* scal_d = nullptr;    // scratch scalars: [0] logdet sum, [1] absdiff
+  double* scal_d = nullptr;    // scalars: [0] sum log d2, [1] absdiff, [2] saved sum log d2, [3] instability max
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;   // brackets of the last enqueued sweep
+  int pending_calls = 0;
   // ---- host state ----
   int current_slice = 0;
   int direction = 1;
@@ -174,10 +180,13 @@ int check_device_error(dqmc_handle* h) {
   return set_err(h, DQMC_ERR_CUDA, "device error flag " + std::to_string(e));
 }
 
+int read_instability(dqmc_handle* h);
+
 int sync(dqmc_handle* h) {
   CU(cudaStreamSynchronize(h->st));
   if (h->timing) resolve_spans(h);
-  return check_device_error(h);
+  CHK(check_device_error(h));
+  return read_instability(h);
 }
 
 size_t nn_bytes(const dqmc_handle* h) { return (size_t)h->n * h->n * sizeof(cplx); }
@@ -201,9 +210,7 @@ int set_identity(dqmc_handle* h, cplx* A) {
 }
 
 int set_ones(dqmc_handle* h, double* d) {
-  std::vector<double> ones(h->n, 1.0);
-  CU(cudaMemcpyAsync(d, ones.data(), h->n * sizeof(double), cudaMemcpyHostToDevice, h->st));
-  CU(cudaStreamSynchronize(h->st));
+  LAUNCH(DQMC_K_MISC, 0.0, 8.0 * h->n, launch_fill(d, h->n, 1.0, h->st));
   return DQMC_OK;
 }
 
@@ -263,7 +270,7 @@ int gemm(dqmc_handle* h, char opA, char opB, const cplx* A, const cplx* B, cplx*
 }
 // pivoted QR of A (destroyed) -> T (physical layout), D; reflectors in h->qr
 int qrp(dqmc_handle* h, cplx* A, cplx* T, double* D) {
-  LAUNCH(DQMC_K_QRP, 16.0 / 3.0 * n3(h), 32.0 * n2(h), launch_qrp(A, h->n, h->qr, h->sm_count, h->st));
+  LAUNCH(DQMC_K_QRP, 16.0 / 3.0 * n3(h), 32.0 * n2(h), launch_qrp(A, h->n, h->qr, h->sm_count, h->st, h->coop_cap));
   LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_qrp_finalize(A, T, D, h->n, h->qr, h->st));
   return DQMC_OK;
 }
@@ -384,10 +391,18 @@ int stack_identity(dqmc_handle* h, int k) {
   return DQMC_OK;
 }
 
+// max |G_wrapped - G_fresh| of this stabilisation folded into the running
+// maximum scal_d[3] on the device (read when the call finishes).
 int instability_check(dqmc_handle* h) {
-  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_max_absdiff(h->Gtmp, h->G, (size_t)h->n * h->n, h->scal_d + 1, h->st));
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h),
+         launch_max_absdiff(h->Gtmp, h->G, (size_t)h->n * h->n, h->scal_d + 3, h->st, false));
+  return DQMC_OK;
+}
+
+// Reads the running instability maximum (stream must be idle).
+int read_instability(dqmc_handle* h) {
   double d = 0.0;
-  CU(cudaMemcpyAsync(&d, h->scal_d + 1, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaMemcpyAsync(&d, h->scal_d + 3, sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CU(cudaStreamSynchronize(h->st));
   if (!(d <= h->max_instability)) h->max_instability = d;
   if (!std::isfinite(d)) return set_err(h, DQMC_ERR_NONFINITE, "non-finite Green's function");
@@ -554,7 +569,7 @@ int ensure_out_capacity(dqmc_handle* h, int calls) {
 // local_updates (src/local_updates.jl:1-38) on device streams; outputs to
 // device arrays (may be null).  delay <= 1: immediate rank-4 updates in one
 // cooperative launch.  delay = k > 1: rounds of [local kernel until k accepts
-// are pending, flush G += X Y (FP64 or split-BF16 GEMM), factor reset]; the
+// are pending, flush G += X Y (FP64 or split-BF16 GEMM)]; the
 // number of rounds is the bound ceil(N/k) + 1 and rounds with nothing left
 // return at once on a device-side flag, so the host never waits.
 int local_updates_dev(dqmc_handle* h, const double* delta_dev, const double* unif_dev, uint8_t* acc_dev,
@@ -581,7 +596,7 @@ int local_updates_dev(dqmc_handle* h, const double* delta_dev, const double* uni
   if (h->delay <= 1) {
     // flops/bytes of the local updates depend on the acceptances; the caller
     // derives them from the accepted count (32 n^2 flops and bytes per accept)
-    LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_updates(a, h->sm_count, h->st));
+    LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_updates(a, h->sm_count, h->st, h->coop_cap));
     return DQMC_OK;
   }
   const int n = h->n, k = h->delay;
@@ -589,12 +604,11 @@ int local_updates_dev(dqmc_handle* h, const double* delta_dev, const double* uni
   CU(cudaMemsetAsync(h->dstate, 0, 2 * sizeof(int), h->st));
   const int rounds = (h->N + k - 1) / k + 1;
   for (int r = 0; r < rounds; ++r) {
-    LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_delayed(a, d, h->sm_count, h->st));
-    // flush G += X Y, skipped on the device when no update is pending
+    LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_delayed(a, d, h->sm_count, h->st, h->coop_cap));
+    // flush G += X Y over the 4p pending columns (p read on the device; no
+    // work when p = 0); the next round clears p
     CHK(zgemm_general(h, n, n, 4 * k, 'N', 'T', cmake(1, 0), h->Xd, n, h->Yd, n, cmake(1, 0), h->G, n, nullptr,
                       nullptr, true, DQMC_K_FLUSH, h->dstate + 1));
-    LAUNCH(DQMC_K_MISC, 0.0, 0.0, launch_delayed_reset(d, n, h->st));
-    h->launches++;
   }
   return DQMC_OK;
 }
@@ -616,6 +630,8 @@ void free_all(dqmc_handle* h) {
   for (void* q : ptrs)
     if (q) cudaFree(q);
   for (auto e : h->event_pool) cudaEventDestroy(e);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->st) cudaStreamDestroy(h->st);
 }
 
@@ -706,7 +722,7 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
   A((void**)&h->qr.beta, n * sizeof(double)); A((void**)&h->qr.V, nn);
   A((void**)&h->qr.bar, sizeof(GridBarrier));
   A((void**)&h->qr.cand_v, 1024 * sizeof(double)); A((void**)&h->qr.cand_q, 1024 * sizeof(int));
-  A((void**)&h->action_d, sizeof(double)); A((void**)&h->nacc_d, sizeof(int));
+  A((void**)&h->action_d, sizeof(double)); A((void**)&h->nacc_d, 2 * sizeof(int));
   A((void**)&h->Acol, 4 * n * sizeof(cplx)); A((void**)&h->Brow, 4 * n * sizeof(cplx));
   A((void**)&h->bar, sizeof(GridBarrier)); A((void**)&h->err_d, sizeof(int));
   A((void**)&h->scal_d, 8 * sizeof(double));
@@ -772,6 +788,7 @@ int dqmc_init(dqmc_handle* h) {
   CU(cudaMemcpyAsync(h->action_d, &S, sizeof(double), cudaMemcpyHostToDevice, h->st));
   CU(cudaMemsetAsync(h->nacc_d, 0, sizeof(int), h->st));
   h->max_instability = 0.0;
+  CU(cudaMemsetAsync(h->scal_d + 3, 0, sizeof(double), h->st));
   CHK(build_stack(h));
   CHK(propagate(h));
   h->initialized = true;
@@ -833,37 +850,51 @@ int dqmc_update(dqmc_handle* h, const double* delta, const double* unif, uint8_t
   return local_updates_host(h, delta, unif, accepted, detratio, p_acc, acc_rate);
 }
 
-static int sweep_impl(dqmc_handle* h, int n_calls, const double* delta_dev, const double* unif_dev,
-                      uint8_t* acc_dev, dqmc_stats* stats) {
-  int before = 0;
-  CHK(read_nacc(h, &before));
+// Enqueues n_calls update() calls on the handle's stream without waiting.
+static int sweep_enqueue(dqmc_handle* h, int n_calls, const double* delta_dev, const double* unif_dev,
+                         uint8_t* acc_dev) {
+  CU(cudaMemcpyAsync(h->nacc_d + 1, h->nacc_d, sizeof(int), cudaMemcpyDeviceToDevice, h->st));
+  CU(cudaMemsetAsync(h->scal_d + 3, 0, sizeof(double), h->st));
   h->max_instability = 0.0;
-  cudaEvent_t e0, e1;
-  CU(cudaEventCreate(&e0));
-  CU(cudaEventCreate(&e1));
-  CU(cudaEventRecord(e0, h->st));
+  if (!h->ev0) {
+    CU(cudaEventCreate(&h->ev0));
+    CU(cudaEventCreate(&h->ev1));
+  }
+  CU(cudaEventRecord(h->ev0, h->st));
   const size_t N = h->N;
   for (int c = 0; c < n_calls; ++c) {
     CHK(propagate(h));
     CHK(local_updates_dev(h, delta_dev + (size_t)c * 3 * N, unif_dev + (size_t)c * N,
                           acc_dev ? acc_dev + (size_t)c * N : nullptr, nullptr, nullptr));
   }
-  CU(cudaEventRecord(e1, h->st));
+  CU(cudaEventRecord(h->ev1, h->st));
+  h->pending_calls = n_calls;
+  return DQMC_OK;
+}
+
+// Waits for an enqueued sweep and fills the statistics.
+static int sweep_finish(dqmc_handle* h, dqmc_stats* stats) {
   CHK(sync(h));
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  int after = 0;
-  CHK(read_nacc(h, &after));
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  int cnt[2] = {0, 0};
+  CU(cudaMemcpyAsync(cnt, h->nacc_d, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaStreamSynchronize(h->st));
   if (stats) {
-    stats->proposals = (int64_t)n_calls * h->N;
-    stats->accepted = after - before;
+    stats->proposals = (int64_t)h->pending_calls * h->N;
+    stats->accepted = cnt[0] - cnt[1];
     stats->acc_rate = stats->proposals ? (double)stats->accepted / stats->proposals : 0.0;
     stats->max_instability = h->max_instability;
     stats->device_ms = ms;
   }
+  h->pending_calls = 0;
   return DQMC_OK;
+}
+
+static int sweep_impl(dqmc_handle* h, int n_calls, const double* delta_dev, const double* unif_dev,
+                      uint8_t* acc_dev, dqmc_stats* stats) {
+  CHK(sweep_enqueue(h, n_calls, delta_dev, unif_dev, acc_dev));
+  return sweep_finish(h, stats);
 }
 
 int dqmc_sweep(dqmc_handle* h, int32_t n_calls, const double* delta_stream, const double* unif_stream,
@@ -893,6 +924,108 @@ int dqmc_sweep_device(dqmc_handle* h, int32_t n_calls, const double* delta_strea
   if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
   if (n_calls == 0) return DQMC_OK;
   return sweep_impl(h, n_calls, delta_stream_dev, unif_stream_dev, accepted_dev, stats);
+}
+
+// ---- batches of independent chains ----------------------------------------
+struct dqmc_batch {
+  std::vector<dqmc_handle*> chains;
+  int inflight = 1;   // chains swept at the same time
+};
+
+// Chains in flight per batch: enough to fill the SMs while each chain's
+// latency-bound kernels keep a useful share of them (measured optimum ~8-12).
+static int batch_inflight(int count) { return count < 12 ? count : 12; }
+
+int dqmc_batch_create(const dqmc_params* params, int32_t count, dqmc_batch** out) {
+  if (!params || !out || count < 1) return DQMC_ERR_ARG;
+  *out = nullptr;
+  dqmc_batch* b = new dqmc_batch();
+  b->inflight = batch_inflight(count);
+  for (int i = 0; i < count; ++i) {
+    dqmc_handle* h = nullptr;
+    int rc = dqmc_create(&params[i], &h);
+    if (rc != DQMC_OK) {
+      for (auto c : b->chains) dqmc_destroy(c);
+      delete b;
+      return rc;
+    }
+    // the chains in flight can all be resident at once: their cooperative
+    // grids add up to at most one CTA per SM
+    h->coop_cap = h->sm_count / b->inflight > 0 ? h->sm_count / b->inflight : 1;
+    b->chains.push_back(h);
+  }
+  *out = b;
+  return DQMC_OK;
+}
+
+int dqmc_batch_destroy(dqmc_batch* b) {
+  if (!b) return DQMC_ERR_ARG;
+  for (auto c : b->chains) dqmc_destroy(c);
+  delete b;
+  return DQMC_OK;
+}
+
+int dqmc_batch_handle(dqmc_batch* b, int32_t i, dqmc_handle** h) {
+  if (!b || !h || i < 0 || i >= (int)b->chains.size()) return DQMC_ERR_ARG;
+  *h = b->chains[i];
+  return DQMC_OK;
+}
+
+// Largest chains first, in waves of `inflight` chains of similar size; within
+// a wave the update calls are issued round-robin over the chains (one call of
+// each chain in turn), so the launch queue always holds work of every chain
+// of the wave and their streams run side by side.
+int dqmc_batch_sweep(dqmc_batch* b, int32_t n_calls, const double* const* delta_dev, const double* const* unif_dev,
+                     dqmc_stats* stats) {
+  if (!b || n_calls < 0 || !delta_dev || !unif_dev) return DQMC_ERR_ARG;
+  const int C = (int)b->chains.size();
+  for (int i = 0; i < C; ++i) {
+    dqmc_handle* h = b->chains[i];
+    if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init on every chain first");
+    if (!delta_dev[i] || !unif_dev[i]) return DQMC_ERR_ARG;
+  }
+  std::vector<int> order(C);
+  for (int i = 0; i < C; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->chains[x]->n > b->chains[y]->n; });
+  int rc = DQMC_OK;
+  for (int w0 = 0; w0 < C; w0 += b->inflight) {
+    const int w1 = std::min(C, w0 + b->inflight);
+    for (int q = w0; q < w1; ++q) {
+      dqmc_handle* h = b->chains[order[q]];
+      cudaSetDevice(h->device);
+      CU(cudaMemcpyAsync(h->nacc_d + 1, h->nacc_d, sizeof(int), cudaMemcpyDeviceToDevice, h->st));
+      CU(cudaMemsetAsync(h->scal_d + 3, 0, sizeof(double), h->st));
+      h->max_instability = 0.0;
+      if (!h->ev0) {
+        CU(cudaEventCreate(&h->ev0));
+        CU(cudaEventCreate(&h->ev1));
+      }
+      CU(cudaEventRecord(h->ev0, h->st));
+      h->pending_calls = n_calls;
+    }
+    for (int c = 0; c < n_calls; ++c)
+      for (int q = w0; q < w1; ++q) {
+        const int i = order[q];
+        dqmc_handle* h = b->chains[i];
+        cudaSetDevice(h->device);
+        const size_t N = h->N;
+        CHK(propagate(h));
+        CHK(local_updates_dev(h, delta_dev[i] + (size_t)c * 3 * N, unif_dev[i] + (size_t)c * N, nullptr, nullptr,
+                              nullptr));
+      }
+    for (int q = w0; q < w1; ++q) {
+      dqmc_handle* h = b->chains[order[q]];
+      cudaSetDevice(h->device);
+      CU(cudaEventRecord(h->ev1, h->st));
+    }
+    for (int q = w0; q < w1; ++q) {
+      dqmc_handle* h = b->chains[order[q]];
+      cudaSetDevice(h->device);
+      int r = sweep_finish(h, stats ? &stats[order[q]] : nullptr);
+      if (r != DQMC_OK && rc == DQMC_OK) rc = r;
+    }
+  }
+  return rc;
 }
 
 int dqmc_get_greens(dqmc_handle* h, double* out, int32_t* slice, int32_t* direction) {

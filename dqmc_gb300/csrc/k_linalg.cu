@@ -33,7 +33,11 @@ __global__ void __launch_bounds__(256) k_zgemm(int m, int nn, int k, char opA, c
                                               int ldb, cplx beta, cplx* __restrict__ C, int ldc,
                                               const double* __restrict__ rs, const double* __restrict__ cs,
                                               const int* __restrict__ active) {
-  if (active && *active == 0) return;
+  if (active) {
+    const int kk = 4 * *active;
+    if (kk == 0) return;
+    if (kk < k) k = kk;
+  }
   __shared__ cplx sA[GB_K][GB_M + 1];
   __shared__ cplx sB[GB_K][GB_N + 1];
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
@@ -517,7 +521,7 @@ cudaError_t launch_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, c
   return cudaGetLastError();
 }
 
-cudaError_t launch_qrp(cplx* A, int n, QRWork& w, int sm_count, cudaStream_t st) {
+cudaError_t launch_qrp(cplx* A, int n, QRWork& w, int sm_count, cudaStream_t st, int max_grid) {
   if (n > 32 * QR_MAXT) return cudaErrorInvalidValue;
   size_t smem = (size_t)n * (sizeof(cplx) + sizeof(int));
   static bool attr = false;
@@ -530,6 +534,7 @@ cudaError_t launch_qrp(cplx* A, int n, QRWork& w, int sm_count, cudaStream_t st)
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   int grid = sm_count;   // one CTA per SM; remaining columns are dealt round-robin over all CTAs
+  if (max_grid > 0 && grid > max_grid) grid = max_grid;
   QRWork copy = w;
   void* args[] = {&A, &n, &copy};
   return cudaLaunchCooperativeKernel((void*)k_qrp, dim3(grid), dim3(QR_THREADS), args, smem, st);
@@ -605,9 +610,21 @@ cudaError_t launch_sum_log(const double* x, int n, double* out, cudaStream_t st)
   return cudaGetLastError();
 }
 
-cudaError_t launch_max_absdiff(const cplx* A, const cplx* B, size_t count, double* out, cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), st);
-  if (e != cudaSuccess) return e;
+__global__ void k_fill(double* d, int n, double v) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) d[i] = v;
+}
+
+cudaError_t launch_fill(double* d, int n, double v, cudaStream_t st) {
+  k_fill<<<(n + 255) / 256, 256, 0, st>>>(d, n, v);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_max_absdiff(const cplx* A, const cplx* B, size_t count, double* out, cudaStream_t st, bool reset) {
+  if (reset) {
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), st);
+    if (e != cudaSuccess) return e;
+  }
   k_max_absdiff<<<grid_for(count, 256, 1024), 256, 0, st>>>(A, B, count, out);
   return cudaGetLastError();
 }

@@ -322,18 +322,23 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_updates(LocalUpdateArgs
 // ---------------------------------------------------------------------------
 // delayed rank-k updates: G_cur = G + X Y with X (n x 4k), Y (4k x n)
 // ---------------------------------------------------------------------------
-// Processes sites state[0] .. N-1 until k accepted updates are pending
-// (state[1] == k) or the slice ends; state[0] is left at the next site.  The
-// flush G += X Y (a separate GEMM launch) resets state[1] to 0.
+// Processes sites state[0] .. N-1 until k accepted updates are pending or the
+// slice ends; state[0] is left at the next site and state[1] at the number of
+// pending factors.  The flush G += X Y (a separate GEMM launch over the first
+// 4 state[1] columns) follows every round.
 __global__ void __launch_bounds__(LU_THREADS, 2) k_local_delayed(LocalUpdateArgs a, DelayedArgs d) {
   const ModelConst& mc = a.mc;
   const int N = mc.N, n = mc.n, K4 = 4 * d.k;
-  __shared__ int s_first, s_p;
-  if (threadIdx.x == 0) { s_first = __ldcg(&d.state[0]); s_p = __ldcg(&d.state[1]); }
+  __shared__ int s_first;
+  if (threadIdx.x == 0) s_first = __ldcg(&d.state[0]);
   __syncthreads();
   const int first = s_first;
-  int p = s_p;
-  if (first >= N || p >= d.k) return;   // nothing to do in this round (uniform over the grid)
+  // every round follows a flush of the previous round's factors, so nothing
+  // is pending at its start; clearing the count here also keeps the flush
+  // after a round with no sites left from applying the factors again
+  int p = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) d.state[1] = 0;
+  if (first >= N) return;               // slice done: nothing to do in this round (uniform over the grid)
   extern __shared__ double4_16a smem_local[];
   const LocalSmem sm = local_smem(smem_local, N);
   cplx* Ysm = reinterpret_cast<cplx*>(sm.phis + 3 * N);   // (4k x 4): Y[j, i + cN] of the current site
@@ -431,22 +436,6 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_delayed(LocalUpdateArgs
   if (blockIdx.x == 0 && threadIdx.x == 0) { d.state[0] = N; d.state[1] = p; }
 }
 
-// After a flush: zero the used factor columns and clear the pending count.
-__global__ void k_delayed_reset(DelayedArgs d, int n) {
-  const int p = __ldcg(&d.state[1]);
-  if (p == 0) return;
-  const size_t used = (size_t)4 * p * n;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < used; e += (size_t)gridDim.x * blockDim.x) {
-    d.X[e] = cmake(0.0, 0.0);
-    d.Y[e] = cmake(0.0, 0.0);
-  }
-  __syncthreads();
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    __threadfence();
-  }
-}
-
-__global__ void k_delayed_clear_count(int* state) { state[1] = 0; }
 
 }  // namespace
 
@@ -454,7 +443,8 @@ static size_t local_smem_bytes(int N) {
   return (size_t)N * (16 * sizeof(cplx) + sizeof(EvEntry)) + (size_t)3 * N * sizeof(double);
 }
 
-cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d, int sm_count, cudaStream_t st) {
+cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d, int sm_count, cudaStream_t st,
+                                 int max_grid) {
   const size_t smem = local_smem_bytes(a.mc.N) + (size_t)2 * 4 * d.k * 4 * sizeof(cplx);
   static bool attr = false;
   if (!attr) {
@@ -472,19 +462,14 @@ cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d,
   // two items (rows of A / columns of B) per warp
   const int need = (a.mc.n + (LU_THREADS / 32) - 1) / (LU_THREADS / 32);
   if (grid > need) grid = need < 1 ? 1 : need;
+  if (max_grid > 0 && grid > max_grid) grid = max_grid;
   LocalUpdateArgs ca = a;
   DelayedArgs cd = d;
   void* args[] = {&ca, &cd};
   return cudaLaunchCooperativeKernel((void*)k_local_delayed, dim3(grid), dim3(LU_THREADS), args, smem, st);
 }
 
-cudaError_t launch_delayed_reset(const DelayedArgs& d, int n, cudaStream_t st) {
-  k_delayed_reset<<<256, 256, 0, st>>>(d, n);
-  k_delayed_clear_count<<<1, 1, 0, st>>>(d.state);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_local_updates(const LocalUpdateArgs& a, int sm_count, cudaStream_t st) {
+cudaError_t launch_local_updates(const LocalUpdateArgs& a, int sm_count, cudaStream_t st, int max_grid) {
   const size_t smem = local_smem_bytes(a.mc.N);
   static bool attr = false;
   if (!attr) {
@@ -504,6 +489,7 @@ cudaError_t launch_local_updates(const LocalUpdateArgs& a, int sm_count, cudaStr
   const int tiles = ((n + 127) / 128) * ((n + 3) / 4);
   const int need = (tiles + (LU_THREADS / 32) - 1) / (LU_THREADS / 32);
   if (grid > need) grid = need < 1 ? 1 : need;
+  if (max_grid > 0 && grid > max_grid) grid = max_grid;
   LocalUpdateArgs copy = a;
   void* args[] = {&copy};
   return cudaLaunchCooperativeKernel((void*)k_local_updates, dim3(grid), dim3(LU_THREADS), args, smem, st);

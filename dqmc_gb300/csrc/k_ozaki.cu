@@ -60,7 +60,12 @@ __global__ void k_oz_split_rows(const cplx* __restrict__ X, int ld, char op, int
                                 int bits, __nv_bfloat16* __restrict__ out, double* __restrict__ scale,
                                 const int* __restrict__ active) {
   const int i = blockIdx.x;
-  if (i >= rows || (active && *active == 0)) return;
+  if (i >= rows) return;
+  if (active) {   // only the first 4p inner indices are live (delayed-update flush)
+    const int kk = 4 * *active;
+    if (kk == 0) return;
+    if (kk < K) K = kk;
+  }
   __shared__ double red[32];
   double m = 0.0;
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
@@ -101,7 +106,12 @@ __global__ void k_oz_split_cols(const cplx* __restrict__ X, int ld, char op, int
                                 int bits, __nv_bfloat16* __restrict__ out_re, __nv_bfloat16* __restrict__ out_im,
                                 double* __restrict__ scale, const int* __restrict__ active) {
   const int j = blockIdx.x;
-  if (j >= cols || (active && *active == 0)) return;
+  if (j >= cols) return;
+  if (active) {
+    const int kk = 4 * *active;
+    if (kk == 0) return;
+    if (kk < K) K = kk;
+  }
   __shared__ double red[32];
   double m = 0.0;
   for (int k = threadIdx.x; k < K; k += blockDim.x) {

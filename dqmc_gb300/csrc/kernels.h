@@ -44,7 +44,7 @@ struct LocalUpdateArgs {
   int* err;
   ModelConst mc;
 };
-cudaError_t launch_local_updates(const LocalUpdateArgs& a, int sm_count, cudaStream_t st);
+cudaError_t launch_local_updates(const LocalUpdateArgs& a, int sm_count, cudaStream_t st, int max_grid = 0);
 // delayed rank-k form: pending factors X (n x 4k, column-major) and Y (4k x n,
 // row j at Y + j*n); state[0] = next site of the slice, state[1] = pending accepts
 struct DelayedArgs {
@@ -53,14 +53,16 @@ struct DelayedArgs {
   int* state;
   int k;
 };
-cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d, int sm_count, cudaStream_t st);
-// zero the used factor columns and the pending count after a flush
-cudaError_t launch_delayed_reset(const DelayedArgs& d, int n, cudaStream_t st);
+cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d, int sm_count, cudaStream_t st,
+                                 int max_grid = 0);
+
 
 // ---- dense linear algebra (k_linalg.cu) ----
 // C = alpha * op(A) * op(B) + beta * C, all n x n column-major; op: 'N', 'C' (conjugate transpose)
 // optional diagonal scalings: rowscale (applied to rows of op(A)), colscale (to columns of op(B)).
-// active: optional device flag; the launch does nothing when *active == 0.
+// active: optional device count p of pending rank-4 factors; when given, the
+// product uses only the first 4p columns of op(A) / rows of op(B), and does
+// nothing when p == 0 (the delayed-update flush).
 cudaError_t launch_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
                          const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
                          const double* colscale, cudaStream_t st, const int* active = nullptr);
@@ -81,7 +83,8 @@ struct QRWork {
 // without physical column swaps).  On return the upper part of A (rows <=
 // logical position of each physical column) holds R in physical column
 // order; V/tau hold the reflectors; order/beta the pivots and diag(R).
-cudaError_t launch_qrp(cplx* A, int n, QRWork& w, int sm_count, cudaStream_t st);
+// max_grid > 0 caps the cooperative grid (chains sharing the GPU)
+cudaError_t launch_qrp(cplx* A, int n, QRWork& w, int sm_count, cudaStream_t st, int max_grid = 0);
 // After launch_qrp: D[k] = |beta[k]|, T (physical layout) = D^-1 R with zeros below.
 cudaError_t launch_qrp_finalize(cplx* A, cplx* T, double* D, int n, const QRWork& w, cudaStream_t st);
 // X (m x n) <- X * Q  with Q = H_0 ... H_{n-1} (reflectors in w).  Also used
@@ -105,7 +108,10 @@ cudaError_t launch_set_identity(cplx* A, int n, cudaStream_t st);
 // out[0] = sum_k log(x[k]) (one deterministic single-CTA reduction)
 cudaError_t launch_sum_log(const double* x, int n, double* out, cudaStream_t st);
 // max |A - B| over n*n entries -> out
-cudaError_t launch_max_absdiff(const cplx* A, const cplx* B, size_t count, double* out, cudaStream_t st);
+cudaError_t launch_max_absdiff(const cplx* A, const cplx* B, size_t count, double* out, cudaStream_t st,
+                               bool reset = true);
+// d[0..n) = v
+cudaError_t launch_fill(double* d, int n, double v, cudaStream_t st);
 // A (rows x cols) scaled: A[r,c] *= rowscale[r] (if non-null) * colscale[c] (if non-null); rowscale may be inverted
 cudaError_t launch_scale(cplx* A, int rows, int cols, const double* rowscale, bool invert_rows,
                          const double* colscale, bool invert_cols, cudaStream_t st);

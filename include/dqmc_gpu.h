@@ -164,6 +164,24 @@ DQMC_API int dqmc_local_updates_noalloc(const dqmc_params* p, double* greens, do
                                         const double* delta, const double* unif, uint8_t* accepted,
                                         double* action, void* stream);
 
+/* ---- batches of independent chains ----------------------------------------- */
+/* A batch holds `count` independent chains (params[i] each; sizes may differ),
+ * each on its own CUDA stream.  Up to 12 chains run at the same time, with
+ * cooperative grids capped so that all of them can be resident on the GPU at
+ * once.  dqmc_batch_handle gives the chain's handle for the single-chain calls
+ * (set_field, init, greens...).  dqmc_batch_sweep runs n_calls update() calls
+ * on every chain (delta_dev[i], unif_dev[i]: device streams of chain i, layouts
+ * as in dqmc_sweep), largest chains first, replacing each finished chain by the
+ * next one, and returns when all are done; stats has `count` entries (may be NULL).
+ * Replaces the reference's SLURM job arrays of independent runs
+ * (app/dqmc.jl:48-57) inside one process and one GPU. */
+typedef struct dqmc_batch dqmc_batch;
+DQMC_API int dqmc_batch_create(const dqmc_params* params, int32_t count, dqmc_batch** out);
+DQMC_API int dqmc_batch_destroy(dqmc_batch* b);
+DQMC_API int dqmc_batch_handle(dqmc_batch* b, int32_t i, dqmc_handle** h);
+DQMC_API int dqmc_batch_sweep(dqmc_batch* b, int32_t n_calls, const double* const* delta_dev,
+                              const double* const* unif_dev, dqmc_stats* stats);
+
 /* ---- Green's functions ------------------------------------------------------ */
 /* s.greens (effective G at the current slice). out: double[2*n*n]. */
 DQMC_API int dqmc_get_greens(dqmc_handle* h, double* out, int32_t* slice, int32_t* direction);
