@@ -6,7 +6,10 @@ A step is one sweep = M `update` calls (propagate + local updates of one
 slice) of the O(3) spin-fermion model on seeded synthetic fields and
 pre-generated proposal streams.  The default workload is the headline
 configuration: L=16 (n=1024), beta=20 (M=200), dtau=0.1, safe_mult=10,
-plain FP64.
+and, by default, both the plain FP64 form and the mixed form (split-BF16
+tensor-core GEMMs) from the same field and streams: value is the mixed form,
+the FP64 sweeps/s, the ratio and max|G_mixed - G_FP64| after the shared warm-up
+are in "mixed_vs_fp64".
 
 value  : sweeps/s with the streams resident on the device (dqmc_sweep_device),
          summed CUDA-event time of the K timed sweeps on the library's stream.
@@ -221,7 +224,8 @@ def run_batch(args, world, rank, local):
         plist.append(api.ModelParams(L=L, slices=M, safe_mult=10, delta_tau=rp.delta_tau, lambda_=rp.lambda_,
                                      r=rp.r, c=rp.c, u=rp.u, mu1=rp.mu1, mu2=rp.mu2, hoppings=rp.hoppings,
                                      box=rp.box, all_checks=not args.no_checks, device=dev,
-                                     precision=args.precision, delay=args.delay))
+                                     precision="mixed" if args.precision == "mixed" else "fp64",
+                                     delay=args.delay if args.precision == "mixed" else args.fp64_delay))
         fields.append(synthetic_field(L * L, M, 3000 + 100 * rank + k))
     batch = api.Batch(plist, fields)
     batch.init()
@@ -268,7 +272,7 @@ def run_batch(args, world, rank, local):
             "metric": METRIC, "value": value, "unit": "chain-sweeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": wall * 1000.0 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "f64 + split-bf16 tensor GEMMs",
+            "dtype": "f64 + split-bf16 tensor GEMMs" if args.precision == "mixed" else "f64",
             "data": "synthetic (seeded uniform[-1,1] fields, uniform proposal/Metropolis streams)",
             "config": {"workload": desc, "chains": args.chains, "L_counts": {L: Ls.count(L) for L in (6, 8, 10, 12)},
                        "slices": M, "precision": args.precision, "delay": args.delay,
@@ -279,36 +283,23 @@ def run_batch(args, world, rank, local):
     batch.close()
 
 
-def run_ours(args, world, rank, local):
-    import torch
-    from dqmc_gb300 import api
-    from oracle.dqmc_ref import synthetic_field, synthetic_streams
-
-    L, M, desc = CONFIGS[args.config]
-    rp = model_params(L, M)
-    dev = local if world > 1 else 0
-    torch.cuda.set_device(dev)
+def _make_chain(api, L, M, rp, args, dev, precision, delay, phi):
     mp = api.ModelParams(L=L, slices=M, safe_mult=rp.safe_mult, delta_tau=rp.delta_tau, lambda_=rp.lambda_,
                          r=rp.r, c=rp.c, u=rp.u, mu1=rp.mu1, mu2=rp.mu2, hoppings=rp.hoppings, box=rp.box,
-                         all_checks=not args.no_checks, device=dev, precision=args.precision, delay=args.delay)
-    N, n = rp.N, rp.n
-    phi = synthetic_field(N, M, 1000 + rank)
-    sweeps = args.warmup + args.steps
-    delta, unif = synthetic_streams(N, sweeps * M, rp.box, 1001 + rank)
-    # (calls, 3, N) -> per call component-fastest layout of the C ABI
-    d_host = np.ascontiguousarray(np.transpose(delta, (0, 2, 1)))
+                         all_checks=not args.no_checks, device=dev, precision=precision, delay=delay)
     chain = api.DQMC(mp, phi)
     chain.init()
+    return chain
 
-    # device-resident streams for `value`
-    d_dev = torch.from_numpy(d_host).to(f"cuda:{dev}")
-    u_dev = torch.from_numpy(np.ascontiguousarray(unif)).to(f"cuda:{dev}")
-    acc_dev = torch.zeros(sweeps * M * N, dtype=torch.uint8, device=f"cuda:{dev}")
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
-    st = api.CStats()
+
+def _measure_form(api, chain, args, M, N, d_dev, u_dev, acc_dev, flush, world):
+    """W warm-up sweeps (accept flags kept), then K timed sweeps with an L2
+    flush before each; returns (device seconds, accepted, instability, timing)."""
     import ctypes
+    import torch
+    st = api.CStats()
 
-    def sweep_dev(s):
+    def sweep(s):
         off = s * M
         rc = chain.lib.dqmc_sweep_device(chain.h, M, ctypes.c_void_p(d_dev.data_ptr() + off * 3 * N * 8),
                                          ctypes.c_void_p(u_dev.data_ptr() + off * N * 8),
@@ -317,36 +308,68 @@ def run_ours(args, world, rank, local):
         return st.device_ms, st.accepted, st.max_instability
 
     for s in range(args.warmup):
-        sweep_dev(s)
+        sweep(s)
     torch.cuda.synchronize()
+    warm_greens = chain.greens
     barrier(world)
     chain.reset_timing(True)
-    clocks = ClockSampler(dev)
-    clocks.start()
     torch.cuda.synchronize()
-    barrier(world)
-    t_wall0 = time.perf_counter()
     dev_ms, accepted, instab = 0.0, 0, 0.0
-    for s in range(args.warmup, sweeps):
+    for s in range(args.warmup, args.warmup + args.steps):
         flush.fill_(float(s))
         torch.cuda.synchronize()
-        ms, acc, ins = sweep_dev(s)
+        ms, acc, ins = sweep(s)
         dev_ms += ms
         accepted += acc
         instab = max(instab, ins)
     torch.cuda.synchronize()
     barrier(world)
-    t_wall = time.perf_counter() - t_wall0
-    clk = clocks.stop()
     tim = chain.timing()
-    dev_s = allreduce_max(dev_ms / 1000.0, world)
-    value = world * args.steps / dev_s
+    chain.reset_timing(False)
+    return dev_ms / 1000.0, accepted, instab, tim, warm_greens
 
-    # ---- e2e through the public host-buffer API ----
+
+def run_ours(args, world, rank, local):
+    import ctypes
+    import torch
+    from dqmc_gb300 import api
+    from oracle.dqmc_ref import synthetic_field, synthetic_streams
+
+    L, M, desc = CONFIGS[args.config]
+    rp = model_params(L, M)
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    N, n = rp.N, rp.n
+    phi = synthetic_field(N, M, 1000 + rank)
+    sweeps = args.warmup + args.steps
+    delta, unif = synthetic_streams(N, sweeps * M, rp.box, 1001 + rank)
+    d_host = np.ascontiguousarray(np.transpose(delta, (0, 2, 1)))   # per call: component fastest (C ABI layout)
+    d_dev = torch.from_numpy(d_host).to(f"cuda:{dev}")
+    u_dev = torch.from_numpy(np.ascontiguousarray(unif)).to(f"cuda:{dev}")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    forms = [("mixed", args.delay)] if args.precision == "mixed" else [("fp64", args.fp64_delay)]
+    if args.precision == "both":
+        forms = [("fp64", args.fp64_delay), ("mixed", args.delay)]
+    res = {}
+    clocks = ClockSampler(dev)
+    clocks.start()
+    for prec, delay in forms:
+        acc_dev = torch.zeros(sweeps * M * N, dtype=torch.uint8, device=f"cuda:{dev}")
+        chain = _make_chain(api, L, M, rp, args, dev, prec, delay, phi)
+        t, acc, ins, tim, wg = _measure_form(api, chain, args, M, N, d_dev, u_dev, acc_dev, flush, world)
+        res[prec] = dict(chain=chain, secs=allreduce_max(t, world), accepted=acc, instab=ins, timing=tim,
+                         warm_greens=wg, warm_acc=acc_dev[: args.warmup * M * N].cpu().numpy())
+    clk = clocks.stop()
+    head = "mixed" if "mixed" in res else "fp64"
+    R = res[head]
+    value = world * args.steps / R["secs"]
+    chain = R["chain"]
+
+    # ---- e2e through the public host-buffer API (headline form) ----
     d_pin = torch.from_numpy(d_host).pin_memory().numpy()
     u_pin = torch.from_numpy(np.ascontiguousarray(unif)).pin_memory().numpy()
     acc_pin = torch.zeros(M * N, dtype=torch.uint8).pin_memory().numpy()
-    chain.reset_timing(False)
+    st = api.CStats()
     e2e_steps = max(1, min(args.steps, args.e2e_steps))
     torch.cuda.synchronize()
     barrier(world)
@@ -362,20 +385,24 @@ def run_ours(args, world, rank, local):
     e2e_s = allreduce_max(time.perf_counter() - t0, world)
     e2e_value = world * e2e_steps / e2e_s
 
-    # ---- roofline of the dominant kernel ----
+    # ---- roofline of the dominant kernel of the headline form ----
+    tim = R["timing"]
     kinds = tim["kinds"]
     top = max(kinds, key=lambda k: kinds[k]["ms"])
-    fl, by = flops_model(top, tim, n, accepted)
+    fl, by = flops_model(top, tim, n, R["accepted"])
     ms_top = kinds[top]["ms"]
     launches_top = max(1, kinds[top]["launches"])
-    peak_fp64 = api.peak_fp64_tflops(dev)
-    achieved = fl / launches_top / (ms_top / launches_top / 1000.0) / 1e12
     peaks, peak_kind = measured_peaks()
-    breakdown = {k: {"ms": round(v["ms"], 3), "launches": v["launches"],
-                     "share": round(v["ms"] / max(1e-9, sum(x["ms"] for x in kinds.values())), 4)}
-                 for k, v in kinds.items()}
+    if top in ("ozaki_gemm",) or (top == "flush" and head == "mixed"):
+        bound, peak, unit, src = "tensor", peaks.get("bf16_tflops"), "TFLOP/s", f"bf16_tflops ({peak_kind})"
+    else:
+        bound, peak, unit = "fp64", api.peak_fp64_tflops(dev), "TFLOP/s"
+        src = "FP64 FMA peak measured live on this GPU (dqmc_peak_fp64)"
+    achieved = fl / launches_top / (ms_top / launches_top / 1000.0) / 1e12
+    tot_ms = sum(x["ms"] for x in kinds.values())
+    breakdown = {k: {"ms": round(v["ms"], 3), "launches": v["launches"], "share": round(v["ms"] / max(1e-9, tot_ms), 4)}
+                 for k, v in kinds.items() if v["launches"]}
 
-    line = None
     if rank == 0:
         cpu = None
         if world == 1 and not args.no_cpu:
@@ -384,32 +411,43 @@ def run_ours(args, world, rank, local):
             cpu = {"value": val, "unit": "sweeps/s", "cores": threads, "kind": "port",
                    "sample": f"{args.cpu_calls} of {M} update calls (numpy/scipy oracle, OpenBLAS "
                              f"{threads} threads), {secs:.1f} s, extrapolated to one sweep"}
+        compare = None
+        if "fp64" in res and "mixed" in res:
+            f64, mix = res["fp64"], res["mixed"]
+            same = bool(np.array_equal(f64["warm_acc"], mix["warm_acc"]))
+            compare = {"fp64_sweeps_per_s": world * args.steps / f64["secs"],
+                       "mixed_sweeps_per_s": world * args.steps / mix["secs"],
+                       "mixed_over_fp64": f64["secs"] / mix["secs"],
+                       "fp64_delay": args.fp64_delay, "mixed_delay": args.delay,
+                       "warmup_accept_sequences_identical": same,
+                       "max_abs_G_mixed_minus_fp64_after_warmup": float(np.max(np.abs(mix["warm_greens"] - f64["warm_greens"]))) if same else None,
+                       "mixed_max_instability": mix["instab"], "fp64_max_instability": f64["instab"]}
         line = {
             "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": dev_s * 1000.0 / args.steps, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": R["secs"] * 1000.0 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "f64 + split-bf16 tensor GEMMs",
+            "dtype": "f64" if head == "fp64" else "f64 + split-bf16 tensor GEMMs",
             "data": "synthetic (seeded uniform[-1,1] fields, uniform proposal/Metropolis streams)",
             "config": {"workload": desc, "L": L, "slices": M, "n": n, "safe_mult": 10, "chains_per_gpu": 1,
-                       "precision": args.precision, "delay": args.delay, "parallelism": f"replicas x{world}",
+                       "form": head, "delay": args.delay if head == "mixed" else args.fp64_delay,
+                       "parallelism": f"replicas x{world}",
                        "l2": "working set > L2 (stack 2x21x16.8 MB) and 256 MB L2 flush before each sweep"},
+            "mixed_vs_fp64": compare,
             "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": int(M * 4 * N * 8),
                     "d2h_bytes_per_step": int(M * N), "steps": e2e_steps},
             "gpu_launches": int(tim["kernel_launches"]),
-            "roofline": {"bound": "fp64", "kernel": top, "achieved": achieved, "peak": peak_fp64,
-                         "unit": "TFLOP/s", "frac": achieved / peak_fp64, "traffic": None,
-                         "peak_source": "FP64 FMA peak measured live on this GPU (dqmc_peak_fp64)",
-                         "hbm_peak_gbs": peaks.get("hbm_gbs"), "bf16_peak_tflops": peaks.get("bf16_tflops"),
-                         "peaks_file": peak_kind},
+            "roofline": {"bound": bound, "kernel": top, "achieved": achieved, "peak": peak, "unit": unit,
+                         "frac": achieved / peak if peak else None, "traffic": None, "peak_source": src,
+                         "hbm_peak_gbs": peaks.get("hbm_gbs"), "bf16_peak_tflops": peaks.get("bf16_tflops")},
             "kernel_breakdown": breakdown,
-            "acc_rate": accepted / (args.steps * M * N),
-            "max_instability": instab,
-            "wall_s_timed": t_wall,
+            "acc_rate": R["accepted"] / (args.steps * M * N),
+            "max_instability": R["instab"],
             "clocks": clk,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
-    chain.close()
+    for r in res.values():
+        r["chain"].close()
 
 
 def main():
@@ -422,10 +460,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-checks", action="store_true", help="all_checks off")
     ap.add_argument("--cpu-calls", type=int, default=10)
-    ap.add_argument("--ref-calls", type=int, default=2)
+    ap.add_argument("--ref-calls", type=int, default=10, help="reference arm: update calls per step "
+                    "(10 = one safe_mult block, one stabilisation included)")
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--delay", type=int, default=16, help="delayed-update depth k (1 = immediate rank-4)")
+    ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"],
+                    help="both: FP64 and mixed forms on the same field and streams; value = mixed")
+    ap.add_argument("--delay", type=int, default=16, help="mixed form: delayed-update depth k")
+    ap.add_argument("--fp64-delay", type=int, default=1, help="FP64 form: delayed-update depth (1 = rank-4)")
     ap.add_argument("--chains", type=int, default=64, help="chains of the batched config c2")
     args = ap.parse_args()
     world, rank, local = dist_setup()

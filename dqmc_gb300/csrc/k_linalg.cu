@@ -130,6 +130,7 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
   int* order = reinterpret_cast<int*>(v + n);         // (n) logical -> physical
   __shared__ double red[32];
   __shared__ int redi[32];
+  __shared__ double nsum[32];   // block_sum scratch, apart from the candidate slots
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int warps = QR_THREADS / 32;
   const int gwarp = blockIdx.x * warps + wid, nwarps = gridDim.x * warps;
@@ -196,27 +197,28 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
         if (r > k) xn2 += cabs2(x);
       }
     }
-    xn2 = block_sum(xn2, red);   // includes __syncthreads
+    xn2 = block_sum(xn2, nsum);   // includes __syncthreads; v[k..n) visible after it
     const cplx alpha = v[k];
     const double xnorm = sqrt(xn2);
     double beta;
-    cplx tau;
+    cplx tau, scal;
     if (xnorm == 0.0 && alpha.y == 0.0) {
       tau = cmake(0.0, 0.0);
       beta = alpha.x;
+      scal = cmake(0.0, 0.0);
     } else {
       double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2);
       beta = alpha.x >= 0.0 ? -nrm : nrm;
       tau = cmake((beta - alpha.x) / beta, -alpha.y / beta);
-      cplx scal = cdiv(cmake(1.0, 0.0), csub(alpha, cmake(beta, 0.0)));
-      for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) v[r] = cmul(v[r], scal);
+      scal = cdiv(cmake(1.0, 0.0), csub(alpha, cmake(beta, 0.0)));
     }
-    __syncthreads();
-    if (threadIdx.x == 0) v[k] = cmake(1.0, 0.0);
-    __syncthreads();
+    // v = (1, scal x_{k+1..n}): the shared buffer keeps the unscaled x and the
+    // scale is folded into each column's coefficients; only CTA 0 writes the
+    // scaled reflector for the later applications of Q
     if (blockIdx.x == 0) {
       if (threadIdx.x == 0) { w.tau[k] = tau; w.beta[k] = beta; }
-      for (int r = threadIdx.x; r < n; r += blockDim.x) w.V[(size_t)k * n + r] = r < k ? cmake(0.0, 0.0) : v[r];
+      for (int r = threadIdx.x; r < n; r += blockDim.x)
+        w.V[(size_t)k * n + r] = r < k ? cmake(0.0, 0.0) : (r == k ? cmake(1.0, 0.0) : cmul(v[r], scal));
     }
     // ---- apply H_k^H to the remaining columns, downdate their norms ----
     // remaining logical positions k+1..n-1 are dealt round-robin over the CTAs
@@ -239,11 +241,18 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
         if (q >= nq) break;
         int r = k + lane + 32 * q;
         x[q] = cmake(0.0, 0.0);
-        if (r < n) { x[q] = ldcg_c(&col[r]); sp[q & 3] = cfma_conj(v[r], x[q], sp[q & 3]); }
+        if (r < n) {
+          x[q] = ldcg_c(&col[r]);
+          if (r > k) sp[q & 3] = cfma_conj(v[r], x[q], sp[q & 3]);
+        }
       }
       cplx s = cadd(cadd(sp[0], sp[1]), cadd(sp[2], sp[3]));
       s = warp_sum(s);
-      cplx f = cmul(ctau, s);
+      // v^H a = a_k + conj(scal) sum_{r>k} conj(x_r) a_r
+      const cplx ak = cmake(__shfl_sync(0xffffffffu, x[0].x, 0), __shfl_sync(0xffffffffu, x[0].y, 0));
+      s = cfma_conj(scal, s, ak);
+      const cplx f = cmul(ctau, s);        // a_k -= f
+      const cplx fs = cmul(f, scal);       // a_r -= f scal x_r, r > k
       double tp[4] = {0.0, 0.0, 0.0, 0.0};
       cplx xk = cmake(0.0, 0.0);
 #pragma unroll
@@ -251,9 +260,10 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
         if (q >= nq) break;
         int r = k + lane + 32 * q;
         if (r < n) {
-          // x -= f v with four fused multiply-adds
-          const cplx vr = v[r];
-          x[q] = cmake(fma(-f.x, vr.x, fma(f.y, vr.y, x[q].x)), fma(-f.x, vr.y, fma(-f.y, vr.x, x[q].y)));
+          // x -= c v with four fused multiply-adds (c = f at r = k, f scal below)
+          const cplx vr = r == k ? cmake(1.0, 0.0) : v[r];
+          const cplx c = r == k ? f : fs;
+          x[q] = cmake(fma(-c.x, vr.x, fma(c.y, vr.y, x[q].x)), fma(-c.x, vr.y, fma(-c.y, vr.x, x[q].y)));
           col[r] = x[q];
           if (q == 0 && lane == 0) xk = x[q];
           else tp[q & 3] = fma(x[q].x, x[q].x, fma(x[q].y, x[q].y, tp[q & 3]));
@@ -381,10 +391,15 @@ __global__ void __launch_bounds__(128) k_trsm_left_upper(const cplx* __restrict_
   __syncwarp();
   for (int q = n - 1; q >= 0; --q) {
     const cplx* tq = T + (size_t)__ldg(&order[q]) * n;
-    cplx yq = cdiv(y[q], __ldg(&tq[q]));
+    const cplx d = __ldg(&tq[q]);
+    // the unit-scaled factor has diagonal beta/|beta| = +-1: a sign, not a division
+    cplx yq = (d.y == 0.0 && fabs(d.x) == 1.0) ? cscale(y[q], d.x) : cdiv(y[q], d);
     __syncwarp();
     if (lane == 0) y[q] = yq;
-    for (int r = lane; r < q; r += 32) y[r] = csub(y[r], cmul(yq, __ldg(&tq[r])));
+    for (int r = lane; r < q; r += 32) {
+      const cplx t = __ldg(&tq[r]);
+      y[r] = cmake(fma(-yq.x, t.x, fma(yq.y, t.y, y[r].x)), fma(-yq.x, t.y, fma(-yq.y, t.x, y[r].y)));
+    }
     __syncwarp();
   }
   for (int r = lane; r < n; r += 32) yg[r] = y[r];
@@ -405,7 +420,11 @@ __global__ void __launch_bounds__(128) k_trsm_right_upper(const cplx* __restrict
     cplx s = cmake(0.0, 0.0);
     for (int r = lane; r < q; r += 32) s = cfma(z[r], __ldg(&tq[r]), s);
     s = warp_sum(s);
-    if (lane == 0) z[q] = cdiv(csub(z[q], s), __ldg(&tq[q]));
+    if (lane == 0) {
+      const cplx d = __ldg(&tq[q]);
+      const cplx t = csub(z[q], s);
+      z[q] = (d.y == 0.0 && fabs(d.x) == 1.0) ? cscale(t, d.x) : cdiv(t, d);
+    }
     __syncwarp();
   }
   for (int c = lane; c < n; c += 32) Y[(size_t)c * m + row] = z[c];
