@@ -124,6 +124,28 @@ __device__ __forceinline__ bool cand_better(double v, int q, double bv, int bq) 
   return v > bv || (v == bv && q < bq);
 }
 
+// a -= c v over the column slots of one lane (c = f at r = k, f scal below,
+// v_k = 1), stored back; with TAIL the squared norm of the updated rows > k.
+template <bool TAIL>
+__device__ __forceinline__ double qr_update_column(cplx (&x)[QR_MAXT], cplx* __restrict__ col, const cplx* v, int k,
+                                                   int n, int nq, int lane, cplx f, cplx fs) {
+  double tp[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+  for (int q = 0; q < QR_MAXT; ++q) {
+    if (q >= nq) break;
+    const int r = k + lane + 32 * q;
+    if (r < n) {
+      // four fused multiply-adds per element
+      const cplx vr = r == k ? cmake(1.0, 0.0) : v[r];
+      const cplx c = r == k ? f : fs;
+      x[q] = cmake(fma(-c.x, vr.x, fma(c.y, vr.y, x[q].x)), fma(-c.x, vr.y, fma(-c.y, vr.x, x[q].y)));
+      col[r] = x[q];
+      if (TAIL && r > k) tp[q & 3] = fma(x[q].x, x[q].x, fma(x[q].y, x[q].y, tp[q & 3]));
+    }
+  }
+  return (tp[0] + tp[1]) + (tp[2] + tp[3]);
+}
+
 __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n, QRWork w) {
   extern __shared__ double smem_qr[];
   cplx* v = reinterpret_cast<cplx*>(smem_qr);         // (n) current reflector
@@ -231,8 +253,7 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
       const int qpos = k + 1 + t;
       const int j = order[qpos];
       cplx* col = A + (size_t)j * n;
-      double vn1 = 0.0, vn2 = 0.0;
-      if (lane == 0) { vn1 = __ldcg(&w.vn1[j]); vn2 = __ldcg(&w.vn2[j]); }   // in flight during the update
+      const double vn1 = __ldcg(&w.vn1[j]), vn2 = __ldcg(&w.vn2[j]);   // in flight during the dot product
       cplx x[QR_MAXT];
       cplx sp[4] = {cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0)};
       const int nq = (n - k + 31) >> 5;   // warp-uniform: no FP64 work on fully masked slots
@@ -253,41 +274,30 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
       s = cfma_conj(scal, s, ak);
       const cplx f = cmul(ctau, s);        // a_k -= f
       const cplx fs = cmul(f, scal);       // a_r -= f scal x_r, r > k
-      double tp[4] = {0.0, 0.0, 0.0, 0.0};
-      cplx xk = cmake(0.0, 0.0);
-#pragma unroll
-      for (int q = 0; q < QR_MAXT; ++q) {
-        if (q >= nq) break;
-        int r = k + lane + 32 * q;
-        if (r < n) {
-          // x -= c v with four fused multiply-adds (c = f at r = k, f scal below)
-          const cplx vr = r == k ? cmake(1.0, 0.0) : v[r];
-          const cplx c = r == k ? f : fs;
-          x[q] = cmake(fma(-c.x, vr.x, fma(c.y, vr.y, x[q].x)), fma(-c.x, vr.y, fma(-c.y, vr.x, x[q].y)));
-          col[r] = x[q];
-          if (q == 0 && lane == 0) xk = x[q];
-          else tp[q & 3] = fma(x[q].x, x[q].x, fma(x[q].y, x[q].y, tp[q & 3]));
-        }
+      // partial norm downdate (zlaqp2), decided from the updated a_k alone, so
+      // the tail norm is only accumulated when it is recomputed
+      double vn1_new = vn1;
+      bool recompute = false;
+      if (vn1 != 0.0) {
+        const cplx xk = csub(ak, f);
+        double ratio = sqrt(cabs2(xk)) / vn1;
+        double temp = 1.0 - ratio * ratio;
+        temp = temp > 0.0 ? temp : 0.0;
+        double r2 = vn1 / vn2;
+        double temp2 = temp * r2 * r2;
+        if (temp2 <= tol3z) recompute = true;
+        else vn1_new = vn1 * sqrt(temp);
       }
-      double tail = warp_sum((tp[0] + tp[1]) + (tp[2] + tp[3]));
+      if (recompute) {
+        const double tail = warp_sum(qr_update_column<true>(x, col, v, k, n, nq, lane, f, fs));
+        vn1_new = (k < n - 1) ? sqrt(tail) : 0.0;
+        if (lane == 0) w.vn2[j] = vn1_new;
+      } else {
+        qr_update_column<false>(x, col, v, k, n, nq, lane, f, fs);
+      }
       if (lane == 0) {
-        if (vn1 != 0.0) {
-          double ratio = sqrt(cabs2(xk)) / vn1;
-          double temp = 1.0 - ratio * ratio;
-          temp = temp > 0.0 ? temp : 0.0;
-          double r2 = vn1 / vn2;
-          double temp2 = temp * r2 * r2;
-          if (temp2 <= tol3z) {
-            double nv = (k < n - 1) ? sqrt(tail) : 0.0;
-            vn1 = nv;
-            vn2 = nv;
-            w.vn2[j] = nv;
-          } else {
-            vn1 = vn1 * sqrt(temp);
-          }
-          w.vn1[j] = vn1;
-        }
-        if (cand_better(vn1, qpos, cbest, cbq)) { cbest = vn1; cbq = qpos; }
+        if (vn1 != 0.0) w.vn1[j] = vn1_new;
+        if (cand_better(vn1_new, qpos, cbest, cbq)) { cbest = vn1_new; cbq = qpos; }
       }
     }
     // this CTA's candidate for the next pivot (lane 0 of each warp holds its best)

@@ -322,13 +322,75 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_updates(LocalUpdateArgs
 // ---------------------------------------------------------------------------
 // delayed rank-k updates: G_cur = G + X Y with X (n x 4k), Y (4k x n)
 // ---------------------------------------------------------------------------
+// On GB300 every FP64 warp instruction occupies a sub-partition's FP64 unit
+// for tens of cycles, so the per-site chain is kept short and split over
+// warps: the per-site constants come from a prepare kernel run once per
+// slice, the 4x4 block G_cur[i + rN, i + cN] is read from a cache that the
+// owner CTA of site i keeps current, and the decision runs on three warps
+// at once (det and 1/det; the adjugate; the action difference).
+
+// Per-site constants of slice l: one warp per site.  Lanes of even parity
+// evaluate the old-field block (power -1), odd lanes the proposed one.
+__global__ void __launch_bounds__(128) k_local_prepare(LocalUpdateArgs a, SitePrep* __restrict__ prep) {
+  const ModelConst& mc = a.mc;
+  const int N = mc.N, M = mc.M, l = a.slice0;
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 4 + (threadIdx.x >> 5);
+  if (i >= N) return;
+  const double* po = &a.phi[((size_t)N * l + i) * 3];
+  const double old[3] = {po[0], po[1], po[2]};
+  const double nw[3] = {old[0] + a.delta[3 * i], old[1] + a.delta[3 * i + 1], old[2] + a.delta[3 * i + 2]};
+  const bool odd = lane & 1;
+  double C, R, shn;
+  cplx S;
+  const double op[3] = {odd ? nw[0] : old[0], odd ? nw[1] : old[1], odd ? nw[2] : old[2]};
+  ev_params(mc, op, odd ? 1.0 : -1.0, C, S, R, shn);
+  const double C1 = __shfl_sync(0xffffffffu, C, 0), R1 = __shfl_sync(0xffffffffu, R, 0);
+  const double C2 = __shfl_sync(0xffffffffu, C, 1), R2 = __shfl_sync(0xffffffffu, R, 1);
+  const cplx S1 = shfl_c(S, 0), S2 = shfl_c(S, 1);
+  const double s2 = __shfl_sync(0xffffffffu, shn, 1);
+  SitePrep* out = prep + i;
+  if (lane < 16) {
+    const int r = lane >> 2, c = lane & 3;
+    cplx v = cmake(0.0, 0.0);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v = cfma(ev_entry(r, k, C1, S1, R1), ev_entry(k, c, C2, S2, R2), v);
+    if (r == c) v.x -= 1.0;
+    out->delta[lane] = v;
+  } else if (lane == 16) {
+    EvEntry e;
+    e.C = C2; e.Sr = -nw[0] * s2; e.Si = nw[1] * s2; e.R = -nw[2] * s2;
+    out->ev = e;
+  } else if (lane == 17) {
+    // boson action difference (src/action.jl:57-100) without the space-neighbour term
+    const int lt_later = (l + 1) % M, lt_earlier = (l - 1 + M) % M;
+    const double diff[3] = {nw[0] - old[0], nw[1] - old[1], nw[2] - old[2]};
+    const double old_sq = old[0] * old[0] + old[1] * old[1] + old[2] * old[2];
+    const double new_sq = nw[0] * nw[0] + nw[1] * nw[1] + nw[2] * nw[2];
+    const double sq_diff = new_sq - old_sq;
+    const double pow4_diff = new_sq * new_sq - old_sq * old_sq;
+    const double* pe = &a.phi[((size_t)N * lt_earlier + i) * 3];
+    const double* pl = &a.phi[((size_t)N * lt_later + i) * 3];
+    double tdot = 0.0;
+    for (int c = 0; c < 3; ++c) tdot += (pl[c] + pe[c]) * diff[c];
+    out->diff[0] = diff[0]; out->diff[1] = diff[1]; out->diff[2] = diff[2];
+    out->dsA = 1.0 / (mc.dtau * mc.c * mc.c) * (sq_diff - tdot);
+    out->dsQ = 4 * sq_diff;
+    out->dsB = mc.dtau * (0.5 * mc.r * sq_diff + 0.25 * mc.u * pow4_diff);
+  }
+}
+
 // Processes sites state[0] .. N-1 until k accepted updates are pending or the
 // slice ends; state[0] is left at the next site and state[1] at the number of
 // pending factors.  The flush G += X Y (a separate GEMM launch over the first
 // 4 state[1] columns) follows every round.
+//
+// CTA b owns sites j = b, b + grid, ...: on each acceptance it forms the 4
+// rows j + rN of the new X columns and the 4 columns j + cN of the new Y rows
+// (one warp per row / column) and refreshes the cached block of site j.
 __global__ void __launch_bounds__(LU_THREADS, 2) k_local_delayed(LocalUpdateArgs a, DelayedArgs d) {
   const ModelConst& mc = a.mc;
-  const int N = mc.N, n = mc.n, K4 = 4 * d.k;
+  const int N = mc.N, n = mc.n, L = mc.L, K4 = 4 * d.k;
   __shared__ int s_first;
   if (threadIdx.x == 0) s_first = __ldcg(&d.state[0]);
   __syncthreads();
@@ -338,93 +400,181 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_delayed(LocalUpdateArgs
   // after a round with no sites left from applying the factors again
   int p = 0;
   if (blockIdx.x == 0 && threadIdx.x == 0) d.state[1] = 0;
-  if (first >= N) return;               // slice done: nothing to do in this round (uniform over the grid)
+  if (first >= N) return;   // slice done: nothing to do in this round (uniform over the grid)
   extern __shared__ double4_16a smem_local[];
-  const LocalSmem sm = local_smem(smem_local, N);
-  cplx* Ysm = reinterpret_cast<cplx*>(sm.phis + 3 * N);   // (4k x 4): Y[j, i + cN] of the current site
-  cplx* Xsm = Ysm + (size_t)K4 * 4;                        // (4 x 4k): X[i + rN, j]
-  __shared__ SiteDecision dec;
+  double* phis = reinterpret_cast<double*>(smem_local);                 // (3, N) field of slice l
+  cplx* Ysm = reinterpret_cast<cplx*>(phis + 3 * N + (N & 1) * 3);     // (4k x 4): Y[j, i + cN]
+  cplx* Xsm = Ysm + (size_t)K4 * 4;                                     // (4 x 4k): X[i + rN, j]
+  __shared__ cplx s_delta[16];      // Delta_i
+  __shared__ cplx s_adj[2][16];     // adj(M)[r][c] (double-buffered by site parity)
+  __shared__ cplx s_det[2], s_inv[2];
+  __shared__ double s_expds[2];
+  __shared__ cplx s_xn[4][4], s_yn[4][4];   // new X rows / Y columns of an owned site
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  local_prologue(a, sm, first);
+  const int l = a.slice0;
+  for (int k = threadIdx.x; k < 3 * N; k += blockDim.x) phis[k] = a.phi[(size_t)3 * N * l + k];
   __syncthreads();
 
   for (int i = first; i < N; ++i) {
     const int J = 4 * p;   // pending columns of X / rows of Y
-    // pending factor entries touching site i
-    for (int t = threadIdx.x; t < 4 * J; t += blockDim.x) {
-      const int j = t >> 2, c = t & 3;
-      Ysm[4 * j + c] = ldcg_c(&d.Y[(size_t)j * n + i + c * N]);
-      Xsm[(size_t)c * K4 + j] = ldcg_c(&d.X[(size_t)j * n + i + c * N]);
-    }
-    __syncthreads();
-    if (wid == 0) {
+    const int slot = i & 1;
+    const SitePrep* sp = d.prep + i;
+    if (wid == 0 || wid == 2) {
+      // ---- M = I + Delta (I - G_cur_ii), lane 4r+c holds M[r][c] (src/local_updates.jl:49-55) ----
       const int r = (lane >> 2) & 3, c = lane & 3;
-      cplx g = cmake(0.0, 0.0);
+      cplx g = cmake(0.0, 0.0), drow[4];
       if (lane < 16) {
-        g = ldcg_c(&a.G[(size_t)(i + c * N) * n + i + r * N]);
-        for (int j = 0; j < J; ++j) g = cfma(Xsm[(size_t)r * K4 + j], Ysm[4 * j + c], g);
+        g = p == 0 ? ldcg_c(&a.G[(size_t)(i + c * N) * n + i + r * N]) : ldcg_c(&d.blk[(size_t)16 * i + lane]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) drow[k] = ldcg_c(&sp->delta[4 * r + k]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) drow[k] = cmake(0.0, 0.0);
       }
-      local_decide(a, sm, i, g, dec);
+      const cplx mt = cmake((r == c ? 1.0 : 0.0) - g.x, -g.y);   // (I - G_ii)[r][c]
+      cplx m = cmake(r == c ? 1.0 : 0.0, 0.0);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) m = cfma(drow[k], shfl_c(mt, 4 * k + c), m);
+      if (wid == 0) {
+        // det M by the permutation expansion (24 lanes); lane 0's sum is the
+        // one used everywhere, so every CTA decides bit for bit alike
+        const int jp = lane < 24 ? lane : 0;
+        cplx pr = shfl_c(m, c_perm[jp][0]);
+#pragma unroll
+        for (int rr = 1; rr < 4; ++rr) pr = cmul(pr, shfl_c(m, 4 * rr + c_perm[jp][rr]));
+        cplx term = cmake(0.0, 0.0);
+        if (lane < 24) term = c_psign[jp] > 0 ? pr : cmake(-pr.x, -pr.y);
+        cplx det = term;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) det = cadd(det, shfl_c(det, lane ^ o));
+        det = shfl_c(det, 0);
+        if (lane == 0) {
+          s_det[slot] = det;
+          s_inv[slot] = cdiv(cmake(1.0, 0.0), det);
+        }
+      } else {
+        // adj(M)[r][c] = cofactor C[c][r]
+        int rows[3], cols[3];
+        for (int t = 0, q = 0; t < 4; ++t) if (t != c) rows[q++] = t;
+        for (int t = 0, q = 0; t < 4; ++t) if (t != r) cols[q++] = t;
+        cplx e[3][3];
+#pragma unroll
+        for (int u3 = 0; u3 < 3; ++u3)
+#pragma unroll
+          for (int v3 = 0; v3 < 3; ++v3) e[u3][v3] = shfl_c(m, (4 * rows[u3] + cols[v3]) & 31);
+        cplx d3 = csub(cmul(e[0][0], csub(cmul(e[1][1], e[2][2]), cmul(e[1][2], e[2][1]))),
+                       cmul(e[0][1], csub(cmul(e[1][0], e[2][2]), cmul(e[1][2], e[2][0]))));
+        d3 = cadd(d3, cmul(e[0][2], csub(cmul(e[1][0], e[2][1]), cmul(e[1][1], e[2][0]))));
+        if ((r + c) & 1) d3 = cmake(-d3.x, -d3.y);
+        if (lane < 16) s_adj[slot][lane] = d3;
+      }
+    } else if (wid == 1) {
+      // ---- boson action difference: prepared part + space-neighbour coupling ----
+      if (lane == 0) {
+        const int y = i % L, x = i / L;
+        const int nbs[4] = {(y + 1) % L + L * x, y + L * ((x + 1) % L), (y - 1 + L) % L + L * x,
+                            y + L * ((x - 1 + L) % L)};
+        double sdot = 0.0;
+        for (int c = 0; c < 3; ++c) {
+          double os = 0.0;
+          for (int q = 0; q < 4; ++q) os = os + phis[3 * nbs[q] + c];
+          sdot += os * __ldcg(&sp->diff[c]);
+        }
+        double dS = __ldcg(&sp->dsA);
+        dS += 0.5 * mc.dtau * (__ldcg(&sp->dsQ) - 2.0 * sdot);
+        dS += __ldcg(&sp->dsB);
+        s_expds[slot] = exp(-dS);
+      }
+    } else if (J > 0 || wid == 3) {
+      // ---- stage Delta_i and the pending factor entries touching site i ----
+      const int t0 = threadIdx.x - 3 * 32, nt = blockDim.x - 3 * 32;
+      if (t0 < 16) s_delta[t0] = ldcg_c(&sp->delta[t0]);
+      for (int t = t0; t < 4 * J; t += nt) {
+        const int j = t >> 2, c = t & 3;
+        Ysm[4 * j + c] = ldcg_c(&d.Y[(size_t)j * n + i + c * N]);
+        Xsm[(size_t)c * K4 + j] = ldcg_c(&d.X[(size_t)j * n + i + c * N]);
+      }
     }
     __syncthreads();
-    const int accepted = dec.accepted;
-    if (!accepted) {
-      __syncthreads();
-      continue;
-    }
-    // ---- A = (G_cur[:, cols] - I[:, cols]) M^-1 -> X[:, J..J+3]; B = Delta G_cur[rows, :] -> Y[J..J+3, :] ----
-    // 16 lanes per item (item < n: row of A, item >= n: column of B); lane
-    // (k, jc) sums the pending terms j = jc, jc+4, ... of output k.
-    const cplx* Dl = &sm.delta_all[16 * i];
-    {
-      const int sub = lane & 15, k = sub >> 2, jc = sub & 3;
-      const int half = lane >> 4;
-      const int gw = blockIdx.x * (LU_THREADS / 32) + wid;
-      const int nw = gridDim.x * (LU_THREADS / 32);
-      for (int base = 2 * gw; base < 2 * n; base += 2 * nw) {   // uniform trip count over the warp
-        const int it = base + half;
-        const bool valid = it < 2 * n;
-        cplx gsum = cmake(0.0, 0.0);
-        if (valid) {
-          if (it < n) {
-            const int row = it;
-            for (int j = jc; j < J; j += 4) gsum = cfma(ldcg_c(&d.X[(size_t)j * n + row]), Ysm[4 * j + k], gsum);
-          } else {
-            const int col = it - n;
-            for (int j = jc; j < J; j += 4) gsum = cfma(Xsm[(size_t)k * K4 + j], ldcg_c(&d.Y[(size_t)j * n + col]), gsum);
-          }
-        }
-        gsum = cadd(gsum, shfl_c(gsum, lane ^ 1));
-        gsum = cadd(gsum, shfl_c(gsum, lane ^ 2));
-        if (valid && jc == 0) {
-          if (it < n) {
-            const int row = it;
-            cplx g = cadd(ldcg_c(&a.G[(size_t)(i + k * N) * n + row]), gsum);
-            if (row == i + k * N) g.x -= 1.0;
-            gsum = g;
-          } else {
-            const int col = it - n;
-            gsum = cadd(ldcg_c(&a.G[(size_t)col * n + i + k * N]), gsum);
-          }
-        }
-        // gather g[0..3] of this item (lanes jc == 0 of the 4 k groups)
-        cplx gk[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) gk[q] = shfl_c(gsum, (half << 4) + 4 * q);
-        if (valid && jc == 0) {
-          if (it < n) {
-            cplx s2 = cmake(0, 0);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) s2 = cfma(gk[q], dec.minv[q][k], s2);
-            d.X[(size_t)(J + k) * n + it] = s2;
-          } else {
-            cplx s2 = cmake(0, 0);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) s2 = cfma(Dl[4 * k + q], gk[q], s2);
-            d.Y[(size_t)(J + k) * n + (it - n)] = s2;
-          }
+    // ---- Metropolis decision, identical in every thread of every CTA ----
+    const cplx det = s_det[slot];
+    const double exp_dS = s_expds[slot];
+    const double pacc = exp_dS * det.x;
+    const double u = __ldg(&a.unif[i]);
+    const bool bad = !isfinite(det.x) || !isfinite(det.y) || (det.x == 0.0 && det.y == 0.0);
+    const bool acc = !bad && (pacc > 1.0 || u < pacc);
+    if (threadIdx.x == 0) {
+      if (acc)
+        for (int q = 0; q < 3; ++q) phis[3 * i + q] += a.delta[3 * i + q];
+      if (blockIdx.x == 0) {
+        if (bad) atomicOr(a.err, DQMC_KERR_NONFINITE);
+        if (a.acc_out) a.acc_out[i] = (uint8_t)acc;
+        if (a.det_out) a.det_out[i] = det;
+        if (a.pacc_out) a.pacc_out[i] = pacc;
+        if (acc) {
+          double* pg = &a.phi[((size_t)N * l + i) * 3];
+          pg[0] = phis[3 * i]; pg[1] = phis[3 * i + 1]; pg[2] = phis[3 * i + 2];
+          if (a.evtab) reinterpret_cast<EvEntry*>(a.evtab)[(size_t)N * l + i] = sp->ev;
+          *a.action += -log(exp_dS);
+          *a.n_acc += 1;
         }
       }
+    }
+    // decision slots are double-buffered: a rejected site needs no second barrier
+    if (!acc) continue;
+    // ---- new factor columns: X[:, J+k] = (G_cur[:, i + qN] - I[:, i + qN]) M^-1,
+    //      Y[J+k, :] = Delta G_cur[i + qN, :]; one warp per row / column ----
+    const cplx inv = s_inv[slot];
+    for (int j = blockIdx.x; j < N; j += gridDim.x) {
+      const bool isX = wid < 4;
+      const int q0 = wid & 3;
+      const int rc = j + q0 * N;              // X: row rc; Y: column rc
+      const int qg = lane >> 3, g8 = lane & 7;   // 8 lanes per term group of G_cur[., i + qg N]
+      cplx part = cmake(0.0, 0.0);
+      if (isX) {
+        for (int jj = g8; jj < J; jj += 8) part = cfma(ldcg_c(&d.X[(size_t)jj * n + rc]), Ysm[4 * jj + qg], part);
+      } else {
+        for (int jj = g8; jj < J; jj += 8) part = cfma(Xsm[(size_t)qg * K4 + jj], ldcg_c(&d.Y[(size_t)jj * n + rc]), part);
+      }
+      part = cadd(part, shfl_c(part, lane ^ 1));
+      part = cadd(part, shfl_c(part, lane ^ 2));
+      part = cadd(part, shfl_c(part, lane ^ 4));
+      cplx gq;
+      if (isX) {
+        gq = ldcg_c(&a.G[(size_t)(i + qg * N) * n + rc]);
+        if (rc == i + qg * N) gq.x -= 1.0;
+      } else {
+        gq = ldcg_c(&a.G[(size_t)rc * n + i + qg * N]);
+      }
+      const cplx gcur = cadd(gq, part);
+      // output k over 4 lanes (q = 0..3) each
+      const int o = lane & 15, ko = o >> 2, qq = o & 3;
+      const cplx gv = shfl_c(gcur, 8 * qq);
+      cplx prod = cmul(gv, isX ? s_adj[slot][4 * qq + ko] : s_delta[4 * ko + qq]);
+      prod = cadd(prod, shfl_c(prod, lane ^ 1));
+      prod = cadd(prod, shfl_c(prod, lane ^ 2));
+      if (lane < 16 && qq == 0) {
+        if (isX) {
+          const cplx xv = cmul(prod, inv);
+          d.X[(size_t)(J + ko) * n + rc] = xv;
+          s_xn[q0][ko] = xv;
+        } else {
+          d.Y[(size_t)(J + ko) * n + rc] = prod;
+          s_yn[ko][q0] = prod;
+        }
+      }
+      // ---- refresh the cached block of site j (needed by later sites only) ----
+      if (j > i) {
+        __syncthreads();
+        if (wid == 0 && lane < 16) {
+          const int r = lane >> 2, c = lane & 3;
+          cplx b = p == 0 ? ldcg_c(&a.G[(size_t)(j + c * N) * n + j + r * N]) : ldcg_c(&d.blk[(size_t)16 * j + lane]);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) b = cfma(s_xn[r][k], s_yn[k][c], b);
+          d.blk[(size_t)16 * j + lane] = b;
+        }
+      }
+      __syncthreads();   // s_xn / s_yn reused by the next owned site
     }
     ++p;
     if (p == d.k || i == N - 1) {
@@ -436,16 +586,21 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_delayed(LocalUpdateArgs
   if (blockIdx.x == 0 && threadIdx.x == 0) { d.state[0] = N; d.state[1] = p; }
 }
 
-
 }  // namespace
 
 static size_t local_smem_bytes(int N) {
   return (size_t)N * (16 * sizeof(cplx) + sizeof(EvEntry)) + (size_t)3 * N * sizeof(double);
 }
 
+cudaError_t launch_local_prepare(const LocalUpdateArgs& a, SitePrep* prep, cudaStream_t st) {
+  k_local_prepare<<<(a.mc.N + 3) / 4, 128, 0, st>>>(a, prep);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d, int sm_count, cudaStream_t st,
                                  int max_grid) {
-  const size_t smem = local_smem_bytes(a.mc.N) + (size_t)2 * 4 * d.k * 4 * sizeof(cplx);
+  const int N = a.mc.N;
+  const size_t smem = (size_t)(3 * N + (N & 1) * 3) * sizeof(double) + (size_t)2 * 4 * d.k * 4 * sizeof(cplx);
   static bool attr = false;
   if (!attr) {
     cudaError_t e = cudaFuncSetAttribute(k_local_delayed, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
@@ -459,9 +614,7 @@ cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d,
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   if (per_sm > 2) per_sm = 2;
   int grid = sm_count * per_sm;
-  // two items (rows of A / columns of B) per warp
-  const int need = (a.mc.n + (LU_THREADS / 32) - 1) / (LU_THREADS / 32);
-  if (grid > need) grid = need < 1 ? 1 : need;
+  if (grid > N) grid = N;   // one CTA per site owner at most
   if (max_grid > 0 && grid > max_grid) grid = max_grid;
   LocalUpdateArgs ca = a;
   DelayedArgs cd = d;

@@ -47,11 +47,23 @@ struct LocalUpdateArgs {
 cudaError_t launch_local_updates(const LocalUpdateArgs& a, int sm_count, cudaStream_t st, int max_grid = 0);
 // delayed rank-k form: pending factors X (n x 4k, column-major) and Y (4k x n,
 // row j at Y + j*n); state[0] = next site of the slice, state[1] = pending accepts
+// Per-site data of one slice, prepared once before its first delayed round
+// (the old field of a site cannot change before its own visit).
+struct SitePrep {
+  cplx delta[16];          // Delta_i = e^{+dtau V(phi_i)} e^{-dtau V(phi_i + delta_i)} - I, row-major
+  EvEntry ev;              // interaction entries of the proposed field
+  double diff[3];          // proposed minus old field
+  double dsA, dsQ, dsB;    // boson action difference, space-neighbour coupling excluded
+  double pad[2];
+};
+cudaError_t launch_local_prepare(const LocalUpdateArgs& a, SitePrep* prep, cudaStream_t st);
 struct DelayedArgs {
   cplx* X;
   cplx* Y;
   int* state;
   int k;
+  const SitePrep* prep;    // (N) from launch_local_prepare for this slice
+  cplx* blk;               // (N, 16) cache of the diagonal blocks G_cur[j + rN, j + cN]
 };
 cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d, int sm_count, cudaStream_t st,
                                  int max_grid = 0);
