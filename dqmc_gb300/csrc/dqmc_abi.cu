@@ -720,7 +720,7 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
   A((void**)&h->W1, nn); A((void**)&h->W2, nn); A((void**)&h->W3, nn); A((void**)&h->W4, nn);
   A((void**)&h->D1, n * sizeof(double)); A((void**)&h->d2, n * sizeof(double));
   A((void**)&h->ord1, n * sizeof(int));
-  A((void**)&h->qr.vn1, n * sizeof(double)); A((void**)&h->qr.vn2, n * sizeof(double));
+  A((void**)&h->qr.vn1, 2 * n * sizeof(double)); A((void**)&h->qr.vn2, 2 * n * sizeof(double));
   A((void**)&h->qr.order, n * sizeof(int)); A((void**)&h->qr.tau, n * sizeof(cplx));
   A((void**)&h->qr.beta, n * sizeof(double)); A((void**)&h->qr.V, nn);
   A((void**)&h->qr.bar, sizeof(GridBarrier));

@@ -120,8 +120,24 @@ constexpr int QR_MAXT = 32;   // elements per lane of one column (n <= 1024)
 
 // Candidate of the next pivot: the CTA-local maximum of the partial norms
 // and its logical position (ties: smaller position, as LAPACK's idamax).
+// Norms are >= +0, so their bit patterns order like their values: the
+// comparison runs on the integer units, not the FP64 unit.
 __device__ __forceinline__ bool cand_better(double v, int q, double bv, int bq) {
-  return v > bv || (v == bv && q < bq);
+  const long long a = __double_as_longlong(v), b = __double_as_longlong(bv);
+  return a > b || (a == b && q < bq);
+}
+
+// Complex warp sum with five FP64 adds: after one exchange the low half of
+// the warp reduces the real parts and the high half the imaginary parts.
+__device__ __forceinline__ cplx warp_sum_c(cplx v) {
+  const int lane = threadIdx.x & 31;
+  const bool hi = lane & 16;
+  double keep = hi ? v.y : v.x;
+  const double send = hi ? v.x : v.y;
+  keep += __shfl_xor_sync(0xffffffffu, send, 16);
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
+  return cmake(__shfl_sync(0xffffffffu, keep, 0), __shfl_sync(0xffffffffu, keep, 16));
 }
 
 // a -= c v over the column slots of one lane (c = f at r = k, f scal below,
@@ -129,7 +145,7 @@ __device__ __forceinline__ bool cand_better(double v, int q, double bv, int bq) 
 template <bool TAIL>
 __device__ __forceinline__ double qr_update_column(cplx (&x)[QR_MAXT], cplx* __restrict__ col, const cplx* v, int k,
                                                    int n, int nq, int lane, cplx f, cplx fs) {
-  double tp[4] = {0.0, 0.0, 0.0, 0.0};
+  double tp = 0.0;
 #pragma unroll
   for (int q = 0; q < QR_MAXT; ++q) {
     if (q >= nq) break;
@@ -140,34 +156,97 @@ __device__ __forceinline__ double qr_update_column(cplx (&x)[QR_MAXT], cplx* __r
       const cplx c = r == k ? f : fs;
       x[q] = cmake(fma(-c.x, vr.x, fma(c.y, vr.y, x[q].x)), fma(-c.x, vr.y, fma(-c.y, vr.x, x[q].y)));
       col[r] = x[q];
-      if (TAIL && r > k) tp[q & 3] = fma(x[q].x, x[q].x, fma(x[q].y, x[q].y, tp[q & 3]));
+      if (TAIL && r > k) tp = fma(x[q].x, x[q].x, fma(x[q].y, x[q].y, tp));
     }
   }
-  return (tp[0] + tp[1]) + (tp[2] + tp[3]);
+  return tp;
+}
+
+// sum_{r > k} conj(x_r) a_r over one lane's slots (loads the column into x)
+__device__ __forceinline__ cplx qr_load_dot(cplx (&x)[QR_MAXT], const cplx* __restrict__ col, const cplx* v, int k,
+                                            int n, int nq, int lane) {
+  cplx sp = cmake(0.0, 0.0);
+#pragma unroll
+  for (int q = 0; q < QR_MAXT; ++q) {
+    if (q >= nq) break;
+    const int r = k + lane + 32 * q;
+    x[q] = cmake(0.0, 0.0);
+    if (r < n) {
+      x[q] = ldcg_c(&col[r]);
+      if (r > k) sp = cfma_conj(v[r], x[q], sp);
+    }
+  }
+  return warp_sum_c(sp);
+}
+
+// One column step after the dot product s0 = sum_{r>k} conj(x_r) a_r:
+// a -= tau^H (v^H a) v with v = (1, scal x_{k+1..n}), then the partial norm
+// downdate of zlaqp2 with stored reciprocals (vn1, vn2 at [j], 1/vn1, 1/vn2
+// at [n + j]); returns the new partial norm.
+__device__ __forceinline__ double qr_finish_column(cplx (&x)[QR_MAXT], cplx* __restrict__ col, const cplx* v, int k,
+                                                   int n, int nq, int lane, int j, cplx s0, cplx ctau, cplx scal,
+                                                   const QRWork& w, double tol3z) {
+  const double vn1 = __ldcg(&w.vn1[j]), vn2 = __ldcg(&w.vn2[j]);
+  const double inv1 = __ldcg(&w.vn1[n + j]), inv2 = __ldcg(&w.vn2[n + j]);
+  // v^H a = a_k + conj(scal) s0
+  const cplx ak = cmake(__shfl_sync(0xffffffffu, x[0].x, 0), __shfl_sync(0xffffffffu, x[0].y, 0));
+  const cplx s = cfma_conj(scal, s0, ak);
+  const cplx f = cmul(ctau, s);     // a_k -= f
+  const cplx fs = cmul(f, scal);    // a_r -= f scal x_r, r > k
+  // zlaqp2: temp = max(0, 1 - (|a_k|/vn1)^2), temp2 = temp (vn1/vn2)^2;
+  // recompute the norm when temp2 <= sqrt(eps), else vn1 *= sqrt(temp)
+  double vn1_new = vn1, inv1_new = inv1;
+  bool recompute = false;
+  if (vn1 != 0.0) {
+    const cplx xk = csub(ak, f);
+    double temp = 1.0 - (cabs2(xk) * inv1) * inv1;
+    temp = temp > 0.0 ? temp : 0.0;
+    const double r2 = vn1 * inv2;
+    if (temp * r2 * r2 <= tol3z) {
+      recompute = true;
+    } else {
+      const double rs = rsqrt(temp);
+      vn1_new = vn1 * temp * rs;
+      inv1_new = inv1 * rs;
+    }
+  }
+  if (recompute) {
+    const double tail = warp_sum(qr_update_column<true>(x, col, v, k, n, nq, lane, f, fs));
+    vn1_new = (k < n - 1) ? sqrt(tail) : 0.0;
+    inv1_new = vn1_new > 0.0 ? 1.0 / vn1_new : 0.0;
+    if (lane == 0) { w.vn2[j] = vn1_new; w.vn2[n + j] = inv1_new; }
+  } else {
+    qr_update_column<false>(x, col, v, k, n, nq, lane, f, fs);
+  }
+  if (lane == 0 && vn1 != 0.0) { w.vn1[j] = vn1_new; w.vn1[n + j] = inv1_new; }
+  return vn1_new;
 }
 
 __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n, QRWork w) {
   extern __shared__ double smem_qr[];
-  cplx* v = reinterpret_cast<cplx*>(smem_qr);         // (n) current reflector
+  cplx* v = reinterpret_cast<cplx*>(smem_qr);         // (n) pivot column: a_k at k, unscaled x below
   int* order = reinterpret_cast<int*>(v + n);         // (n) logical -> physical
   __shared__ double red[32];
   __shared__ int redi[32];
-  __shared__ double nsum[32];   // block_sum scratch, apart from the candidate slots
+  __shared__ double nsum[32];
+  __shared__ cplx s_tau, s_scal;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int warps = QR_THREADS / 32;
+  const int scal_warp = warps - 1;   // holds no column while rem < (warps - 1) * grid
   const int gwarp = blockIdx.x * warps + wid, nwarps = gridDim.x * warps;
   const double tol3z = sqrt(DBL_EPSILON);
 
   for (int q = threadIdx.x; q < n; q += blockDim.x) order[q] = q;
   // initial column norms (zgeqp3: vn1 = vn2 = ||A(:, j)||) and the first candidates
-  double cb = -1.0;
+  double cb = 0.0;
   int cq = n;
   for (int j = gwarp; j < n; j += nwarps) {
     double s = 0.0;
     for (int r = lane; r < n; r += 32) s += cabs2(A[(size_t)j * n + r]);
     s = warp_sum(s);
-    if (lane == 0) { w.vn1[j] = sqrt(s); w.vn2[j] = sqrt(s); }
-    if (cand_better(sqrt(s), j, cb, cq)) { cb = sqrt(s); cq = j; }
+    const double nv = sqrt(s), iv = nv > 0.0 ? 1.0 / nv : 0.0;
+    if (lane == 0) { w.vn1[j] = nv; w.vn2[j] = nv; w.vn1[n + j] = iv; w.vn2[n + j] = iv; }
+    if (cand_better(nv, j, cb, cq)) { cb = nv; cq = j; }
   }
   if (lane == 0) { red[wid] = cb; redi[wid] = cq; }
   __syncthreads();
@@ -180,12 +259,13 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
   }
   if (!grid_barrier(w.bar, w.err)) return;
 
+  const int chunk = (n + gridDim.x - 1) / gridDim.x;   // rows of V written by this CTA
   for (int k = 0; k < n; ++k) {
-    // ---- pivot: best of the per-CTA candidates (first position of maximal norm) ----
-    {
-      double best = -1.0;
+    // ---- pivot: best of the per-CTA candidates (first position of maximal norm), warp 0 ----
+    if (wid == 0) {
+      double best = 0.0;
       int bestq = n;
-      for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x) {
+      for (int c = lane; c < (int)gridDim.x; c += 32) {
         double val = __ldcg(&w.cand_v[c]);
         int q = __ldcg(&w.cand_q[c]);
         if (cand_better(val, q, best, bestq)) { best = val; bestq = q; }
@@ -196,19 +276,14 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
         int oq = __shfl_xor_sync(0xffffffffu, bestq, o);
         if (cand_better(ob, oq, best, bestq)) { best = ob; bestq = oq; }
       }
-      if (lane == 0) { red[wid] = best; redi[wid] = bestq; }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        double b = red[0]; int bq = redi[0];
-        for (int q = 1; q < warps; ++q)
-          if (cand_better(red[q], redi[q], b, bq)) { b = red[q]; bq = redi[q]; }
-        if (bq < k || bq >= n) bq = k;   // no candidate (all norms zero): keep the order
-        int t = order[k]; order[k] = order[bq]; order[bq] = t;
+      if (lane == 0) {
+        if (bestq < k || bestq >= n) bestq = k;   // no candidate: keep the order
+        int t = order[k]; order[k] = order[bestq]; order[bestq] = t;
       }
-      __syncthreads();
     }
+    __syncthreads();
     const int p = order[k];
-    // ---- reflector from A[k:n, p] (zlarfg); independent loads, 4 per thread at n <= 1024 ----
+    // ---- reflector from A[k:n, p] (zlarfg): partial squared norms, 4 loads per thread at n <= 1024 ----
     double xn2 = 0.0;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -216,89 +291,76 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
       if (r < n) {
         cplx x = ldcg_c(&A[(size_t)p * n + r]);
         v[r] = x;
-        if (r > k) xn2 += cabs2(x);
+        if (r > k) xn2 = fma(x.x, x.x, fma(x.y, x.y, xn2));
       }
     }
-    xn2 = block_sum(xn2, nsum);   // includes __syncthreads; v[k..n) visible after it
-    const cplx alpha = v[k];
-    const double xnorm = sqrt(xn2);
-    double beta;
-    cplx tau, scal;
-    if (xnorm == 0.0 && alpha.y == 0.0) {
-      tau = cmake(0.0, 0.0);
-      beta = alpha.x;
-      scal = cmake(0.0, 0.0);
-    } else {
-      double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2);
-      beta = alpha.x >= 0.0 ? -nrm : nrm;
-      tau = cmake((beta - alpha.x) / beta, -alpha.y / beta);
-      scal = cdiv(cmake(1.0, 0.0), csub(alpha, cmake(beta, 0.0)));
-    }
-    // v = (1, scal x_{k+1..n}): the shared buffer keeps the unscaled x and the
-    // scale is folded into each column's coefficients; only CTA 0 writes the
-    // scaled reflector for the later applications of Q
-    if (blockIdx.x == 0) {
-      if (threadIdx.x == 0) { w.tau[k] = tau; w.beta[k] = beta; }
-      for (int r = threadIdx.x; r < n; r += blockDim.x)
-        w.V[(size_t)k * n + r] = r < k ? cmake(0.0, 0.0) : (r == k ? cmake(1.0, 0.0) : cmul(v[r], scal));
+    xn2 = warp_sum(xn2);
+    if (lane == 0) nsum[wid] = xn2;
+    __syncthreads();
+    // ---- one warp forms beta, tau and the reflector scale while the others
+    //      start the dot products of their first column (which need neither) ----
+    if (wid == scal_warp) {
+      double t = lane < warps ? nsum[lane] : 0.0;
+#pragma unroll
+      for (int o = 4; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);   // warps <= 8
+      const cplx alpha = v[k];
+      double beta;
+      cplx tau, scal;
+      if (t == 0.0 && alpha.y == 0.0) {
+        tau = cmake(0.0, 0.0);
+        beta = alpha.x;
+        scal = cmake(0.0, 0.0);
+      } else {
+        const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + t);
+        beta = alpha.x >= 0.0 ? -nrm : nrm;
+        const double rb = 1.0 / beta;
+        tau = cmake((beta - alpha.x) * rb, -alpha.y * rb);
+        // scal = 1 / (alpha - beta), formed on (alpha - beta) / nrm (modulus in [1, 2])
+        const double an = fabs(rb);
+        const cplx dd = cmake((alpha.x - beta) * an, alpha.y * an);
+        const double rd = an / (dd.x * dd.x + dd.y * dd.y);
+        scal = cmake(dd.x * rd, -dd.y * rd);
+      }
+      if (lane == 0) {
+        s_tau = tau;
+        s_scal = scal;
+        if (blockIdx.x == 0) { w.tau[k] = tau; w.beta[k] = beta; }
+      }
     }
     // ---- apply H_k^H to the remaining columns, downdate their norms ----
     // remaining logical positions k+1..n-1 are dealt round-robin over the CTAs
     // first, so every SM keeps an equal share of the columns as k grows
-    const cplx ctau = cconj(tau);
     const int rem = n - k - 1;
-    double cbest = -1.0;
+    const int nq = (n - k + 31) >> 5;   // warp-uniform: no FP64 work on fully masked slots
+    double cbest = 0.0;
     int cbq = n;
-    for (int t = blockIdx.x + gridDim.x * wid; t < rem; t += gridDim.x * warps) {
+    const int t_first = blockIdx.x + gridDim.x * wid;
+    cplx x[QR_MAXT];
+    cplx s_first = cmake(0.0, 0.0);
+    int j_first = -1;
+    if (t_first < rem && wid != scal_warp) {
+      j_first = order[k + 1 + t_first];
+      s_first = qr_load_dot(x, A + (size_t)j_first * n, v, k, n, nq, lane);
+    }
+    __syncthreads();   // tau, scal visible
+    const cplx ctau = cconj(s_tau), scal = s_scal;
+    // rows of V written by this CTA: v = (1, scal x_{k+1..n}), zero above k
+    for (int r = blockIdx.x * chunk + threadIdx.x; r < n && r < (blockIdx.x + 1) * chunk; r += blockDim.x)
+      w.V[(size_t)k * n + r] = r < k ? cmake(0.0, 0.0) : (r == k ? cmake(1.0, 0.0) : cmul(v[r], scal));
+    if (j_first >= 0) {
+      const double nv = qr_finish_column(x, A + (size_t)j_first * n, v, k, n, nq, lane, j_first, s_first, ctau, scal,
+                                         w, tol3z);
+      if (lane == 0 && cand_better(nv, k + 1 + t_first, cbest, cbq)) { cbest = nv; cbq = k + 1 + t_first; }
+    }
+    // further columns of this warp (more columns than warps), and the scal
+    // warp's share when it has one
+    for (int t = (wid == scal_warp ? t_first : t_first + gridDim.x * warps); t < rem; t += gridDim.x * warps) {
       const int qpos = k + 1 + t;
       const int j = order[qpos];
       cplx* col = A + (size_t)j * n;
-      const double vn1 = __ldcg(&w.vn1[j]), vn2 = __ldcg(&w.vn2[j]);   // in flight during the dot product
-      cplx x[QR_MAXT];
-      cplx sp[4] = {cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0)};
-      const int nq = (n - k + 31) >> 5;   // warp-uniform: no FP64 work on fully masked slots
-#pragma unroll
-      for (int q = 0; q < QR_MAXT; ++q) {
-        if (q >= nq) break;
-        int r = k + lane + 32 * q;
-        x[q] = cmake(0.0, 0.0);
-        if (r < n) {
-          x[q] = ldcg_c(&col[r]);
-          if (r > k) sp[q & 3] = cfma_conj(v[r], x[q], sp[q & 3]);
-        }
-      }
-      cplx s = cadd(cadd(sp[0], sp[1]), cadd(sp[2], sp[3]));
-      s = warp_sum(s);
-      // v^H a = a_k + conj(scal) sum_{r>k} conj(x_r) a_r
-      const cplx ak = cmake(__shfl_sync(0xffffffffu, x[0].x, 0), __shfl_sync(0xffffffffu, x[0].y, 0));
-      s = cfma_conj(scal, s, ak);
-      const cplx f = cmul(ctau, s);        // a_k -= f
-      const cplx fs = cmul(f, scal);       // a_r -= f scal x_r, r > k
-      // partial norm downdate (zlaqp2), decided from the updated a_k alone, so
-      // the tail norm is only accumulated when it is recomputed
-      double vn1_new = vn1;
-      bool recompute = false;
-      if (vn1 != 0.0) {
-        const cplx xk = csub(ak, f);
-        double ratio = sqrt(cabs2(xk)) / vn1;
-        double temp = 1.0 - ratio * ratio;
-        temp = temp > 0.0 ? temp : 0.0;
-        double r2 = vn1 / vn2;
-        double temp2 = temp * r2 * r2;
-        if (temp2 <= tol3z) recompute = true;
-        else vn1_new = vn1 * sqrt(temp);
-      }
-      if (recompute) {
-        const double tail = warp_sum(qr_update_column<true>(x, col, v, k, n, nq, lane, f, fs));
-        vn1_new = (k < n - 1) ? sqrt(tail) : 0.0;
-        if (lane == 0) w.vn2[j] = vn1_new;
-      } else {
-        qr_update_column<false>(x, col, v, k, n, nq, lane, f, fs);
-      }
-      if (lane == 0) {
-        if (vn1 != 0.0) w.vn1[j] = vn1_new;
-        if (cand_better(vn1_new, qpos, cbest, cbq)) { cbest = vn1_new; cbq = qpos; }
-      }
+      const cplx s0 = qr_load_dot(x, col, v, k, n, nq, lane);
+      const double nv = qr_finish_column(x, col, v, k, n, nq, lane, j, s0, ctau, scal, w, tol3z);
+      if (lane == 0 && cand_better(nv, qpos, cbest, cbq)) { cbest = nv; cbq = qpos; }
     }
     // this CTA's candidate for the next pivot (lane 0 of each warp holds its best)
     if (lane == 0) { red[wid] = cbest; redi[wid] = cbq; }
@@ -357,16 +419,17 @@ __global__ void __launch_bounds__(128) k_apply_q_right(cplx* __restrict__ X, int
     if (tk.x == 0.0 && tk.y == 0.0) continue;
     if (conj_q) tk = cconj(tk);
     // X H = X - tau (X v) v^H
-    cplx dp[4] = {cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0), cmake(0.0, 0.0)};
+    // one accumulator: the FP64 unit's issue rate, not its latency, bounds the chain
+    cplx dp = cmake(0.0, 0.0);
     const int t0 = k >> 5, t1 = (n + 31) >> 5;   // warp-uniform range of slots holding columns >= k
 #pragma unroll
     for (int t = 0; t < QR_MAXT; ++t) {
       if (t < t0) continue;
       if (t >= t1) break;
       int c = lane + 32 * t;
-      if (c >= k && c < n) dp[t & 3] = cfma(x[t], __ldg(&vk[c]), dp[t & 3]);
+      if (c >= k && c < n) dp = cfma(x[t], __ldg(&vk[c]), dp);
     }
-    cplx d = warp_sum(cadd(cadd(dp[0], dp[1]), cadd(dp[2], dp[3])));
+    cplx d = warp_sum_c(dp);
     cplx f = cmul(tk, d);
 #pragma unroll
     for (int t = 0; t < QR_MAXT; ++t) {

@@ -80,8 +80,8 @@ cudaError_t launch_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, c
                          const double* colscale, cudaStream_t st, const int* active = nullptr);
 
 struct QRWork {
-  double* vn1;       // (n)
-  double* vn2;       // (n)
+  double* vn1;       // (2n) partial column norms, reciprocals at [n + j]
+  double* vn2;       // (2n) norms at the last recomputation, reciprocals at [n + j]
   int* order;        // (n) logical position -> physical column
   cplx* tau;         // (n)
   double* beta;      // (n) real diagonal of R in logical order
