@@ -68,19 +68,21 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier* b, int* err) {
   __shared__ int s_ok;
   if (threadIdx.x == 0) {
     volatile unsigned int* vgen = &b->gen;
-    unsigned int g = *vgen;
+    const unsigned int g = *vgen;
     __threadfence();
-    unsigned int arrived = atomicAdd(&b->count, 1u);
+    // atomicInc wraps the count to 0 on the last arrival, so no separate reset
+    const unsigned int arrived = atomicInc(&b->count, gridDim.x - 1);
     int ok = 1;
     if (arrived == gridDim.x - 1) {
-      atomicExch(&b->count, 0u);
       __threadfence();
       atomicAdd(&b->gen, 1u);
     } else {
       long long spins = 0;
       while (*vgen == g) {
-        if (++spins > (1ll << 26)) { atomicOr(err, 2); ok = 0; break; }
-        if (*(volatile int*)err & 2) { ok = 0; break; }
+        if ((++spins & 1023) == 0) {
+          if (spins > (1ll << 26)) { atomicOr(err, 2); ok = 0; break; }
+          if (*(volatile int*)err & 2) { ok = 0; break; }
+        }
       }
     }
     __threadfence();

@@ -70,6 +70,7 @@ struct dqmc_handle {
   int* dstate = nullptr;
   SitePrep* prep = nullptr;   // (N) per-site constants of the slice being updated
   cplx* blk = nullptr;        // (N, 16) cached diagonal blocks of G_cur
+  int* pub = nullptr;         // (N) per-site publication counters of the delayed rounds
   double* force_d = nullptr;   // (3, N, M) d log|det M| / d phi
   // global updates: backup of stack, G, field and interaction table (allocated on first use)
   cplx *gb_u = nullptr, *gb_t = nullptr, *gb_G = nullptr;
@@ -602,7 +603,7 @@ int local_updates_dev(dqmc_handle* h, const double* delta_dev, const double* uni
     return DQMC_OK;
   }
   const int n = h->n, k = h->delay;
-  DelayedArgs d{h->Xd, h->Yd, h->dstate, k, h->prep, h->blk};
+  DelayedArgs d{h->Xd, h->Yd, h->dstate, k, h->prep, h->blk, h->pub};
   CU(cudaMemsetAsync(h->dstate, 0, 2 * sizeof(int), h->st));
   LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_prepare(a, h->prep, h->st));
   const int rounds = (h->N + k - 1) / k + 1;
@@ -629,7 +630,7 @@ void free_all(dqmc_handle* h) {
                   h->Tr, h->Dl, h->Dr, h->W1, h->W2, h->W3, h->W4, h->D1, h->d2, h->ord1, h->qr.vn1,
                   h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->qr.cand_v, h->qr.cand_q, h->delta_d, h->unif_d,
                   h->acc_d, h->det_d, h->pacc_d, h->action_d, h->nacc_d, h->Acol, h->Brow, h->bar, h->err_d,
-                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
+                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   for (auto e : h->event_pool) cudaEventDestroy(e);
@@ -736,6 +737,7 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
     A((void**)&h->dstate, 2 * sizeof(int));
     A((void**)&h->prep, (size_t)h->N * sizeof(SitePrep));
     A((void**)&h->blk, (size_t)16 * h->N * sizeof(cplx));
+    A((void**)&h->pub, (size_t)h->N * sizeof(int));
   }
   if (p->precision == DQMC_PREC_MIXED) {
     h->oz_target = p->ozaki_bits > 0 ? p->ozaki_bits : 40;

@@ -380,18 +380,58 @@ __global__ void __launch_bounds__(128) k_local_prepare(LocalUpdateArgs a, SitePr
   }
 }
 
+// adj(M)[r][c] = cofactor C[c][r] for lane 4r+c (lanes < 16), from the 2x2
+// minors of rows {0,1} and {2,3} (Laplace expansion of each 3x3 minor along
+// its single row from the other pair); m[r][c] in lane 4r+c.
+__device__ __forceinline__ cplx adjugate_entry(cplx m, int lane) {
+  // pair index of columns (a, b), a < b: 0:(0,1) 1:(0,2) 2:(0,3) 3:(1,2) 4:(1,3) 5:(2,3)
+  const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {1, 2, 3, 2, 3, 3};
+  // lanes 0-5: top minors T_ab (rows 0, 1); lanes 6-11: bottom minors B_ab (rows 2, 3)
+  const int mi = lane < 12 ? lane : 0;
+  const int pr = mi < 6 ? 0 : 2, pp = mi < 6 ? mi : mi - 6;
+  const cplx e00 = shfl_c(m, 4 * pr + pa[pp]), e01 = shfl_c(m, 4 * pr + pb[pp]);
+  const cplx e10 = shfl_c(m, 4 * (pr + 1) + pa[pp]), e11 = shfl_c(m, 4 * (pr + 1) + pb[pp]);
+  const cplx minor = csub(cmul(e00, e11), cmul(e01, e10));
+  // lane 4r+c: cofactor with row c and column r removed
+  const int r = (lane >> 2) & 3, c = lane & 3;
+  const int rr = c, cc = r;                        // removed row / column
+  const int other = rr < 2 ? 1 - rr : 5 - rr;      // remaining row of the removed row's pair
+  const int base = rr < 2 ? 6 : 0;                 // minors of the complementary pair
+  int cols[3];
+  for (int t = 0, q = 0; t < 4; ++t) if (t != cc) cols[q++] = t;
+  cplx d3 = cmake(0.0, 0.0);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const int u = a == 0 ? cols[1] : cols[0];
+    const int v = a == 2 ? cols[1] : cols[2];
+    const int pidx = u == 0 ? (v - 1) : (u == 1 ? v + 1 : 5);   // (0,1)0 (0,2)1 (0,3)2 (1,2)3 (1,3)4 (2,3)5
+    const cplx mn = shfl_c(minor, base + pidx);
+    const cplx ent = shfl_c(m, 4 * other + cols[a]);
+    const cplx t = cmul(ent, mn);
+    d3 = (a == 1) ? csub(d3, t) : cadd(d3, t);
+  }
+  if ((rr + cc) & 1) d3 = cmake(-d3.x, -d3.y);
+  return d3;
+}
+
 // Processes sites state[0] .. N-1 until k accepted updates are pending or the
 // slice ends; state[0] is left at the next site and state[1] at the number of
 // pending factors.  The flush G += X Y (a separate GEMM launch over the first
 // 4 state[1] columns) follows every round.
 //
-// CTA b owns sites j = b, b + grid, ...: on each acceptance it forms the 4
-// rows j + rN of the new X columns and the 4 columns j + cN of the new Y rows
-// (one warp per row / column) and refreshes the cached block of site j.
-__global__ void __launch_bounds__(LU_THREADS, 2) k_local_delayed(LocalUpdateArgs a, DelayedArgs d) {
+// One CTA per SM; CTA b owns sites j = b, b + grid, ...  On each acceptance
+// it forms the 4 rows j + rN of the new X columns (one warp, 8 lanes per row)
+// and the 4 columns j + cN of the new Y rows (another warp), refreshes the
+// cached diagonal block of j, and publishes the number of acceptances it has
+// folded into site j.  Deciding site i waits only for that counter of site
+// i's owner (no grid-wide barrier per acceptance).  With CACHE the owner
+// also keeps its X rows / Y columns in shared memory, so the new factor
+// entries need no global loads.
+template <bool CACHE>
+__global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs a, DelayedArgs d) {
   const ModelConst& mc = a.mc;
   const int N = mc.N, n = mc.n, L = mc.L, K4 = 4 * d.k;
-  __shared__ int s_first;
+  __shared__ int s_first, s_ok, s_acc;
   if (threadIdx.x == 0) s_first = __ldcg(&d.state[0]);
   __syncthreads();
   const int first = s_first;
@@ -401,25 +441,69 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_delayed(LocalUpdateArgs
   int p = 0;
   if (blockIdx.x == 0 && threadIdx.x == 0) d.state[1] = 0;
   if (first >= N) return;   // slice done: nothing to do in this round (uniform over the grid)
+  const int owned = (N - blockIdx.x + gridDim.x - 1) / gridDim.x;   // sites j = blockIdx.x + t grid
   extern __shared__ double4_16a smem_local[];
-  double* phis = reinterpret_cast<double*>(smem_local);                 // (3, N) field of slice l
-  cplx* Ysm = reinterpret_cast<cplx*>(phis + 3 * N + (N & 1) * 3);     // (4k x 4): Y[j, i + cN]
-  cplx* Xsm = Ysm + (size_t)K4 * 4;                                     // (4 x 4k): X[i + rN, j]
+  cplx* s_blk = reinterpret_cast<cplx*>(smem_local);                   // (owned, 16) G_cur blocks
+  cplx* s_xn = s_blk + (size_t)16 * owned;                              // (4 sites, 4 x 4) new X rows
+  cplx* s_yn = s_xn + 64;                                              // (4 sites, 4 x 4) new Y columns
+  cplx* Ysm = s_yn + 64;                                               // (4k x 4): Y[j, i + cN]
+  cplx* Xsm = Ysm + (size_t)K4 * 4;                                    // (4 x 4k): X[i + rN, j]
+  cplx* s_xrow = Xsm + (size_t)K4 * 4;                                 // CACHE: (owned, 4, 4k) X[j', j + rN]
+  cplx* s_ycol = s_xrow + (CACHE ? (size_t)owned * 4 * K4 : 0);        // CACHE: (owned, 4, 4k) Y[j', j + cN]
+  double* phis = reinterpret_cast<double*>(s_ycol + (CACHE ? (size_t)owned * 4 * K4 : 0));   // (3, N)
   __shared__ cplx s_delta[16];      // Delta_i
   __shared__ cplx s_adj[2][16];     // adj(M)[r][c] (double-buffered by site parity)
-  __shared__ cplx s_det[2], s_inv[2];
+  __shared__ cplx s_det[2];
   __shared__ double s_expds[2];
-  __shared__ cplx s_xn[4][4], s_yn[4][4];   // new X rows / Y columns of an owned site
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int l = a.slice0;
   for (int k = threadIdx.x; k < 3 * N; k += blockDim.x) phis[k] = a.phi[(size_t)3 * N * l + k];
-  __syncthreads();
+  for (int e = threadIdx.x; e < 16 * owned; e += blockDim.x) {
+    const int j = blockIdx.x + (e >> 4) * gridDim.x, r = (e >> 2) & 3, c = e & 3;
+    s_blk[e] = ldcg_c(&a.G[(size_t)(j + c * N) * n + j + r * N]);
+  }
+  // publication counters of the owned sites start the round at 0
+  for (int t = threadIdx.x; t < owned; t += blockDim.x) d.pub[blockIdx.x + t * gridDim.x] = 0;
+  if (!grid_barrier(a.bar, a.err)) return;
+
+  // phase-1 role of this warp in the first pass of owned sites
+  const int sub = lane >> 3, qg = (lane >> 1) & 3, h = lane & 1;
+  const bool isX = (wid & 1) == 0;
 
   for (int i = first; i < N; ++i) {
     const int J = 4 * p;   // pending columns of X / rows of Y
     const int slot = i & 1;
     const SitePrep* sp = d.prep + i;
-    if (wid == 0 || wid == 2) {
+    // ---- wait until the owner of site i has folded in all p acceptances ----
+    if (p > 0) {
+      if (threadIdx.x == 0) {
+        volatile int* f = d.pub + i;
+        int ok = 1;
+        long long spins = 0;
+        while (*f < p) {
+          if ((++spins & 1023) == 0) {
+            if (spins > (1ll << 24)) { atomicOr(a.err, 2); ok = 0; break; }
+            if (*(volatile int*)a.err & 2) { ok = 0; break; }
+          }
+        }
+        __threadfence();
+        s_ok = ok;
+      }
+      __syncthreads();
+      if (!s_ok) return;
+    }
+    // ---- G entries of the first pass's phase 1 (independent of the decision) ----
+    cplx gq_pref = cmake(0.0, 0.0);
+    if ((wid >> 1) < owned) {
+      const int rc = blockIdx.x + (wid >> 1) * gridDim.x + sub * N;
+      if (isX) {
+        gq_pref = ldcg_c(&a.G[(size_t)(i + qg * N) * n + rc]);
+        if (rc == i + qg * N) gq_pref.x -= 1.0;
+      } else {
+        gq_pref = ldcg_c(&a.G[(size_t)rc * n + i + qg * N]);
+      }
+    }
+    if (wid == 4 || wid == 6) {
       // ---- M = I + Delta (I - G_cur_ii), lane 4r+c holds M[r][c] (src/local_updates.jl:49-55) ----
       const int r = (lane >> 2) & 3, c = lane & 3;
       cplx g = cmake(0.0, 0.0), drow[4];
@@ -435,7 +519,7 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_delayed(LocalUpdateArgs
       cplx m = cmake(r == c ? 1.0 : 0.0, 0.0);
 #pragma unroll
       for (int k = 0; k < 4; ++k) m = cfma(drow[k], shfl_c(mt, 4 * k + c), m);
-      if (wid == 0) {
+      if (wid == 4) {
         // det M by the permutation expansion (24 lanes); lane 0's sum is the
         // one used everywhere, so every CTA decides bit for bit alike
         const int jp = lane < 24 ? lane : 0;
@@ -447,28 +531,12 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_delayed(LocalUpdateArgs
         cplx det = term;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) det = cadd(det, shfl_c(det, lane ^ o));
-        det = shfl_c(det, 0);
-        if (lane == 0) {
-          s_det[slot] = det;
-          s_inv[slot] = cdiv(cmake(1.0, 0.0), det);
-        }
+        if (lane == 0) s_det[slot] = det;
       } else {
-        // adj(M)[r][c] = cofactor C[c][r]
-        int rows[3], cols[3];
-        for (int t = 0, q = 0; t < 4; ++t) if (t != c) rows[q++] = t;
-        for (int t = 0, q = 0; t < 4; ++t) if (t != r) cols[q++] = t;
-        cplx e[3][3];
-#pragma unroll
-        for (int u3 = 0; u3 < 3; ++u3)
-#pragma unroll
-          for (int v3 = 0; v3 < 3; ++v3) e[u3][v3] = shfl_c(m, (4 * rows[u3] + cols[v3]) & 31);
-        cplx d3 = csub(cmul(e[0][0], csub(cmul(e[1][1], e[2][2]), cmul(e[1][2], e[2][1]))),
-                       cmul(e[0][1], csub(cmul(e[1][0], e[2][2]), cmul(e[1][2], e[2][0]))));
-        d3 = cadd(d3, cmul(e[0][2], csub(cmul(e[1][0], e[2][1]), cmul(e[1][1], e[2][0]))));
-        if ((r + c) & 1) d3 = cmake(-d3.x, -d3.y);
-        if (lane < 16) s_adj[slot][lane] = d3;
+        const cplx adj = adjugate_entry(m, lane);
+        if (lane < 16) s_adj[slot][lane] = adj;
       }
-    } else if (wid == 1) {
+    } else if (wid == 5) {
       // ---- boson action difference: prepared part + space-neighbour coupling ----
       if (lane == 0) {
         const int y = i % L, x = i / L;
@@ -485,25 +553,41 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_delayed(LocalUpdateArgs
         dS += __ldcg(&sp->dsB);
         s_expds[slot] = exp(-dS);
       }
-    } else if (J > 0 || wid == 3) {
-      // ---- stage Delta_i and the pending factor entries touching site i ----
-      const int t0 = threadIdx.x - 3 * 32, nt = blockDim.x - 3 * 32;
-      if (t0 < 16) s_delta[t0] = ldcg_c(&sp->delta[t0]);
-      for (int t = t0; t < 4 * J; t += nt) {
-        const int j = t >> 2, c = t & 3;
-        Ysm[4 * j + c] = ldcg_c(&d.Y[(size_t)j * n + i + c * N]);
-        Xsm[(size_t)c * K4 + j] = ldcg_c(&d.X[(size_t)j * n + i + c * N]);
+    } else if (wid == 7 && lane < 16) {
+      s_delta[lane] = ldcg_c(&sp->delta[lane]);
+    }
+    if (wid < 4 || wid == 7) {
+      // ---- stage the pending factor entries touching site i (160 threads, loads issued together) ----
+      constexpr int kStage = 160;
+      const int st = wid < 4 ? threadIdx.x : 128 + lane;
+      for (int t = st; t < 4 * J; t += 2 * kStage) {
+        const int t2 = t + kStage;
+        const int j1 = t >> 2, c1 = t & 3, j2 = t2 >> 2, c2 = t2 & 3;
+        const cplx y1 = ldcg_c(&d.Y[(size_t)j1 * n + i + c1 * N]);
+        const cplx x1 = ldcg_c(&d.X[(size_t)j1 * n + i + c1 * N]);
+        cplx y2 = cmake(0.0, 0.0), x2 = cmake(0.0, 0.0);
+        if (t2 < 4 * J) {
+          y2 = ldcg_c(&d.Y[(size_t)j2 * n + i + c2 * N]);
+          x2 = ldcg_c(&d.X[(size_t)j2 * n + i + c2 * N]);
+        }
+        Ysm[4 * j1 + c1] = y1;
+        Xsm[(size_t)c1 * K4 + j1] = x1;
+        if (t2 < 4 * J) {
+          Ysm[4 * j2 + c2] = y2;
+          Xsm[(size_t)c2 * K4 + j2] = x2;
+        }
       }
     }
     __syncthreads();
-    // ---- Metropolis decision, identical in every thread of every CTA ----
-    const cplx det = s_det[slot];
-    const double exp_dS = s_expds[slot];
-    const double pacc = exp_dS * det.x;
-    const double u = __ldg(&a.unif[i]);
-    const bool bad = !isfinite(det.x) || !isfinite(det.y) || (det.x == 0.0 && det.y == 0.0);
-    const bool acc = !bad && (pacc > 1.0 || u < pacc);
+    // ---- Metropolis decision (thread 0; the same in every CTA) ----
     if (threadIdx.x == 0) {
+      const cplx det = s_det[slot];
+      const double exp_dS = s_expds[slot];
+      const double pacc = exp_dS * det.x;
+      const double u = __ldg(&a.unif[i]);
+      const bool bad = !isfinite(det.x) || !isfinite(det.y) || (det.x == 0.0 && det.y == 0.0);
+      const bool acc = !bad && (pacc > 1.0 || u < pacc);
+      s_acc = acc;
       if (acc)
         for (int q = 0; q < 3; ++q) phis[3 * i + q] += a.delta[3 * i + q];
       if (blockIdx.x == 0) {
@@ -520,68 +604,98 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_delayed(LocalUpdateArgs
         }
       }
     }
-    // decision slots are double-buffered: a rejected site needs no second barrier
-    if (!acc) continue;
-    // ---- new factor columns: X[:, J+k] = (G_cur[:, i + qN] - I[:, i + qN]) M^-1,
-    //      Y[J+k, :] = Delta G_cur[i + qN, :]; one warp per row / column ----
-    const cplx inv = s_inv[slot];
-    for (int j = blockIdx.x; j < N; j += gridDim.x) {
-      const bool isX = wid < 4;
-      const int q0 = wid & 3;
-      const int rc = j + q0 * N;              // X: row rc; Y: column rc
-      const int qg = lane >> 3, g8 = lane & 7;   // 8 lanes per term group of G_cur[., i + qg N]
-      cplx part = cmake(0.0, 0.0);
-      if (isX) {
-        for (int jj = g8; jj < J; jj += 8) part = cfma(ldcg_c(&d.X[(size_t)jj * n + rc]), Ysm[4 * jj + qg], part);
-      } else {
-        for (int jj = g8; jj < J; jj += 8) part = cfma(Xsm[(size_t)qg * K4 + jj], ldcg_c(&d.Y[(size_t)jj * n + rc]), part);
-      }
-      part = cadd(part, shfl_c(part, lane ^ 1));
-      part = cadd(part, shfl_c(part, lane ^ 2));
-      part = cadd(part, shfl_c(part, lane ^ 4));
-      cplx gq;
-      if (isX) {
-        gq = ldcg_c(&a.G[(size_t)(i + qg * N) * n + rc]);
-        if (rc == i + qg * N) gq.x -= 1.0;
-      } else {
-        gq = ldcg_c(&a.G[(size_t)rc * n + i + qg * N]);
-      }
-      const cplx gcur = cadd(gq, part);
-      // output k over 4 lanes (q = 0..3) each
-      const int o = lane & 15, ko = o >> 2, qq = o & 3;
-      const cplx gv = shfl_c(gcur, 8 * qq);
-      cplx prod = cmul(gv, isX ? s_adj[slot][4 * qq + ko] : s_delta[4 * ko + qq]);
-      prod = cadd(prod, shfl_c(prod, lane ^ 1));
-      prod = cadd(prod, shfl_c(prod, lane ^ 2));
-      if (lane < 16 && qq == 0) {
+    __syncthreads();
+    // decision slots are double-buffered: a rejected site needs no further barrier
+    if (!s_acc) continue;
+    // ---- new factor columns: X[:, J+k] = (G_cur[:, i + qN] - I[:, i + qN]) adj(M),
+    //      Y[J+k, :] = Delta G_cur[i + qN, :] / det  (X Y = (G_cur - I) M^-1 Delta G_cur) ----
+    // owned sites in passes of 4: site t of a pass -> warps 2t (X rows) and 2t+1 (Y columns)
+    for (int t0 = 0; t0 < owned; t0 += 4) {
+      const int ts = t0 + (wid >> 1);
+      if (ts < owned) {
+        const int j = blockIdx.x + ts * gridDim.x;
+        const int rc = j + sub * N;   // X: row rc; Y: column rc
+        cplx gq = gq_pref;
+        if (t0 > 0) {
+          if (isX) {
+            gq = ldcg_c(&a.G[(size_t)(i + qg * N) * n + rc]);
+            if (rc == i + qg * N) gq.x -= 1.0;
+          } else {
+            gq = ldcg_c(&a.G[(size_t)rc * n + i + qg * N]);
+          }
+        }
+        cplx inv = cmake(0.0, 0.0);
+        if (!isX) {
+          const cplx det = s_det[slot];
+          const double rd = 1.0 / (det.x * det.x + det.y * det.y);
+          inv = cmake(det.x * rd, -det.y * rd);
+        }
+        cplx part = cmake(0.0, 0.0);
+        const cplx* own = CACHE ? (isX ? s_xrow : s_ycol) + (size_t)(4 * ts + sub) * K4 : nullptr;
         if (isX) {
-          const cplx xv = cmul(prod, inv);
-          d.X[(size_t)(J + ko) * n + rc] = xv;
-          s_xn[q0][ko] = xv;
+          if (CACHE) {
+            for (int jj = h; jj < J; jj += 2) part = cfma(own[jj], Ysm[4 * jj + qg], part);
+          } else {
+            for (int jj = h; jj < J; jj += 2) part = cfma(ldcg_c(&d.X[(size_t)jj * n + rc]), Ysm[4 * jj + qg], part);
+          }
         } else {
-          d.Y[(size_t)(J + ko) * n + rc] = prod;
-          s_yn[ko][q0] = prod;
+          if (CACHE) {
+            for (int jj = h; jj < J; jj += 2) part = cfma(Xsm[(size_t)qg * K4 + jj], own[jj], part);
+          } else {
+            for (int jj = h; jj < J; jj += 2) part = cfma(Xsm[(size_t)qg * K4 + jj], ldcg_c(&d.Y[(size_t)jj * n + rc]), part);
+          }
+        }
+        part = cadd(part, shfl_c(part, lane ^ 1));
+        const cplx gcur = cadd(gq, part);   // G_cur[rc, i + qN] (- delta) or G_cur[i + qN, rc]
+        // output k = qg of this lane over q' = 2h, 2h + 1, then the pair sum
+        const int ko = qg;
+        const cplx g0 = shfl_c(gcur, 8 * sub + 4 * h), g1 = shfl_c(gcur, 8 * sub + 4 * h + 2);
+        cplx prod;
+        if (isX) prod = cfma(g1, s_adj[slot][4 * (2 * h + 1) + ko], cmul(g0, s_adj[slot][4 * (2 * h) + ko]));
+        else prod = cfma(s_delta[4 * ko + 2 * h + 1], g1, cmul(s_delta[4 * ko + 2 * h], g0));
+        prod = cadd(prod, shfl_c(prod, lane ^ 1));
+        if (!isX) prod = cmul(prod, inv);
+        if (h == 0) {
+          const int ls = ts - t0;
+          if (isX) {
+            d.X[(size_t)(J + ko) * n + rc] = prod;
+            s_xn[16 * ls + 4 * sub + ko] = prod;        // X_new[j + sub N, k]
+          } else {
+            d.Y[(size_t)(J + ko) * n + rc] = prod;
+            s_yn[16 * ls + 4 * ko + sub] = prod;        // Y_new[k, j + sub N]
+          }
+          if (CACHE) const_cast<cplx*>(own)[J + ko] = prod;
         }
       }
-      // ---- refresh the cached block of site j (needed by later sites only) ----
-      if (j > i) {
-        __syncthreads();
-        if (wid == 0 && lane < 16) {
+      __syncthreads();
+      // ---- refresh the cached blocks of the pass's sites (needed by later sites only) ----
+      if (!(wid & 1) && lane < 16) {
+        const int ls = wid >> 1, tsr = t0 + ls;
+        const int j = blockIdx.x + tsr * gridDim.x;
+        if (tsr < owned && j > i) {
           const int r = lane >> 2, c = lane & 3;
-          cplx b = p == 0 ? ldcg_c(&a.G[(size_t)(j + c * N) * n + j + r * N]) : ldcg_c(&d.blk[(size_t)16 * j + lane]);
+          cplx b = s_blk[16 * tsr + lane];
 #pragma unroll
-          for (int k = 0; k < 4; ++k) b = cfma(s_xn[r][k], s_yn[k][c], b);
+          for (int k = 0; k < 4; ++k) b = cfma(s_xn[16 * ls + 4 * r + k], s_yn[16 * ls + 4 * k + c], b);
+          s_blk[16 * tsr + lane] = b;
           d.blk[(size_t)16 * j + lane] = b;
         }
       }
-      __syncthreads();   // s_xn / s_yn reused by the next owned site
+      __threadfence();   // this thread's factor and block stores before the publication
+      __syncthreads();   // s_xn / s_yn reused by the next pass
     }
     ++p;
     if (p == d.k || i == N - 1) {
       if (blockIdx.x == 0 && threadIdx.x == 0) { d.state[0] = i + 1; d.state[1] = p; }
       return;   // the flush follows as its own launch
     }
-    if (!grid_barrier(a.bar, a.err)) return;
+    // ---- publish: the owned later sites now include p acceptances ----
+    if (threadIdx.x == 0) {
+      for (int t = 0; t < owned; ++t) {
+        const int j = blockIdx.x + t * gridDim.x;
+        if (j > i) *(volatile int*)(d.pub + j) = p;
+      }
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) { d.state[0] = N; d.state[1] = p; }
 }
@@ -597,29 +711,40 @@ cudaError_t launch_local_prepare(const LocalUpdateArgs& a, SitePrep* prep, cudaS
   return cudaGetLastError();
 }
 
+static size_t local_delayed_smem(int N, int k, int grid, bool cache) {
+  const size_t owned = (size_t)(N + grid - 1) / grid;
+  size_t c = 16 * owned + 128 + (size_t)2 * 16 * k;
+  if (cache) c += 2 * owned * 4 * 4 * (size_t)k;
+  return c * sizeof(cplx) + (size_t)3 * N * sizeof(double);
+}
+
 cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d, int sm_count, cudaStream_t st,
                                  int max_grid) {
+  constexpr size_t kMaxSmem = 200 * 1024;
   const int N = a.mc.N;
-  const size_t smem = (size_t)(3 * N + (N & 1) * 3) * sizeof(double) + (size_t)2 * 4 * d.k * 4 * sizeof(cplx);
+  int grid = sm_count;    // one CTA per SM
+  if (grid > N) grid = N;
+  if (max_grid > 0 && grid > max_grid) grid = max_grid;
+  const bool cache = local_delayed_smem(N, d.k, grid, true) <= kMaxSmem;
+  const size_t smem = local_delayed_smem(N, d.k, grid, cache);
+  if (smem > kMaxSmem) return cudaErrorInvalidValue;
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_local_delayed, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(k_local_delayed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_local_delayed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  if (smem > 100 * 1024) return cudaErrorInvalidValue;
+  const void* fn = cache ? (const void*)k_local_delayed<true> : (const void*)k_local_delayed<false>;
   int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local_delayed, LU_THREADS, smem);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, LU_THREADS, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  if (per_sm > 2) per_sm = 2;
-  int grid = sm_count * per_sm;
-  if (grid > N) grid = N;   // one CTA per site owner at most
-  if (max_grid > 0 && grid > max_grid) grid = max_grid;
   LocalUpdateArgs ca = a;
   DelayedArgs cd = d;
   void* args[] = {&ca, &cd};
-  return cudaLaunchCooperativeKernel((void*)k_local_delayed, dim3(grid), dim3(LU_THREADS), args, smem, st);
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(LU_THREADS), args, smem, st);
 }
 
 cudaError_t launch_local_updates(const LocalUpdateArgs& a, int sm_count, cudaStream_t st, int max_grid) {
