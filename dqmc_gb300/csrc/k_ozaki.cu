@@ -26,6 +26,7 @@
 // cp.async double buffering.
 #include <cuda_bf16.h>
 #include <cmath>
+#include <type_traits>
 #include "common.cuh"
 #include "kernels.h"
 
@@ -188,9 +189,11 @@ struct OzArgs {
   const double* rs;          // optional extra row scaling
   const double* cs;          // optional extra column scaling
   const int* active;         // optional: nothing to do when *active == 0
+  int int_combine;           // group sums combined exactly in 64-bit integers
 };
 
 // One CTA: 64 x 64 output tile; 8 warps in a 2 x 4 grid of 32 x 16 warp tiles.
+template <bool INT>
 __global__ void __launch_bounds__(OZ_THREADS) k_oz_gemm(OzArgs a) {
   if (a.active && *a.active == 0) return;
   __shared__ __align__(16) __nv_bfloat16 sA[2][OZ_BM * OZ_LDS];
@@ -202,14 +205,16 @@ __global__ void __launch_bounds__(OZ_THREADS) k_oz_gemm(OzArgs a) {
   const size_t Kp = a.Kp;
   const size_t sliceA = (size_t)a.m * Kp, sliceB = (size_t)a.n * Kp;
 
-  // FP64 accumulators: 2 (m16) x 2 (n8) mma tiles x 4 values, re and im
-  double accr[2][2][4], acci[2][2][4];
+  // accumulators over the groups: 2 (m16) x 2 (n8) mma tiles x 4 values, re
+  // and im; exact 64-bit integers (Horner in 2^bits) or FP64 with weights
+  typedef typename std::conditional<INT, long long, double>::type acc_t;
+  acc_t accr[2][2][4], acci[2][2][4];
 #pragma unroll
   for (int x = 0; x < 2; ++x)
 #pragma unroll
     for (int y = 0; y < 2; ++y)
 #pragma unroll
-      for (int z = 0; z < 4; ++z) { accr[x][y][z] = 0.0; acci[x][y][z] = 0.0; }
+      for (int z = 0; z < 4; ++z) { accr[x][y][z] = 0; acci[x][y][z] = 0; }
 
   // staging of one K step of pair (p, q) into buffer `buf`
   auto stage = [&](int buf, int p, int q, int k0) {
@@ -283,17 +288,34 @@ __global__ void __launch_bounds__(OZ_THREADS) k_oz_gemm(OzArgs a) {
       }
       __syncthreads();   // buffers free before the next pair stages into them
     }
-    const double wgt = ldexp(1.0, -a.bits * t);
+    if constexpr (INT) {
+      // every group sum is an integer below 2^24 (exact in FP32): no FP64 work
+      const long long step = 1ll << a.bits;
 #pragma unroll
-    for (int x = 0; x < 2; ++x)
+      for (int x = 0; x < 2; ++x)
 #pragma unroll
-      for (int y = 0; y < 2; ++y)
+        for (int y = 0; y < 2; ++y)
 #pragma unroll
-        for (int z = 0; z < 4; ++z) {
-          accr[x][y][z] = fma(wgt, (double)fr[x][y][z], accr[x][y][z]);
-          acci[x][y][z] = fma(wgt, (double)fi[x][y][z], acci[x][y][z]);
-        }
+          for (int z = 0; z < 4; ++z) {
+            accr[x][y][z] = accr[x][y][z] * step + (long long)__float2int_rn(fr[x][y][z]);
+            acci[x][y][z] = acci[x][y][z] * step + (long long)__float2int_rn(fi[x][y][z]);
+          }
+    } else {
+      const double wgt = ldexp(1.0, -a.bits * t);
+#pragma unroll
+      for (int x = 0; x < 2; ++x)
+#pragma unroll
+        for (int y = 0; y < 2; ++y)
+#pragma unroll
+          for (int z = 0; z < 4; ++z) {
+            accr[x][y][z] = fma(wgt, (double)fr[x][y][z], accr[x][y][z]);
+            acci[x][y][z] = fma(wgt, (double)fi[x][y][z], acci[x][y][z]);
+          }
+    }
   }
+  // integer form: value = acc * 2^{-bits (S + 1)}
+  const double wint = INT ? ldexp(1.0, -a.bits * (a.S + 1)) : 1.0;
+  const bool plain = a.alpha.x == 1.0 && a.alpha.y == 0.0 && a.beta.y == 0.0 && (a.beta.x == 0.0 || a.beta.x == 1.0);
   // epilogue: mma C fragment layout (m16n8): value z of lane -> row (lane/4) + 8*(z/2), col 2*(lane%4) + (z%2)
 #pragma unroll
   for (int x = 0; x < 2; ++x)
@@ -304,13 +326,26 @@ __global__ void __launch_bounds__(OZ_THREADS) k_oz_gemm(OzArgs a) {
         const int row = i0 + 32 * wm + 16 * x + (lane >> 2) + 8 * (z >> 1);
         const int col = j0 + 16 * wn + 8 * y + 2 * (lane & 3) + (z & 1);
         if (row < a.m && col < a.n) {
-          double f = a.sA[row] * a.sB[col];
+          double f = a.sA[row] * a.sB[col] * wint;
           if (a.rs) f *= a.rs[row];
           if (a.cs) f *= a.cs[col];
-          cplx v = cmake(accr[x][y][z] * f, acci[x][y][z] * f);
-          v = cmul(a.alpha, v);
+          double vr, vi;
+          if constexpr (INT) {
+            vr = __ll2double_rn(accr[x][y][z]);
+            vi = __ll2double_rn(acci[x][y][z]);
+          } else {
+            vr = accr[x][y][z];
+            vi = acci[x][y][z];
+          }
+          cplx v = cmake(vr * f, vi * f);
           cplx* cp = &a.C[(size_t)col * a.ldc + row];
-          if (a.beta.x != 0.0 || a.beta.y != 0.0) v = cfma(a.beta, *cp, v);
+          if (plain) {
+            // alpha = 1, beta in {0, 1}: one multiply and at most one add per value
+            if (a.beta.x != 0.0) v = cadd(*cp, v);
+          } else {
+            v = cmul(a.alpha, v);
+            if (a.beta.x != 0.0 || a.beta.y != 0.0) v = cfma(a.beta, *cp, v);
+          }
           *cp = v;
         }
       }
@@ -366,7 +401,10 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
   a.As = As; a.Bre = Bre; a.Bim = Bim; a.sA = sA; a.sB = sB;
   a.m = m; a.n = nn; a.Kp = (int)Kp; a.S = S; a.bits = bits;
   a.alpha = alpha; a.beta = beta; a.C = C; a.ldc = ldc; a.rs = rowscale; a.cs = colscale; a.active = active;
+  // |sum_t g_t 2^{bits (S+1-t)}| < 2^{24 + bits (S-1) + 1}: exact in int64 below 2^63
+  a.int_combine = 24 + bits * (S - 1) <= 61 ? 1 : 0;
   dim3 grid((nn + OZ_BN - 1) / OZ_BN, (m + OZ_BM - 1) / OZ_BM);
-  k_oz_gemm<<<grid, OZ_THREADS, 0, st>>>(a);
+  if (a.int_combine) k_oz_gemm<true><<<grid, OZ_THREADS, 0, st>>>(a);
+  else k_oz_gemm<false><<<grid, OZ_THREADS, 0, st>>>(a);
   return cudaGetLastError();
 }
