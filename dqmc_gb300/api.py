@@ -37,7 +37,8 @@ class CParams(ctypes.Structure):
                 ("r", ctypes.c_double), ("c", ctypes.c_double), ("u", ctypes.c_double),
                 ("mu1", ctypes.c_double), ("mu2", ctypes.c_double), ("hoppings", ctypes.c_double * 4),
                 ("all_checks", ctypes.c_int32), ("precision", ctypes.c_int32), ("device", ctypes.c_int32),
-                ("ozaki_bits", ctypes.c_int32), ("delay", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("ozaki_bits", ctypes.c_int32), ("delay", ctypes.c_int32), ("greens_method", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
 
 
 class CStats(ctypes.Structure):
@@ -141,6 +142,7 @@ class ModelParams:
     precision: str = "fp64"        # "fp64" or "mixed"
     ozaki_bits: int = 0            # mantissa bits per GEMM operand in the mixed form (0 = default 40)
     delay: int = 0                 # delayed-update depth (0/1 = immediate rank-4)
+    greens_method: str = "scales"  # calculate_greens: "scales" (D-scale separation + LU) or "two_qr" (reference)
 
     @property
     def N(self):
@@ -162,6 +164,9 @@ class ModelParams:
         p.device = self.device
         p.ozaki_bits = self.ozaki_bits
         p.delay = self.delay
+        if self.greens_method not in ("scales", "two_qr"):
+            raise ValueError("greens_method must be 'scales' or 'two_qr'")
+        p.greens_method = 0 if self.greens_method == "scales" else 1
         return p
 
 

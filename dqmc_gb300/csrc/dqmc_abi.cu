@@ -71,6 +71,9 @@ struct dqmc_handle {
   SitePrep* prep = nullptr;   // (N) per-site constants of the slice being updated
   cplx* blk = nullptr;        // (N, 16) cached diagonal blocks of G_cur
   int* pub = nullptr;         // (N) per-site publication counters of the delayed rounds
+  int greens_method = DQMC_GREENS_SCALES;
+  LUWork lu{};                // LU of the D-scale separated calculate_greens
+  double* lu_scales = nullptr;   // (4n) 1/max(Dl,1), min(Dl,1), 1/max(Dr,1), min(Dr,1)
   double* force_d = nullptr;   // (3, N, M) d log|det M| / d phi
   // global updates: backup of stack, G, field and interaction table (allocated on first use)
   cplx *gb_u = nullptr, *gb_t = nullptr, *gb_G = nullptr;
@@ -283,7 +286,7 @@ int apply_q(dqmc_handle* h, cplx* X) {
   return DQMC_OK;
 }
 int trsm_left(dqmc_handle* h, const cplx* T, const int* order, cplx* Y) {
-  LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_upper(T, order, Y, h->n, h->n, h->st));
+  LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_upper(T, order, nullptr, Y, h->n, h->n, h->st));
   return DQMC_OK;
 }
 int trsm_right(dqmc_handle* h, const cplx* T, const int* order, cplx* Y) {
@@ -336,7 +339,7 @@ int add_slice_sequence_right(dqmc_handle* h, int idx) {
 //     = Ur P1 That1^-1 P2 That2^-1 diag(1/d2) (U Q2)^dag.
 // log|det G| = -sum log d2 (|det| of the unitary and unit-triangular
 // factors is 1).
-int calculate_greens_into(dqmc_handle* h, cplx* out) {
+int calculate_greens_two_qr(dqmc_handle* h, cplx* out) {
   const int n = h->n;
   // 1. X = Dl (Tl Tr^dag) Dr
   CHK(gemm(h, 'N', 'C', h->Tl, h->Tr, h->W1, h->Dl, h->Dr));
@@ -365,6 +368,43 @@ int calculate_greens_into(dqmc_handle* h, cplx* out) {
   CHK(gemm(h, 'N', 'N', h->Ur, h->W1, out));
   LAUNCH(DQMC_K_MISC, 0.0, 8.0 * n, launch_sum_log(h->d2, n, h->scal_d, h->st));
   return DQMC_OK;
+}
+
+// D-scale separated calculate_greens: with D = Dmax Dmin, Dmax = max(D, 1),
+//   I + Ul Dl Tl Tr^dag Dr Ur^dag = Ul Dlmax M Drmax Ur^dag,
+//   M = Dlmax^-1 (Ul^dag Ur) Drmax^-1 + Dlmin (Tl Tr^dag) Drmin,
+// whose entries carry no large scales; M = P^T L U by one LU with partial
+// pivoting, so G = (Ur Drmax^-1) U^-1 L^-1 P (Dlmax^-1 Ul^dag) and
+// log|det G| = -(sum log|U_ii| + sum log Dlmax + sum log Drmax).
+int calculate_greens_scales(dqmc_handle* h, cplx* out) {
+  const int n = h->n;
+  double* s = h->lu_scales;   // [1/Dlmax, Dlmin, 1/Drmax, Drmin]
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n, launch_split_scales(h->Dl, h->Dr, n, s, h->st));
+  // M = diag(1/Dlmax) Ul^dag Ur diag(1/Drmax) + diag(Dlmin) Tl Tr^dag diag(Drmin)
+  CHK(zgemm_general(h, n, n, n, 'C', 'N', cmake(1, 0), h->Ul, n, h->Ur, n, cmake(0, 0), h->W1, n, s, s + 2 * n, true));
+  CHK(zgemm_general(h, n, n, n, 'N', 'C', cmake(1, 0), h->Tl, n, h->Tr, n, cmake(1, 0), h->W1, n, s + n, s + 3 * n,
+                    true));
+  // P M = L U (U in W1's strict upper part and lu.udiag, L in W2)
+  LAUNCH(DQMC_K_QRP, 8.0 / 3.0 * n3(h), 32.0 * n2(h), launch_lup(h->W1, h->W2, n, h->lu, h->sm_count, h->st,
+                                                                 h->coop_cap));
+  // right-hand side P diag(1/Dlmax) Ul^dag
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_conj_transpose(h->Ul, h->W4, n, h->st));
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_scale(h->W4, n, n, s, false, nullptr, false, h->st));
+  CHK(permute(h, h->W4, h->W3, h->lu.perm, true, false));
+  // U^-1 L^-1 (.), then diag(1/Drmax)
+  LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_lower_unit(h->W2, h->W3, n, n, h->st));
+  LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_upper(h->W1, nullptr, h->lu.rdiag, h->W3, n, n,
+                                                                         h->st));
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_scale(h->W3, n, n, s + 2 * n, false, nullptr, false, h->st));
+  // G = Ur (.)
+  CHK(gemm(h, 'N', 'N', h->Ur, h->W3, out));
+  // scal_d[0] = -log|det G|, the convention of the two-QR form (sum log d2)
+  LAUNCH(DQMC_K_MISC, 0.0, 24.0 * n, launch_lu_logdet(h->lu.udiag, h->Dl, h->Dr, n, h->scal_d, h->st));
+  return DQMC_OK;
+}
+
+int calculate_greens_into(dqmc_handle* h, cplx* out) {
+  return h->greens_method == DQMC_GREENS_TWO_QR ? calculate_greens_two_qr(h, out) : calculate_greens_scales(h, out);
 }
 
 int calculate_greens(dqmc_handle* h) { return calculate_greens_into(h, h->G); }
@@ -630,7 +670,7 @@ void free_all(dqmc_handle* h) {
                   h->Tr, h->Dl, h->Dr, h->W1, h->W2, h->W3, h->W4, h->D1, h->d2, h->ord1, h->qr.vn1,
                   h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->qr.cand_v, h->qr.cand_q, h->delta_d, h->unif_d,
                   h->acc_d, h->det_d, h->pacc_d, h->action_d, h->nacc_d, h->Acol, h->Brow, h->bar, h->err_d,
-                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
+                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lu.pivrow, h->lu_scales, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   for (auto e : h->event_pool) cudaEventDestroy(e);
@@ -730,6 +770,12 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
   A((void**)&h->Acol, 4 * n * sizeof(cplx)); A((void**)&h->Brow, 4 * n * sizeof(cplx));
   A((void**)&h->bar, sizeof(GridBarrier)); A((void**)&h->err_d, sizeof(int));
   A((void**)&h->scal_d, 8 * sizeof(double));
+  h->greens_method = p->greens_method == DQMC_GREENS_TWO_QR ? DQMC_GREENS_TWO_QR : DQMC_GREENS_SCALES;
+  A((void**)&h->lu.perm, n * sizeof(int)); A((void**)&h->lu.udiag, n * sizeof(cplx));
+  A((void**)&h->lu.rdiag, n * sizeof(cplx)); A((void**)&h->lu.pivrow, 2 * sizeof(int));
+  A((void**)&h->lu_scales, 4 * n * sizeof(double));
+  h->lu.bar = h->qr.bar;
+  h->lu.err = h->err_d;
   h->delay = p->delay > 1 ? p->delay : 1;
   if (h->delay > 1) {
     A((void**)&h->Xd, (size_t)4 * h->delay * n * sizeof(cplx));

@@ -378,6 +378,157 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
     for (int q = threadIdx.x; q < n; q += blockDim.x) w.order[q] = order[q];
 }
 
+// ---------------------------------------------------------------------------
+// LU with partial pivoting (cooperative, one grid barrier per column step)
+// ---------------------------------------------------------------------------
+// P A = L U as LAPACK zgetf2 (pivot: first row of maximal |Re| + |Im|, as
+// izamax), rows exchanged physically in the trailing columns.  Column k of
+// A is read, never written, in step k: the multipliers go to Lb (strictly
+// lower part; earlier columns receive the same row exchanges) and the
+// diagonal of U to udiag, so the CTAs need no ordering among themselves
+// inside a step.  The owner of column k+1 publishes the next pivot row.
+__device__ __forceinline__ bool piv_better(double v, int r, double bv, int br) {
+  const long long a = __double_as_longlong(v), b = __double_as_longlong(bv);   // v >= 0
+  return a > b || (a == b && r < br);
+}
+
+__device__ __forceinline__ void warp_argmax(double& best, int& row) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int orow = __shfl_xor_sync(0xffffffffu, row, o);
+    if (piv_better(ob, orow, best, row)) { best = ob; row = orow; }
+  }
+}
+
+__global__ void __launch_bounds__(QR_THREADS) k_lup(cplx* __restrict__ A, cplx* __restrict__ Lb, int n, LUWork w) {
+  extern __shared__ double smem_lu[];
+  cplx* v = reinterpret_cast<cplx*>(smem_lu);   // (n) column k after the row exchange (rows > k)
+  int* perm = reinterpret_cast<int*>(v + n);    // (n) position -> original row
+  __shared__ cplx s_rinv;
+  __shared__ int s_piv;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int warps = QR_THREADS / 32;
+  const int scal_warp = warps - 1;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) perm[q] = q;
+  if (blockIdx.x == 0 && wid == 0) {
+    double best = 0.0;
+    int row = n;
+    for (int r = lane; r < n; r += 32) {
+      const cplx x = A[r];
+      const double a = fabs(x.x) + fabs(x.y);
+      if (piv_better(a, r, best, row)) { best = a; row = r; }
+    }
+    warp_argmax(best, row);
+    if (lane == 0) w.pivrow[0] = row < n ? row : 0;
+  }
+  if (!grid_barrier(w.bar, w.err)) return;
+
+  const int chunk = (n + gridDim.x - 1) / gridDim.x;   // rows of Lb written by this CTA
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) s_piv = __ldcg(&w.pivrow[k & 1]);
+    __syncthreads();
+    const int p = s_piv;
+    const cplx* colk = A + (size_t)k * n;
+    const cplx piv = ldcg_c(&colk[p]);
+    for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) v[r] = ldcg_c(&colk[r == p ? k : r]);
+    if (threadIdx.x == 0 && p != k) { const int t = perm[k]; perm[k] = perm[p]; perm[p] = t; }
+    if (wid == scal_warp) {
+      const bool zero = piv.x == 0.0 && piv.y == 0.0;
+      const cplx rinv = zero ? cmake(0.0, 0.0) : cdiv(cmake(1.0, 0.0), piv);
+      if (lane == 0) {
+        s_rinv = rinv;
+        if (blockIdx.x == 0) {
+          w.udiag[k] = piv;
+          w.rdiag[k] = rinv;
+          if (zero) atomicOr(w.err, DQMC_KERR_SINGULAR);
+        }
+      }
+    }
+    // the same row exchange in the multiplier columns formed so far
+    if (p != k)
+      for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < k; j += gridDim.x * blockDim.x) {
+        cplx* lj = Lb + (size_t)j * n;
+        const cplx a = ldcg_c(&lj[k]), b = ldcg_c(&lj[p]);
+        lj[k] = b;
+        lj[p] = a;
+      }
+    __syncthreads();   // v, s_rinv
+    const cplx rinv = s_rinv;
+    {
+      const int r0 = blockIdx.x * chunk, r1 = r0 + chunk < n ? r0 + chunk : n;
+      for (int r = (r0 > k + 1 ? r0 : k + 1) + threadIdx.x; r < r1; r += blockDim.x)
+        Lb[(size_t)k * n + r] = cmul(v[r], rinv);
+    }
+    // ---- trailing columns j > k, dealt round-robin over the CTAs ----
+    const int rem = n - k - 1;
+    const int nq = (rem + 31) >> 5;   // warp-uniform slot count of rows k+1..n-1
+    for (int t = blockIdx.x + gridDim.x * wid; t < rem; t += gridDim.x * warps) {
+      const int j = k + 1 + t;
+      cplx* col = A + (size_t)j * n;
+      const cplx u = ldcg_c(&col[p]), wk = ldcg_c(&col[k]);
+      cplx x[QR_MAXT];
+#pragma unroll
+      for (int q = 0; q < QR_MAXT; ++q) {
+        if (q >= nq) break;
+        const int r = k + 1 + lane + 32 * q;
+        x[q] = r < n ? (r == p ? wk : ldcg_c(&col[r])) : cmake(0.0, 0.0);
+      }
+      const cplx c = cmul(u, rinv);   // a_rj -= (a_rk / piv) u_kj
+      double best = 0.0;
+      int brow = n;
+#pragma unroll
+      for (int q = 0; q < QR_MAXT; ++q) {
+        if (q >= nq) break;
+        const int r = k + 1 + lane + 32 * q;
+        if (r < n) {
+          const cplx vr = v[r];
+          x[q] = cmake(fma(-vr.x, c.x, fma(vr.y, c.y, x[q].x)), fma(-vr.x, c.y, fma(-vr.y, c.x, x[q].y)));
+          col[r] = x[q];
+          if (t == 0) {
+            const double a = fabs(x[q].x) + fabs(x[q].y);
+            if (piv_better(a, r, best, brow)) { best = a; brow = r; }
+          }
+        }
+      }
+      if (lane == 0) col[k] = u;
+      if (t == 0) {   // column k+1: pivot row of the next step
+        warp_argmax(best, brow);
+        if (lane == 0) w.pivrow[(k + 1) & 1] = brow < n ? brow : k + 1;
+      }
+    }
+    if (!grid_barrier(w.bar, w.err)) return;
+  }
+  if (blockIdx.x == 0)
+    for (int q = threadIdx.x; q < n; q += blockDim.x) w.perm[q] = perm[q];
+}
+
+// D-scale separation helpers: s[0..n) = 1/max(Dl,1), s[n..2n) = min(Dl,1),
+// s[2n..3n) = 1/max(Dr,1), s[3n..4n) = min(Dr,1)
+__global__ void k_split_scales(const double* __restrict__ Dl, const double* __restrict__ Dr, int n,
+                               double* __restrict__ s) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double l = Dl[i], r = Dr[i];
+    s[i] = 1.0 / (l > 1.0 ? l : 1.0);
+    s[n + i] = l < 1.0 ? l : 1.0;
+    s[2 * n + i] = 1.0 / (r > 1.0 ? r : 1.0);
+    s[3 * n + i] = r < 1.0 ? r : 1.0;
+  }
+}
+
+// out[0] = sum_i log|u_i| + log max(Dl_i, 1) + log max(Dr_i, 1)  (single CTA)
+__global__ void k_lu_logdet(const cplx* __restrict__ udiag, const double* __restrict__ Dl,
+                            const double* __restrict__ Dr, int n, double* out) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double l = Dl[i], r = Dr[i];
+    s += 0.5 * log(cabs2(udiag[i])) + log(l > 1.0 ? l : 1.0) + log(r > 1.0 ? r : 1.0);
+  }
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) out[0] = s;
+}
+
 // T (physical layout) = D^-1 R, zero below the logical diagonal; D = |beta|.
 __global__ void k_qrp_finalize(const cplx* __restrict__ A, cplx* __restrict__ T, double* __restrict__ D, int n,
                                const int* __restrict__ order, const double* __restrict__ beta) {
@@ -453,7 +604,8 @@ __global__ void __launch_bounds__(128) k_apply_q_right(cplx* __restrict__ X, int
 // Y <- That^-1 Y, That[r, q] = T[r, order[q]] upper triangular (logical order).
 // One warp per column of Y (column staged in shared memory).
 __global__ void __launch_bounds__(128) k_trsm_left_upper(const cplx* __restrict__ T, const int* __restrict__ order,
-                                                        cplx* __restrict__ Y, int n, int m) {
+                                                        const cplx* __restrict__ rdiag, cplx* __restrict__ Y, int n,
+                                                        int m) {
   extern __shared__ double smem_t[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int col = blockIdx.x * (blockDim.x / 32) + wid;
@@ -463,14 +615,43 @@ __global__ void __launch_bounds__(128) k_trsm_left_upper(const cplx* __restrict_
   for (int r = lane; r < n; r += 32) y[r] = yg[r];
   __syncwarp();
   for (int q = n - 1; q >= 0; --q) {
-    const cplx* tq = T + (size_t)__ldg(&order[q]) * n;
-    const cplx d = __ldg(&tq[q]);
-    // the unit-scaled factor has diagonal beta/|beta| = +-1: a sign, not a division
-    cplx yq = (d.y == 0.0 && fabs(d.x) == 1.0) ? cscale(y[q], d.x) : cdiv(y[q], d);
+    const cplx* tq = T + (size_t)(order ? __ldg(&order[q]) : q) * n;
+    cplx yq;
+    if (rdiag) {
+      yq = cmul(y[q], __ldg(&rdiag[q]));
+    } else {
+      // the unit-scaled factor of a QR has diagonal beta/|beta| = +-1: a sign, not a division
+      const cplx d = __ldg(&tq[q]);
+      yq = (d.y == 0.0 && fabs(d.x) == 1.0) ? cscale(y[q], d.x) : cdiv(y[q], d);
+    }
     __syncwarp();
     if (lane == 0) y[q] = yq;
     for (int r = lane; r < q; r += 32) {
       const cplx t = __ldg(&tq[r]);
+      y[r] = cmake(fma(-yq.x, t.x, fma(yq.y, t.y, y[r].x)), fma(-yq.x, t.y, fma(-yq.y, t.x, y[r].y)));
+    }
+    __syncwarp();
+  }
+  for (int r = lane; r < n; r += 32) yg[r] = y[r];
+}
+
+// Y <- L^-1 Y with L unit lower triangular (strictly lower part of Lc,
+// column-major), one warp per column of Y (column staged in shared memory).
+__global__ void __launch_bounds__(128) k_trsm_left_lower_unit(const cplx* __restrict__ Lc, cplx* __restrict__ Y, int n,
+                                                             int m) {
+  extern __shared__ double smem_t[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int col = blockIdx.x * (blockDim.x / 32) + wid;
+  if (col >= m) return;
+  cplx* y = reinterpret_cast<cplx*>(smem_t) + (size_t)wid * n;
+  cplx* yg = Y + (size_t)col * n;
+  for (int r = lane; r < n; r += 32) y[r] = yg[r];
+  __syncwarp();
+  for (int q = 0; q < n - 1; ++q) {
+    const cplx* lq = Lc + (size_t)q * n;
+    const cplx yq = y[q];
+    for (int r = q + 1 + lane; r < n; r += 32) {
+      const cplx t = __ldg(&lq[r]);
       y[r] = cmake(fma(-yq.x, t.x, fma(yq.y, t.y, y[r].x)), fma(-yq.x, t.y, fma(-yq.y, t.x, y[r].y)));
     }
     __syncwarp();
@@ -646,14 +827,56 @@ cudaError_t launch_apply_q_right(cplx* X, int m, int n, const QRWork& w, bool co
   return cudaGetLastError();
 }
 
-cudaError_t launch_trsm_left_upper(const cplx* T, const int* order, cplx* Y, int n, int m, cudaStream_t st) {
+cudaError_t launch_trsm_left_upper(const cplx* T, const int* order, const cplx* rdiag, cplx* Y, int n, int m,
+                                   cudaStream_t st) {
   size_t smem = (size_t)4 * n * sizeof(cplx);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_trsm_left_upper, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  k_trsm_left_upper<<<(m + 3) / 4, 128, smem, st>>>(T, order, Y, n, m);
+  k_trsm_left_upper<<<(m + 3) / 4, 128, smem, st>>>(T, order, rdiag, Y, n, m);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trsm_left_lower_unit(const cplx* Lc, cplx* Y, int n, int m, cudaStream_t st) {
+  size_t smem = (size_t)4 * n * sizeof(cplx);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_trsm_left_lower_unit, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  k_trsm_left_lower_unit<<<(m + 3) / 4, 128, smem, st>>>(Lc, Y, n, m);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lup(cplx* A, cplx* Lb, int n, LUWork& w, int sm_count, cudaStream_t st, int max_grid) {
+  if (n > 32 * QR_MAXT) return cudaErrorInvalidValue;
+  size_t smem = (size_t)n * (sizeof(cplx) + sizeof(int));
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_lup, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+    attr = true;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lup, QR_THREADS, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int grid = sm_count;
+  if (max_grid > 0 && grid > max_grid) grid = max_grid;
+  LUWork copy = w;
+  void* args[] = {&A, &Lb, &n, &copy};
+  return cudaLaunchCooperativeKernel((void*)k_lup, dim3(grid), dim3(QR_THREADS), args, smem, st);
+}
+
+cudaError_t launch_split_scales(const double* Dl, const double* Dr, int n, double* s, cudaStream_t st) {
+  k_split_scales<<<(n + 255) / 256, 256, 0, st>>>(Dl, Dr, n, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lu_logdet(const cplx* udiag, const double* Dl, const double* Dr, int n, double* out,
+                             cudaStream_t st) {
+  k_lu_logdet<<<1, 256, 0, st>>>(udiag, Dl, Dr, n, out);
   return cudaGetLastError();
 }
 

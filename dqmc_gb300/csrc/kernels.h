@@ -109,7 +109,27 @@ cudaError_t launch_apply_q_right(cplx* X, int m, int n, const QRWork& w, bool co
 //   right: Y <- Y That^-1       (Y is m x n)
 // Row/column permutation by the pivot order is applied by the caller with
 // launch_permute.
-cudaError_t launch_trsm_left_upper(const cplx* T, const int* order, cplx* Y, int n, int m, cudaStream_t st);
+// order == nullptr: T itself is upper triangular; rdiag != nullptr: 1 / diagonal (else the diagonal of T)
+cudaError_t launch_trsm_left_upper(const cplx* T, const int* order, const cplx* rdiag, cplx* Y, int n, int m,
+                                   cudaStream_t st);
+// Y <- L^-1 Y, L unit lower triangular (strictly lower part of Lc)
+cudaError_t launch_trsm_left_lower_unit(const cplx* Lc, cplx* Y, int n, int m, cudaStream_t st);
+// LU with partial pivoting of A (n x n, destroyed): P A = L U (zgetrf semantics).
+struct LUWork {
+  int* perm;         // (n) out: row perm[i] of A is row i of P A
+  cplx* udiag;       // (n) out: diagonal of U
+  cplx* rdiag;       // (n) out: 1 / diagonal of U
+  int* pivrow;       // (2) pivot row of the next step, by step parity
+  GridBarrier* bar;
+  int* err;
+};
+// On return the strict upper part of A holds U, Lb the strict lower part of L.
+cudaError_t launch_lup(cplx* A, cplx* Lb, int n, LUWork& w, int sm_count, cudaStream_t st, int max_grid = 0);
+// D-scale separation: s = [1/max(Dl,1), min(Dl,1), 1/max(Dr,1), min(Dr,1)] (4n)
+cudaError_t launch_split_scales(const double* Dl, const double* Dr, int n, double* s, cudaStream_t st);
+// out[0] = sum log|udiag| + sum log max(Dl,1) + sum log max(Dr,1)
+cudaError_t launch_lu_logdet(const cplx* udiag, const double* Dl, const double* Dr, int n, double* out,
+                             cudaStream_t st);
 cudaError_t launch_trsm_right_upper(const cplx* T, const int* order, cplx* Y, int m, int n, cudaStream_t st);
 // dst = src with rows (by_rows) or columns permuted: dst[order[k]] = src[k] (scatter) when scatter, else gather.
 cudaError_t launch_permute(const cplx* src, cplx* dst, int rows, int cols, const int* order, bool by_rows,

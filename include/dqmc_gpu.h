@@ -65,8 +65,18 @@ typedef struct dqmc_params {
   int32_t device;      /* CUDA device ordinal; -1 = the calling thread's current device */
   int32_t ozaki_bits;  /* mixed form: mantissa bits kept per GEMM operand (0 = default 40, max 60) */
   int32_t delay;       /* delayed-update depth k (0 or 1 = immediate rank-4 updates) */
-  int32_t reserved[3];
+  int32_t greens_method; /* DQMC_GREENS_SCALES (default) or DQMC_GREENS_TWO_QR */
+  int32_t reserved[2];
 } dqmc_params;
+
+/* calculate_greens (src/stack.jl:338-369) formulations; both give
+ * G = [I + Ul Dl Tl (Ur Dr Tr)^dag]^-1 and log|det G|:
+ *  DQMC_GREENS_SCALES: D-scale separation, D = Dmax Dmin with Dmax = max(D, 1),
+ *    G = Ur Drmax^-1 [Dlmax^-1 Ul^dag Ur Drmax^-1 + Dlmin Tl Tr^dag Drmin]^-1 Dlmax^-1 Ul^dag,
+ *    the bracket (entries bounded by 1 in scale) inverted through one LU with partial pivoting;
+ *  DQMC_GREENS_TWO_QR: the reference's two pivoted QRs (inv_one_plus_two_udts!, src/linalg.jl:237-283). */
+#define DQMC_GREENS_SCALES 0
+#define DQMC_GREENS_TWO_QR 1
 
 typedef struct dqmc_stats {
   int64_t proposals;        /* site proposals made */

@@ -21,11 +21,16 @@ def relerr(a, b):
     return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(1.0, float(np.max(np.abs(b)))))
 
 
-def api_params(p: R.Params, all_checks=True):
+def api_params(p: R.Params, all_checks=True, greens_method="scales"):
     from dqmc_gb300.api import ModelParams
     return ModelParams(L=p.L, slices=p.slices, safe_mult=p.safe_mult, delta_tau=p.delta_tau, lambda_=p.lambda_,
                        r=p.r, c=p.c, u=p.u, mu1=p.mu1, mu2=p.mu2, hoppings=tuple(p.hoppings), box=p.box,
-                       all_checks=all_checks)
+                       all_checks=all_checks, greens_method=greens_method)
+
+
+# calculate_greens formulations: D-scale separation with one LU (default) and
+# the reference's two pivoted QRs; both must reproduce the oracle
+METHODS = ["scales", "two_qr"]
 
 
 @pytest.fixture(scope="module")
@@ -55,9 +60,10 @@ def test_multiply_B_all_modes(lib, golden, small_params):
             assert relerr(got, want) < 1e-13, (sl, name, relerr(got, want))
 
 
-def test_calculate_greens_kat(lib, golden, small_params):
+@pytest.mark.parametrize("method", METHODS)
+def test_calculate_greens_kat(lib, golden, small_params, method):
     # tests_O3.jl:217-227 through the C ABI
-    gpu = lib.DQMC(api_params(small_params), golden["randconf"])
+    gpu = lib.DQMC(api_params(small_params, greens_method=method), golden["randconf"])
     G, ld = gpu.calculate_greens_udt(golden["Ul"], golden["Dl"], golden["Tl"], golden["Ur"], golden["Dr"],
                                      golden["Tr"])
     assert relerr(G, golden["greens"]) < TOL
@@ -79,13 +85,14 @@ def test_decompose_udt(lib, small_params):
     assert np.allclose(np.abs(T), np.abs(Tr), atol=1e-10)
 
 
+@pytest.mark.parametrize("method", METHODS)
 @pytest.mark.parametrize("cfg", ["small", "c0"])
-def test_init_and_full_propagation(lib, golden, small_params, cfg):
+def test_init_and_full_propagation(lib, golden, small_params, cfg, method):
     p = small_params if cfg == "small" else C0
     phi = golden["randconf"] if cfg == "small" else R.synthetic_field(p.N, p.slices, 100)
     ref = R.DQMCRef(p, phi)
     ref.init()
-    gpu = lib.DQMC(api_params(p), phi)
+    gpu = lib.DQMC(api_params(p, greens_method=method), phi)
     gpu.init()
     assert gpu.state == (ref.current_slice, ref.direction)
     assert relerr(gpu.greens, ref.greens) < TOL
@@ -98,11 +105,12 @@ def test_init_and_full_propagation(lib, golden, small_params, cfg):
         assert relerr(gpu.greens, ref.greens) < TOL, gpu.state
 
 
-def test_calc_greens_from_scratch(lib, golden, small_params):
+@pytest.mark.parametrize("method", METHODS)
+def test_calc_greens_from_scratch(lib, golden, small_params, method):
     p = C0
     phi = R.synthetic_field(p.N, p.slices, 5)
     ref = R.DQMCRef(p, phi)
-    gpu = lib.DQMC(api_params(p), phi)
+    gpu = lib.DQMC(api_params(p, greens_method=method), phi)
     gpu.init()
     for sl in (1, 7, 20, 40):
         G, ld = gpu.calc_greens_and_logdet(sl)
@@ -149,8 +157,9 @@ def test_local_updates_one_slice(lib, golden, small_params):
     assert abs(gpu.boson_action - ref.boson_action_value) < 1e-10 * abs(ref.boson_action_value)
 
 
-@pytest.mark.parametrize("delay", [1, 4, 16])
-def test_sweep_config0_accept_sequence(lib, delay):
+@pytest.mark.parametrize("delay,method", [(1, "scales"), (4, "scales"), (16, "scales"), (1, "two_qr"),
+                                          (16, "two_qr")])
+def test_sweep_config0_accept_sequence(lib, delay, method):
     """Config 0: one full sweep (M update calls) on shared streams, with
     immediate rank-4 updates (delay 1) and delayed rank-k updates."""
     p = C0
@@ -160,7 +169,7 @@ def test_sweep_config0_accept_sequence(lib, delay):
     ref.init()
     rec = []
     ref.sweep(p.slices, delta, u, record=rec)
-    mp = api_params(p)
+    mp = api_params(p, greens_method=method)
     mp.delay = delay
     gpu = lib.DQMC(mp, phi)
     gpu.init()
