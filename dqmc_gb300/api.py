@@ -47,7 +47,7 @@ class CStats(ctypes.Structure):
 
 
 KERNEL_KINDS = ["slice_cols", "slice_rows", "local_updates", "zgemm", "qrp", "apply_q", "trsm", "misc",
-                "ozaki_gemm", "flush"]
+                "ozaki_gemm", "flush", "lu"]
 NK = len(KERNEL_KINDS)
 
 

@@ -385,7 +385,7 @@ int calculate_greens_scales(dqmc_handle* h, cplx* out) {
   CHK(zgemm_general(h, n, n, n, 'N', 'C', cmake(1, 0), h->Tl, n, h->Tr, n, cmake(1, 0), h->W1, n, s + n, s + 3 * n,
                     true));
   // P M = L U (U in W1's strict upper part and lu.udiag, L in W2)
-  LAUNCH(DQMC_K_QRP, 8.0 / 3.0 * n3(h), 32.0 * n2(h), launch_lup(h->W1, h->W2, n, h->lu, h->sm_count, h->st,
+  LAUNCH(DQMC_K_LU, 8.0 / 3.0 * n3(h), 32.0 * n2(h), launch_lup(h->W1, h->W2, n, h->lu, h->sm_count, h->st,
                                                                  h->coop_cap));
   // right-hand side P diag(1/Dlmax) Ul^dag
   LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_conj_transpose(h->Ul, h->W4, n, h->st));

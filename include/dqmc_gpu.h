@@ -97,7 +97,8 @@ typedef struct dqmc_stats {
 #define DQMC_K_MISC 7         /* permutations, scalings, reductions, fills */
 #define DQMC_K_OZGEMM 8       /* split-BF16 tensor-core complex GEMM (mixed form); flops = tensor flops */
 #define DQMC_K_FLUSH 9        /* delayed-update flush G += X Y */
-#define DQMC_NKINDS 10
+#define DQMC_K_LU 10          /* LU with partial pivoting (D-scale separated calculate_greens) */
+#define DQMC_NKINDS 11
 
 typedef struct dqmc_timing {
   double ms[DQMC_NKINDS];           /* accumulated device time per kernel kind */
