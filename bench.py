@@ -51,9 +51,10 @@ CONFIGS = {
 METRIC = "O(3) L=16 sweeps/s: mixed vs FP64 at G err≤1e-8; batched chain-sweeps/s"
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# roofline kernels at L=16 (n = 1024), from the ncu captures summarised in
-# profiles/kernels_L16_ncu.md (None: not captured)
-TRAFFIC = {"qrp": None, "lu": None, "apply_q": None, "trsm": None, "flush": None, "ozaki_gemm": None}
+# roofline kernels at L=16 (n = 1024), one ncu capture each of this bench's
+# L=16 mixed workload (None: not captured)
+TRAFFIC = {"qrp": 21.385e6, "lu": 21.337e6, "apply_q": 25.293e6, "trsm": 25.249e6, "flush": None,
+           "ozaki_gemm": 263.785e6}
 
 
 def model_params(L, M):
