@@ -74,6 +74,10 @@ struct dqmc_handle {
   int greens_method = DQMC_GREENS_SCALES;
   LUWork lu{};                // LU of the D-scale separated calculate_greens
   double* lu_scales = nullptr;   // (4n) 1/max(Dl,1), min(Dl,1), 1/max(Dr,1), min(Dr,1)
+  cplx* wy_v = nullptr;       // mixed form: (n x kWyBlock) reflector block
+  cplx* wy_s = nullptr;       // (kWyBlock^2) Vb^H Vb
+  cplx* wy_z = nullptr;       // (kWyBlock x n) T Vb^H W
+  cplx* wy_t = nullptr;       // (kWyBlock) tau of the block
   double* force_d = nullptr;   // (3, N, M) d log|det M| / d phi
   // global updates: backup of stack, G, field and interaction table (allocated on first use)
   cplx *gb_u = nullptr, *gb_t = nullptr, *gb_G = nullptr;
@@ -258,9 +262,16 @@ int zgemm_general(dqmc_handle* h, int m, int nn, int k, char opA, char opB, cplx
   if (allow_split && h->p.precision == DQMC_PREC_MIXED) {
     int S = 0, bits = 0;
     if (!ozaki_plan(k, h->oz_target, &S, &bits)) return set_err(h, DQMC_ERR_ARG, "no exact slicing for this K");
+    // few output tiles and a long K: split K over more CTAs (exact integer partial sums)
+    const int tiles = ((m + 63) / 64) * ((nn + 63) / 64);
+    int splitk = 1;
+    if (!active && tiles * 2 < h->sm_count && k >= 256) {
+      splitk = (h->sm_count + tiles - 1) / tiles;
+      if (splitk > k / 64) splitk = k / 64;
+    }
     LAUNCH(kind >= 0 ? kind : DQMC_K_OZGEMM, ozaki_tensor_flops(m, nn, k, S), gemm_bytes(m, nn, k),
            launch_ozaki_zgemm(m, nn, k, opA, opB, alpha, A, lda, B, ldb, beta, C, ldc, rs, cs, S, bits,
-                              h->oz_scratch, h->oz_bytes, h->st, active));
+                              h->oz_scratch, h->oz_bytes, h->st, active, splitk));
     h->launches += 2;   // the two slicing kernels
     return DQMC_OK;
   }
@@ -298,10 +309,38 @@ int permute(dqmc_handle* h, const cplx* src, cplx* dst, const int* order, bool b
   return DQMC_OK;
 }
 
+// Q = H_0 ... H_{n-1} formed explicitly from the reflectors of the last qrp
+// in compact-WY blocks of kWyBlock reflectors, backward (W <- B_j W, B_j =
+// I - V_j T_j V_j^H, T_j^-1 = diag(1/tau) + striu(V_j^H V_j)), the products as
+// split-BF16 GEMMs (mixed form).  Before step j, W differs from I only in
+// rows and columns >= (j+1) b, so every product acts on W[jb:, jb:].
+constexpr int kWyBlock = 64;
+int form_q_wy(dqmc_handle* h, cplx* W) {
+  const int n = h->n, b = kWyBlock;
+  CHK(set_identity(h, W));
+  for (int jb = ((n - 1) / b) * b; jb >= 0; jb -= b) {
+    const int m = n - jb, bs = m < b ? m : b;
+    LAUNCH(DQMC_K_APPLYQ, 0.0, 32.0 * m * bs, launch_wy_prep(h->qr.V, h->qr.tau, n, jb, bs, h->wy_v, h->wy_t, h->st));
+    // S = Vb^H Vb, Z = Vb^H W[jb:, jb:]
+    CHK(zgemm_general(h, bs, bs, m, 'C', 'N', cmake(1, 0), h->wy_v, m, h->wy_v, m, cmake(0, 0), h->wy_s, bs, nullptr,
+                      nullptr, true, DQMC_K_APPLYQ));
+    CHK(zgemm_general(h, bs, m, m, 'C', 'N', cmake(1, 0), h->wy_v, m, W + (size_t)jb * n + jb, n, cmake(0, 0),
+                      h->wy_z, bs, nullptr, nullptr, true, DQMC_K_APPLYQ));
+    // Z <- T Z: solve T^-1 Y = Z (upper: strict part S, diagonal 1/tau)
+    LAUNCH(DQMC_K_APPLYQ, 4.0 * bs * bs * m, 32.0 * bs * m,
+           launch_trsm_diag_block(h->wy_s, bs, h->wy_t, h->wy_z, bs, 0, bs, m, false, h->st));
+    // W[jb:, jb:] -= Vb Z
+    CHK(zgemm_general(h, m, m, bs, 'N', 'N', cmake(-1, 0), h->wy_v, m, h->wy_z, bs, cmake(1, 0),
+                      W + (size_t)jb * n + jb, n, nullptr, nullptr, true, DQMC_K_APPLYQ));
+  }
+  return DQMC_OK;
+}
+
 // ---- UDT ------------------------------------------------------------------
 // decompose_udt! (src/linalg.jl:20-39) of A (destroyed): U (explicit), D, T.
 int decompose_udt(dqmc_handle* h, cplx* A, cplx* U, double* D, cplx* T) {
   CHK(qrp(h, A, T, D));
+  if (h->p.precision == DQMC_PREC_MIXED) return form_q_wy(h, U);
   CHK(set_identity(h, U));
   CHK(apply_q(h, U));
   return DQMC_OK;
@@ -370,6 +409,32 @@ int calculate_greens_two_qr(dqmc_handle* h, cplx* out) {
   return DQMC_OK;
 }
 
+// Y <- T^-1 Y (n x n) in blocks of kTrsmBlock rows: FP64 solves of the
+// diagonal blocks, the off-diagonal updates as split-BF16 GEMMs.  lower: T
+// unit lower triangular (strict lower part), forward; else upper with the
+// reciprocal diagonal rdiag, backward.
+constexpr int kTrsmBlock = 64;
+int trsm_blocked(dqmc_handle* h, const cplx* T, const cplx* rdiag, cplx* Y, bool lower) {
+  const int n = h->n, b = kTrsmBlock;
+  const int nb = (n + b - 1) / b;
+  for (int t = 0; t < nb; ++t) {
+    const int blk = lower ? t : nb - 1 - t;
+    const int j0 = blk * b, bs = (j0 + b <= n) ? b : n - j0;
+    LAUNCH(DQMC_K_TRSM, 4.0 * bs * bs * n, 32.0 * bs * n,
+           launch_trsm_diag_block(T, n, rdiag, Y, n, j0, bs, n, lower, h->st));
+    if (lower && j0 + bs < n) {
+      // Y[j0+bs:, :] -= T[j0+bs:, j0:j0+bs] Y[j0:j0+bs, :]
+      CHK(zgemm_general(h, n - j0 - bs, n, bs, 'N', 'N', cmake(-1, 0), T + (size_t)j0 * n + j0 + bs, n, Y + j0, n,
+                        cmake(1, 0), Y + j0 + bs, n, nullptr, nullptr, true, DQMC_K_TRSM));
+    } else if (!lower && j0 > 0) {
+      // Y[:j0, :] -= T[:j0, j0:j0+bs] Y[j0:j0+bs, :]
+      CHK(zgemm_general(h, j0, n, bs, 'N', 'N', cmake(-1, 0), T + (size_t)j0 * n, n, Y + j0, n, cmake(1, 0), Y, n,
+                        nullptr, nullptr, true, DQMC_K_TRSM));
+    }
+  }
+  return DQMC_OK;
+}
+
 // D-scale separated calculate_greens: with D = Dmax Dmin, Dmax = max(D, 1),
 //   I + Ul Dl Tl Tr^dag Dr Ur^dag = Ul Dlmax M Drmax Ur^dag,
 //   M = Dlmax^-1 (Ul^dag Ur) Drmax^-1 + Dlmin (Tl Tr^dag) Drmin,
@@ -392,9 +457,14 @@ int calculate_greens_scales(dqmc_handle* h, cplx* out) {
   LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_scale(h->W4, n, n, s, false, nullptr, false, h->st));
   CHK(permute(h, h->W4, h->W3, h->lu.perm, true, false));
   // U^-1 L^-1 (.), then diag(1/Drmax)
-  LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_lower_unit(h->W2, h->W3, n, n, h->st));
-  LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_upper(h->W1, nullptr, h->lu.rdiag, h->W3, n, n,
-                                                                         h->st));
+  if (h->p.precision == DQMC_PREC_MIXED) {
+    CHK(trsm_blocked(h, h->W2, nullptr, h->W3, true));
+    CHK(trsm_blocked(h, h->W1, h->lu.rdiag, h->W3, false));
+  } else {
+    LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_lower_unit(h->W2, h->W3, n, n, h->st));
+    LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_upper(h->W1, nullptr, h->lu.rdiag, h->W3, n, n,
+                                                                           h->st));
+  }
   LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_scale(h->W3, n, n, s + 2 * n, false, nullptr, false, h->st));
   // G = Ur (.)
   CHK(gemm(h, 'N', 'N', h->Ur, h->W3, out));
@@ -670,7 +740,7 @@ void free_all(dqmc_handle* h) {
                   h->Tr, h->Dl, h->Dr, h->W1, h->W2, h->W3, h->W4, h->D1, h->d2, h->ord1, h->qr.vn1,
                   h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->qr.cand_v, h->qr.cand_q, h->delta_d, h->unif_d,
                   h->acc_d, h->det_d, h->pacc_d, h->action_d, h->nacc_d, h->Acol, h->Brow, h->bar, h->err_d,
-                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lu.pivrow, h->lu_scales, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
+                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lu.pivrow, h->lu_scales, h->wy_v, h->wy_s, h->wy_z, h->wy_t, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   for (auto e : h->event_pool) cudaEventDestroy(e);
@@ -786,6 +856,10 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
     A((void**)&h->pub, (size_t)h->N * sizeof(int));
   }
   if (p->precision == DQMC_PREC_MIXED) {
+    A((void**)&h->wy_v, (size_t)n * kWyBlock * sizeof(cplx));
+    A((void**)&h->wy_s, (size_t)kWyBlock * kWyBlock * sizeof(cplx));
+    A((void**)&h->wy_z, (size_t)kWyBlock * n * sizeof(cplx));
+    A((void**)&h->wy_t, (size_t)kWyBlock * sizeof(cplx));
     h->oz_target = p->ozaki_bits > 0 ? p->ozaki_bits : 40;
     // the largest products are n x n x n; the flush (K = 4k) needs fewer slices
     int S = 0, bits = 0;

@@ -503,6 +503,23 @@ __global__ void __launch_bounds__(QR_THREADS) k_lup(cplx* __restrict__ A, cplx* 
     for (int q = threadIdx.x; q < n; q += blockDim.x) w.perm[q] = perm[q];
 }
 
+// Block j of the compact-WY form of Q = H_0 ... H_{n-1}: Vb (m x b, m = n - jb,
+// leading dimension m) = rows jb.. of reflector columns jb..jb+b; a reflector
+// with tau = 0 is the identity and is stored as v = 0 with tau' = 1, so that
+// T^-1 = diag(1/tau') + striu(Vb^H Vb) stays valid.  trd = tau'.
+__global__ void k_wy_prep(const cplx* __restrict__ V, const cplx* __restrict__ tau, int n, int jb, int b,
+                          cplx* __restrict__ Vb, cplx* __restrict__ trd) {
+  const int m = n - jb;
+  const size_t total = (size_t)m * b;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(e / m), r = (int)(e - (size_t)c * m);
+    const cplx t = tau[jb + c];
+    const bool ident = t.x == 0.0 && t.y == 0.0;
+    Vb[e] = ident ? cmake(0.0, 0.0) : V[(size_t)(jb + c) * n + jb + r];
+    if (r == 0) trd[c] = ident ? cmake(1.0, 0.0) : t;
+  }
+}
+
 // D-scale separation helpers: s[0..n) = 1/max(Dl,1), s[n..2n) = min(Dl,1),
 // s[2n..3n) = 1/max(Dr,1), s[3n..4n) = min(Dr,1)
 __global__ void k_split_scales(const double* __restrict__ Dl, const double* __restrict__ Dr, int n,
@@ -657,6 +674,48 @@ __global__ void __launch_bounds__(128) k_trsm_left_lower_unit(const cplx* __rest
     __syncwarp();
   }
   for (int r = lane; r < n; r += 32) yg[r] = y[r];
+}
+
+// Diagonal-block solve of a blocked triangular solve: the b x b block of T
+// at (j0, j0) (leading dimension ldT) applied to rows j0..j0+b of the m
+// columns of Y (leading dimension ldY), one warp per column (segment in
+// shared memory).  lower: unit lower triangular, forward; otherwise upper
+// with the reciprocal diagonal rdiag[j0 + q], backward.
+__global__ void __launch_bounds__(128) k_trsm_diag_block(const cplx* __restrict__ T, int ldT,
+                                                        const cplx* __restrict__ rdiag, cplx* __restrict__ Y,
+                                                        int ldY, int j0, int b, int m, int lower) {
+  __shared__ cplx ys[4][128];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int col = blockIdx.x * 4 + wid;
+  if (col >= m) return;
+  cplx* y = ys[wid];
+  cplx* yg = Y + (size_t)col * ldY + j0;
+  for (int r = lane; r < b; r += 32) y[r] = yg[r];
+  __syncwarp();
+  if (lower) {
+    for (int q = 0; q < b - 1; ++q) {
+      const cplx* tq = T + (size_t)(j0 + q) * ldT + j0;
+      const cplx yq = y[q];
+      for (int r = q + 1 + lane; r < b; r += 32) {
+        const cplx t = __ldg(&tq[r]);
+        y[r] = cmake(fma(-yq.x, t.x, fma(yq.y, t.y, y[r].x)), fma(-yq.x, t.y, fma(-yq.y, t.x, y[r].y)));
+      }
+      __syncwarp();
+    }
+  } else {
+    for (int q = b - 1; q >= 0; --q) {
+      const cplx* tq = T + (size_t)(j0 + q) * ldT + j0;
+      const cplx yq = cmul(y[q], __ldg(&rdiag[j0 + q]));
+      __syncwarp();
+      if (lane == 0) y[q] = yq;
+      for (int r = lane; r < q; r += 32) {
+        const cplx t = __ldg(&tq[r]);
+        y[r] = cmake(fma(-yq.x, t.x, fma(yq.y, t.y, y[r].x)), fma(-yq.x, t.y, fma(-yq.y, t.x, y[r].y)));
+      }
+      __syncwarp();
+    }
+  }
+  for (int r = lane; r < b; r += 32) yg[r] = y[r];
 }
 
 // Y <- Y That^-1 (Y is m x n), one warp per row: z That = y, forward over columns.
@@ -839,6 +898,13 @@ cudaError_t launch_trsm_left_upper(const cplx* T, const int* order, const cplx* 
   return cudaGetLastError();
 }
 
+cudaError_t launch_trsm_diag_block(const cplx* T, int ldT, const cplx* rdiag, cplx* Y, int ldY, int j0, int b, int m,
+                                   bool lower, cudaStream_t st) {
+  if (b < 1 || b > 128) return cudaErrorInvalidValue;
+  k_trsm_diag_block<<<(m + 3) / 4, 128, 0, st>>>(T, ldT, rdiag, Y, ldY, j0, b, m, lower ? 1 : 0);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_trsm_left_lower_unit(const cplx* Lc, cplx* Y, int n, int m, cudaStream_t st) {
   size_t smem = (size_t)4 * n * sizeof(cplx);
   static bool attr = false;
@@ -867,6 +933,12 @@ cudaError_t launch_lup(cplx* A, cplx* Lb, int n, LUWork& w, int sm_count, cudaSt
   LUWork copy = w;
   void* args[] = {&A, &Lb, &n, &copy};
   return cudaLaunchCooperativeKernel((void*)k_lup, dim3(grid), dim3(QR_THREADS), args, smem, st);
+}
+
+cudaError_t launch_wy_prep(const cplx* V, const cplx* tau, int n, int jb, int b, cplx* Vb, cplx* trd,
+                           cudaStream_t st) {
+  k_wy_prep<<<grid_for((size_t)(n - jb) * b), 256, 0, st>>>(V, tau, n, jb, b, Vb, trd);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_split_scales(const double* Dl, const double* Dr, int n, double* s, cudaStream_t st) {

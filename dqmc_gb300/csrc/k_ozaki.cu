@@ -190,11 +190,38 @@ struct OzArgs {
   const double* cs;          // optional extra column scaling
   const int* active;         // optional: nothing to do when *active == 0
   int int_combine;           // group sums combined exactly in 64-bit integers
+  int kchunk;                // split K: K steps per CTA layer (blockIdx.z); 0 = all
+  unsigned long long* acc;   // split K: exact integer sums (m x n x {re, im}), finished by k_oz_finalize
 };
+
+// Final scaling and accumulation of one output value (shared by the GEMM and
+// the split-K finaliser).
+__device__ __forceinline__ void oz_store(const OzArgs& a, int row, int col, double vr, double vi, double wint,
+                                         bool plain) {
+  double f = a.sA[row] * a.sB[col] * wint;
+  if (a.rs) f *= a.rs[row];
+  if (a.cs) f *= a.cs[col];
+  cplx v = cmake(vr * f, vi * f);
+  cplx* cp = &a.C[(size_t)col * a.ldc + row];
+  if (plain) {
+    // alpha = +-1, beta in {0, 1}: one multiply and at most one add per value
+    if (a.alpha.x < 0.0) v = cmake(-v.x, -v.y);
+    if (a.beta.x != 0.0) v = cadd(*cp, v);
+  } else {
+    v = cmul(a.alpha, v);
+    if (a.beta.x != 0.0 || a.beta.y != 0.0) v = cfma(a.beta, *cp, v);
+  }
+  *cp = v;
+}
+
+__device__ __forceinline__ bool oz_plain(const OzArgs& a) {
+  return (a.alpha.x == 1.0 || a.alpha.x == -1.0) && a.alpha.y == 0.0 && a.beta.y == 0.0 &&
+         (a.beta.x == 0.0 || a.beta.x == 1.0);
+}
 
 // One CTA: 64 x 64 output tile; 8 warps in a 2 x 4 grid of 32 x 16 warp tiles.
 template <bool INT>
-__global__ void __launch_bounds__(OZ_THREADS) k_oz_gemm(OzArgs a) {
+__global__ void __launch_bounds__(OZ_THREADS, 2) k_oz_gemm(OzArgs a) {
   if (a.active && *a.active == 0) return;
   __shared__ __align__(16) __nv_bfloat16 sA[2][OZ_BM * OZ_LDS];
   __shared__ __align__(16) __nv_bfloat16 sBr[2][OZ_BN * OZ_LDS];
@@ -241,7 +268,9 @@ __global__ void __launch_bounds__(OZ_THREADS) k_oz_gemm(OzArgs a) {
     cp_async_commit();
   };
 
-  const int ksteps = (int)(Kp / OZ_BK);
+  const int ksteps_all = (int)(Kp / OZ_BK);
+  const int ks0 = a.kchunk ? (int)blockIdx.z * a.kchunk : 0;
+  const int ksteps = a.kchunk ? min(ksteps_all, ks0 + a.kchunk) : ksteps_all;
   for (int t = 2; t <= a.S + 1; ++t) {
     float fr[2][2][4], fi[2][2][4];
 #pragma unroll
@@ -253,8 +282,8 @@ __global__ void __launch_bounds__(OZ_THREADS) k_oz_gemm(OzArgs a) {
     const int pmin = t - a.S > 1 ? t - a.S : 1, pmax = t - 1 < a.S ? t - 1 : a.S;
     for (int p = pmin; p <= pmax; ++p) {
       const int q = t - p;
-      stage(0, p - 1, q - 1, 0);
-      for (int ks = 0; ks < ksteps; ++ks) {
+      stage(ks0 & 1, p - 1, q - 1, ks0 * OZ_BK);
+      for (int ks = ks0; ks < ksteps; ++ks) {
         const int buf = ks & 1;
         cp_async_wait_all();
         __syncthreads();
@@ -315,7 +344,7 @@ __global__ void __launch_bounds__(OZ_THREADS) k_oz_gemm(OzArgs a) {
   }
   // integer form: value = acc * 2^{-bits (S + 1)}
   const double wint = INT ? ldexp(1.0, -a.bits * (a.S + 1)) : 1.0;
-  const bool plain = a.alpha.x == 1.0 && a.alpha.y == 0.0 && a.beta.y == 0.0 && (a.beta.x == 0.0 || a.beta.x == 1.0);
+  const bool plain = oz_plain(a);
   // epilogue: mma C fragment layout (m16n8): value z of lane -> row (lane/4) + 8*(z/2), col 2*(lane%4) + (z%2)
 #pragma unroll
   for (int x = 0; x < 2; ++x)
@@ -326,29 +355,31 @@ __global__ void __launch_bounds__(OZ_THREADS) k_oz_gemm(OzArgs a) {
         const int row = i0 + 32 * wm + 16 * x + (lane >> 2) + 8 * (z >> 1);
         const int col = j0 + 16 * wn + 8 * y + 2 * (lane & 3) + (z & 1);
         if (row < a.m && col < a.n) {
-          double f = a.sA[row] * a.sB[col] * wint;
-          if (a.rs) f *= a.rs[row];
-          if (a.cs) f *= a.cs[col];
-          double vr, vi;
           if constexpr (INT) {
-            vr = __ll2double_rn(accr[x][y][z]);
-            vi = __ll2double_rn(acci[x][y][z]);
+            if (a.acc) {
+              // split K: integer partial sums add exactly (and in any order)
+              unsigned long long* q = a.acc + 2 * ((size_t)col * a.m + row);
+              atomicAdd(q, (unsigned long long)accr[x][y][z]);
+              atomicAdd(q + 1, (unsigned long long)acci[x][y][z]);
+            } else {
+              oz_store(a, row, col, __ll2double_rn(accr[x][y][z]), __ll2double_rn(acci[x][y][z]), wint, plain);
+            }
           } else {
-            vr = accr[x][y][z];
-            vi = acci[x][y][z];
+            oz_store(a, row, col, accr[x][y][z], acci[x][y][z], wint, plain);
           }
-          cplx v = cmake(vr * f, vi * f);
-          cplx* cp = &a.C[(size_t)col * a.ldc + row];
-          if (plain) {
-            // alpha = 1, beta in {0, 1}: one multiply and at most one add per value
-            if (a.beta.x != 0.0) v = cadd(*cp, v);
-          } else {
-            v = cmul(a.alpha, v);
-            if (a.beta.x != 0.0 || a.beta.y != 0.0) v = cfma(a.beta, *cp, v);
-          }
-          *cp = v;
         }
       }
+}
+
+__global__ void k_oz_finalize(OzArgs a) {
+  const double wint = ldexp(1.0, -a.bits * (a.S + 1));
+  const bool plain = oz_plain(a);
+  const size_t total = (size_t)a.m * a.n;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int col = (int)(e / a.m), row = (int)(e - (size_t)col * a.m);
+    const long long vr = (long long)a.acc[2 * e], vi = (long long)a.acc[2 * e + 1];
+    oz_store(a, row, col, __ll2double_rn(vr), __ll2double_rn(vi), wint, plain);
+  }
 }
 
 }  // namespace
@@ -382,7 +413,7 @@ size_t ozaki_scratch_bytes(int m, int n, int K, int S) {
 cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
                                const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
                                const double* colscale, int S, int bits, void* scratch, size_t scratch_bytes,
-                               cudaStream_t st, const int* active) {
+                               cudaStream_t st, const int* active, int splitk) {
   if (S < 1 || S > 12 || bits < 1 || bits > 8) return cudaErrorInvalidValue;
   const int Kpad = (k + 15) / 16 * 16;
   const size_t Kp = 2 * (size_t)Kpad;
@@ -403,8 +434,29 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
   a.alpha = alpha; a.beta = beta; a.C = C; a.ldc = ldc; a.rs = rowscale; a.cs = colscale; a.active = active;
   // |sum_t g_t 2^{bits (S+1-t)}| < 2^{24 + bits (S-1) + 1}: exact in int64 below 2^63
   a.int_combine = 24 + bits * (S - 1) <= 61 ? 1 : 0;
+  a.kchunk = 0;
+  a.acc = nullptr;
   dim3 grid((nn + OZ_BN - 1) / OZ_BN, (m + OZ_BM - 1) / OZ_BM);
+  const int ksteps = (int)(Kp / OZ_BK);
+  if (splitk > 1 && a.int_combine && !active && ksteps > 1) {
+    // split K over blockIdx.z: exact 64-bit integer partial sums behind the slices
+    const size_t off = (ozaki_scratch_bytes(m, nn, k, S) + 255) / 256 * 256;
+    const size_t need = off + (size_t)m * nn * 2 * sizeof(unsigned long long);
+    if (need <= scratch_bytes) {
+      if (splitk > ksteps) splitk = ksteps;
+      a.kchunk = (ksteps + splitk - 1) / splitk;
+      grid.z = (ksteps + a.kchunk - 1) / a.kchunk;
+      a.acc = reinterpret_cast<unsigned long long*>(base + off);
+      cudaError_t e = cudaMemsetAsync(a.acc, 0, (size_t)m * nn * 2 * sizeof(unsigned long long), st);
+      if (e != cudaSuccess) return e;
+    }
+  }
   if (a.int_combine) k_oz_gemm<true><<<grid, OZ_THREADS, 0, st>>>(a);
   else k_oz_gemm<false><<<grid, OZ_THREADS, 0, st>>>(a);
+  if (a.acc) {
+    const size_t total = (size_t)m * nn;
+    const int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+    k_oz_finalize<<<blocks, 256, 0, st>>>(a);
+  }
   return cudaGetLastError();
 }

@@ -112,6 +112,10 @@ cudaError_t launch_apply_q_right(cplx* X, int m, int n, const QRWork& w, bool co
 // order == nullptr: T itself is upper triangular; rdiag != nullptr: 1 / diagonal (else the diagonal of T)
 cudaError_t launch_trsm_left_upper(const cplx* T, const int* order, const cplx* rdiag, cplx* Y, int n, int m,
                                    cudaStream_t st);
+// rows j0..j0+b of the m columns of Y <- (b x b diagonal block of T at j0)^-1 (.) (b <= 128):
+// lower: unit lower triangular; else upper with reciprocal diagonal rdiag
+cudaError_t launch_trsm_diag_block(const cplx* T, int ldT, const cplx* rdiag, cplx* Y, int ldY, int j0, int b, int m,
+                                   bool lower, cudaStream_t st);
 // Y <- L^-1 Y, L unit lower triangular (strictly lower part of Lc)
 cudaError_t launch_trsm_left_lower_unit(const cplx* Lc, cplx* Y, int n, int m, cudaStream_t st);
 // LU with partial pivoting of A (n x n, destroyed): P A = L U (zgetrf semantics).
@@ -125,6 +129,9 @@ struct LUWork {
 };
 // On return the strict upper part of A holds U, Lb the strict lower part of L.
 cudaError_t launch_lup(cplx* A, cplx* Lb, int n, LUWork& w, int sm_count, cudaStream_t st, int max_grid = 0);
+// compact-WY block jb..jb+b of the reflectors in V/tau: Vb ((n-jb) x b), trd (b) (tau, 1 for identity reflectors)
+cudaError_t launch_wy_prep(const cplx* V, const cplx* tau, int n, int jb, int b, cplx* Vb, cplx* trd,
+                           cudaStream_t st);
 // D-scale separation: s = [1/max(Dl,1), min(Dl,1), 1/max(Dr,1), min(Dr,1)] (4n)
 cudaError_t launch_split_scales(const double* Dl, const double* Dr, int n, double* s, cudaStream_t st);
 // out[0] = sum log|udiag| + sum log max(Dl,1) + sum log max(Dr,1)
@@ -159,7 +166,7 @@ size_t ozaki_scratch_bytes(int m, int n, int K, int S);
 cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
                                const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
                                const double* colscale, int S, int bits, void* scratch, size_t scratch_bytes,
-                               cudaStream_t st, const int* active = nullptr);
+                               cudaStream_t st, const int* active = nullptr, int splitk = 1);
 
 // ---- adjoint force (k_force.cu) ----
 // grad[:, :, slice0] = d log|det M| / d phi[:, :, slice0] from G of that slice
