@@ -211,31 +211,35 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def run_batch(args, world, rank, local):
-    """Config c2: 64 chains of uneven L swept concurrently (dqmc_batch_*);
-    value = chain-sweeps/s of all chains (wall clock around the batch sweep,
-    synchronised; the device streams are resident)."""
+def measure_batch(args, world, rank, dev, warmup, steps, precision):
+    """64 chains of uneven L (config c2) swept concurrently through
+    dqmc_batch_*: delayed-update depth per L from the autotuner (or
+    --batch-delay), device-resident streams; returns the chain-sweeps/s of
+    all ranks (wall clock around the timed sweeps, synchronised) and the
+    details."""
     import torch
     from dqmc_gb300 import api
     from oracle.dqmc_ref import synthetic_field, synthetic_streams
 
     _, M, desc = CONFIGS["c2"]
-    dev = local if world > 1 else 0
     torch.cuda.set_device(dev)
     rng = np.random.default_rng(2000 + rank)
     Ls = [int(x) for x in rng.choice([6, 8, 10, 12], size=args.chains)]
+    auto = precision == "mixed" and args.batch_delay == "auto"
     plist, fields = [], []
     for k, L in enumerate(Ls):
         rp = model_params(L, M)
+        delay = (16 if auto else int(args.batch_delay)) if precision == "mixed" else args.fp64_delay
         plist.append(api.ModelParams(L=L, slices=M, safe_mult=10, delta_tau=rp.delta_tau, lambda_=rp.lambda_,
                                      r=rp.r, c=rp.c, u=rp.u, mu1=rp.mu1, mu2=rp.mu2, hoppings=rp.hoppings,
-                                     box=rp.box, all_checks=not args.no_checks, device=dev,
-                                     precision="mixed" if args.precision == "mixed" else "fp64",
-                                     delay=args.delay if args.precision == "mixed" else args.fp64_delay))
+                                     box=rp.box, all_checks=not args.no_checks, device=dev, precision=precision,
+                                     delay=delay))
         fields.append(synthetic_field(L * L, M, 3000 + 100 * rank + k))
-    batch = api.Batch(plist, fields)
+    batch = api.Batch(plist, fields, autotune=auto)
+    delays = {f"L={key[0]}": val[0] for key, val in batch.tuned.items()} if auto else \
+        {f"L={L}": plist[0].delay for L in sorted(set(Ls))}
     batch.init()
-    sweeps = args.warmup + args.steps
+    sweeps = warmup + steps
     d_dev, u_dev = [], []
     for k, L in enumerate(Ls):
         delta, unif = synthetic_streams(L * L, sweeps * M, 0.2, 4000 + 100 * rank + k)
@@ -248,7 +252,7 @@ def run_batch(args, world, rank, local):
         return batch.sweep_device(M, [t.data_ptr() + off * 3 * (L * L) * 8 for t, L in zip(d_dev, Ls)],
                                   [t.data_ptr() + off * (L * L) * 8 for t, L in zip(u_dev, Ls)])
 
-    for s in range(args.warmup):
+    for s in range(warmup):
         run(s)
     torch.cuda.synchronize()
     barrier(world)
@@ -256,7 +260,7 @@ def run_batch(args, world, rank, local):
     clocks.start()
     t0 = time.perf_counter()
     acc = prop = 0
-    for s in range(args.warmup, sweeps):
+    for s in range(warmup, sweeps):
         st = run(s)
         acc += sum(x["accepted"] for x in st)
         prop += sum(x["proposals"] for x in st)
@@ -264,7 +268,21 @@ def run_batch(args, world, rank, local):
     barrier(world)
     wall = allreduce_max(time.perf_counter() - t0, world)
     clk = clocks.stop()
-    value = world * args.chains * args.steps / wall
+    batch.close()
+    value = world * args.chains * steps / wall
+    info = {"chains": args.chains, "L_counts": {L: Ls.count(L) for L in (6, 8, 10, 12)}, "slices": M,
+            "precision": precision, "delays": delays, "autotuned": auto, "warmup": warmup, "steps": steps,
+            "acc_rate": acc / max(1, prop)}
+    return value, wall, clk, info, desc
+
+
+def run_batch(args, world, rank, local):
+    """Config c2: 64 chains of uneven L swept concurrently (dqmc_batch_*);
+    value = chain-sweeps/s of all chains."""
+    dev = local if world > 1 else 0
+    precision = "mixed" if args.precision in ("mixed", "both") else "fp64"
+    value, wall, clk, info, desc = measure_batch(args, world, rank, dev, args.warmup, args.steps, precision)
+    M = info["slices"]
     if rank == 0:
         cpu = None
         if world == 1 and not args.no_cpu:
@@ -278,15 +296,12 @@ def run_batch(args, world, rank, local):
             "metric": METRIC, "value": value, "unit": "chain-sweeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": wall * 1000.0 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64 + split-bf16 tensor GEMMs" if args.precision == "mixed" else "f64",
+            "dtype": "f64 + split-bf16 tensor GEMMs" if precision == "mixed" else "f64",
             "data": "synthetic (seeded uniform[-1,1] fields, uniform proposal/Metropolis streams)",
-            "config": {"workload": desc, "chains": args.chains, "L_counts": {L: Ls.count(L) for L in (6, 8, 10, 12)},
-                       "slices": M, "precision": args.precision, "delay": args.delay,
-                       "parallelism": f"{args.chains} chains per GPU, replicas x{world}"},
-            "acc_rate": acc / max(1, prop), "clocks": clk, "cpu_baseline": cpu,
+            "config": dict(workload=desc, parallelism=f"{args.chains} chains per GPU, replicas x{world}", **info),
+            "clocks": clk, "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
-    batch.close()
 
 
 def _make_chain(api, L, M, rp, args, dev, precision, delay, phi):
@@ -417,6 +432,13 @@ def run_ours(args, world, rank, local):
     hbm_gbs = by / (ms_top / 1000.0) / 1e9
     breakdown = {k: {"ms": round(v["ms"], 3), "launches": v["launches"], "share": round(v["ms"] / max(1e-9, tot_ms), 4)}
                  for k, v in kinds.items() if v["launches"]}
+    # the batched part of the metric: 64 chains of L in {6, 8, 10, 12} (config c2), mixed form
+    batched = None
+    if not args.no_batch and args.config == "c3":
+        for r in res.values():
+            r["chain"].close()
+        bval, bwall, bclk, binfo, bdesc = measure_batch(args, world, rank, dev, 1, 2, "mixed")
+        batched = dict(value=bval, unit="chain-sweeps/s", workload=bdesc, seconds=bwall, clocks=bclk, **binfo)
 
     if rank == 0:
         cpu = None
@@ -465,10 +487,12 @@ def run_ours(args, world, rank, local):
             "max_instability": R["instab"],
             "clocks": clk,
             "cpu_baseline": cpu,
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
-    for r in res.values():
-        r["chain"].close()
+    if batched is None:
+        for r in res.values():
+            r["chain"].close()
 
 
 def main():
@@ -489,6 +513,9 @@ def main():
     ap.add_argument("--delay", type=int, default=16, help="mixed form: delayed-update depth k")
     ap.add_argument("--fp64-delay", type=int, default=1, help="FP64 form: delayed-update depth (1 = rank-4)")
     ap.add_argument("--chains", type=int, default=64, help="chains of the batched config c2")
+    ap.add_argument("--batch-delay", default="auto", help="batched chains: delayed-update depth, or 'auto' "
+                    "(autotuned per L over 8, 16, 32)")
+    ap.add_argument("--no-batch", action="store_true", help="default run: skip the batched-chains measurement")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

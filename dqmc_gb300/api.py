@@ -12,6 +12,7 @@ from __future__ import annotations
 import ctypes
 import dataclasses
 import os
+import time
 
 import numpy as np
 
@@ -436,11 +437,46 @@ class DQMC:
         self._check(self.lib.dqmc_reset_timing(self.h, 1 if enable else 0))
 
 
+def tune_delay(params: ModelParams, candidates=(8, 16, 32), calls=None, seed=12345):
+    """Delayed-update depth autotuner: times `calls` update() calls (default
+    two stabilisation intervals) of one chain of `params` for every candidate
+    k on a seeded synthetic field and proposal stream, after one untimed
+    pass, and returns (fastest k, {k: seconds})."""
+    rng = np.random.default_rng(seed)
+    N, M = params.N, params.slices
+    calls = calls or min(M, 2 * params.safe_mult)
+    phi = rng.uniform(-1.0, 1.0, size=(3, N, M))
+    delta = rng.uniform(-params.box, params.box, size=(calls, 3, N))
+    unif = rng.uniform(size=(calls, N))
+    times = {}
+    for k in candidates:
+        chain = DQMC(dataclasses.replace(params, delay=int(k)), phi)
+        chain.init()
+        chain.sweep(calls, delta, unif)
+        t0 = time.perf_counter()
+        chain.sweep(calls, delta, unif)
+        times[int(k)] = time.perf_counter() - t0
+        chain.close()
+    best = min(times, key=times.get)
+    return best, times
+
+
 class Batch:
     """Independent chains sharing one GPU (dqmc_batch_*).  `chains[i]` is a
-    DQMC view of chain i for the single-chain calls."""
+    DQMC view of chain i for the single-chain calls.  autotune=True picks the
+    delayed-update depth per distinct (L, slices, precision) with tune_delay
+    (the choices are kept in `tuned`)."""
 
-    def __init__(self, params_list, fields=None):
+    def __init__(self, params_list, fields=None, autotune=False, candidates=(8, 16, 32)):
+        self.tuned = {}
+        if autotune:
+            tuned = []
+            for p in params_list:
+                key = (p.L, p.slices, p.precision)
+                if key not in self.tuned:
+                    self.tuned[key] = tune_delay(p, candidates)
+                tuned.append(dataclasses.replace(p, delay=self.tuned[key][0]))
+            params_list = tuned
         self.lib = load_library()
         arr = (CParams * len(params_list))(*[p.to_c() for p in params_list])
         b = ctypes.c_void_p()
