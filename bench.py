@@ -12,7 +12,10 @@ the FP64 sweeps/s, the ratio and max|G_mixed - G_FP64| after the shared warm-up
 are in "mixed_vs_fp64".
 
 value  : sweeps/s with the streams resident on the device (dqmc_sweep_device),
-         summed CUDA-event time of the K timed sweeps on the library's stream.
+         summed CUDA-event time of the K timed sweeps on the library's stream
+         (each sweep one CUDA-graph launch of the captured sweep).  The kernel
+         breakdown comes from one extra sweep launched kernel by kernel with a
+         CUDA-event pair around every launch.
 e2e    : sweeps/s through dqmc_sweep with host (pinned) buffers: the H2D copy
          of each sweep's streams and the D2H copy of its accept flags are
          inside the timed region (wall clock, synchronised).
@@ -333,7 +336,7 @@ def _measure_form(api, chain, args, M, N, d_dev, u_dev, acc_dev, flush, world):
     torch.cuda.synchronize()
     warm_greens = chain.greens
     barrier(world)
-    chain.reset_timing(True)
+    chain.reset_timing(False)
     torch.cuda.synchronize()
     dev_ms, accepted, instab = 0.0, 0, 0.0
     for s in range(args.warmup, args.warmup + args.steps):
@@ -345,6 +348,14 @@ def _measure_form(api, chain, args, M, N, d_dev, u_dev, acc_dev, flush, world):
         instab = max(instab, ins)
     torch.cuda.synchronize()
     barrier(world)
+    # kernel breakdown: one more sweep with a CUDA-event pair around every
+    # launch (the library enqueues launch by launch while timing, instead of
+    # replaying its captured sweep graph), on the first timed sweep's streams
+    chain.reset_timing(True)
+    flush.fill_(-1.0)
+    torch.cuda.synchronize()
+    sweep(args.warmup)
+    torch.cuda.synchronize()
     tim = chain.timing()
     chain.reset_timing(False)
     return dev_ms / 1000.0, accepted, instab, tim, warm_greens
@@ -437,7 +448,8 @@ def run_ours(args, world, rank, local):
     if not args.no_batch and args.config == "c3":
         for r in res.values():
             r["chain"].close()
-        bval, bwall, bclk, binfo, bdesc = measure_batch(args, world, rank, dev, 1, 2, "mixed")
+        # warm-up: both start states of a sweep (down and up) captured as graphs
+        bval, bwall, bclk, binfo, bdesc = measure_batch(args, world, rank, dev, 3, 2, "mixed")
         batched = dict(value=bval, unit="chain-sweeps/s", workload=bdesc, seconds=bwall, clocks=bclk, **binfo)
 
     if rank == 0:
@@ -472,7 +484,8 @@ def run_ours(args, world, rank, local):
             "mixed_vs_fp64": compare,
             "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": int(M * 4 * N * 8),
                     "d2h_bytes_per_step": int(M * N), "steps": e2e_steps},
-            "gpu_launches": int(tim["kernel_launches"]),
+            # launches of the timed region: K sweeps x the launches of one sweep
+            "gpu_launches": int(tim["kernel_launches"]) * args.steps,
             "roofline": {"bound": bound, "kernel": top, "achieved": achieved, "peak": peak, "unit": unit,
                          "frac": achieved / peak if peak else None, "traffic": TRAFFIC.get(top),
                          "peak_source": src, "share": round(kinds[top]["ms"] / max(1e-9, tot_ms), 4),

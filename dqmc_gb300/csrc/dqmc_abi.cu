@@ -96,6 +96,17 @@ struct dqmc_handle {
   std::string last_error;
   // timing
   bool timing = false;
+  // CUDA graphs of whole sweeps, one per (start slice, direction, calls, flags output)
+  struct SweepGraph {
+    int slice0 = 0, dir0 = 0, n_calls = 0, acc = 0, slice1 = 0, dir1 = 0;
+    cudaGraphExec_t exec = nullptr;
+    int64_t cnt[DQMC_NKINDS] = {};
+    double flops[DQMC_NKINDS] = {}, bytes[DQMC_NKINDS] = {};
+    int64_t launches = 0;
+  };
+  std::vector<SweepGraph> graphs;
+  bool graphs_off = false;    // capture refused once: direct launches from then on
+  cudaEvent_t done = nullptr; // end of the last enqueued sweep (batch pipelining)
   std::vector<TimedSpan> spans;
   std::vector<cudaEvent_t> event_pool;
   size_t event_next = 0;
@@ -652,8 +663,17 @@ void boson_gradient_host(const dqmc_handle* h, const std::vector<double>& phi, d
       }
 }
 
+// Captured sweeps hold the device addresses of the handle's buffers: they are
+// dropped whenever one of those addresses changes.
+void clear_graphs(dqmc_handle* h) {
+  for (auto& g : h->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  h->graphs.clear();
+}
+
 int ensure_stream_capacity(dqmc_handle* h, int calls) {
   if (calls <= h->stream_cap) return DQMC_OK;
+  clear_graphs(h);
   if (h->delta_d) cudaFree(h->delta_d);
   if (h->unif_d) cudaFree(h->unif_d);
   h->delta_d = nullptr;
@@ -667,6 +687,7 @@ int ensure_stream_capacity(dqmc_handle* h, int calls) {
 
 int ensure_out_capacity(dqmc_handle* h, int calls) {
   if (calls <= h->out_cap) return DQMC_OK;
+  clear_graphs(h);
   if (h->acc_d) cudaFree(h->acc_d);
   if (h->det_d) cudaFree(h->det_d);
   if (h->pacc_d) cudaFree(h->pacc_d);
@@ -743,6 +764,8 @@ void free_all(dqmc_handle* h) {
                   h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lu.pivrow, h->lu_scales, h->wy_v, h->wy_s, h->wy_z, h->wy_t, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
   for (void* q : ptrs)
     if (q) cudaFree(q);
+  clear_graphs(h);
+  if (h->done) cudaEventDestroy(h->done);
   for (auto e : h->event_pool) cudaEventDestroy(e);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -978,8 +1001,65 @@ int dqmc_update(dqmc_handle* h, const double* delta, const double* unif, uint8_t
 }
 
 // Enqueues n_calls update() calls on the handle's stream without waiting.
+// n_calls update() calls (propagate + local updates) enqueued on the stream.
+static int sweep_body(dqmc_handle* h, int n_calls, const double* delta_dev, const double* unif_dev,
+                      uint8_t* acc_dev) {
+  const size_t N = h->N;
+  for (int c = 0; c < n_calls; ++c) {
+    CHK(propagate(h));
+    CHK(local_updates_dev(h, delta_dev + (size_t)c * 3 * N, unif_dev + (size_t)c * N,
+                          acc_dev ? acc_dev + (size_t)c * N : nullptr, nullptr, nullptr));
+  }
+  return DQMC_OK;
+}
+
+// Captures the sweep from the current state into a CUDA graph (streams in the
+// handle's own buffers).  The host state is left as before the capture (no
+// work has run); the caller launches the graph and moves the state to the
+// graph's end state.  Returns null (and stops trying) if capture is refused.
+static dqmc_handle::SweepGraph* capture_sweep(dqmc_handle* h, int n_calls, bool acc) {
+  dqmc_handle::SweepGraph g;
+  g.slice0 = h->current_slice; g.dir0 = h->direction; g.n_calls = n_calls; g.acc = acc ? 1 : 0;
+  int64_t cnt0[DQMC_NKINDS]; double fl0[DQMC_NKINDS], by0[DQMC_NKINDS];
+  for (int k = 0; k < DQMC_NKINDS; ++k) { cnt0[k] = h->cnt[k]; fl0[k] = h->flops[k]; by0[k] = h->bytes[k]; }
+  const int64_t l0 = h->launches;
+  cudaGetLastError();
+  bool ok = cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  int rc = DQMC_OK;
+  cudaGraph_t graph = nullptr;
+  if (ok) {
+    rc = sweep_body(h, n_calls, h->delta_d, h->unif_d, acc ? h->acc_d : nullptr);
+    ok = cudaStreamEndCapture(h->st, &graph) == cudaSuccess && rc == DQMC_OK && graph;
+  }
+  if (ok) ok = cudaGraphInstantiate(&g.exec, graph, 0) == cudaSuccess;
+  if (graph) cudaGraphDestroy(graph);
+  g.slice1 = h->current_slice; g.dir1 = h->direction;
+  for (int k = 0; k < DQMC_NKINDS; ++k) {
+    g.cnt[k] = h->cnt[k] - cnt0[k]; g.flops[k] = h->flops[k] - fl0[k]; g.bytes[k] = h->bytes[k] - by0[k];
+    h->cnt[k] = cnt0[k]; h->flops[k] = fl0[k]; h->bytes[k] = by0[k];
+  }
+  g.launches = h->launches - l0;
+  h->launches = l0;
+  h->current_slice = g.slice0; h->direction = g.dir0;
+  cudaGetLastError();
+  if (!ok) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    h->graphs_off = true;
+    h->last_error.clear();
+    return nullptr;
+  }
+  h->graphs.push_back(g);
+  return &h->graphs.back();
+}
+
 static int sweep_enqueue(dqmc_handle* h, int n_calls, const double* delta_dev, const double* unif_dev,
                          uint8_t* acc_dev) {
+  // graphs need the streams at fixed addresses: reserve before the first event
+  const bool graphed = !h->timing && !h->graphs_off;
+  if (graphed) {
+    CHK(ensure_stream_capacity(h, n_calls));
+    if (acc_dev) CHK(ensure_out_capacity(h, n_calls));
+  }
   CU(cudaMemcpyAsync(h->nacc_d + 1, h->nacc_d, sizeof(int), cudaMemcpyDeviceToDevice, h->st));
   CU(cudaMemsetAsync(h->scal_d + 3, 0, sizeof(double), h->st));
   h->max_instability = 0.0;
@@ -988,11 +1068,30 @@ static int sweep_enqueue(dqmc_handle* h, int n_calls, const double* delta_dev, c
     CU(cudaEventCreate(&h->ev1));
   }
   CU(cudaEventRecord(h->ev0, h->st));
-  const size_t N = h->N;
-  for (int c = 0; c < n_calls; ++c) {
-    CHK(propagate(h));
-    CHK(local_updates_dev(h, delta_dev + (size_t)c * 3 * N, unif_dev + (size_t)c * N,
-                          acc_dev ? acc_dev + (size_t)c * N : nullptr, nullptr, nullptr));
+  dqmc_handle::SweepGraph* g = nullptr;
+  if (graphed) {
+    const size_t N = h->N;
+    if (delta_dev != h->delta_d)
+      CU(cudaMemcpyAsync(h->delta_d, delta_dev, (size_t)n_calls * 3 * N * sizeof(double), cudaMemcpyDeviceToDevice,
+                         h->st));
+    if (unif_dev != h->unif_d)
+      CU(cudaMemcpyAsync(h->unif_d, unif_dev, (size_t)n_calls * N * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    for (auto& x : h->graphs)
+      if (x.slice0 == h->current_slice && x.dir0 == h->direction && x.n_calls == n_calls &&
+          x.acc == (acc_dev ? 1 : 0))
+        g = &x;
+    if (!g) g = capture_sweep(h, n_calls, acc_dev != nullptr);
+  }
+  if (g) {
+    CU(cudaGraphLaunch(g->exec, h->st));
+    h->current_slice = g->slice1;
+    h->direction = g->dir1;
+    for (int k = 0; k < DQMC_NKINDS; ++k) { h->cnt[k] += g->cnt[k]; h->flops[k] += g->flops[k]; h->bytes[k] += g->bytes[k]; }
+    h->launches += g->launches;
+    if (acc_dev && acc_dev != h->acc_d)
+      CU(cudaMemcpyAsync(acc_dev, h->acc_d, (size_t)n_calls * h->N, cudaMemcpyDeviceToDevice, h->st));
+  } else {
+    CHK(sweep_body(h, n_calls, delta_dev, unif_dev, acc_dev));
   }
   CU(cudaEventRecord(h->ev1, h->st));
   h->pending_calls = n_calls;
@@ -1115,42 +1214,23 @@ int dqmc_batch_sweep(dqmc_batch* b, int32_t n_calls, const double* const* delta_
   for (int i = 0; i < C; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->chains[x]->n > b->chains[y]->n; });
   int rc = DQMC_OK;
-  for (int w0 = 0; w0 < C; w0 += b->inflight) {
-    const int w1 = std::min(C, w0 + b->inflight);
-    for (int q = w0; q < w1; ++q) {
-      dqmc_handle* h = b->chains[order[q]];
-      cudaSetDevice(h->device);
-      CU(cudaMemcpyAsync(h->nacc_d + 1, h->nacc_d, sizeof(int), cudaMemcpyDeviceToDevice, h->st));
-      CU(cudaMemsetAsync(h->scal_d + 3, 0, sizeof(double), h->st));
-      h->max_instability = 0.0;
-      if (!h->ev0) {
-        CU(cudaEventCreate(&h->ev0));
-        CU(cudaEventCreate(&h->ev1));
-      }
-      CU(cudaEventRecord(h->ev0, h->st));
-      h->pending_calls = n_calls;
-    }
-    for (int c = 0; c < n_calls; ++c)
-      for (int q = w0; q < w1; ++q) {
-        const int i = order[q];
-        dqmc_handle* h = b->chains[i];
-        cudaSetDevice(h->device);
-        const size_t N = h->N;
-        CHK(propagate(h));
-        CHK(local_updates_dev(h, delta_dev[i] + (size_t)c * 3 * N, unif_dev[i] + (size_t)c * N, nullptr, nullptr,
-                              nullptr));
-      }
-    for (int q = w0; q < w1; ++q) {
-      dqmc_handle* h = b->chains[order[q]];
-      cudaSetDevice(h->device);
-      CU(cudaEventRecord(h->ev1, h->st));
-    }
-    for (int q = w0; q < w1; ++q) {
-      dqmc_handle* h = b->chains[order[q]];
-      cudaSetDevice(h->device);
-      int r = sweep_finish(h, stats ? &stats[order[q]] : nullptr);
-      if (r != DQMC_OK && rc == DQMC_OK) rc = r;
-    }
+  // largest chains first; chain q starts once chain q - inflight has finished
+  // (a stream wait on its end event), so `inflight` chains run at a time, each
+  // with its capped cooperative grids; every chain's sweep is one graph launch
+  for (int q = 0; q < C; ++q) {
+    dqmc_handle* h = b->chains[order[q]];
+    cudaSetDevice(h->device);
+    if (!h->done) CU(cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming));
+    if (q >= b->inflight) CU(cudaStreamWaitEvent(h->st, b->chains[order[q - b->inflight]]->done, 0));
+    const int i = order[q];
+    CHK(sweep_enqueue(h, n_calls, delta_dev[i], unif_dev[i], nullptr));
+    CU(cudaEventRecord(h->done, h->st));
+  }
+  for (int q = 0; q < C; ++q) {
+    dqmc_handle* h = b->chains[order[q]];
+    cudaSetDevice(h->device);
+    int r = sweep_finish(h, stats ? &stats[order[q]] : nullptr);
+    if (r != DQMC_OK && rc == DQMC_OK) rc = r;
   }
   return rc;
 }
@@ -1309,6 +1389,7 @@ int dqmc_global_update(dqmc_handle* h, const double* shift, double u, int32_t* a
   CU(cudaMemcpyAsync(&ldsum_old, h->scal_d + 2, sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CHK(sync(h));
   // back up (stack and G by pointer swap, field and table by copy), shift, rebuild
+  clear_graphs(h);
   std::swap(h->u_stack, h->gb_u);
   std::swap(h->t_stack, h->gb_t);
   std::swap(h->d_stack, h->gb_d);
