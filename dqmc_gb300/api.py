@@ -39,7 +39,7 @@ class CParams(ctypes.Structure):
                 ("mu1", ctypes.c_double), ("mu2", ctypes.c_double), ("hoppings", ctypes.c_double * 4),
                 ("all_checks", ctypes.c_int32), ("precision", ctypes.c_int32), ("device", ctypes.c_int32),
                 ("ozaki_bits", ctypes.c_int32), ("delay", ctypes.c_int32), ("greens_method", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 2)]
+                ("inflight", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
 
 
 class CStats(ctypes.Structure):
@@ -144,6 +144,7 @@ class ModelParams:
     ozaki_bits: int = 0            # mantissa bits per GEMM operand in the mixed form (0 = default 40)
     delay: int = 0                 # delayed-update depth (0/1 = immediate rank-4)
     greens_method: str = "scales"  # calculate_greens: "scales" (D-scale separation + LU) or "two_qr" (reference)
+    inflight: int = 0              # batches: chains swept at the same time (0 = min(count, 8))
 
     @property
     def N(self):
@@ -168,6 +169,7 @@ class ModelParams:
         if self.greens_method not in ("scales", "two_qr"):
             raise ValueError("greens_method must be 'scales' or 'two_qr'")
         p.greens_method = 0 if self.greens_method == "scales" else 1
+        p.inflight = self.inflight
         return p
 
 

@@ -1160,13 +1160,19 @@ struct dqmc_batch {
 
 // Chains in flight per batch: enough to fill the SMs while each chain's
 // latency-bound kernels keep a useful share of them (measured optimum ~8-12).
-static int batch_inflight(int count) { return count < 12 ? count : 12; }
+// Chains in flight: 8 by default (64 chains of L in {6..12} on GB300 gave
+// 18.6 / 24.4 / 22.9 / 19.8 / 13.2 / 7.8 chain-sweeps/s for 4 / 8 / 12 / 19 /
+// 32 / 64: beyond ~8 the capped cooperative grids compete for the SMs).
+static int batch_inflight(int count, int requested) {
+  const int k = requested > 0 ? requested : 8;
+  return count < k ? count : k;
+}
 
 int dqmc_batch_create(const dqmc_params* params, int32_t count, dqmc_batch** out) {
   if (!params || !out || count < 1) return DQMC_ERR_ARG;
   *out = nullptr;
   dqmc_batch* b = new dqmc_batch();
-  b->inflight = batch_inflight(count);
+  b->inflight = batch_inflight(count, params[0].inflight);
   for (int i = 0; i < count; ++i) {
     dqmc_handle* h = nullptr;
     int rc = dqmc_create(&params[i], &h);

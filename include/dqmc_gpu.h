@@ -66,7 +66,8 @@ typedef struct dqmc_params {
   int32_t ozaki_bits;  /* mixed form: mantissa bits kept per GEMM operand (0 = default 40, max 60) */
   int32_t delay;       /* delayed-update depth k (0 or 1 = immediate rank-4 updates) */
   int32_t greens_method; /* DQMC_GREENS_SCALES (default) or DQMC_GREENS_TWO_QR */
-  int32_t reserved[2];
+  int32_t inflight;    /* dqmc_batch_create: chains swept at the same time (0 = min(count, 8)); first chain's value */
+  int32_t reserved[1];
 } dqmc_params;
 
 /* calculate_greens (src/stack.jl:338-369) formulations; both give
