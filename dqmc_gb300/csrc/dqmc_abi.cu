@@ -73,6 +73,7 @@ struct dqmc_handle {
   int* pub = nullptr;         // (N) per-site publication counters of the delayed rounds
   int greens_method = DQMC_GREENS_SCALES;
   LUWork lu{};                // LU of the D-scale separated calculate_greens
+  LUPanel lup{};              // blocked LU: pivots and per-step candidate copies
   double* lu_scales = nullptr;   // (4n) 1/max(Dl,1), min(Dl,1), 1/max(Dr,1), min(Dr,1)
   cplx* wy_v = nullptr;       // mixed form: (n x kWyBlock) reflector block
   cplx* wy_s = nullptr;       // (kWyBlock^2) Vb^H Vb
@@ -446,6 +447,31 @@ int trsm_blocked(dqmc_handle* h, const cplx* T, const cplx* rdiag, cplx* Y, bool
   return DQMC_OK;
 }
 
+// zgetrf of A (n x n, in place: L strict lower, U upper) in panels of LU_PB
+// columns: panel factorisation with partial pivoting, the panel's row
+// exchanges on the other columns, U12 = L11^-1 A12, A22 -= L21 U12 (a GEMM,
+// split-BF16 in the mixed form).  lu.perm, lu.udiag, lu.rdiag on return.
+int lu_blocked(dqmc_handle* h, cplx* A) {
+  const int n = h->n;
+  LAUNCH(DQMC_K_LU, 0.0, 4.0 * n, launch_iota(h->lu.perm, n, h->st));
+  for (int p0 = 0; p0 < n; p0 += LU_PB) {
+    const int b = n - p0 < LU_PB ? n - p0 : LU_PB;
+    const int m = n - p0 - b;
+    LAUNCH(DQMC_K_LU, 8.0 * (n - p0) * b * b / 2.0, 32.0 * (n - p0) * b,
+           launch_lu_panel(A, n, p0, b, h->lup, h->sm_count, h->st, h->coop_cap));
+    LAUNCH(DQMC_K_LU, 0.0, 64.0 * b * n, launch_lu_apply_swaps(A, n, p0, b, h->lup.piv, h->lu.perm, h->st));
+    if (m > 0) {
+      LAUNCH(DQMC_K_LU, 4.0 * b * b * m, 32.0 * b * m,
+             launch_trsm_diag_block(A, n, nullptr, A + (size_t)(p0 + b) * n, n, p0, b, m, true, h->st));
+      CHK(zgemm_general(h, m, m, b, 'N', 'N', cmake(-1, 0), A + (size_t)p0 * n + p0 + b, n,
+                        A + (size_t)(p0 + b) * n + p0, n, cmake(1, 0), A + (size_t)(p0 + b) * n + p0 + b, n, nullptr,
+                        nullptr, true, DQMC_K_LU));
+    }
+  }
+  LAUNCH(DQMC_K_LU, 0.0, 32.0 * n, launch_lu_diag(A, n, h->lu.udiag, h->lu.rdiag, h->st));
+  return DQMC_OK;
+}
+
 // D-scale separated calculate_greens: with D = Dmax Dmin, Dmax = max(D, 1),
 //   I + Ul Dl Tl Tr^dag Dr Ur^dag = Ul Dlmax M Drmax Ur^dag,
 //   M = Dlmax^-1 (Ul^dag Ur) Drmax^-1 + Dlmin (Tl Tr^dag) Drmin,
@@ -460,19 +486,18 @@ int calculate_greens_scales(dqmc_handle* h, cplx* out) {
   CHK(zgemm_general(h, n, n, n, 'C', 'N', cmake(1, 0), h->Ul, n, h->Ur, n, cmake(0, 0), h->W1, n, s, s + 2 * n, true));
   CHK(zgemm_general(h, n, n, n, 'N', 'C', cmake(1, 0), h->Tl, n, h->Tr, n, cmake(1, 0), h->W1, n, s + n, s + 3 * n,
                     true));
-  // P M = L U (U in W1's strict upper part and lu.udiag, L in W2)
-  LAUNCH(DQMC_K_LU, 8.0 / 3.0 * n3(h), 32.0 * n2(h), launch_lup(h->W1, h->W2, n, h->lu, h->sm_count, h->st,
-                                                                 h->coop_cap));
+  // P M = L U in place in W1 (L strict lower, U upper; lu.udiag, lu.rdiag, lu.perm)
+  CHK(lu_blocked(h, h->W1));
   // right-hand side P diag(1/Dlmax) Ul^dag
   LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_conj_transpose(h->Ul, h->W4, n, h->st));
   LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_scale(h->W4, n, n, s, false, nullptr, false, h->st));
   CHK(permute(h, h->W4, h->W3, h->lu.perm, true, false));
   // U^-1 L^-1 (.), then diag(1/Drmax)
   if (h->p.precision == DQMC_PREC_MIXED) {
-    CHK(trsm_blocked(h, h->W2, nullptr, h->W3, true));
+    CHK(trsm_blocked(h, h->W1, nullptr, h->W3, true));
     CHK(trsm_blocked(h, h->W1, h->lu.rdiag, h->W3, false));
   } else {
-    LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_lower_unit(h->W2, h->W3, n, n, h->st));
+    LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_lower_unit(h->W1, h->W3, n, n, h->st));
     LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_upper(h->W1, nullptr, h->lu.rdiag, h->W3, n, n,
                                                                            h->st));
   }
@@ -761,7 +786,7 @@ void free_all(dqmc_handle* h) {
                   h->Tr, h->Dl, h->Dr, h->W1, h->W2, h->W3, h->W4, h->D1, h->d2, h->ord1, h->qr.vn1,
                   h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->qr.cand_v, h->qr.cand_q, h->delta_d, h->unif_d,
                   h->acc_d, h->det_d, h->pacc_d, h->action_d, h->nacc_d, h->Acol, h->Brow, h->bar, h->err_d,
-                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lu.pivrow, h->lu_scales, h->wy_v, h->wy_s, h->wy_z, h->wy_t, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
+                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lu.pivrow, h->lup.piv, h->lup.cand_rows, h->lup.rowk, h->lu_scales, h->wy_v, h->wy_s, h->wy_z, h->wy_t, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   clear_graphs(h);
@@ -869,6 +894,13 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
   A((void**)&h->lu_scales, 4 * n * sizeof(double));
   h->lu.bar = h->qr.bar;
   h->lu.err = h->err_d;
+  A((void**)&h->lup.piv, n * sizeof(int));
+  A((void**)&h->lup.cand_rows, (size_t)1024 * LU_PB * sizeof(cplx));
+  A((void**)&h->lup.rowk, (size_t)2 * LU_PB * sizeof(cplx));
+  h->lup.cand_v = h->qr.cand_v;
+  h->lup.cand_r = h->qr.cand_q;
+  h->lup.bar = h->qr.bar;
+  h->lup.err = h->err_d;
   h->delay = p->delay > 1 ? p->delay : 1;
   if (h->delay > 1) {
     A((void**)&h->Xd, (size_t)4 * h->delay * n * sizeof(cplx));

@@ -520,6 +520,210 @@ __global__ void k_wy_prep(const cplx* __restrict__ V, const cplx* __restrict__ t
   }
 }
 
+// ---------------------------------------------------------------------------
+// blocked LU with partial pivoting (zgetrf semantics, in place)
+// ---------------------------------------------------------------------------
+// Panel of LU_PB columns [p0, p0 + b) over rows [p0, n), rows dealt to the CTAs
+// in contiguous chunks.  Per column step the CTAs publish their pivot
+// candidate (|Re| + |Im|, row, and that row's panel values) and the owner of
+// row k publishes row k; after the grid barrier every CTA reads the pivot
+// row (the U row) and row k (which moves to the pivot's place) from those
+// copies, so no CTA reads a row another one is rewriting.
+__global__ void __launch_bounds__(256) k_lu_panel(cplx* __restrict__ A, int n, int p0, int b, LUPanel w) {
+  extern __shared__ double4_16a smem_panel[];
+  cplx* prow = reinterpret_cast<cplx*>(smem_panel);   // (own rows, LU_PB): this CTA's rows of the panel
+  const int rows = n - p0;
+  const int chunk = (rows + gridDim.x - 1) / gridDim.x;
+  const int r0 = p0 + blockIdx.x * chunk;
+  const int r1 = r0 + chunk < n ? r0 + chunk : n;
+  const int nrw = r1 > r0 ? r1 - r0 : 0;
+  __shared__ cplx urow[LU_PB], krow[LU_PB];
+  __shared__ double s_v[8];
+  __shared__ int s_r[8];
+  __shared__ int s_p, s_wc;
+  __shared__ cplx s_rinv;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int e = threadIdx.x; e < nrw * b; e += blockDim.x) {
+    const int rr = e / b, j = e - rr * b;
+    prow[rr * LU_PB + j] = ldcg_c(&A[(size_t)(p0 + j) * n + r0 + rr]);
+  }
+  __syncthreads();
+
+  // candidate of this CTA for panel column jc over its rows >= rlo, published with the row's panel values
+  auto publish_candidate = [&](int jc, int rlo) {
+    double best = 0.0;
+    int brow = n;
+    for (int r = (r0 > rlo ? r0 : rlo) + threadIdx.x; r < r1; r += blockDim.x) {
+      const cplx x = prow[(r - r0) * LU_PB + jc];
+      const double a = fabs(x.x) + fabs(x.y);
+      if (piv_better(a, r, best, brow)) { best = a; brow = r; }
+    }
+    warp_argmax(best, brow);
+    if (lane == 0) { s_v[wid] = best; s_r[wid] = brow; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double bv = s_v[0]; int br = s_r[0];
+      for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
+        if (piv_better(s_v[q], s_r[q], bv, br)) { bv = s_v[q]; br = s_r[q]; }
+      w.cand_v[blockIdx.x] = bv;
+      w.cand_r[blockIdx.x] = br;
+      s_r[0] = br;
+    }
+    __syncthreads();
+    const int br = s_r[0];
+    if (br < n)
+      for (int j = threadIdx.x; j < b; j += blockDim.x)
+        w.cand_rows[(size_t)blockIdx.x * LU_PB + j] = prow[(br - r0) * LU_PB + j];
+  };
+  auto publish_rowk = [&](int k, int slot) {
+    if (r0 <= k && k < r1)
+      for (int j = threadIdx.x; j < b; j += blockDim.x) w.rowk[slot * LU_PB + j] = prow[(k - r0) * LU_PB + j];
+  };
+
+  publish_candidate(0, p0);
+  publish_rowk(p0, 0);
+  if (!grid_barrier(w.bar, w.err)) return;
+
+  for (int kk = 0; kk < b; ++kk) {
+    const int k = p0 + kk;
+    // ---- pivot: best candidate (first row of maximal |Re| + |Im|) ----
+    if (wid == 0) {
+      double best = 0.0;
+      int brow = n, bc = 0;
+      for (int c = lane; c < (int)gridDim.x; c += 32) {
+        const double v = __ldcg(&w.cand_v[c]);
+        const int r = __ldcg(&w.cand_r[c]);
+        if (piv_better(v, r, best, brow)) { best = v; brow = r; bc = c; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int orow = __shfl_xor_sync(0xffffffffu, brow, o), oc = __shfl_xor_sync(0xffffffffu, bc, o);
+        if (piv_better(ob, orow, best, brow)) { best = ob; brow = orow; bc = oc; }
+      }
+      if (lane == 0) { s_p = brow; s_wc = bc; }
+    }
+    __syncthreads();
+    const bool none = s_p >= n;   // all candidates zero: no exchange, singular pivot
+    const int p = none ? k : s_p;
+    for (int j = threadIdx.x; j < b; j += blockDim.x) {
+      const cplx kv = ldcg_c(&w.rowk[(kk & 1) * LU_PB + j]);
+      krow[j] = kv;
+      urow[j] = none ? kv : ldcg_c(&w.cand_rows[(size_t)s_wc * LU_PB + j]);
+    }
+    __syncthreads();
+    if (wid == 0) {
+      // 1 / pivot = conj(pv) / |pv|^2 (the D-scale separated matrix has no large scales)
+      const cplx pv = urow[kk];
+      const double d2 = pv.x * pv.x + pv.y * pv.y;
+      const bool zero = d2 == 0.0;
+      const double rd = zero ? 0.0 : 1.0 / d2;
+      if (lane == 0) {
+        s_rinv = cmake(pv.x * rd, -pv.y * rd);
+        if (zero) atomicOr(w.err, DQMC_KERR_SINGULAR);
+        if (blockIdx.x == 0) w.piv[k] = p;
+      }
+    }
+    // the exchanged rows: row k <- pivot row (U), row p <- old row k
+    if (r0 <= k && k < r1)
+      for (int j = threadIdx.x; j < b; j += blockDim.x) prow[(k - r0) * LU_PB + j] = urow[j];
+    if (p != k && r0 <= p && p < r1)
+      for (int j = threadIdx.x; j < b; j += blockDim.x) prow[(p - r0) * LU_PB + j] = krow[j];
+    __syncthreads();
+    const cplx rinv = s_rinv;
+    // ---- multipliers of the own rows below k, then the rank-1 update of the panel ----
+    const int ra = r0 > k + 1 ? r0 : k + 1;
+    const int nr = r1 > ra ? r1 - ra : 0;
+    for (int t = threadIdx.x; t < nr; t += blockDim.x) {
+      cplx* e = &prow[(ra + t - r0) * LU_PB + kk];
+      *e = cmul(*e, rinv);
+    }
+    __syncthreads();
+    const int nc = b - kk - 1;
+    for (int t = threadIdx.x; t < nr * nc; t += blockDim.x) {
+      const int rr = t % nr, jj = kk + 1 + t / nr;
+      cplx* rowp = &prow[(ra + rr - r0) * LU_PB];
+      const cplx l = rowp[kk], u = urow[jj], x = rowp[jj];
+      rowp[jj] = cmake(fma(-l.x, u.x, fma(l.y, u.y, x.x)), fma(-l.x, u.y, fma(-l.y, u.x, x.y)));
+    }
+    __syncthreads();
+    if (kk + 1 < b) {
+      publish_candidate(kk + 1, k + 1);
+      publish_rowk(k + 1, (kk + 1) & 1);
+    }
+    if (!grid_barrier(w.bar, w.err)) return;
+  }
+  for (int e = threadIdx.x; e < nrw * b; e += blockDim.x) {
+    const int rr = e / b, j = e - rr * b;
+    A[(size_t)(p0 + j) * n + r0 + rr] = prow[rr * LU_PB + j];
+  }
+}
+
+// Row exchanges of one panel applied to the columns outside it, and to the
+// running permutation: the b exchanges (k, piv[k]) touch at most 2b rows,
+// whose net permutation one thread works out; every column is then gathered
+// over those rows.
+__global__ void k_lu_apply_swaps(cplx* __restrict__ A, int n, int p0, int b, const int* __restrict__ piv,
+                                 int* __restrict__ perm) {
+  __shared__ int rowof[2 * LU_PB], src[2 * LU_PB];
+  __shared__ int s_cnt;
+  if (threadIdx.x == 0) {
+    int cnt = b;
+    for (int s2 = 0; s2 < b; ++s2) { rowof[s2] = p0 + s2; src[s2] = p0 + s2; }
+    for (int kk = 0; kk < b; ++kk) {
+      const int k = p0 + kk, pr = piv[k];
+      if (pr == k) continue;
+      int sp = -1;
+      for (int s2 = 0; s2 < cnt; ++s2)
+        if (rowof[s2] == pr) { sp = s2; break; }
+      if (sp < 0) { sp = cnt++; rowof[sp] = pr; src[sp] = pr; }
+      const int t = src[kk]; src[kk] = src[sp]; src[sp] = t;
+    }
+    s_cnt = cnt;
+  }
+  __syncthreads();
+  const int cnt = s_cnt;
+  // permutation (block 0): perm[rowof[s]] <- old perm[src[s]]
+  if (blockIdx.x == 0) {
+    __shared__ int pv[2 * LU_PB];
+    for (int s2 = threadIdx.x; s2 < cnt; s2 += blockDim.x) pv[s2] = perm[src[s2]];
+    __syncthreads();
+    for (int s2 = threadIdx.x; s2 < cnt; s2 += blockDim.x) perm[rowof[s2]] = pv[s2];
+  }
+  // columns outside the panel, one warp per column
+  const int lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  for (int c = blockIdx.x * nw + (threadIdx.x >> 5); c < n; c += gridDim.x * nw) {
+    if (c >= p0 && c < p0 + b) continue;
+    cplx* col = A + (size_t)c * n;
+    cplx v[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int s2 = lane + 32 * q;
+      if (s2 < cnt) v[q] = ldcg_c(&col[src[s2]]);
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int s2 = lane + 32 * q;
+      if (s2 < cnt) col[rowof[s2]] = v[q];
+    }
+  }
+}
+
+// udiag = diag(U) of the in-place LU, rdiag = 1 / udiag
+__global__ void k_lu_diag(const cplx* __restrict__ A, int n, cplx* __restrict__ udiag, cplx* __restrict__ rdiag) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const cplx d = A[(size_t)i * n + i];
+    udiag[i] = d;
+    rdiag[i] = (d.x == 0.0 && d.y == 0.0) ? cmake(0.0, 0.0) : cdiv(cmake(1.0, 0.0), d);
+  }
+}
+
+__global__ void k_iota(int* __restrict__ p, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = i;
+}
+
 // D-scale separation helpers: s[0..n) = 1/max(Dl,1), s[n..2n) = min(Dl,1),
 // s[2n..3n) = 1/max(Dr,1), s[3n..4n) = min(Dr,1)
 __global__ void k_split_scales(const double* __restrict__ Dl, const double* __restrict__ Dr, int n,
@@ -938,6 +1142,46 @@ cudaError_t launch_lup(cplx* A, cplx* Lb, int n, LUWork& w, int sm_count, cudaSt
 cudaError_t launch_wy_prep(const cplx* V, const cplx* tau, int n, int jb, int b, cplx* Vb, cplx* trd,
                            cudaStream_t st) {
   k_wy_prep<<<grid_for((size_t)(n - jb) * b), 256, 0, st>>>(V, tau, n, jb, b, Vb, trd);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lu_panel(cplx* A, int n, int p0, int b, LUPanel& w, int sm_count, cudaStream_t st, int max_grid) {
+  if (b < 1 || b > LU_PB) return cudaErrorInvalidValue;
+  int grid = sm_count;
+  if (max_grid > 0 && grid > max_grid) grid = max_grid;
+  if (grid > n - p0) grid = n - p0;
+  if (grid > 1024) grid = 1024;
+  const int chunk = (n - p0 + grid - 1) / grid;
+  const size_t smem = (size_t)chunk * LU_PB * sizeof(cplx);
+  constexpr size_t kMax = 160 * 1024;
+  if (smem > kMax) return cudaErrorInvalidValue;   // grid too small for the panel rows
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_lu_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMax);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lu_panel, 256, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  LUPanel copy = w;
+  void* args[] = {&A, &n, &p0, &b, &copy};
+  return cudaLaunchCooperativeKernel((void*)k_lu_panel, dim3(grid), dim3(256), args, smem, st);
+}
+
+cudaError_t launch_lu_apply_swaps(cplx* A, int n, int p0, int b, const int* piv, int* perm, cudaStream_t st) {
+  k_lu_apply_swaps<<<(n + 7) / 8, 256, 0, st>>>(A, n, p0, b, piv, perm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lu_diag(const cplx* A, int n, cplx* udiag, cplx* rdiag, cudaStream_t st) {
+  k_lu_diag<<<(n + 255) / 256, 256, 0, st>>>(A, n, udiag, rdiag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_iota(int* p, int n, cudaStream_t st) {
+  k_iota<<<(n + 255) / 256, 256, 0, st>>>(p, n);
   return cudaGetLastError();
 }
 

@@ -132,6 +132,23 @@ cudaError_t launch_lup(cplx* A, cplx* Lb, int n, LUWork& w, int sm_count, cudaSt
 // compact-WY block jb..jb+b of the reflectors in V/tau: Vb ((n-jb) x b), trd (b) (tau, 1 for identity reflectors)
 cudaError_t launch_wy_prep(const cplx* V, const cplx* tau, int n, int jb, int b, cplx* Vb, cplx* trd,
                            cudaStream_t st);
+// Blocked LU (in place): panel factorisation of columns [p0, p0+b) (b <= LU_PB) over rows [p0, n)
+constexpr int LU_PB = 64;
+struct LUPanel {
+  int* piv;            // (n) pivot row of each step
+  double* cand_v;      // (grid) per-CTA pivot candidates: |Re| + |Im|
+  int* cand_r;         // (grid) and row
+  cplx* cand_rows;     // (grid, LU_PB) the candidate rows' panel values
+  cplx* rowk;          // (2, LU_PB) row k of the step, by step parity
+  GridBarrier* bar;
+  int* err;
+};
+cudaError_t launch_lu_panel(cplx* A, int n, int p0, int b, LUPanel& w, int sm_count, cudaStream_t st,
+                            int max_grid = 0);
+// the panel's row exchanges applied to the columns outside [p0, p0+b) and to perm
+cudaError_t launch_lu_apply_swaps(cplx* A, int n, int p0, int b, const int* piv, int* perm, cudaStream_t st);
+cudaError_t launch_lu_diag(const cplx* A, int n, cplx* udiag, cplx* rdiag, cudaStream_t st);
+cudaError_t launch_iota(int* p, int n, cudaStream_t st);
 // D-scale separation: s = [1/max(Dl,1), min(Dl,1), 1/max(Dr,1), min(Dr,1)] (4n)
 cudaError_t launch_split_scales(const double* Dl, const double* Dr, int n, double* s, cudaStream_t st);
 // out[0] = sum log|udiag| + sum log max(Dl,1) + sum log max(Dr,1)
