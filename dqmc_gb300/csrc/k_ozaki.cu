@@ -46,13 +46,51 @@ __device__ __forceinline__ cplx op_elem(const cplx* X, int ld, int r, int c, cha
   return op == 'C' ? cconj(v) : v;
 }
 
-// Power-of-two scale >= m (1 for m == 0).
-__device__ __forceinline__ double pow2_ceil(double m) {
-  if (!(m > 0.0)) return 1.0;
-  int e;
-  double f = frexp(m, &e);   // m = f * 2^e, f in [0.5, 1)
-  (void)f;
-  return ldexp(1.0, e);      // 2^e >= m
+// The slicing runs on the integer units.  A row (column) scale is 2^E with
+// E the frexp exponent of its largest |Re|/|Im|, taken from the exponent
+// fields; x 2^-E (|.| < 1) becomes a 62-bit fixed-point integer built from
+// the mantissa, and the S signed digits are cut off it by shifts, each
+// rounded half to even: the same digits as rint on the FP64 value, which is
+// exact at every step.
+__device__ __forceinline__ int expo_field(double x) {
+  return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
+}
+
+// x 2^(62 - E) as an integer (|x| < 2^E); values below 2^(E-62) are dropped
+__device__ __forceinline__ long long fixed62(double x, int E) {
+  const long long b = __double_as_longlong(x);
+  const int ef = (int)((b >> 52) & 0x7FF);
+  if (ef == 0) return 0;
+  const long long m = (b & 0xFFFFFFFFFFFFFll) | 0x10000000000000ll;   // x = m 2^(ef - 1075)
+  const int sh = ef - 1075 - E + 62;                                   // <= 9
+  long long X = 0;
+  if (sh >= 0) X = m << sh;
+  else if (sh > -63) X = m >> (-sh);
+  return b < 0 ? -X : X;
+}
+
+// next digit: round(X / 2^s) half to even, X <- X - digit 2^s
+__device__ __forceinline__ int next_digit(long long& X, int s) {
+  if (s <= 0) {
+    const long long d = s == 0 ? X : X * (1ll << -s);
+    X = 0;
+    return (int)d;
+  }
+  long long q = X >> s;                        // floor
+  const long long r = X - (q << s);            // in [0, 2^s)
+  const long long half = 1ll << (s - 1);
+  if (r > half || (r == half && (q & 1))) ++q;
+  X -= q << s;
+  return (int)q;
+}
+
+__device__ __forceinline__ int block_max_int(int v, int* red) {
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  int t = 0;
+  for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t = max(t, red[q]);
+  return t;
 }
 
 // A side: op(A) is rows x K; writes S slices of A' (rows x Kp, row-major,
@@ -67,35 +105,25 @@ __global__ void k_oz_split_rows(const cplx* __restrict__ X, int ld, char op, int
     if (kk == 0) return;
     if (kk < K) K = kk;
   }
-  __shared__ double red[32];
-  double m = 0.0;
+  __shared__ int red[32];
+  int me = 0;
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
-    cplx v = op_elem(X, ld, i, k, op);
-    m = fmax(m, fmax(fabs(v.x), fabs(v.y)));
+    const cplx v = op_elem(X, ld, i, k, op);
+    me = max(me, max(expo_field(v.x), expo_field(v.y)));
   }
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t = fmax(t, red[q]);
-    red[0] = pow2_ceil(t);
-  }
-  __syncthreads();
-  const double sc = red[0];
-  if (threadIdx.x == 0) scale[i] = sc;
-  const double inv = 1.0 / sc, step = ldexp(1.0, bits);
+  me = block_max_int(me, red);
+  const int E = me > 0 ? me - 1022 : 0;   // 2^E > max |.| (frexp exponent)
+  if (threadIdx.x == 0) scale[i] = ldexp(1.0, E);
   const size_t Kp = 2 * (size_t)Kpad;
   for (int k = threadIdx.x; k < Kpad; k += blockDim.x) {
-    cplx v = k < K ? op_elem(X, ld, i, k, op) : cmake(0.0, 0.0);
-    double xr = v.x * inv, xi = v.y * inv;
+    const cplx v = k < K ? op_elem(X, ld, i, k, op) : cmake(0.0, 0.0);
+    long long xr = fixed62(v.x, E), xi = fixed62(v.y, E);
     for (int p = 0; p < S; ++p) {
-      double ar = rint(xr * step), ai = rint(xi * step);
-      xr = xr * step - ar;
-      xi = xi * step - ai;
+      const int sft = 62 - (p + 1) * bits;
+      const int ar = next_digit(xr, sft), ai = next_digit(xi, sft);
       __nv_bfloat16* o = out + (size_t)p * rows * Kp + (size_t)i * Kp;
-      o[k] = __double2bfloat16(ar);
-      o[Kpad + k] = __double2bfloat16(ai);
+      o[k] = __float2bfloat16_rn((float)ar);
+      o[Kpad + k] = __float2bfloat16_rn((float)ai);
     }
   }
 }
@@ -113,37 +141,27 @@ __global__ void k_oz_split_cols(const cplx* __restrict__ X, int ld, char op, int
     if (kk == 0) return;
     if (kk < K) K = kk;
   }
-  __shared__ double red[32];
-  double m = 0.0;
+  __shared__ int red[32];
+  int me = 0;
   for (int k = threadIdx.x; k < K; k += blockDim.x) {
-    cplx v = op_elem(X, ld, k, j, op);
-    m = fmax(m, fmax(fabs(v.x), fabs(v.y)));
+    const cplx v = op_elem(X, ld, k, j, op);
+    me = max(me, max(expo_field(v.x), expo_field(v.y)));
   }
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t = fmax(t, red[q]);
-    red[0] = pow2_ceil(t);
-  }
-  __syncthreads();
-  const double sc = red[0];
-  if (threadIdx.x == 0) scale[j] = sc;
-  const double inv = 1.0 / sc, step = ldexp(1.0, bits);
+  me = block_max_int(me, red);
+  const int E = me > 0 ? me - 1022 : 0;
+  if (threadIdx.x == 0) scale[j] = ldexp(1.0, E);
   const size_t Kp = 2 * (size_t)Kpad;
   for (int k = threadIdx.x; k < Kpad; k += blockDim.x) {
-    cplx v = k < K ? op_elem(X, ld, k, j, op) : cmake(0.0, 0.0);
-    double xr = v.x * inv, xi = v.y * inv;
+    const cplx v = k < K ? op_elem(X, ld, k, j, op) : cmake(0.0, 0.0);
+    long long xr = fixed62(v.x, E), xi = fixed62(v.y, E);
     for (int p = 0; p < S; ++p) {
-      double ar = rint(xr * step), ai = rint(xi * step);
-      xr = xr * step - ar;
-      xi = xi * step - ai;
-      size_t base = (size_t)p * cols * Kp + (size_t)j * Kp;
-      out_re[base + k] = __double2bfloat16(ar);
-      out_re[base + Kpad + k] = __double2bfloat16(-ai);
-      out_im[base + k] = __double2bfloat16(ai);
-      out_im[base + Kpad + k] = __double2bfloat16(ar);
+      const int sft = 62 - (p + 1) * bits;
+      const int ar = next_digit(xr, sft), ai = next_digit(xi, sft);
+      const size_t base = (size_t)p * cols * Kp + (size_t)j * Kp;
+      out_re[base + k] = __float2bfloat16_rn((float)ar);
+      out_re[base + Kpad + k] = __float2bfloat16_rn((float)-ai);
+      out_im[base + k] = __float2bfloat16_rn((float)ai);
+      out_im[base + Kpad + k] = __float2bfloat16_rn((float)ar);
     }
   }
 }
