@@ -681,16 +681,17 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
           d.blk[(size_t)16 * j + lane] = b;
         }
       }
-      __threadfence();   // this thread's factor and block stores before the publication
-      __syncthreads();   // s_xn / s_yn reused by the next pass
+      __syncthreads();   // s_xn / s_yn reused by the next pass; all stores precede the publication
     }
     ++p;
     if (p == d.k || i == N - 1) {
       if (blockIdx.x == 0 && threadIdx.x == 0) { d.state[0] = i + 1; d.state[1] = p; }
       return;   // the flush follows as its own launch
     }
-    // ---- publish: the owned later sites now include p acceptances ----
+    // ---- publish: the owned later sites now include p acceptances (the CTA
+    //      barrier above orders every thread's stores before this fence) ----
     if (threadIdx.x == 0) {
+      __threadfence();
       for (int t = 0; t < owned; ++t) {
         const int j = blockIdx.x + t * gridDim.x;
         if (j > i) *(volatile int*)(d.pub + j) = p;
