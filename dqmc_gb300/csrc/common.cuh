@@ -57,32 +57,36 @@ struct EvEntry { double C, Sr, Si, R; };
 
 // Cross-CTA barrier for cooperative (co-resident) grids, with a bounded spin.
 // On timeout it sets *err (bit 1) and returns false: the kernel must then
-// leave its loop and return; it never hangs the device.
+// leave its loop and return; it never hangs the device.  The launcher zeroes
+// the counter before each launch.
 struct GridBarrier {
   unsigned int count;
   unsigned int gen;
 };
 
-__device__ __forceinline__ bool grid_barrier(GridBarrier* b, int* err) {
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// count is zeroed before every launch that uses the barrier; the e-th
+// barrier of the launch completes when all CTAs have added their arrival,
+// i.e. when count reaches e * gridDim.x (no returning atomic, no reset).
+__device__ __forceinline__ bool grid_barrier(GridBarrier* b, int* err, unsigned& epoch) {
   __syncthreads();
   __shared__ int s_ok;
+  ++epoch;
   if (threadIdx.x == 0) {
-    volatile unsigned int* vgen = &b->gen;
-    const unsigned int g = *vgen;
+    const unsigned target = epoch * gridDim.x;
     __threadfence();
-    // atomicInc wraps the count to 0 on the last arrival, so no separate reset
-    const unsigned int arrived = atomicInc(&b->count, gridDim.x - 1);
+    atomicAdd(&b->count, 1u);
     int ok = 1;
-    if (arrived == gridDim.x - 1) {
-      __threadfence();
-      atomicAdd(&b->gen, 1u);
-    } else {
-      long long spins = 0;
-      while (*vgen == g) {
-        if ((++spins & 1023) == 0) {
-          if (spins > (1ll << 26)) { atomicOr(err, 2); ok = 0; break; }
-          if (*(volatile int*)err & 2) { ok = 0; break; }
-        }
+    long long spins = 0;
+    while (ld_acquire_u32(&b->count) < target) {
+      if ((++spins & 1023) == 0) {
+        if (spins > (1ll << 26)) { atomicOr(err, 2); ok = 0; break; }
+        if (*(volatile int*)err & 2) { ok = 0; break; }
       }
     }
     __threadfence();

@@ -786,7 +786,7 @@ void free_all(dqmc_handle* h) {
                   h->Tr, h->Dl, h->Dr, h->W1, h->W2, h->W3, h->W4, h->D1, h->d2, h->ord1, h->qr.vn1,
                   h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->qr.cand_v, h->qr.cand_q, h->delta_d, h->unif_d,
                   h->acc_d, h->det_d, h->pacc_d, h->action_d, h->nacc_d, h->Acol, h->Brow, h->bar, h->err_d,
-                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lu.pivrow, h->lup.piv, h->lup.cand_rows, h->lup.rowk, h->lu_scales, h->wy_v, h->wy_s, h->wy_z, h->wy_t, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
+                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lup.piv, h->lup.cand_rows, h->lup.rowk, h->lu_scales, h->wy_v, h->wy_s, h->wy_z, h->wy_t, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   clear_graphs(h);
@@ -890,10 +890,8 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
   A((void**)&h->scal_d, 8 * sizeof(double));
   h->greens_method = p->greens_method == DQMC_GREENS_TWO_QR ? DQMC_GREENS_TWO_QR : DQMC_GREENS_SCALES;
   A((void**)&h->lu.perm, n * sizeof(int)); A((void**)&h->lu.udiag, n * sizeof(cplx));
-  A((void**)&h->lu.rdiag, n * sizeof(cplx)); A((void**)&h->lu.pivrow, 2 * sizeof(int));
+  A((void**)&h->lu.rdiag, n * sizeof(cplx));
   A((void**)&h->lu_scales, 4 * n * sizeof(double));
-  h->lu.bar = h->qr.bar;
-  h->lu.err = h->err_d;
   A((void**)&h->lup.piv, n * sizeof(int));
   A((void**)&h->lup.cand_rows, (size_t)1024 * LU_PB * sizeof(cplx));
   A((void**)&h->lup.rowk, (size_t)2 * LU_PB * sizeof(cplx));

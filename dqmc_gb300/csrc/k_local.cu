@@ -226,6 +226,7 @@ __device__ void local_decide(const LocalUpdateArgs& a, const LocalSmem& sm, int 
 // immediate rank-4 updates
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(LU_THREADS, 2) k_local_updates(LocalUpdateArgs a) {
+  unsigned bar_epoch = 0;
   const ModelConst& mc = a.mc;
   const int N = mc.N, n = mc.n;
   extern __shared__ double4_16a smem_local[];
@@ -282,7 +283,7 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_updates(LocalUpdateArgs
         }
       }
     }
-    if (!grid_barrier(a.bar, a.err)) return;
+    if (!grid_barrier(a.bar, a.err, bar_epoch)) return;
     // ---- phase 2: G += A B over warp tiles of 128 rows x 4 columns ----
     const int tiles_r = (n + 127) / 128, tiles_c = (n + 3) / 4;
     for (int tile = gwarp; tile < tiles_r * tiles_c; tile += nwarps) {
@@ -315,7 +316,7 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_updates(LocalUpdateArgs
         }
       }
     }
-    if (!grid_barrier(a.bar, a.err)) return;
+    if (!grid_barrier(a.bar, a.err, bar_epoch)) return;
   }
 }
 
@@ -429,6 +430,7 @@ __device__ __forceinline__ cplx adjugate_entry(cplx m, int lane) {
 // entries need no global loads.
 template <bool CACHE>
 __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs a, DelayedArgs d) {
+  unsigned bar_epoch = 0;
   const ModelConst& mc = a.mc;
   const int N = mc.N, n = mc.n, L = mc.L, K4 = 4 * d.k;
   __shared__ int s_first, s_ok, s_acc;
@@ -464,7 +466,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   }
   // publication counters of the owned sites start the round at 0
   for (int t = threadIdx.x; t < owned; t += blockDim.x) d.pub[blockIdx.x + t * gridDim.x] = 0;
-  if (!grid_barrier(a.bar, a.err)) return;
+  if (!grid_barrier(a.bar, a.err, bar_epoch)) return;
 
   // phase-1 role of this warp in the first pass of owned sites
   const int sub = lane >> 3, qg = (lane >> 1) & 3, h = lane & 1;
@@ -742,6 +744,8 @@ cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d,
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, LU_THREADS, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  e = cudaMemsetAsync(a.bar, 0, sizeof(GridBarrier), st);
+  if (e != cudaSuccess) return e;
   LocalUpdateArgs ca = a;
   DelayedArgs cd = d;
   void* args[] = {&ca, &cd};
@@ -769,6 +773,8 @@ cudaError_t launch_local_updates(const LocalUpdateArgs& a, int sm_count, cudaStr
   const int need = (tiles + (LU_THREADS / 32) - 1) / (LU_THREADS / 32);
   if (grid > need) grid = need < 1 ? 1 : need;
   if (max_grid > 0 && grid > max_grid) grid = max_grid;
+  e = cudaMemsetAsync(a.bar, 0, sizeof(GridBarrier), st);
+  if (e != cudaSuccess) return e;
   LocalUpdateArgs copy = a;
   void* args[] = {&copy};
   return cudaLaunchCooperativeKernel((void*)k_local_updates, dim3(grid), dim3(LU_THREADS), args, smem, st);

@@ -118,17 +118,12 @@ cudaError_t launch_trsm_diag_block(const cplx* T, int ldT, const cplx* rdiag, cp
                                    bool lower, cudaStream_t st);
 // Y <- L^-1 Y, L unit lower triangular (strictly lower part of Lc)
 cudaError_t launch_trsm_left_lower_unit(const cplx* Lc, cplx* Y, int n, int m, cudaStream_t st);
-// LU with partial pivoting of A (n x n, destroyed): P A = L U (zgetrf semantics).
+// Results of the LU with partial pivoting P A = L U (zgetrf semantics).
 struct LUWork {
-  int* perm;         // (n) out: row perm[i] of A is row i of P A
-  cplx* udiag;       // (n) out: diagonal of U
-  cplx* rdiag;       // (n) out: 1 / diagonal of U
-  int* pivrow;       // (2) pivot row of the next step, by step parity
-  GridBarrier* bar;
-  int* err;
+  int* perm;         // (n) row perm[i] of A is row i of P A
+  cplx* udiag;       // (n) diagonal of U
+  cplx* rdiag;       // (n) 1 / diagonal of U
 };
-// On return the strict upper part of A holds U, Lb the strict lower part of L.
-cudaError_t launch_lup(cplx* A, cplx* Lb, int n, LUWork& w, int sm_count, cudaStream_t st, int max_grid = 0);
 // compact-WY block jb..jb+b of the reflectors in V/tau: Vb ((n-jb) x b), trd (b) (tau, 1 for identity reflectors)
 cudaError_t launch_wy_prep(const cplx* V, const cplx* tau, int n, int jb, int b, cplx* Vb, cplx* trd,
                            cudaStream_t st);
