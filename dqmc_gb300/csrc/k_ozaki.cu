@@ -35,6 +35,7 @@ namespace {
 constexpr int OZ_BM = 64, OZ_BN = 64, OZ_BK = 32;
 constexpr int OZ_THREADS = 256;
 constexpr int OZ_LDS = OZ_BK + 8;   // padded shared-memory row (bf16 elements): 80 B, conflict-free ldmatrix
+constexpr int OZ_STAGES = 3;        // cp.async pipeline depth (46 KB of static shared memory)
 
 // ---------------------------------------------------------------------------
 // split: slices of op(X) scaled per row ("row" side = A) or per column (B side)
@@ -175,6 +176,7 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::); }
 
 __device__ __forceinline__ void ldmatrix_x4(unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3, const void* p) {
   unsigned s = (unsigned)__cvta_generic_to_shared(p);
@@ -241,9 +243,9 @@ __device__ __forceinline__ bool oz_plain(const OzArgs& a) {
 template <bool INT>
 __global__ void __launch_bounds__(OZ_THREADS, 2) k_oz_gemm(OzArgs a) {
   if (a.active && *a.active == 0) return;
-  __shared__ __align__(16) __nv_bfloat16 sA[2][OZ_BM * OZ_LDS];
-  __shared__ __align__(16) __nv_bfloat16 sBr[2][OZ_BN * OZ_LDS];
-  __shared__ __align__(16) __nv_bfloat16 sBi[2][OZ_BN * OZ_LDS];
+  __shared__ __align__(16) __nv_bfloat16 sA[OZ_STAGES][OZ_BM * OZ_LDS];
+  __shared__ __align__(16) __nv_bfloat16 sBr[OZ_STAGES][OZ_BN * OZ_LDS];
+  __shared__ __align__(16) __nv_bfloat16 sBi[OZ_STAGES][OZ_BN * OZ_LDS];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int wm = wid >> 2, wn = wid & 3;          // warp tile origin: rows 32*wm, cols 16*wn
   const int i0 = blockIdx.y * OZ_BM, j0 = blockIdx.x * OZ_BN;
@@ -289,77 +291,105 @@ __global__ void __launch_bounds__(OZ_THREADS, 2) k_oz_gemm(OzArgs a) {
   const int ksteps_all = (int)(Kp / OZ_BK);
   const int ks0 = a.kchunk ? (int)blockIdx.z * a.kchunk : 0;
   const int ksteps = a.kchunk ? min(ksteps_all, ks0 + a.kchunk) : ksteps_all;
-  for (int t = 2; t <= a.S + 1; ++t) {
-    float fr[2][2][4], fi[2][2][4];
+  // one stream of (group t, slice pair (p, q = t - p), K step) items, staged
+  // OZ_STAGES - 1 items ahead across pair and group boundaries
+  auto pmin_of = [&](int t) { return t - a.S > 1 ? t - a.S : 1; };
+  auto pmax_of = [&](int t) { return t - 1 < a.S ? t - 1 : a.S; };
+  auto advance = [&](int& t, int& p, int& ks) {
+    if (++ks < ksteps) return;
+    ks = ks0;
+    if (++p <= pmax_of(t)) return;
+    ++t;
+    p = pmin_of(t);
+  };
+  int lt = 2, lp = pmin_of(2), lks = ks0;   // next item to stage
+  int ct = 2, cp = pmin_of(2), cks = ks0;   // item being computed
+  const bool any = ks0 < ksteps;
+  int staged = 0;                           // items staged so far
+  for (int pre = 0; any && pre < OZ_STAGES - 1 && lt <= a.S + 1; ++pre) {
+    stage(staged % OZ_STAGES, lp - 1, lt - lp - 1, lks * OZ_BK);
+    ++staged;
+    advance(lt, lp, lks);
+  }
+  float fr[2][2][4], fi[2][2][4];
 #pragma unroll
-    for (int x = 0; x < 2; ++x)
+  for (int x = 0; x < 2; ++x)
 #pragma unroll
-      for (int y = 0; y < 2; ++y)
+    for (int y = 0; y < 2; ++y)
 #pragma unroll
-        for (int z = 0; z < 4; ++z) { fr[x][y][z] = 0.f; fi[x][y][z] = 0.f; }
-    const int pmin = t - a.S > 1 ? t - a.S : 1, pmax = t - 1 < a.S ? t - 1 : a.S;
-    for (int p = pmin; p <= pmax; ++p) {
-      const int q = t - p;
-      stage(ks0 & 1, p - 1, q - 1, ks0 * OZ_BK);
-      for (int ks = ks0; ks < ksteps; ++ks) {
-        const int buf = ks & 1;
-        cp_async_wait_all();
-        __syncthreads();
-        if (ks + 1 < ksteps) stage(buf ^ 1, p - 1, q - 1, (ks + 1) * OZ_BK);
-#pragma unroll
-        for (int kk = 0; kk < OZ_BK; kk += 16) {
-          unsigned af[2][4];
-#pragma unroll
-          for (int x = 0; x < 2; ++x) {
-            // rows 32*wm + 16*x + (lane % 16), k columns kk + 8*(lane / 16)
-            const __nv_bfloat16* pa = &sA[buf][(32 * wm + 16 * x + (lane & 15)) * OZ_LDS + kk + 8 * (lane >> 4)];
-            ldmatrix_x4(af[x][0], af[x][1], af[x][2], af[x][3], pa);
-          }
-          unsigned br[2][2], bi[2][2];
-#pragma unroll
-          for (int y = 0; y < 2; ++y) {
-            // columns 16*wn + 8*y + (lane % 8), k rows kk + 8*((lane / 8) % 2)
-            const int rowb = 16 * wn + 8 * y + (lane & 7);
-            const int kof = kk + 8 * ((lane >> 3) & 1);
-            ldmatrix_x2(br[y][0], br[y][1], &sBr[buf][rowb * OZ_LDS + kof]);
-            ldmatrix_x2(bi[y][0], bi[y][1], &sBi[buf][rowb * OZ_LDS + kof]);
-          }
-#pragma unroll
-          for (int x = 0; x < 2; ++x)
-#pragma unroll
-            for (int y = 0; y < 2; ++y) {
-              mma_bf16(fr[x][y], af[x], br[y]);
-              mma_bf16(fi[x][y], af[x], bi[y]);
-            }
-        }
-      }
-      __syncthreads();   // buffers free before the next pair stages into them
+      for (int z = 0; z < 4; ++z) { fr[x][y][z] = 0.f; fi[x][y][z] = 0.f; }
+  for (int c = 0; any && ct <= a.S + 1; ++c) {
+    const int buf = c % OZ_STAGES;
+    // item c is complete when at most (staged - c - 1) later groups are pending
+    if (staged - c - 1 >= 1) cp_async_wait_one(); else cp_async_wait_all();
+    __syncthreads();
+    if (lt <= a.S + 1) {   // the buffer of item c - 1 is free: stage item c + OZ_STAGES - 1
+      stage(staged % OZ_STAGES, lp - 1, lt - lp - 1, lks * OZ_BK);
+      ++staged;
+      advance(lt, lp, lks);
     }
-    if constexpr (INT) {
-      // every group sum is an integer below 2^24 (exact in FP32): no FP64 work
-      const long long step = 1ll << a.bits;
+#pragma unroll
+    for (int kk = 0; kk < OZ_BK; kk += 16) {
+      unsigned af[2][4];
+#pragma unroll
+      for (int x = 0; x < 2; ++x) {
+        // rows 32*wm + 16*x + (lane % 16), k columns kk + 8*(lane / 16)
+        const __nv_bfloat16* pa = &sA[buf][(32 * wm + 16 * x + (lane & 15)) * OZ_LDS + kk + 8 * (lane >> 4)];
+        ldmatrix_x4(af[x][0], af[x][1], af[x][2], af[x][3], pa);
+      }
+      unsigned br[2][2], bi[2][2];
+#pragma unroll
+      for (int y = 0; y < 2; ++y) {
+        // columns 16*wn + 8*y + (lane % 8), k rows kk + 8*((lane / 8) % 2)
+        const int rowb = 16 * wn + 8 * y + (lane & 7);
+        const int kof = kk + 8 * ((lane >> 3) & 1);
+        ldmatrix_x2(br[y][0], br[y][1], &sBr[buf][rowb * OZ_LDS + kof]);
+        ldmatrix_x2(bi[y][0], bi[y][1], &sBi[buf][rowb * OZ_LDS + kof]);
+      }
+#pragma unroll
+      for (int x = 0; x < 2; ++x)
+#pragma unroll
+        for (int y = 0; y < 2; ++y) {
+          mma_bf16(fr[x][y], af[x], br[y]);
+          mma_bf16(fi[x][y], af[x], bi[y]);
+        }
+    }
+    const int t_done = ct;
+    advance(ct, cp, cks);
+    if (ct != t_done) {
+      // group t_done complete: fold its exact FP32 sums into the accumulators
+      if constexpr (INT) {
+        const long long step = 1ll << a.bits;
+#pragma unroll
+        for (int x = 0; x < 2; ++x)
+#pragma unroll
+          for (int y = 0; y < 2; ++y)
+#pragma unroll
+            for (int z = 0; z < 4; ++z) {
+              accr[x][y][z] = accr[x][y][z] * step + (long long)__float2int_rn(fr[x][y][z]);
+              acci[x][y][z] = acci[x][y][z] * step + (long long)__float2int_rn(fi[x][y][z]);
+            }
+      } else {
+        const double wgt = ldexp(1.0, -a.bits * t_done);
+#pragma unroll
+        for (int x = 0; x < 2; ++x)
+#pragma unroll
+          for (int y = 0; y < 2; ++y)
+#pragma unroll
+            for (int z = 0; z < 4; ++z) {
+              accr[x][y][z] = fma(wgt, (double)fr[x][y][z], accr[x][y][z]);
+              acci[x][y][z] = fma(wgt, (double)fi[x][y][z], acci[x][y][z]);
+            }
+      }
 #pragma unroll
       for (int x = 0; x < 2; ++x)
 #pragma unroll
         for (int y = 0; y < 2; ++y)
 #pragma unroll
-          for (int z = 0; z < 4; ++z) {
-            accr[x][y][z] = accr[x][y][z] * step + (long long)__float2int_rn(fr[x][y][z]);
-            acci[x][y][z] = acci[x][y][z] * step + (long long)__float2int_rn(fi[x][y][z]);
-          }
-    } else {
-      const double wgt = ldexp(1.0, -a.bits * t);
-#pragma unroll
-      for (int x = 0; x < 2; ++x)
-#pragma unroll
-        for (int y = 0; y < 2; ++y)
-#pragma unroll
-          for (int z = 0; z < 4; ++z) {
-            accr[x][y][z] = fma(wgt, (double)fr[x][y][z], accr[x][y][z]);
-            acci[x][y][z] = fma(wgt, (double)fi[x][y][z], acci[x][y][z]);
-          }
+          for (int z = 0; z < 4; ++z) { fr[x][y][z] = 0.f; fi[x][y][z] = 0.f; }
     }
   }
+  __syncthreads();
   // integer form: value = acc * 2^{-bits (S + 1)}
   const double wint = INT ? ldexp(1.0, -a.bits * (a.S + 1)) : 1.0;
   const bool plain = oz_plain(a);
