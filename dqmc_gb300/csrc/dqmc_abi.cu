@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <thread>
 #include <utility>
@@ -75,10 +76,16 @@ struct dqmc_handle {
   LUWork lu{};                // LU of the D-scale separated calculate_greens
   LUPanel lup{};              // blocked LU: pivots and per-step candidate copies
   double* lu_scales = nullptr;   // (4n) 1/max(Dl,1), min(Dl,1), 1/max(Dr,1), min(Dr,1)
-  cplx* wy_v = nullptr;       // mixed form: (n x kWyBlock) reflector block
-  cplx* wy_s = nullptr;       // (kWyBlock^2) Vb^H Vb
-  cplx* wy_z = nullptr;       // (kWyBlock x n) T Vb^H W
-  cplx* wy_t = nullptr;       // (kWyBlock) tau of the block
+  // block sizes of the mixed-form factorisations and the LU panel grid
+  // (DQMC_TUNE="wy=128,trsm=64,lu_grid=64" overrides; lu_grid 0 = one CTA per
+  // SM).  Defaults measured at L=16 on GB300: WY 32/64/128 -> 213/128/102 ms
+  // per sweep, triangular solves 32/64/128 -> 119/97/107 ms, LU panel grid
+  // 32/64/152 -> 186/184/194 ms.
+  int wy_block = 128, trsm_block = 64, lu_grid = 64;
+  cplx* wy_v = nullptr;       // mixed form: (n x kWyMax) reflector block
+  cplx* wy_s = nullptr;       // (kWyMax^2) Vb^H Vb
+  cplx* wy_z = nullptr;       // (kWyMax x n) T Vb^H W
+  cplx* wy_t = nullptr;       // (kWyMax) tau of the block
   double* force_d = nullptr;   // (3, N, M) d log|det M| / d phi
   // global updates: backup of stack, G, field and interaction table (allocated on first use)
   cplx *gb_u = nullptr, *gb_t = nullptr, *gb_G = nullptr;
@@ -322,13 +329,13 @@ int permute(dqmc_handle* h, const cplx* src, cplx* dst, const int* order, bool b
 }
 
 // Q = H_0 ... H_{n-1} formed explicitly from the reflectors of the last qrp
-// in compact-WY blocks of kWyBlock reflectors, backward (W <- B_j W, B_j =
+// in compact-WY blocks of h->wy_block reflectors, backward (W <- B_j W, B_j =
 // I - V_j T_j V_j^H, T_j^-1 = diag(1/tau) + striu(V_j^H V_j)), the products as
 // split-BF16 GEMMs (mixed form).  Before step j, W differs from I only in
 // rows and columns >= (j+1) b, so every product acts on W[jb:, jb:].
-constexpr int kWyBlock = 64;
+constexpr int kWyMax = 128;   // largest compact-WY block (buffer sizes; k_trsm_diag_block limit)
 int form_q_wy(dqmc_handle* h, cplx* W) {
-  const int n = h->n, b = kWyBlock;
+  const int n = h->n, b = h->wy_block;
   CHK(set_identity(h, W));
   for (int jb = ((n - 1) / b) * b; jb >= 0; jb -= b) {
     const int m = n - jb, bs = m < b ? m : b;
@@ -421,13 +428,12 @@ int calculate_greens_two_qr(dqmc_handle* h, cplx* out) {
   return DQMC_OK;
 }
 
-// Y <- T^-1 Y (n x n) in blocks of kTrsmBlock rows: FP64 solves of the
+// Y <- T^-1 Y (n x n) in blocks of h->trsm_block rows: FP64 solves of the
 // diagonal blocks, the off-diagonal updates as split-BF16 GEMMs.  lower: T
 // unit lower triangular (strict lower part), forward; else upper with the
 // reciprocal diagonal rdiag, backward.
-constexpr int kTrsmBlock = 64;
 int trsm_blocked(dqmc_handle* h, const cplx* T, const cplx* rdiag, cplx* Y, bool lower) {
-  const int n = h->n, b = kTrsmBlock;
+  const int n = h->n, b = h->trsm_block;
   const int nb = (n + b - 1) / b;
   for (int t = 0; t < nb; ++t) {
     const int blk = lower ? t : nb - 1 - t;
@@ -457,8 +463,10 @@ int lu_blocked(dqmc_handle* h, cplx* A) {
   for (int p0 = 0; p0 < n; p0 += LU_PB) {
     const int b = n - p0 < LU_PB ? n - p0 : LU_PB;
     const int m = n - p0 - b;
+    int lu_cap = h->coop_cap;
+    if (h->lu_grid > 0 && (lu_cap == 0 || h->lu_grid < lu_cap)) lu_cap = h->lu_grid;
     LAUNCH(DQMC_K_LU, 8.0 * (n - p0) * b * b / 2.0, 32.0 * (n - p0) * b,
-           launch_lu_panel(A, n, p0, b, h->lup, h->sm_count, h->st, h->coop_cap));
+           launch_lu_panel(A, n, p0, b, h->lup, h->sm_count, h->st, lu_cap));
     LAUNCH(DQMC_K_LU, 0.0, 64.0 * b * n, launch_lu_apply_swaps(A, n, p0, b, h->lup.piv, h->lu.perm, h->st));
     if (m > 0) {
       LAUNCH(DQMC_K_LU, 4.0 * b * b * m, 32.0 * b * m,
@@ -852,6 +860,12 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
   if (p->device >= 0 && cudaSetDevice(p->device) != cudaSuccess) return DQMC_ERR_CUDA;
   dqmc_handle* h = new dqmc_handle();
   h->p = *p;
+  if (const char* tune = std::getenv("DQMC_TUNE")) {
+    int v = 0;
+    if (const char* q = std::strstr(tune, "wy=")) if (std::sscanf(q + 3, "%d", &v) == 1 && v >= 16 && v <= kWyMax) h->wy_block = v;
+    if (const char* q = std::strstr(tune, "trsm=")) if (std::sscanf(q + 5, "%d", &v) == 1 && v >= 16 && v <= 128) h->trsm_block = v;
+    if (const char* q = std::strstr(tune, "lu_grid=")) if (std::sscanf(q + 8, "%d", &v) == 1 && v >= 0) h->lu_grid = v;
+  }
   h->L = p->L; h->N = p->L * p->L; h->n = 4 * h->N; h->M = p->slices; h->s = p->safe_mult;
   h->ne = h->M / h->s + 1;
   host_model_constants(h);
@@ -909,10 +923,10 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
     A((void**)&h->pub, (size_t)h->N * sizeof(int));
   }
   if (p->precision == DQMC_PREC_MIXED) {
-    A((void**)&h->wy_v, (size_t)n * kWyBlock * sizeof(cplx));
-    A((void**)&h->wy_s, (size_t)kWyBlock * kWyBlock * sizeof(cplx));
-    A((void**)&h->wy_z, (size_t)kWyBlock * n * sizeof(cplx));
-    A((void**)&h->wy_t, (size_t)kWyBlock * sizeof(cplx));
+    A((void**)&h->wy_v, (size_t)n * kWyMax * sizeof(cplx));
+    A((void**)&h->wy_s, (size_t)kWyMax * kWyMax * sizeof(cplx));
+    A((void**)&h->wy_z, (size_t)kWyMax * n * sizeof(cplx));
+    A((void**)&h->wy_t, (size_t)kWyMax * sizeof(cplx));
     h->oz_target = p->ozaki_bits > 0 ? p->ozaki_bits : 40;
     // the largest products are n x n x n; the flush (K = 4k) needs fewer slices
     int S = 0, bits = 0;
