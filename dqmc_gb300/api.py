@@ -92,6 +92,7 @@ SIGNATURES = {
     "dqmc_peak_fp64": ([_I32, _D], ctypes.c_int),
     "dqmc_gemm_check": ([_P, _I32, _D, _D, _D], ctypes.c_int),
     "dqmc_force": ([_P, _D, _D], ctypes.c_int),
+    "dqmc_measure_tdgfs": ([_P, _D, _D, _I32], ctypes.c_int),
     "dqmc_global_update": ([_P, _D, ctypes.c_double, ctypes.POINTER(_I32), _D], ctypes.c_int),
     "dqmc_batch_create": ([ctypes.POINTER(CParams), _I32, ctypes.POINTER(_P)], ctypes.c_int),
     "dqmc_batch_destroy": ([_P], ctypes.c_int),
@@ -426,6 +427,17 @@ class DQMC:
         self._check(self.lib.dqmc_gemm_check(self.h, int(mode), A.ctypes.data_as(_D), B.ctypes.data_as(_D),
                                              C.ctypes.data_as(_D)))
         return C
+
+    def measure_tdgfs(self):
+        """measure_tdgfs! (src/fermion_measurements.jl:1343-1403): time-displaced
+        Green's functions of the current field as two (M, n, n) arrays,
+        Gt0[tau-1] = G(tau, 0) and G0t[tau-1] = -G(0, tau)."""
+        M, n = self.M, self.n
+        gt0 = np.empty((M, n, n), dtype=np.complex128)
+        g0t = np.empty((M, n, n), dtype=np.complex128)
+        self._check(self.lib.dqmc_measure_tdgfs(self.h, gt0.ctypes.data_as(_D), g0t.ctypes.data_as(_D), 0))
+        # each slice's matrix is column-major
+        return gt0.transpose(0, 2, 1), g0t.transpose(0, 2, 1)
 
     def timing(self):
         """Per kernel kind: device ms, launches, algorithmic flops and bytes."""

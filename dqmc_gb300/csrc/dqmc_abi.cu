@@ -842,6 +842,224 @@ void fill_model_const(const dqmc_params& p, ModelConst& m) {
 // ===========================================================================
 // C ABI
 // ===========================================================================
+// ---- time-displaced Green's functions (src/fermion_measurements.jl:1343-1523) ----
+namespace tdgf {
+
+// Work matrices of one measurement (allocated per call).
+struct Work {
+  cplx* m[8] = {};            // n x n temporaries
+  double* v[4] = {};          // n vectors
+  double* s4 = nullptr;       // (4n) split scales
+  double* neg = nullptr;      // (n) -1
+};
+
+// X <- A^-1 X: LU with partial pivoting of a copy of A, then P, L^-1, U^-1.
+int solve_left(dqmc_handle* h, const cplx* A, cplx* X, cplx* wa, cplx* wb) {
+  const int n = h->n;
+  CHK(copy_nn(h, wa, A));
+  CHK(lu_blocked(h, wa));
+  CHK(permute(h, X, wb, h->lu.perm, true, false));
+  if (h->p.precision == DQMC_PREC_MIXED) {
+    CHK(trsm_blocked(h, wa, nullptr, wb, true));
+    CHK(trsm_blocked(h, wa, h->lu.rdiag, wb, false));
+  } else {
+    LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_lower_unit(wa, wb, n, n, h->st));
+    LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_upper(wa, nullptr, h->lu.rdiag, wb, n, n, h->st));
+  }
+  return copy_nn(h, X, wb);
+}
+
+int scale(dqmc_handle* h, cplx* A, const double* rs, bool inv_r, const double* cs, bool inv_c) {
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_scale(A, h->n, h->n, rs, inv_r, cs, inv_c, h->st));
+  return DQMC_OK;
+}
+int ctrans(dqmc_handle* h, const cplx* A, cplx* B) {
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_conj_transpose(A, B, h->n, h->st));
+  return DQMC_OK;
+}
+int diag_of(dqmc_handle* h, cplx* X, const double* d, bool inv) {   // X = diag(d) or diag(1/d)
+  CHK(set_identity(h, X));
+  return scale(h, X, d, inv, nullptr, false);
+}
+
+// calc_Bchain_udts! (src/fermion_measurements.jl:1411-1488) into us/ds/ts
+// (nr entries each, in the reference's order after its reverse for RIGHT).
+int bchain_udts(dqmc_handle* h, Work& w, bool invert, bool right, cplx* us, double* ds, cplx* ts) {
+  const int n = h->n, s = h->s, nr = h->M / h->s;
+  const size_t nn = (size_t)n * n;
+  const bool rightmult = (right && !invert) || (!right && invert);
+  const int mode = !invert ? (right ? SLICE_RIGHT_B : SLICE_LEFT_B) : (right ? SLICE_LEFT_BINV : SLICE_RIGHT_BINV);
+  const bool rows = mode == SLICE_RIGHT_B || mode == SLICE_RIGHT_BINV;
+  cplx* cur = w.m[0];
+  cplx* tmp = w.m[1];
+  for (int i = 0; i < nr; ++i) {
+    const int ridx = right ? nr - 1 - i : i;          // range processed
+    const int pos = right ? nr - 1 - i : i;           // slot after the reverse
+    const int prev = right ? pos + 1 : pos - 1;
+    if (i == 0) CHK(set_identity(h, cur));
+    else CHK(copy_nn(h, cur, rightmult ? ts + (size_t)prev * nn : us + (size_t)prev * nn));
+    const int first0 = right ? (ridx + 1) * s - 1 : ridx * s, step = right ? -1 : 1;
+    if (rows) CHK(apply_rows(h, cur, first0, s, step, mode));
+    else CHK(apply_cols(h, cur, first0, s, step, mode, nullptr));
+    if (i != 0) {
+      const double* dp = ds + (size_t)prev * n;
+      CHK(rightmult ? scale(h, cur, dp, false, nullptr, false) : scale(h, cur, nullptr, false, dp, false));
+    }
+    cplx* u = us + (size_t)pos * nn;
+    cplx* t = ts + (size_t)pos * nn;
+    double* d = ds + (size_t)pos * n;
+    if (!rightmult) {
+      CHK(decompose_udt(h, cur, u, d, tmp));
+      if (i == 0) CHK(copy_nn(h, t, tmp));
+      else CHK(gemm(h, 'N', 'N', tmp, ts + (size_t)prev * nn, t));
+    } else {
+      CHK(decompose_udt(h, cur, tmp, d, t));
+      if (i == 0) CHK(copy_nn(h, u, tmp));
+      else CHK(gemm(h, 'N', 'N', us + (size_t)prev * nn, tmp, u));
+    }
+  }
+  return DQMC_OK;
+}
+
+// inv_one_plus_udt_scalettar! (src/linalg.jl:310-339): res = [1 + U D T]^-1
+int inv_one_plus_udt(dqmc_handle* h, Work& w, const cplx* U, const double* D, const cplx* T, cplx* res) {
+  const int n = h->n;
+  cplx *l = w.m[2], *r = w.m[3], *u = w.m[4], *t = w.m[5], *wa = w.m[6], *wb = w.m[7];
+  double* s = w.s4;   // [1/max(D,1), min(D,1), ...]
+  double* d = w.v[0];
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n, launch_split_scales(D, D, n, s, h->st));
+  CHK(diag_of(h, l, s, false));                       // l = T \ Diagonal(1/Dp)
+  CHK(solve_left(h, T, l, wa, wb));
+  CHK(copy_nn(h, r, U));                              // r = U Diagonal(Dm) + l
+  CHK(scale(h, r, nullptr, false, s + n, false));
+  LAUNCH(DQMC_K_MISC, 0.0, 48.0 * n2(h), launch_add(r, l, r, (size_t)n * n, h->st));
+  CHK(decompose_udt(h, r, u, d, t));                  // r = u d t
+  CHK(diag_of(h, r, d, true));                        // r = t \ Diagonal(1/d)
+  CHK(solve_left(h, t, r, wa, wb));
+  CHK(gemm(h, 'N', 'C', r, u, l));                    // l = r u'
+  CHK(scale(h, l, s, false, nullptr, false));         // l = Diagonal(1/Dp) l
+  CHK(decompose_udt(h, l, u, d, t));                  // l = u d t
+  CHK(copy_nn(h, l, u));                              // l = T \ u
+  CHK(solve_left(h, T, l, wa, wb));
+  CHK(scale(h, l, nullptr, false, d, false));         // l = l Diagonal(d)
+  return gemm(h, 'N', 'N', l, t, res);                // res = l t
+}
+
+// inv_sum_udts_scalettar! (src/linalg.jl:512-567): res = [Ua Da Ta + Ub Db Tb]^-1
+int inv_sum_udts(dqmc_handle* h, Work& w, const cplx* Ua, const double* Da, const cplx* Ta, const cplx* Ub,
+                 const double* Db, const cplx* Tb, cplx* res) {
+  const int n = h->n;
+  cplx *m1 = w.m[2], *m2 = w.m[3], *u = w.m[4], *t = w.m[5], *wa = w.m[6], *wb = w.m[7];
+  double* s = w.s4;   // [1/Dap, Dam, 1/Dbp, Dbm]
+  double* d = w.v[0];
+  LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n, launch_split_scales(Da, Db, n, s, h->st));
+  // mat1 = Ta / Tb = (Tb' \ Ta')'
+  CHK(ctrans(h, Ta, m2));
+  CHK(ctrans(h, Tb, u));
+  CHK(solve_left(h, u, m2, wa, wb));
+  CHK(ctrans(h, m2, m1));
+  CHK(scale(h, m1, s + n, false, s + 2 * n, false));  // Dam[j] / Dbp[k]
+  // mat2 = Diagonal(1/Dap) Ua' Ub Diagonal(Dbm); mat1 += mat2
+  CHK(zgemm_general(h, n, n, n, 'C', 'N', cmake(1, 0), Ua, n, Ub, n, cmake(0, 0), m2, n, s, s + 3 * n, true));
+  LAUNCH(DQMC_K_MISC, 0.0, 48.0 * n2(h), launch_add(m1, m2, m1, (size_t)n * n, h->st));
+  CHK(decompose_udt(h, m1, u, d, t));                 // mat1 = U D T
+  CHK(scale(h, t, d, false, nullptr, false));         // T = Diagonal(D) T
+  CHK(ctrans(h, u, m1));                              // mat1 = T \ U'
+  CHK(solve_left(h, t, m1, wa, wb));
+  CHK(scale(h, m1, s + 2 * n, false, s, false));      // mat1 / Dbp[j] / Dap[k]
+  CHK(decompose_udt(h, m1, u, d, t));                 // mat1 = U D T
+  CHK(copy_nn(h, m1, u));                             // mat1 = Tb \ U
+  CHK(solve_left(h, Tb, m1, wa, wb));
+  CHK(gemm(h, 'N', 'C', t, Ua, m2));                  // mat2 = T Ua'
+  CHK(scale(h, m1, nullptr, false, d, false));        // res = (mat1 Diagonal(D)) mat2
+  return gemm(h, 'N', 'N', m1, m2, res);
+}
+
+int effective_to_true(dqmc_handle* h, cplx* G) {
+  CHK(apply_rows(h, G, 0, 1, 1, SLICE_EFF_RIGHT));
+  return apply_cols(h, G, 0, 1, 1, SLICE_EFF_LEFT_INV, nullptr);
+}
+
+// measure_tdgfs! (src/fermion_measurements.jl:1343-1403) into device arrays
+// Gt0 and G0t of M n x n matrices (slice tau at offset (tau-1) n^2).
+int measure(dqmc_handle* h, cplx* Gt0, cplx* G0t) {
+  const int n = h->n, s = h->s, M = h->M, nr = M / s;
+  const size_t nn = (size_t)n * n;
+  Work w;
+  std::vector<void*> owned;
+  auto alloc = [&](void** p, size_t bytes) -> int {
+    if (cudaMalloc(p, bytes) != cudaSuccess) return DQMC_ERR_CUDA;
+    owned.push_back(*p);
+    return DQMC_OK;
+  };
+  int rc = DQMC_OK;
+  cplx* st_u[4] = {}; cplx* st_t[4] = {}; double* st_d[4] = {};
+  for (int k = 0; k < 8 && rc == DQMC_OK; ++k) rc = alloc((void**)&w.m[k], nn * sizeof(cplx));
+  for (int k = 0; k < 4 && rc == DQMC_OK; ++k) rc = alloc((void**)&w.v[k], n * sizeof(double));
+  if (rc == DQMC_OK) rc = alloc((void**)&w.s4, 4 * n * sizeof(double));
+  if (rc == DQMC_OK) rc = alloc((void**)&w.neg, n * sizeof(double));
+  for (int k = 0; k < 4 && rc == DQMC_OK; ++k) {
+    rc = alloc((void**)&st_u[k], nr * nn * sizeof(cplx));
+    if (rc == DQMC_OK) rc = alloc((void**)&st_t[k], nr * nn * sizeof(cplx));
+    if (rc == DQMC_OK) rc = alloc((void**)&st_d[k], (size_t)nr * n * sizeof(double));
+  }
+  auto body = [&]() -> int {
+    // stacks: 0 = B(tau,1)^-1 (LEFT, inverse), 1 = B(beta,tau) (RIGHT), 2 = B(tau,1) (LEFT), 3 = B(beta,tau)^-1 (RIGHT, inverse)
+    CHK(bchain_udts(h, w, true, false, st_u[0], st_d[0], st_t[0]));
+    CHK(bchain_udts(h, w, false, true, st_u[1], st_d[1], st_t[1]));
+    CHK(bchain_udts(h, w, false, false, st_u[2], st_d[2], st_t[2]));
+    CHK(bchain_udts(h, w, true, true, st_u[3], st_d[3], st_t[3]));
+    auto U = [&](int k, int i) { return st_u[k] + (size_t)i * nn; };
+    auto T = [&](int k, int i) { return st_t[k] + (size_t)i * nn; };
+    auto D = [&](int k, int i) { return st_d[k] + (size_t)i * n; };
+    for (int i = 0; i < nr; ++i) {
+      const int tau = 1 + i * s;
+      cplx* g1 = Gt0 + (size_t)(tau - 1) * nn;
+      cplx* g2 = G0t + (size_t)(tau - 1) * nn;
+      if (i != 0) {
+        CHK(inv_sum_udts(h, w, U(0, i - 1), D(0, i - 1), T(0, i - 1), U(1, i), D(1, i), T(1, i), g1));
+        CHK(inv_sum_udts(h, w, U(2, i - 1), D(2, i - 1), T(2, i - 1), U(3, i), D(3, i), T(3, i), g2));
+      } else {
+        CHK(inv_one_plus_udt(h, w, U(1, 0), D(1, 0), T(1, 0), g1));
+        CHK(inv_one_plus_udt(h, w, U(3, 0), D(3, 0), T(3, 0), g2));
+      }
+      CHK(effective_to_true(h, g1));
+      CHK(effective_to_true(h, g2));
+    }
+    // fill_tdgf! (src/fermion_measurements.jl:1497-1523)
+    const int Mhalf = M / 2 + 1;
+    for (int tau = Mhalf; tau <= M; ++tau) {
+      if ((tau - 1) % s == 0) continue;
+      cplx* a = Gt0 + (size_t)(tau - 1) * nn;
+      cplx* b = G0t + (size_t)(tau - 1) * nn;
+      CHK(copy_nn(h, a, a - nn));
+      CHK(apply_cols(h, a, tau - 1, 1, 1, SLICE_LEFT_B, nullptr));
+      CHK(copy_nn(h, b, b - nn));
+      CHK(apply_rows(h, b, tau - 1, 1, 1, SLICE_RIGHT_BINV));
+    }
+    for (int tau = Mhalf - 1; tau >= 1; --tau) {
+      if ((tau - 1) % s == 0) continue;
+      cplx* a = Gt0 + (size_t)(tau - 1) * nn;
+      cplx* b = G0t + (size_t)(tau - 1) * nn;
+      CHK(copy_nn(h, a, a + nn));
+      CHK(apply_cols(h, a, tau, 1, 1, SLICE_LEFT_BINV, nullptr));
+      CHK(copy_nn(h, b, b + nn));
+      CHK(apply_rows(h, b, tau, 1, 1, SLICE_RIGHT_B));
+    }
+    // G0t *= -1
+    LAUNCH(DQMC_K_MISC, 0.0, 8.0 * n, launch_fill(w.neg, n, -1.0, h->st));
+    LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h) * M,
+           launch_scale(G0t, n, (int)((size_t)n * M), w.neg, false, nullptr, false, h->st));
+    return DQMC_OK;
+  };
+  if (rc == DQMC_OK) rc = body();
+  cudaStreamSynchronize(h->st);
+  for (void* q : owned) cudaFree(q);
+  return rc;
+}
+
+}  // namespace tdgf
+
 extern "C" {
 
 const char* dqmc_version(void) { return DQMC_VERSION_STRING; }
@@ -1613,6 +1831,27 @@ int dqmc_reset_timing(dqmc_handle* h, int32_t enable) {
   h->launches = 0;
   h->timing = enable != 0;
   return DQMC_OK;
+}
+
+int dqmc_measure_tdgfs(dqmc_handle* h, double* Gt0, double* G0t, int32_t device_ptrs) {
+  if (h) cudaSetDevice(h->device);
+  if (!h || !Gt0 || !G0t) return DQMC_ERR_ARG;
+  if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
+  const size_t bytes = (size_t)h->M * h->n * h->n * sizeof(cplx);
+  if (device_ptrs) {
+    CHK(tdgf::measure(h, reinterpret_cast<cplx*>(Gt0), reinterpret_cast<cplx*>(G0t)));
+    return sync(h);
+  }
+  cplx *a = nullptr, *b = nullptr;
+  CU(cudaMalloc(&a, bytes));
+  if (cudaMalloc(&b, bytes) != cudaSuccess) { cudaFree(a); return set_err(h, DQMC_ERR_CUDA, "out of device memory"); }
+  int rc = tdgf::measure(h, a, b);
+  if (rc == DQMC_OK && cudaMemcpy(Gt0, a, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) rc = DQMC_ERR_CUDA;
+  if (rc == DQMC_OK && cudaMemcpy(G0t, b, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) rc = DQMC_ERR_CUDA;
+  cudaFree(a);
+  cudaFree(b);
+  if (rc != DQMC_OK) return rc;
+  return sync(h);
 }
 
 }  // extern "C"

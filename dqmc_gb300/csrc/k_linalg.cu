@@ -615,6 +615,12 @@ __global__ void k_lu_diag(const cplx* __restrict__ A, int n, cplx* __restrict__ 
   }
 }
 
+// C = A + B over count complex entries
+__global__ void k_add(const cplx* __restrict__ A, const cplx* __restrict__ B, cplx* __restrict__ C, size_t count) {
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
+    C[e] = cadd(A[e], B[e]);
+}
+
 __global__ void k_iota(int* __restrict__ p, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = i;
 }
@@ -1057,6 +1063,11 @@ cudaError_t launch_lu_apply_swaps(cplx* A, int n, int p0, int b, const int* piv,
 
 cudaError_t launch_lu_diag(const cplx* A, int n, cplx* udiag, cplx* rdiag, cudaStream_t st) {
   k_lu_diag<<<(n + 255) / 256, 256, 0, st>>>(A, n, udiag, rdiag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_add(const cplx* A, const cplx* B, cplx* C, size_t count, cudaStream_t st) {
+  k_add<<<grid_for(count), 256, 0, st>>>(A, B, C, count);
   return cudaGetLastError();
 }
 

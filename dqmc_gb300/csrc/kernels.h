@@ -144,6 +144,8 @@ cudaError_t launch_lu_panel(cplx* A, int n, int p0, int b, LUPanel& w, int sm_co
 cudaError_t launch_lu_apply_swaps(cplx* A, int n, int p0, int b, const int* piv, int* perm, cudaStream_t st);
 cudaError_t launch_lu_diag(const cplx* A, int n, cplx* udiag, cplx* rdiag, cudaStream_t st);
 cudaError_t launch_iota(int* p, int n, cudaStream_t st);
+// C = A + B (count complex entries)
+cudaError_t launch_add(const cplx* A, const cplx* B, cplx* C, size_t count, cudaStream_t st);
 // D-scale separation: s = [1/max(Dl,1), min(Dl,1), 1/max(Dr,1), min(Dr,1)] (4n)
 cudaError_t launch_split_scales(const double* Dl, const double* Dr, int n, double* s, cudaStream_t st);
 // out[0] = sum log|udiag| + sum log max(Dl,1) + sum log max(Dr,1)

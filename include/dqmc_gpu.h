@@ -253,6 +253,14 @@ DQMC_API int dqmc_global_update(dqmc_handle* h, const double* shift, double u, i
  * one down pass, after which the state returns to (slice M, direction -1).
  * Needs the state (M, -1), i.e. right after dqmc_init or after 2M updates.
  * No counterpart in the reference; either output may be NULL. */
+/* measure_tdgfs! (src/fermion_measurements.jl:1343-1403, with calc_Bchain_udts! :1411-1488,
+ * fill_tdgf! :1497-1523, inv_sum_udts_scalettar! and inv_one_plus_udt_scalettar!
+ * src/linalg.jl:310-339, 512-567): the time-displaced Green's functions Gt0[tau] = G(tau, 0)
+ * and G0t[tau] = -G(0, tau) of the current field for tau = 1..M, each n x n column-major
+ * complex at offset (tau - 1) n^2 (2 M n^2 doubles per array).  device_ptrs != 0: Gt0 and
+ * G0t are device addresses on the handle's device; otherwise host buffers. */
+DQMC_API int dqmc_measure_tdgfs(dqmc_handle* h, double* Gt0, double* G0t, int32_t device_ptrs);
+
 DQMC_API int dqmc_force(dqmc_handle* h, double* grad_logdet, double* grad_boson);
 
 /* ---- diagnostics ------------------------------------------------------------- */

@@ -349,6 +349,42 @@ def greens_from_udts(Ul, Dl, Tl, Ur, Dr, Tr):
     return G, logdet
 
 
+def inv_one_plus_udt_scalettar(U, D, T):
+    """[1 + U D T]^-1 with the scales separated (src/linalg.jl:310-339)."""
+    Dp = np.maximum(D, 1.0)
+    Dm = np.minimum(D, 1.0)
+    Dpinv = 1.0 / Dp
+    l = sla.solve(T, np.diag(Dpinv).astype(np.complex128))     # T \ Diagonal(Dpinv)
+    r = U * Dm[None, :] + l
+    u, d, t = decompose_udt(r)
+    r = sla.solve(t, np.diag(1.0 / d).astype(np.complex128))     # t \ Diagonal(1/d)
+    l = r @ u.conj().T
+    l = Dpinv[:, None] * l
+    u, d, t = decompose_udt(l)
+    l = sla.solve(T, u)
+    l = l * d[None, :]
+    return l @ t
+
+
+def inv_sum_udts_scalettar(Ua, Da, Ta, Ub, Db, Tb):
+    """[Ua Da Ta + Ub Db Tb]^-1 with the scales separated (src/linalg.jl:512-567)."""
+    Dap, Dam = np.maximum(Da, 1.0), np.minimum(Da, 1.0)
+    Dbp, Dbm = np.maximum(Db, 1.0), np.minimum(Db, 1.0)
+    mat1 = sla.solve(Tb.T, Ta.T).T                              # Ta / Tb
+    mat1 = mat1 * (Dam[:, None] / Dbp[None, :])
+    mat2 = Ua.conj().T @ Ub
+    mat2 = mat2 * (Dbm[None, :] / Dap[:, None])
+    mat1 = mat1 + mat2
+    U, D, T = decompose_udt(mat1)
+    T = D[:, None] * T
+    mat1 = sla.solve(T, U.conj().T)                              # T \ U'
+    mat1 = mat1 / Dbp[:, None] / Dap[None, :]
+    U, D, T = decompose_udt(mat1)
+    mat1 = sla.solve(Tb, U)
+    mat2 = T @ Ua.conj().T
+    return (mat1 * D[None, :]) @ mat2
+
+
 def _logdet(A):
     sign, ld = np.linalg.slogdet(A)
     return ld  # real part of log(det A)
@@ -734,6 +770,93 @@ class DQMCRef:
         (src/dqmc_framework.jl:378-381)."""
         g = self.wrap_greens(self.greens, self.current_slice, 1)
         return self.effective_greens2greens(g)
+
+    # ---- time-displaced Green's functions (src/fermion_measurements.jl:1343-1516) ----
+    def calc_Bchain_udts(self, invert, direction):
+        """calc_Bchain_udts! (src/fermion_measurements.jl:1411-1488): UDTs of
+        the B chains at the safe_mult ranges.  direction 'left': B(tau, 1) =
+        B(tau)...B(1) (invert: its inverse, accumulated from the right);
+        'right': B(beta, tau) = B(beta)...B(tau) (invert: its inverse,
+        accumulated from the left).  Lists indexed by range i (0-based), in the
+        reference's order after its final reverse for 'right'."""
+        s, M, n = self.p.safe_mult, self.M, self.n
+        ranges = [list(range(i * s + 1, (i + 1) * s + 1)) for i in range(M // s)]
+        rightmult = (direction == "right" and not invert) or (direction == "left" and invert)
+        order = list(range(len(ranges)))
+        if direction == "right":
+            order = order[::-1]
+        us, ds, ts = [], [], []
+        for i, ridx in enumerate(order):
+            if i == 0:
+                cur = np.eye(n, dtype=np.complex128)
+            else:
+                cur = (ts[i - 1] if rightmult else us[i - 1]).copy()
+            seq = ranges[ridx][::-1] if direction == "right" else ranges[ridx]
+            for sl in seq:
+                if not invert:
+                    if direction == "left":
+                        self.multiply_B_left(sl, cur)
+                    else:
+                        self.multiply_B_right(sl, cur)
+                else:
+                    if direction == "left":
+                        self.multiply_B_inv_right(sl, cur)
+                    else:
+                        self.multiply_B_inv_left(sl, cur)
+            if i != 0:
+                cur = ds[i - 1][:, None] * cur if rightmult else cur * ds[i - 1][None, :]
+            U, D, T = decompose_udt(cur)
+            if not rightmult:
+                us.append(U)
+                ts.append(T if i == 0 else T @ ts[i - 1])
+            else:
+                ts.append(T)
+                us.append(U if i == 0 else us[i - 1] @ U)
+            ds.append(D)
+        if direction == "right":
+            us.reverse(), ds.reverse(), ts.reverse()
+        return us, ds, ts
+
+    def fill_tdgf(self, Gt0, G0t):
+        """fill_tdgf! (src/fermion_measurements.jl:1497-1523): propagate from the
+        safe_mult slices to the others; Gt0, G0t are lists indexed by slice-1."""
+        s, M = self.p.safe_mult, self.M
+        safe = set(range(1, M + 1, s))
+        Mhalf = M // 2 + 1
+        for tau in range(Mhalf, M + 1):
+            if tau in safe:
+                continue
+            Gt0[tau - 1] = self.multiply_B_left(tau, Gt0[tau - 2].copy())
+            G0t[tau - 1] = self.multiply_B_inv_right(tau, G0t[tau - 2].copy())
+        for tau in range(Mhalf - 1, 0, -1):
+            if tau in safe:
+                continue
+            Gt0[tau - 1] = self.multiply_B_inv_left(tau + 1, Gt0[tau].copy())
+            G0t[tau - 1] = self.multiply_B_right(tau + 1, G0t[tau].copy())
+
+    def measure_tdgfs(self):
+        """measure_tdgfs! (src/fermion_measurements.jl:1343-1403): Gt0[tau] and
+        G0t[tau] (tau = 1..M, returned as (M, n, n) arrays) for the current field."""
+        s, M = self.p.safe_mult, self.M
+        BT0Inv = self.calc_Bchain_udts(True, "left")
+        BBetaT = self.calc_Bchain_udts(False, "right")
+        BT0 = self.calc_Bchain_udts(False, "left")
+        BBetaTInv = self.calc_Bchain_udts(True, "right")
+        Gt0 = [None] * M
+        G0t = [None] * M
+        for i, tau in enumerate(range(1, M + 1, s)):
+            if i != 0:
+                g1 = inv_sum_udts_scalettar(BT0Inv[0][i - 1], BT0Inv[1][i - 1], BT0Inv[2][i - 1],
+                                            BBetaT[0][i], BBetaT[1][i], BBetaT[2][i])
+                g2 = inv_sum_udts_scalettar(BT0[0][i - 1], BT0[1][i - 1], BT0[2][i - 1],
+                                            BBetaTInv[0][i], BBetaTInv[1][i], BBetaTInv[2][i])
+            else:
+                g1 = inv_one_plus_udt_scalettar(BBetaT[0][0], BBetaT[1][0], BBetaT[2][0])
+                g2 = inv_one_plus_udt_scalettar(BBetaTInv[0][0], BBetaTInv[1][0], BBetaTInv[2][0])
+            Gt0[tau - 1] = self.effective_greens2greens(g1)
+            G0t[tau - 1] = self.effective_greens2greens(g2)
+        self.fill_tdgf(Gt0, G0t)
+        return np.array(Gt0), -np.array(G0t)
 
     def kinetic_energy(self, G_true):
         """E_kin = sum_ij T_ij <c_i^dag c_j> with <c_i^dag c_j> = delta_ij - G_ji.

@@ -409,3 +409,22 @@ def test_batch_matches_single_chains(lib):
         assert np.array_equal(batch.chains[k].get_field(), single.get_field())
         single.close()
     batch.close()
+
+
+@pytest.mark.parametrize("cfg,prec", [("small", "fp64"), ("c0", "fp64"), ("c0", "mixed")])
+def test_time_displaced_greens(lib, golden, small_params, cfg, prec):
+    """measure_tdgfs! (time-displaced G(tau, 0) and -G(0, tau) for every slice)
+    against the oracle's restatement; mixed form within 1e-8."""
+    p = dataclasses.replace(small_params, slices=20, safe_mult=5) if cfg == "small" else C0
+    phi = R.synthetic_field(p.N, p.slices, 41)
+    ref = R.DQMCRef(p, phi)
+    gt0_r, g0t_r = ref.measure_tdgfs()
+    mp = api_params(p)
+    mp.precision = prec
+    gpu = lib.DQMC(mp, phi)
+    gpu.init()
+    gt0, g0t = gpu.measure_tdgfs()
+    tol = TOL if prec == "fp64" else 1e-8
+    for tau in range(p.slices):
+        assert relerr(gt0[tau], gt0_r[tau]) < tol, (tau, relerr(gt0[tau], gt0_r[tau]))
+        assert relerr(g0t[tau], g0t_r[tau]) < tol, (tau, relerr(g0t[tau], g0t_r[tau]))

@@ -125,3 +125,28 @@ def test_force_formula_matches_finite_differences(small_params):
         fd_boson = (vals[0][1] - vals[1][1]) / (2 * h)
         assert abs(gl[a, i, l] - fd_logdet) <= 1e-6 * max(1.0, abs(fd_logdet))
         assert abs(gb[a, i, l] - fd_boson) <= 1e-6 * max(1.0, abs(fd_boson))
+
+
+def test_time_displaced_greens_at_safe_slices(small_params):
+    """measure_tdgfs! at the safe_mult slices against the direct formulas
+    G(tau, 0) = B(tau-1, 1) G0 and G(0, tau) = -(1 - G0) B(tau-1, 1)^-1
+    (effective -> true), G0 = [1 + B(M, 1)]^-1 (src/fermion_measurements.jl:1343-1403,
+    calc_tdgf_direct :1527-1550)."""
+    p = dataclasses.replace(small_params, slices=20, safe_mult=5)
+    m = R.DQMCRef(p, R.synthetic_field(p.N, p.slices, 3))
+    Gt0, G0t = m.measure_tdgfs()
+    n = p.n
+    B = [m.slice_matrix(t) for t in range(1, p.slices + 1)]
+
+    def chain(a, b):
+        X = np.eye(n, dtype=complex)
+        for t in range(b, a + 1):
+            X = B[t - 1] @ X
+        return X
+
+    G0 = np.linalg.inv(np.eye(n) + chain(p.slices, 1))
+    for tau in range(1, p.slices + 1, p.safe_mult):
+        want = m.effective_greens2greens(chain(tau - 1, 1) @ G0)
+        assert np.max(np.abs(Gt0[tau - 1] - want)) < 1e-12
+        want0 = m.effective_greens2greens(-(np.eye(n) - G0) @ np.linalg.inv(chain(tau - 1, 1)))
+        assert np.max(np.abs(G0t[tau - 1] - want0)) < 1e-10 * max(1.0, np.max(np.abs(want0)))
