@@ -279,6 +279,51 @@ def measure_batch(args, world, rank, dev, warmup, steps, precision):
     return value, wall, clk, info, desc
 
 
+def measure_tdgf(args, dev):
+    """Time-displaced Green's functions (measure_tdgfs!) at L=10, beta=10
+    (M=100): device time of one GPU measurement per form (results in device
+    buffers), max relative difference mixed vs FP64, and the oracle on the
+    host cores for the same field."""
+    import ctypes
+    import torch
+    from dqmc_gb300 import api
+    from oracle import dqmc_ref as R
+    L, M = 10, 100
+    rp = model_params(L, M)
+    phi = R.synthetic_field(rp.N, M, 77)
+    n = rp.n
+    out = {"workload": f"O(3) L={L} beta=10 (M={M}): G(tau,0) and -G(0,tau) for all {M} slices"}
+    res = {}
+    for prec in ("fp64", "mixed"):
+        chain = _make_chain(api, L, M, rp, args, dev, prec, args.delay if prec == "mixed" else 1, phi)
+        a = torch.empty(M * n * n * 2, dtype=torch.float64, device=f"cuda:{dev}")
+        b = torch.empty_like(a)
+        def call():
+            chain._check(chain.lib.dqmc_measure_tdgfs(chain.h, ctypes.cast(a.data_ptr(), api._D),
+                                                      ctypes.cast(b.data_ptr(), api._D), 1))
+        call()   # warm-up (allocations, first launches)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        call()
+        torch.cuda.synchronize()
+        out[f"seconds_{prec}"] = time.perf_counter() - t0
+        res[prec] = (a.clone(), b.clone())
+        chain.close()
+    ga, gb = res["fp64"]
+    ma, mb = res["mixed"]
+    out["max_abs_diff_mixed_vs_fp64"] = float(max((ma - ga).abs().max(), (mb - gb).abs().max()))
+    if not args.no_cpu:
+        ref = R.DQMCRef(rp, phi)
+        t0 = time.perf_counter()
+        gt0, g0t = ref.measure_tdgfs()
+        out["seconds_cpu_oracle"] = time.perf_counter() - t0
+        out["cpu_threads"] = os.cpu_count() or 1
+        g = ga.view(M, n, n, 2)
+        gpu_gt0 = torch.complex(g[..., 0], g[..., 1]).transpose(1, 2).cpu().numpy()
+        out["max_abs_diff_fp64_vs_oracle"] = float(np.max(np.abs(gpu_gt0 - gt0)))
+    return out
+
+
 def run_batch(args, world, rank, local):
     """Config c2: 64 chains of uneven L swept concurrently (dqmc_batch_*);
     value = chain-sweeps/s of all chains."""
@@ -443,6 +488,10 @@ def run_ours(args, world, rank, local):
     hbm_gbs = by / (ms_top / 1000.0) / 1e9
     breakdown = {k: {"ms": round(v["ms"], 3), "launches": v["launches"], "share": round(v["ms"] / max(1e-9, tot_ms), 4)}
                  for k, v in kinds.items() if v["launches"]}
+    # time-displaced Green's functions (the measurement step after the sweep)
+    tdgf = None
+    if not args.no_batch and args.config == "c3" and rank == 0:
+        tdgf = measure_tdgf(args, dev)
     # the batched part of the metric: 64 chains of L in {6, 8, 10, 12} (config c2), mixed form
     batched = None
     if not args.no_batch and args.config == "c3":
@@ -501,6 +550,7 @@ def run_ours(args, world, rank, local):
             "clocks": clk,
             "cpu_baseline": cpu,
             "batched": batched,
+            "tdgf": tdgf,
         }
         print(json.dumps(line), flush=True)
     if batched is None:
