@@ -57,11 +57,14 @@ struct EvEntry { double C, Sr, Si, R; };
 
 // Cross-CTA barrier for cooperative (co-resident) grids, with a bounded spin.
 // On timeout it sets *err (bit 1) and returns false: the kernel must then
-// leave its loop and return; it never hangs the device.  The launcher zeroes
-// the counter before each launch.
+// leave its loop and return; it never hangs the device.  count holds the
+// arrivals of the launch, exits the CTAs that have left it; both start at
+// zero (zeroed at allocation) and the last CTA to leave zeroes them again
+// for the next launch on the stream (GridBarrierExit), so the launcher
+// needs no memset node per launch.
 struct GridBarrier {
   unsigned int count;
-  unsigned int gen;
+  unsigned int exits;
 };
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
@@ -95,6 +98,24 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier* b, int* err, unsigned&
   __syncthreads();
   return s_ok != 0;
 }
+
+// Declared at the top of a kernel that uses grid_barrier: its destructor runs
+// on every return path, after the CTA's last barrier; the last CTA out (all
+// others have stopped polling by then) zeroes the barrier.
+struct GridBarrierExit {
+  GridBarrier* b;
+  __device__ __forceinline__ explicit GridBarrierExit(GridBarrier* bar) : b(bar) {}
+  __device__ __forceinline__ ~GridBarrierExit() {
+    if (threadIdx.x == 0) {
+      __threadfence();
+      if (atomicAdd(&b->exits, 1u) == gridDim.x - 1) {
+        b->count = 0;
+        b->exits = 0;
+        __threadfence();
+      }
+    }
+  }
+};
 
 // Error bits reported by kernels through a device int.
 enum {

@@ -75,13 +75,17 @@ struct dqmc_handle {
   int greens_method = DQMC_GREENS_SCALES;
   LUWork lu{};                // LU of the D-scale separated calculate_greens
   LUPanel lup{};              // blocked LU: pivots and per-step candidate copies
+  cplx* lu_L = nullptr;       // (n x n) unit lower factor of the unblocked LU (strict lower part)
+  int* lu_pivrow = nullptr;   // (2) unblocked LU: next pivot row by step parity
   double* lu_scales = nullptr;   // (4n) 1/max(Dl,1), min(Dl,1), 1/max(Dr,1), min(Dr,1)
   // block sizes of the mixed-form factorisations and the LU panel grid
-  // (DQMC_TUNE="wy=128,trsm=64,lu_grid=64" overrides; lu_grid 0 = one CTA per
-  // SM).  Defaults measured at L=16 on GB300: WY 32/64/128 -> 213/128/102 ms
-  // per sweep, triangular solves 32/64/128 -> 119/97/107 ms, LU panel grid
-  // 32/64/152 -> 186/184/194 ms.
-  int wy_block = 128, trsm_block = 64, lu_grid = 64;
+  // (DQMC_TUNE="wy=128,trsm=64,lu_grid=64,lu_small=576" overrides; lu_grid 0
+  // = one CTA per SM; n <= lu_small takes the unblocked LU).  Defaults
+  // measured at L=16 on GB300: WY 32/64/128 -> 213/128/102 ms per sweep,
+  // triangular solves 32/64/128 -> 119/97/107 ms, LU panel grid 32/64/152 ->
+  // 186/184/194 ms; LU per sweep blocked/unblocked: n = 144 9.0/5.8 ms,
+  // n = 576 39.8/33.9 ms, n = 1024 184/232 ms.
+  int wy_block = 128, trsm_block = 64, lu_grid = 64, lu_small = 576;
   cplx* wy_v = nullptr;       // mixed form: (n x kWyMax) reflector block
   cplx* wy_s = nullptr;       // (kWyMax^2) Vb^H Vb
   cplx* wy_z = nullptr;       // (kWyMax x n) T Vb^H W
@@ -457,8 +461,17 @@ int trsm_blocked(dqmc_handle* h, const cplx* T, const cplx* rdiag, cplx* Y, bool
 // columns: panel factorisation with partial pivoting, the panel's row
 // exchanges on the other columns, U12 = L11^-1 A12, A22 -= L21 U12 (a GEMM,
 // split-BF16 in the mixed form).  lu.perm, lu.udiag, lu.rdiag on return.
-int lu_blocked(dqmc_handle* h, cplx* A) {
+// For n <= lu_small the unblocked cooperative LU runs instead (one launch;
+// L then in lu_L).  *Lm receives the matrix whose strict lower part is L.
+int lu_blocked(dqmc_handle* h, cplx* A, const cplx** Lm) {
   const int n = h->n;
+  if (n <= h->lu_small) {
+    LUKernel w{h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lu_pivrow, h->qr.bar, h->err_d};
+    LAUNCH(DQMC_K_LU, 8.0 * n3(h) / 3.0, 32.0 * n2(h), launch_lup(A, h->lu_L, n, w, h->sm_count, h->st, h->coop_cap));
+    *Lm = h->lu_L;
+    return DQMC_OK;
+  }
+  *Lm = A;
   LAUNCH(DQMC_K_LU, 0.0, 4.0 * n, launch_iota(h->lu.perm, n, h->st));
   for (int p0 = 0; p0 < n; p0 += LU_PB) {
     const int b = n - p0 < LU_PB ? n - p0 : LU_PB;
@@ -495,17 +508,18 @@ int calculate_greens_scales(dqmc_handle* h, cplx* out) {
   CHK(zgemm_general(h, n, n, n, 'N', 'C', cmake(1, 0), h->Tl, n, h->Tr, n, cmake(1, 0), h->W1, n, s + n, s + 3 * n,
                     true));
   // P M = L U in place in W1 (L strict lower, U upper; lu.udiag, lu.rdiag, lu.perm)
-  CHK(lu_blocked(h, h->W1));
+  const cplx* Lm = nullptr;
+  CHK(lu_blocked(h, h->W1, &Lm));
   // right-hand side P diag(1/Dlmax) Ul^dag
   LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_conj_transpose(h->Ul, h->W4, n, h->st));
   LAUNCH(DQMC_K_MISC, 0.0, 32.0 * n2(h), launch_scale(h->W4, n, n, s, false, nullptr, false, h->st));
   CHK(permute(h, h->W4, h->W3, h->lu.perm, true, false));
   // U^-1 L^-1 (.), then diag(1/Drmax)
   if (h->p.precision == DQMC_PREC_MIXED) {
-    CHK(trsm_blocked(h, h->W1, nullptr, h->W3, true));
+    CHK(trsm_blocked(h, Lm, nullptr, h->W3, true));
     CHK(trsm_blocked(h, h->W1, h->lu.rdiag, h->W3, false));
   } else {
-    LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_lower_unit(h->W1, h->W3, n, n, h->st));
+    LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_lower_unit(Lm, h->W3, n, n, h->st));
     LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_upper(h->W1, nullptr, h->lu.rdiag, h->W3, n, n,
                                                                            h->st));
   }
@@ -794,7 +808,7 @@ void free_all(dqmc_handle* h) {
                   h->Tr, h->Dl, h->Dr, h->W1, h->W2, h->W3, h->W4, h->D1, h->d2, h->ord1, h->qr.vn1,
                   h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->qr.cand_v, h->qr.cand_q, h->delta_d, h->unif_d,
                   h->acc_d, h->det_d, h->pacc_d, h->action_d, h->nacc_d, h->Acol, h->Brow, h->bar, h->err_d,
-                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lup.piv, h->lup.cand_rows, h->lup.rowk, h->lu_scales, h->wy_v, h->wy_s, h->wy_z, h->wy_t, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
+                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lup.piv, h->lup.cand_rows, h->lup.rowk, h->lu_L, h->lu_pivrow, h->lu_scales, h->wy_v, h->wy_s, h->wy_z, h->wy_t, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   clear_graphs(h);
@@ -857,13 +871,14 @@ struct Work {
 int solve_left(dqmc_handle* h, const cplx* A, cplx* X, cplx* wa, cplx* wb) {
   const int n = h->n;
   CHK(copy_nn(h, wa, A));
-  CHK(lu_blocked(h, wa));
+  const cplx* Lm = nullptr;
+  CHK(lu_blocked(h, wa, &Lm));
   CHK(permute(h, X, wb, h->lu.perm, true, false));
   if (h->p.precision == DQMC_PREC_MIXED) {
-    CHK(trsm_blocked(h, wa, nullptr, wb, true));
+    CHK(trsm_blocked(h, Lm, nullptr, wb, true));
     CHK(trsm_blocked(h, wa, h->lu.rdiag, wb, false));
   } else {
-    LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_lower_unit(wa, wb, n, n, h->st));
+    LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_lower_unit(Lm, wb, n, n, h->st));
     LAUNCH(DQMC_K_TRSM, 4.0 * n3(h), 40.0 * n2(h), launch_trsm_left_upper(wa, nullptr, h->lu.rdiag, wb, n, n, h->st));
   }
   return copy_nn(h, X, wb);
@@ -1083,6 +1098,7 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
     if (const char* q = std::strstr(tune, "wy=")) if (std::sscanf(q + 3, "%d", &v) == 1 && v >= 16 && v <= kWyMax) h->wy_block = v;
     if (const char* q = std::strstr(tune, "trsm=")) if (std::sscanf(q + 5, "%d", &v) == 1 && v >= 16 && v <= 128) h->trsm_block = v;
     if (const char* q = std::strstr(tune, "lu_grid=")) if (std::sscanf(q + 8, "%d", &v) == 1 && v >= 0) h->lu_grid = v;
+    if (const char* q = std::strstr(tune, "lu_small=")) if (std::sscanf(q + 9, "%d", &v) == 1 && v >= 0) h->lu_small = v;
   }
   h->L = p->L; h->N = p->L * p->L; h->n = 4 * h->N; h->M = p->slices; h->s = p->safe_mult;
   h->ne = h->M / h->s + 1;
@@ -1124,6 +1140,7 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
   A((void**)&h->lu.perm, n * sizeof(int)); A((void**)&h->lu.udiag, n * sizeof(cplx));
   A((void**)&h->lu.rdiag, n * sizeof(cplx));
   A((void**)&h->lu_scales, 4 * n * sizeof(double));
+  A((void**)&h->lu_L, n * n * sizeof(cplx)); A((void**)&h->lu_pivrow, 2 * sizeof(int));
   A((void**)&h->lup.piv, n * sizeof(int));
   A((void**)&h->lup.cand_rows, (size_t)1024 * LU_PB * sizeof(cplx));
   A((void**)&h->lup.rowk, (size_t)2 * LU_PB * sizeof(cplx));

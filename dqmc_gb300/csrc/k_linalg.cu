@@ -224,6 +224,7 @@ __device__ __forceinline__ double qr_finish_column(cplx (&x)[QR_MAXT], cplx* __r
 
 __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n, QRWork w) {
   unsigned bar_epoch = 0;
+  GridBarrierExit bar_exit(w.bar);
   extern __shared__ double smem_qr[];
   cplx* v = reinterpret_cast<cplx*>(smem_qr);         // (n) pivot column: a_k at k, unscaled x below
   int* order = reinterpret_cast<int*>(v + n);         // (n) logical -> physical
@@ -414,6 +415,118 @@ __global__ void k_wy_prep(const cplx* __restrict__ V, const cplx* __restrict__ t
   }
 }
 
+// Unblocked LU with partial pivoting (cooperative, one grid barrier per
+// column step), for small n where the blocked form's launches dominate:
+// P A = L U as LAPACK zgetf2 (pivot: first row of maximal |Re| + |Im|, as
+// izamax), rows exchanged physically in the trailing columns.  Column k of
+// A is read, never written, in step k: the multipliers go to Lb (strictly
+// lower part; earlier columns receive the same row exchanges) and the
+// diagonal of U to udiag, so the CTAs need no ordering among themselves
+// inside a step.  The owner of column k+1 publishes the next pivot row.
+__global__ void __launch_bounds__(QR_THREADS) k_lup(cplx* __restrict__ A, cplx* __restrict__ Lb, int n, LUKernel w) {
+  unsigned bar_epoch = 0;
+  GridBarrierExit bar_exit(w.bar);
+  extern __shared__ double smem_lu[];
+  cplx* v = reinterpret_cast<cplx*>(smem_lu);   // (n) column k after the row exchange (rows > k)
+  int* perm = reinterpret_cast<int*>(v + n);    // (n) position -> original row
+  __shared__ cplx s_rinv;
+  __shared__ int s_piv;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int warps = QR_THREADS / 32;
+  const int scal_warp = warps - 1;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) perm[q] = q;
+  if (blockIdx.x == 0 && wid == 0) {
+    double best = 0.0;
+    int row = n;
+    for (int r = lane; r < n; r += 32) {
+      const cplx x = A[r];
+      const double a = fabs(x.x) + fabs(x.y);
+      if (piv_better(a, r, best, row)) { best = a; row = r; }
+    }
+    warp_argmax(best, row);
+    if (lane == 0) w.pivrow[0] = row < n ? row : 0;
+  }
+  if (!grid_barrier(w.bar, w.err, bar_epoch)) return;
+
+  const int chunk = (n + gridDim.x - 1) / gridDim.x;   // rows of Lb written by this CTA
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) s_piv = __ldcg(&w.pivrow[k & 1]);
+    __syncthreads();
+    const int p = s_piv;
+    const cplx* colk = A + (size_t)k * n;
+    const cplx piv = ldcg_c(&colk[p]);
+    for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) v[r] = ldcg_c(&colk[r == p ? k : r]);
+    if (threadIdx.x == 0 && p != k) { const int t = perm[k]; perm[k] = perm[p]; perm[p] = t; }
+    if (wid == scal_warp) {
+      const bool zero = piv.x == 0.0 && piv.y == 0.0;
+      const cplx rinv = zero ? cmake(0.0, 0.0) : cdiv(cmake(1.0, 0.0), piv);
+      if (lane == 0) {
+        s_rinv = rinv;
+        if (blockIdx.x == 0) {
+          w.udiag[k] = piv;
+          w.rdiag[k] = rinv;
+          if (zero) atomicOr(w.err, DQMC_KERR_SINGULAR);
+        }
+      }
+    }
+    // the same row exchange in the multiplier columns formed so far
+    if (p != k)
+      for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < k; j += gridDim.x * blockDim.x) {
+        cplx* lj = Lb + (size_t)j * n;
+        const cplx a = ldcg_c(&lj[k]), b = ldcg_c(&lj[p]);
+        lj[k] = b;
+        lj[p] = a;
+      }
+    __syncthreads();   // v, s_rinv
+    const cplx rinv = s_rinv;
+    {
+      const int r0 = blockIdx.x * chunk, r1 = r0 + chunk < n ? r0 + chunk : n;
+      for (int r = (r0 > k + 1 ? r0 : k + 1) + threadIdx.x; r < r1; r += blockDim.x)
+        Lb[(size_t)k * n + r] = cmul(v[r], rinv);
+    }
+    // ---- trailing columns j > k, dealt round-robin over the CTAs ----
+    const int rem = n - k - 1;
+    const int nq = (rem + 31) >> 5;   // warp-uniform slot count of rows k+1..n-1
+    for (int t = blockIdx.x + gridDim.x * wid; t < rem; t += gridDim.x * warps) {
+      const int j = k + 1 + t;
+      cplx* col = A + (size_t)j * n;
+      const cplx u = ldcg_c(&col[p]), wk = ldcg_c(&col[k]);
+      cplx x[QR_MAXT];
+#pragma unroll
+      for (int q = 0; q < QR_MAXT; ++q) {
+        if (q >= nq) break;
+        const int r = k + 1 + lane + 32 * q;
+        x[q] = r < n ? (r == p ? wk : ldcg_c(&col[r])) : cmake(0.0, 0.0);
+      }
+      const cplx c = cmul(u, rinv);   // a_rj -= (a_rk / piv) u_kj
+      double best = 0.0;
+      int brow = n;
+#pragma unroll
+      for (int q = 0; q < QR_MAXT; ++q) {
+        if (q >= nq) break;
+        const int r = k + 1 + lane + 32 * q;
+        if (r < n) {
+          const cplx vr = v[r];
+          x[q] = cmake(fma(-vr.x, c.x, fma(vr.y, c.y, x[q].x)), fma(-vr.x, c.y, fma(-vr.y, c.x, x[q].y)));
+          col[r] = x[q];
+          if (t == 0) {
+            const double a = fabs(x[q].x) + fabs(x[q].y);
+            if (piv_better(a, r, best, brow)) { best = a; brow = r; }
+          }
+        }
+      }
+      if (lane == 0) col[k] = u;
+      if (t == 0) {   // column k+1: pivot row of the next step
+        warp_argmax(best, brow);
+        if (lane == 0) w.pivrow[(k + 1) & 1] = brow < n ? brow : k + 1;
+      }
+    }
+    if (!grid_barrier(w.bar, w.err, bar_epoch)) return;
+  }
+  if (blockIdx.x == 0)
+    for (int q = threadIdx.x; q < n; q += blockDim.x) w.perm[q] = perm[q];
+}
+
 // ---------------------------------------------------------------------------
 // blocked LU with partial pivoting (zgetrf semantics, in place)
 // ---------------------------------------------------------------------------
@@ -425,6 +538,7 @@ __global__ void k_wy_prep(const cplx* __restrict__ V, const cplx* __restrict__ t
 // copies, so no CTA reads a row another one is rewriting.
 __global__ void __launch_bounds__(256) k_lu_panel(cplx* __restrict__ A, int n, int p0, int b, LUPanel w) {
   unsigned bar_epoch = 0;
+  GridBarrierExit bar_exit(w.bar);
   extern __shared__ double4_16a smem_panel[];
   cplx* prow = reinterpret_cast<cplx*>(smem_panel);   // (own rows, LU_PB): this CTA's rows of the panel
   const int rows = n - p0;
@@ -972,8 +1086,6 @@ cudaError_t launch_qrp(cplx* A, int n, QRWork& w, int sm_count, cudaStream_t st,
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   int grid = sm_count;   // one CTA per SM; remaining columns are dealt round-robin over all CTAs
   if (max_grid > 0 && grid > max_grid) grid = max_grid;
-  e = cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), st);
-  if (e != cudaSuccess) return e;
   QRWork copy = w;
   void* args[] = {&A, &n, &copy};
   return cudaLaunchCooperativeKernel((void*)k_qrp, dim3(grid), dim3(QR_THREADS), args, smem, st);
@@ -1029,6 +1141,25 @@ cudaError_t launch_wy_prep(const cplx* V, const cplx* tau, int n, int jb, int b,
   return cudaGetLastError();
 }
 
+cudaError_t launch_lup(cplx* A, cplx* Lb, int n, LUKernel& w, int sm_count, cudaStream_t st, int max_grid) {
+  if (n > 32 * QR_MAXT) return cudaErrorInvalidValue;
+  size_t smem = (size_t)n * (sizeof(cplx) + sizeof(int));
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_lup, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+    attr = true;
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lup, QR_THREADS, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int grid = sm_count;
+  if (max_grid > 0 && grid > max_grid) grid = max_grid;
+  LUKernel copy = w;
+  void* args[] = {&A, &Lb, &n, &copy};
+  return cudaLaunchCooperativeKernel((void*)k_lup, dim3(grid), dim3(QR_THREADS), args, smem, st);
+}
+
 cudaError_t launch_lu_panel(cplx* A, int n, int p0, int b, LUPanel& w, int sm_count, cudaStream_t st, int max_grid) {
   if (b < 1 || b > LU_PB) return cudaErrorInvalidValue;
   int grid = sm_count;
@@ -1049,8 +1180,6 @@ cudaError_t launch_lu_panel(cplx* A, int n, int p0, int b, LUPanel& w, int sm_co
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lu_panel, 256, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  e = cudaMemsetAsync(w.bar, 0, sizeof(GridBarrier), st);
-  if (e != cudaSuccess) return e;
   LUPanel copy = w;
   void* args[] = {&A, &n, &p0, &b, &copy};
   return cudaLaunchCooperativeKernel((void*)k_lu_panel, dim3(grid), dim3(256), args, smem, st);

@@ -227,6 +227,7 @@ __device__ void local_decide(const LocalUpdateArgs& a, const LocalSmem& sm, int 
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(LU_THREADS, 2) k_local_updates(LocalUpdateArgs a) {
   unsigned bar_epoch = 0;
+  GridBarrierExit bar_exit(a.bar);
   const ModelConst& mc = a.mc;
   const int N = mc.N, n = mc.n;
   extern __shared__ double4_16a smem_local[];
@@ -431,6 +432,7 @@ __device__ __forceinline__ cplx adjugate_entry(cplx m, int lane) {
 template <bool CACHE>
 __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs a, DelayedArgs d) {
   unsigned bar_epoch = 0;
+  GridBarrierExit bar_exit(a.bar);
   const ModelConst& mc = a.mc;
   const int N = mc.N, n = mc.n, L = mc.L, K4 = 4 * d.k;
   __shared__ int s_first, s_ok, s_acc;
@@ -744,8 +746,6 @@ cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d,
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, LU_THREADS, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  e = cudaMemsetAsync(a.bar, 0, sizeof(GridBarrier), st);
-  if (e != cudaSuccess) return e;
   LocalUpdateArgs ca = a;
   DelayedArgs cd = d;
   void* args[] = {&ca, &cd};
@@ -773,8 +773,6 @@ cudaError_t launch_local_updates(const LocalUpdateArgs& a, int sm_count, cudaStr
   const int need = (tiles + (LU_THREADS / 32) - 1) / (LU_THREADS / 32);
   if (grid > need) grid = need < 1 ? 1 : need;
   if (max_grid > 0 && grid > max_grid) grid = max_grid;
-  e = cudaMemsetAsync(a.bar, 0, sizeof(GridBarrier), st);
-  if (e != cudaSuccess) return e;
   LocalUpdateArgs copy = a;
   void* args[] = {&copy};
   return cudaLaunchCooperativeKernel((void*)k_local_updates, dim3(grid), dim3(LU_THREADS), args, smem, st);

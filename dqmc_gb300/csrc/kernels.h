@@ -124,6 +124,16 @@ struct LUWork {
   cplx* udiag;       // (n) diagonal of U
   cplx* rdiag;       // (n) 1 / diagonal of U
 };
+// Unblocked cooperative LU (small n): U in A's strict upper part, L in Lb's strict lower part.
+struct LUKernel {
+  int* perm;
+  cplx* udiag;
+  cplx* rdiag;
+  int* pivrow;       // (2) pivot row of the next step, by step parity
+  GridBarrier* bar;
+  int* err;
+};
+cudaError_t launch_lup(cplx* A, cplx* Lb, int n, LUKernel& w, int sm_count, cudaStream_t st, int max_grid = 0);
 // compact-WY block jb..jb+b of the reflectors in V/tau: Vb ((n-jb) x b), trd (b) (tau, 1 for identity reflectors)
 cudaError_t launch_wy_prep(const cplx* V, const cplx* tau, int n, int jb, int b, cplx* Vb, cplx* trd,
                            cudaStream_t st);
