@@ -51,6 +51,8 @@ struct dqmc_handle {
   // mixed form: split-BF16 GEMM scratch and slicing
   void* oz_scratch = nullptr;
   size_t oz_bytes = 0;
+  unsigned long long* oz_acc = nullptr;   // split-K integer sums, zero between products
+  size_t oz_acc_bytes = 0;
   int oz_target = 40;   // mantissa bits kept per operand
   // local updates
   double* delta_d = nullptr;
@@ -292,10 +294,12 @@ int zgemm_general(dqmc_handle* h, int m, int nn, int k, char opA, char opB, cplx
       splitk = (h->sm_count + tiles - 1) / tiles;
       if (splitk > k / 64) splitk = k / 64;
     }
+    int kernels = 3;
     LAUNCH(kind >= 0 ? kind : DQMC_K_OZGEMM, ozaki_tensor_flops(m, nn, k, S), gemm_bytes(m, nn, k),
            launch_ozaki_zgemm(m, nn, k, opA, opB, alpha, A, lda, B, ldb, beta, C, ldc, rs, cs, S, bits,
-                              h->oz_scratch, h->oz_bytes, h->st, active, splitk));
-    h->launches += 2;   // the two slicing kernels
+                              h->oz_scratch, h->oz_bytes, h->oz_acc, h->oz_acc_bytes, h->st, active, splitk,
+                              &kernels));
+    h->launches += kernels - 1;   // slicing kernels and the split-K finaliser
     return DQMC_OK;
   }
   LAUNCH(kind >= 0 ? kind : DQMC_K_GEMM, gemm_flops(m, nn, k), gemm_bytes(m, nn, k),
@@ -782,8 +786,7 @@ int local_updates_dev(dqmc_handle* h, const double* delta_dev, const double* uni
   }
   const int n = h->n, k = h->delay;
   DelayedArgs d{h->Xd, h->Yd, h->dstate, k, h->prep, h->blk, h->pub};
-  CU(cudaMemsetAsync(h->dstate, 0, 2 * sizeof(int), h->st));
-  LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_prepare(a, h->prep, h->st));
+  LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_prepare(a, h->prep, h->dstate, h->st));
   const int rounds = (h->N + k - 1) / k + 1;
   for (int r = 0; r < rounds; ++r) {
     LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_delayed(a, d, h->sm_count, h->st, h->coop_cap));
@@ -808,7 +811,7 @@ void free_all(dqmc_handle* h) {
                   h->Tr, h->Dl, h->Dr, h->W1, h->W2, h->W3, h->W4, h->D1, h->d2, h->ord1, h->qr.vn1,
                   h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->qr.cand_v, h->qr.cand_q, h->delta_d, h->unif_d,
                   h->acc_d, h->det_d, h->pacc_d, h->action_d, h->nacc_d, h->Acol, h->Brow, h->bar, h->err_d,
-                  h->scal_d, h->oz_scratch, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lup.piv, h->lup.cand_rows, h->lup.rowk, h->lu_L, h->lu_pivrow, h->lu_scales, h->wy_v, h->wy_s, h->wy_z, h->wy_t, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
+                  h->scal_d, h->oz_scratch, h->oz_acc, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lup.piv, h->lup.cand_rows, h->lup.rowk, h->lu_L, h->lu_pivrow, h->lu_scales, h->wy_v, h->wy_s, h->wy_z, h->wy_t, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   clear_graphs(h);
@@ -1173,6 +1176,10 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
     }
     h->oz_bytes = need;
     A(&h->oz_scratch, h->oz_bytes);
+    // split K is taken for fewer than sm_count / 2 output tiles of 64 x 64
+    const size_t tiles = (size_t)(h->sm_count / 2 + 1);
+    h->oz_acc_bytes = std::min((size_t)n * n, tiles * 64 * 64) * 2 * sizeof(unsigned long long);
+    A((void**)&h->oz_acc, h->oz_acc_bytes);
   }
   if (!ok) return fail(DQMC_ERR_CUDA);
   h->qr.err = h->err_d;

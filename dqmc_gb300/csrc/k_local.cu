@@ -333,11 +333,13 @@ __global__ void __launch_bounds__(LU_THREADS, 2) k_local_updates(LocalUpdateArgs
 
 // Per-site constants of slice l: one warp per site.  Lanes of even parity
 // evaluate the old-field block (power -1), odd lanes the proposed one.
-__global__ void __launch_bounds__(128) k_local_prepare(LocalUpdateArgs a, SitePrep* __restrict__ prep) {
+__global__ void __launch_bounds__(128) k_local_prepare(LocalUpdateArgs a, SitePrep* __restrict__ prep, int* state) {
   const ModelConst& mc = a.mc;
   const int N = mc.N, M = mc.M, l = a.slice0;
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * 4 + (threadIdx.x >> 5);
+  // delayed rounds of this slice start from site 0 with nothing pending
+  if (state && blockIdx.x == 0 && threadIdx.x == 0) { state[0] = 0; state[1] = 0; }
   if (i >= N) return;
   const double* po = &a.phi[((size_t)N * l + i) * 3];
   const double old[3] = {po[0], po[1], po[2]};
@@ -711,8 +713,8 @@ static size_t local_smem_bytes(int N) {
   return (size_t)N * (16 * sizeof(cplx) + sizeof(EvEntry)) + (size_t)3 * N * sizeof(double);
 }
 
-cudaError_t launch_local_prepare(const LocalUpdateArgs& a, SitePrep* prep, cudaStream_t st) {
-  k_local_prepare<<<(a.mc.N + 3) / 4, 128, 0, st>>>(a, prep);
+cudaError_t launch_local_prepare(const LocalUpdateArgs& a, SitePrep* prep, int* state, cudaStream_t st) {
+  k_local_prepare<<<(a.mc.N + 3) / 4, 128, 0, st>>>(a, prep, state);
   return cudaGetLastError();
 }
 

@@ -212,6 +212,7 @@ struct OzArgs {
   int int_combine;           // group sums combined exactly in 64-bit integers
   int kchunk;                // split K: K steps per CTA layer (blockIdx.z); 0 = all
   unsigned long long* acc;   // split K: exact integer sums (m x n x {re, im}), finished by k_oz_finalize
+                             // (zero on entry; the finaliser zeroes what it read)
 };
 
 // Final scaling and accumulation of one output value (shared by the GEMM and
@@ -426,6 +427,8 @@ __global__ void k_oz_finalize(OzArgs a) {
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
     const int col = (int)(e / a.m), row = (int)(e - (size_t)col * a.m);
     const long long vr = (long long)a.acc[2 * e], vi = (long long)a.acc[2 * e + 1];
+    a.acc[2 * e] = 0ull;
+    a.acc[2 * e + 1] = 0ull;
     oz_store(a, row, col, __ll2double_rn(vr), __ll2double_rn(vi), wint, plain);
   }
 }
@@ -461,7 +464,8 @@ size_t ozaki_scratch_bytes(int m, int n, int K, int S) {
 cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
                                const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
                                const double* colscale, int S, int bits, void* scratch, size_t scratch_bytes,
-                               cudaStream_t st, const int* active, int splitk) {
+                               unsigned long long* acc, size_t acc_bytes, cudaStream_t st, const int* active,
+                               int splitk, int* kernels) {
   if (S < 1 || S > 12 || bits < 1 || bits > 8) return cudaErrorInvalidValue;
   const int Kpad = (k + 15) / 16 * 16;
   const size_t Kp = 2 * (size_t)Kpad;
@@ -486,19 +490,16 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
   a.acc = nullptr;
   dim3 grid((nn + OZ_BN - 1) / OZ_BN, (m + OZ_BM - 1) / OZ_BM);
   const int ksteps = (int)(Kp / OZ_BK);
-  if (splitk > 1 && a.int_combine && !active && ksteps > 1) {
-    // split K over blockIdx.z: exact 64-bit integer partial sums behind the slices
-    const size_t off = (ozaki_scratch_bytes(m, nn, k, S) + 255) / 256 * 256;
-    const size_t need = off + (size_t)m * nn * 2 * sizeof(unsigned long long);
-    if (need <= scratch_bytes) {
-      if (splitk > ksteps) splitk = ksteps;
-      a.kchunk = (ksteps + splitk - 1) / splitk;
-      grid.z = (ksteps + a.kchunk - 1) / a.kchunk;
-      a.acc = reinterpret_cast<unsigned long long*>(base + off);
-      cudaError_t e = cudaMemsetAsync(a.acc, 0, (size_t)m * nn * 2 * sizeof(unsigned long long), st);
-      if (e != cudaSuccess) return e;
-    }
+  if (splitk > 1 && a.int_combine && !active && ksteps > 1 && acc &&
+      (size_t)m * nn * 2 * sizeof(unsigned long long) <= acc_bytes) {
+    // split K over blockIdx.z: exact 64-bit integer partial sums in acc, which
+    // is zero between products (zeroed at allocation, re-zeroed by the finaliser)
+    if (splitk > ksteps) splitk = ksteps;
+    a.kchunk = (ksteps + splitk - 1) / splitk;
+    grid.z = (ksteps + a.kchunk - 1) / a.kchunk;
+    a.acc = acc;
   }
+  if (kernels) *kernels = a.acc ? 4 : 3;
   if (a.int_combine) k_oz_gemm<true><<<grid, OZ_THREADS, 0, st>>>(a);
   else k_oz_gemm<false><<<grid, OZ_THREADS, 0, st>>>(a);
   if (a.acc) {

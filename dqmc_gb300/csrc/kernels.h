@@ -56,7 +56,8 @@ struct SitePrep {
   double dsA, dsQ, dsB;    // boson action difference, space-neighbour coupling excluded
   double pad[2];
 };
-cudaError_t launch_local_prepare(const LocalUpdateArgs& a, SitePrep* prep, cudaStream_t st);
+// state (2 ints, nullable): delayed-round state of the slice, zeroed here
+cudaError_t launch_local_prepare(const LocalUpdateArgs& a, SitePrep* prep, int* state, cudaStream_t st);
 struct DelayedArgs {
   cplx* X;
   cplx* Y;
@@ -190,7 +191,8 @@ size_t ozaki_scratch_bytes(int m, int n, int K, int S);
 cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
                                const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
                                const double* colscale, int S, int bits, void* scratch, size_t scratch_bytes,
-                               cudaStream_t st, const int* active = nullptr, int splitk = 1);
+                               unsigned long long* acc, size_t acc_bytes, cudaStream_t st,
+                               const int* active = nullptr, int splitk = 1, int* kernels = nullptr);
 
 // ---- adjoint force (k_force.cu) ----
 // grad[:, :, slice0] = d log|det M| / d phi[:, :, slice0] from G of that slice
