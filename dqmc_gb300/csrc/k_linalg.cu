@@ -670,25 +670,44 @@ __global__ void __launch_bounds__(256) k_lu_panel(cplx* __restrict__ A, int n, i
 
 // Row exchanges of one panel applied to the columns outside it, and to the
 // running permutation: the b exchanges (k, piv[k]) touch at most 2b rows,
-// whose net permutation one thread works out; every column is then gathered
-// over those rows.
+// whose net permutation warp 0 works out (panel rows indexed directly, rows
+// below the panel found by a ballot over the ones met so far); every column
+// is then gathered over those rows.
 __global__ void k_lu_apply_swaps(cplx* __restrict__ A, int n, int p0, int b, const int* __restrict__ piv,
                                  int* __restrict__ perm) {
-  __shared__ int rowof[2 * LU_PB], src[2 * LU_PB];
+  __shared__ int rowof[2 * LU_PB], src[2 * LU_PB], spiv[LU_PB];
   __shared__ int s_cnt;
-  if (threadIdx.x == 0) {
-    int cnt = b;
-    for (int s2 = 0; s2 < b; ++s2) { rowof[s2] = p0 + s2; src[s2] = p0 + s2; }
-    for (int kk = 0; kk < b; ++kk) {
-      const int k = p0 + kk, pr = piv[k];
-      if (pr == k) continue;
-      int sp = -1;
-      for (int s2 = 0; s2 < cnt; ++s2)
-        if (rowof[s2] == pr) { sp = s2; break; }
-      if (sp < 0) { sp = cnt++; rowof[sp] = pr; src[sp] = pr; }
-      const int t = src[kk]; src[kk] = src[sp]; src[sp] = t;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    for (int s2 = lane; s2 < b; s2 += 32) {
+      rowof[s2] = p0 + s2;
+      src[s2] = p0 + s2;
+      spiv[s2] = piv[p0 + s2];
     }
-    s_cnt = cnt;
+    __syncwarp();
+    int cnt = b;
+    for (int kk = 0; kk < b; ++kk) {
+      const int k = p0 + kk, pr = spiv[kk];
+      if (pr == k) continue;   // warp-uniform
+      int sp = -1;
+      if (pr < p0 + b) {
+        sp = pr - p0;
+      } else {
+        for (int base = b; base < cnt && sp < 0; base += 32) {
+          const int s2 = base + lane;
+          const unsigned hit = __ballot_sync(0xffffffffu, s2 < cnt && rowof[s2] == pr);
+          if (hit) sp = base + __ffs(hit) - 1;
+        }
+        if (sp < 0) {
+          sp = cnt++;
+          if (lane == 0) { rowof[sp] = pr; src[sp] = pr; }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) { const int t = src[kk]; src[kk] = src[sp]; src[sp] = t; }
+      __syncwarp();
+    }
+    if (lane == 0) s_cnt = cnt;
   }
   __syncthreads();
   const int cnt = s_cnt;
@@ -897,44 +916,93 @@ __global__ void __launch_bounds__(128) k_trsm_left_lower_unit(const cplx* __rest
 
 // Diagonal-block solve of a blocked triangular solve: the b x b block of T
 // at (j0, j0) (leading dimension ldT) applied to rows j0..j0+b of the m
-// columns of Y (leading dimension ldY), one warp per column (segment in
-// shared memory).  lower: unit lower triangular, forward; otherwise upper
-// with the reciprocal diagonal rdiag[j0 + q], backward.
-__global__ void __launch_bounds__(128) k_trsm_diag_block(const cplx* __restrict__ T, int ldT,
-                                                        const cplx* __restrict__ rdiag, cplx* __restrict__ Y,
-                                                        int ldY, int j0, int b, int m, int lower) {
-  __shared__ cplx ys[4][128];
+// columns of Y (leading dimension ldY).  lower: unit lower triangular,
+// forward; otherwise upper with the reciprocal diagonal rdiag[j0 + q],
+// backward.  Each CTA stages the strict triangle of the block, packed by
+// columns, in shared memory once (no L2 round trip inside the dependent
+// column steps); each warp solves one column with its b values in registers
+// (row lane + 32 i in slot i) and broadcasts y_q by shuffle.
+constexpr int TRSM_DB_WARPS = 8;
+__device__ __forceinline__ int trsm_pack_lower(int q, int b) { return q * (b - 1) - q * (q - 1) / 2; }
+__device__ __forceinline__ int trsm_pack_upper(int q) { return q * (q - 1) / 2; }
+
+__global__ void __launch_bounds__(32 * TRSM_DB_WARPS) k_trsm_diag_block(const cplx* __restrict__ T, int ldT,
+                                                                       const cplx* __restrict__ rdiag,
+                                                                       cplx* __restrict__ Y, int ldY, int j0, int b,
+                                                                       int m, int lower) {
+  extern __shared__ double4_16a smem_tdb[];
+  cplx* tp = reinterpret_cast<cplx*>(smem_tdb);   // (b (b - 1) / 2) packed strict triangle
+  cplx* rd = tp + (size_t)b * (b - 1) / 2;        // (b) reciprocal diagonal (upper)
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int col = blockIdx.x * 4 + wid;
+  const int bb = b * b;
+  for (int e0 = threadIdx.x; e0 < bb; e0 += 8 * blockDim.x) {
+    cplx v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = e0 + u * blockDim.x;
+      const int q = e / b, r = e - q * b;
+      if (e < bb && (lower ? r > q : r < q)) v[u] = __ldg(&T[(size_t)(j0 + q) * ldT + j0 + r]);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = e0 + u * blockDim.x;
+      const int q = e / b, r = e - q * b;
+      if (e < bb && (lower ? r > q : r < q))
+        tp[lower ? trsm_pack_lower(q, b) + (r - q - 1) : trsm_pack_upper(q) + r] = v[u];
+    }
+  }
+  if (!lower)
+    for (int q = threadIdx.x; q < b; q += blockDim.x) rd[q] = __ldg(&rdiag[j0 + q]);
+  __syncthreads();
+  const int col = blockIdx.x * TRSM_DB_WARPS + wid;
   if (col >= m) return;
-  cplx* y = ys[wid];
   cplx* yg = Y + (size_t)col * ldY + j0;
-  for (int r = lane; r < b; r += 32) y[r] = yg[r];
-  __syncwarp();
+  cplx y[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = lane + 32 * i;
+    y[i] = r < b ? yg[r] : cmake(0.0, 0.0);
+  }
+  auto bcast = [&](int q) {
+    const int slot = q >> 5, src = q & 31;
+    const cplx v = slot == 0 ? y[0] : slot == 1 ? y[1] : slot == 2 ? y[2] : y[3];
+    return cmake(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+  };
   if (lower) {
     for (int q = 0; q < b - 1; ++q) {
-      const cplx* tq = T + (size_t)(j0 + q) * ldT + j0;
-      const cplx yq = y[q];
-      for (int r = q + 1 + lane; r < b; r += 32) {
-        const cplx t = __ldg(&tq[r]);
-        y[r] = cmake(fma(-yq.x, t.x, fma(yq.y, t.y, y[r].x)), fma(-yq.x, t.y, fma(-yq.y, t.x, y[r].y)));
+      const cplx yq = bcast(q);
+      const cplx* tq = tp + trsm_pack_lower(q, b) - q - 1;   // tq[r], r > q
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        if (32 * i + 31 <= q || 32 * i >= b) continue;   // warp-uniform
+        const int r = lane + 32 * i;
+        if (r > q && r < b) {
+          const cplx t = tq[r];
+          y[i] = cmake(fma(-yq.x, t.x, fma(yq.y, t.y, y[i].x)), fma(-yq.x, t.y, fma(-yq.y, t.x, y[i].y)));
+        }
       }
-      __syncwarp();
     }
   } else {
     for (int q = b - 1; q >= 0; --q) {
-      const cplx* tq = T + (size_t)(j0 + q) * ldT + j0;
-      const cplx yq = cmul(y[q], __ldg(&rdiag[j0 + q]));
-      __syncwarp();
-      if (lane == 0) y[q] = yq;
-      for (int r = lane; r < q; r += 32) {
-        const cplx t = __ldg(&tq[r]);
-        y[r] = cmake(fma(-yq.x, t.x, fma(yq.y, t.y, y[r].x)), fma(-yq.x, t.y, fma(-yq.y, t.x, y[r].y)));
+      const cplx yq = cmul(bcast(q), rd[q]);
+      const cplx* tq = tp + trsm_pack_upper(q);   // tq[r], r < q
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        if (32 * i > q) continue;   // warp-uniform
+        const int r = lane + 32 * i;
+        if (r == q) y[i] = yq;
+        else if (r < q) {
+          const cplx t = tq[r];
+          y[i] = cmake(fma(-yq.x, t.x, fma(yq.y, t.y, y[i].x)), fma(-yq.x, t.y, fma(-yq.y, t.x, y[i].y)));
+        }
       }
-      __syncwarp();
     }
   }
-  for (int r = lane; r < b; r += 32) yg[r] = y[r];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = lane + 32 * i;
+    if (r < b) yg[r] = y[i];
+  }
 }
 
 // Y <- Y That^-1 (Y is m x n), one warp per row: z That = y, forward over columns.
@@ -1120,7 +1188,17 @@ cudaError_t launch_trsm_left_upper(const cplx* T, const int* order, const cplx* 
 cudaError_t launch_trsm_diag_block(const cplx* T, int ldT, const cplx* rdiag, cplx* Y, int ldY, int j0, int b, int m,
                                    bool lower, cudaStream_t st) {
   if (b < 1 || b > 128) return cudaErrorInvalidValue;
-  k_trsm_diag_block<<<(m + 3) / 4, 128, 0, st>>>(T, ldT, rdiag, Y, ldY, j0, b, m, lower ? 1 : 0);
+  if (!lower && !rdiag) return cudaErrorInvalidValue;
+  const size_t smem = ((size_t)b * (b - 1) / 2 + b) * sizeof(cplx);
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_trsm_diag_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)((128 * 127 / 2 + 128) * sizeof(cplx)));
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  k_trsm_diag_block<<<(m + TRSM_DB_WARPS - 1) / TRSM_DB_WARPS, 32 * TRSM_DB_WARPS, smem, st>>>(
+      T, ldT, rdiag, Y, ldY, j0, b, m, lower ? 1 : 0);
   return cudaGetLastError();
 }
 

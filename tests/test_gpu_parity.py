@@ -428,3 +428,28 @@ def test_time_displaced_greens(lib, golden, small_params, cfg, prec):
     for tau in range(p.slices):
         assert relerr(gt0[tau], gt0_r[tau]) < tol, (tau, relerr(gt0[tau], gt0_r[tau]))
         assert relerr(g0t[tau], g0t_r[tau]) < tol, (tau, relerr(g0t[tau], g0t_r[tau]))
+
+
+@pytest.mark.parametrize("tune", ["lu_small=0", "lu_small=4096"])
+@pytest.mark.parametrize("L,prec", [(6, "fp64"), (10, "fp64"), (10, "mixed")])
+def test_lu_blocked_and_unblocked(lib, monkeypatch, tune, L, prec):
+    """calculate_greens through the blocked LU (panels of 64 columns, ragged last
+    panel at n = 400) and through the unblocked cooperative LU, selected per
+    handle by DQMC_TUNE; both reproduce the oracle (1e-10 FP64, 1e-8 mixed)."""
+    monkeypatch.setenv("DQMC_TUNE", tune)
+    p = dataclasses.replace(C0, L=L, slices=20)
+    phi = R.synthetic_field(p.N, p.slices, 31 + L)
+    ref = R.DQMCRef(p, phi)
+    prm = api_params(p)
+    prm.precision = prec
+    gpu = lib.DQMC(prm, phi)
+    try:
+        gpu.init()
+        tol = TOL if prec == "fp64" else 1e-8
+        for sl in (1, 10, 20):
+            G, ld = gpu.calc_greens_and_logdet(sl)
+            Gr, ldr = ref.calc_greens_and_logdet(sl)
+            assert relerr(G, Gr) < tol
+            assert abs(ld - ldr) < 10 * tol * max(1.0, abs(ldr))
+    finally:
+        gpu.close()
