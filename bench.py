@@ -526,7 +526,8 @@ def run_ours(args, world, rank, local):
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if head == "fp64" else "f64 + split-bf16 tensor GEMMs",
             "data": "synthetic (seeded uniform[-1,1] fields, uniform proposal/Metropolis streams)",
-            "config": {"workload": desc, "L": L, "slices": M, "n": n, "safe_mult": 10, "chains_per_gpu": 1,
+            "config": {"workload": desc if head == "fp64" else
+                       desc.replace(" FP64", "") + ", mixed form (FP64 factorisations, split-BF16 GEMMs)", "L": L, "slices": M, "n": n, "safe_mult": 10, "chains_per_gpu": 1,
                        "form": head, "delay": args.delay if head == "mixed" else args.fp64_delay,
                        "parallelism": f"replicas x{world}",
                        "l2": "working set > L2 (stack 2x21x16.8 MB) and 256 MB L2 flush before each sweep"},

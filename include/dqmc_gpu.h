@@ -253,6 +253,9 @@ DQMC_API int dqmc_global_update(dqmc_handle* h, const double* shift, double u, i
  * one down pass, after which the state returns to (slice M, direction -1).
  * Needs the state (M, -1), i.e. right after dqmc_init or after 2M updates.
  * No counterpart in the reference; either output may be NULL. */
+DQMC_API int dqmc_force(dqmc_handle* h, double* grad_logdet, double* grad_boson);
+
+/* ---- time-displaced Green's functions --------------------------------------- */
 /* measure_tdgfs! (src/fermion_measurements.jl:1343-1403, with calc_Bchain_udts! :1411-1488,
  * fill_tdgf! :1497-1523, inv_sum_udts_scalettar! and inv_one_plus_udt_scalettar!
  * src/linalg.jl:310-339, 512-567): the time-displaced Green's functions Gt0[tau] = G(tau, 0)
@@ -260,8 +263,6 @@ DQMC_API int dqmc_global_update(dqmc_handle* h, const double* shift, double u, i
  * complex at offset (tau - 1) n^2 (2 M n^2 doubles per array).  device_ptrs != 0: Gt0 and
  * G0t are device addresses on the handle's device; otherwise host buffers. */
 DQMC_API int dqmc_measure_tdgfs(dqmc_handle* h, double* Gt0, double* G0t, int32_t device_ptrs);
-
-DQMC_API int dqmc_force(dqmc_handle* h, double* grad_logdet, double* grad_boson);
 
 /* ---- diagnostics ------------------------------------------------------------- */
 /* Per-group device times (CUDA events on the handle's stream) and the number
