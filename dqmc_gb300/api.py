@@ -87,6 +87,8 @@ SIGNATURES = {
     "dqmc_boson_action": ([_P, _D], ctypes.c_int),
     "dqmc_calc_boson_action": ([_P, _D], ctypes.c_int),
     "dqmc_measure": ([_P, _D, _D, _D], ctypes.c_int),
+    "dqmc_measure_equal_time": ([_P, _D, _D, _D, _D, _D, ctypes.c_int32], ctypes.c_int),
+    "dqmc_measure_zfpc": ([_P, _D, _D, _D, ctypes.c_int32], ctypes.c_int),
     "dqmc_get_timing": ([_P, ctypes.POINTER(CTiming)], ctypes.c_int),
     "dqmc_reset_timing": ([_P, _I32], ctypes.c_int),
     "dqmc_peak_fp64": ([_I32, _D], ctypes.c_int),
@@ -392,6 +394,39 @@ class DQMC:
         occ, ek = ctypes.c_double(), ctypes.c_double()
         self._check(self.lib.dqmc_measure(self.h, G.ctypes.data_as(_D), ctypes.byref(occ), ctypes.byref(ek)))
         return dict(greens=G, occupation=occ.value, e_kin=ek.value)
+
+    def measure_equal_time(self, greens=None):
+        """measure_etpc! and measure_etcdc! (src/fermion_measurements.jl:388-427,
+        580-620) of the true G `greens` (n x n), or of the measurement hook's G
+        when None.  Returns (etpc_plus, etpc_minus, etcdc_plus, etcdc_minus),
+        each L x L indexed [y, x] by the displacement."""
+        L = self.p.L
+        g = None
+        if greens is not None:
+            g = np.asfortranarray(np.asarray(greens, dtype=np.complex128).reshape(self.n, self.n))
+        pp = np.zeros((L, L), order="F")
+        pm = np.zeros((L, L), order="F")
+        cp = np.zeros((L, L), dtype=np.complex128, order="F")
+        cm = np.zeros((L, L), dtype=np.complex128, order="F")
+        self._check(self.lib.dqmc_measure_equal_time(self.h, g.ctypes.data_as(_D) if g is not None else None,
+                                                     pp.ctypes.data_as(_D), pm.ctypes.data_as(_D),
+                                                     cp.ctypes.data_as(_D), cm.ctypes.data_as(_D), 0))
+        return pp, pm, cp, cm
+
+    def measure_zfpc(self, gt0=None):
+        """measure_zfpc! (src/fermion_measurements.jl:486-530) over G(tau, 0)
+        given as an (M, n, n) array (as measure_tdgfs returns), or computed on
+        the device when None.  Returns (zfpc_plus, zfpc_minus), L x L [y, x]."""
+        L = self.p.L
+        g = None
+        if gt0 is not None:
+            # (M, n, n) row-major per block -> column-major n x n blocks
+            g = np.ascontiguousarray(np.asarray(gt0, dtype=np.complex128).transpose(0, 2, 1))
+        pp = np.zeros((L, L), order="F")
+        pm = np.zeros((L, L), order="F")
+        self._check(self.lib.dqmc_measure_zfpc(self.h, g.ctypes.data_as(_D) if g is not None else None,
+                                               pp.ctypes.data_as(_D), pm.ctypes.data_as(_D), 0))
+        return pp, pm
 
     def global_update(self, shift, u):
         """global_update (src/global_updates.jl:18-58) with a fixed-slot shift

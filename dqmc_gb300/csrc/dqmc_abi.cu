@@ -93,6 +93,7 @@ struct dqmc_handle {
   cplx* wy_z = nullptr;       // (kWyMax x n) T Vb^H W
   cplx* wy_t = nullptr;       // (kWyMax) tau of the block
   double* force_d = nullptr;   // (3, N, M) d log|det M| / d phi
+  double* etc_d = nullptr;     // (6 N) equal-time correlators P+, P-, C+, C-
   // global updates: backup of stack, G, field and interaction table (allocated on first use)
   cplx *gb_u = nullptr, *gb_t = nullptr, *gb_G = nullptr;
   double *gb_d = nullptr, *gb_phi = nullptr;
@@ -811,7 +812,7 @@ void free_all(dqmc_handle* h) {
                   h->Tr, h->Dl, h->Dr, h->W1, h->W2, h->W3, h->W4, h->D1, h->d2, h->ord1, h->qr.vn1,
                   h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->qr.cand_v, h->qr.cand_q, h->delta_d, h->unif_d,
                   h->acc_d, h->det_d, h->pacc_d, h->action_d, h->nacc_d, h->Acol, h->Brow, h->bar, h->err_d,
-                  h->scal_d, h->oz_scratch, h->oz_acc, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lup.piv, h->lup.cand_rows, h->lup.rowk, h->lu_L, h->lu_pivrow, h->lu_scales, h->wy_v, h->wy_s, h->wy_z, h->wy_t, h->force_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
+                  h->scal_d, h->oz_scratch, h->oz_acc, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lup.piv, h->lup.cand_rows, h->lup.rowk, h->lu_L, h->lu_pivrow, h->lu_scales, h->wy_v, h->wy_s, h->wy_z, h->wy_t, h->force_d, h->etc_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   clear_graphs(h);
@@ -1070,6 +1071,12 @@ int measure(dqmc_handle* h, cplx* Gt0, cplx* G0t) {
            launch_scale(G0t, n, (int)((size_t)n * M), w.neg, false, nullptr, false, h->st));
     return DQMC_OK;
   };
+  // zero blocks as allocate_tdgfs! (src/fermion_measurements.jl:1247-1248):
+  // when M/2 is not a multiple of safe_mult, fill_tdgf! propagates from a
+  // slice it has not filled yet, which the reference holds as zeros
+  if (rc == DQMC_OK && (cudaMemsetAsync(Gt0, 0, (size_t)M * nn * sizeof(cplx), h->st) != cudaSuccess ||
+                        cudaMemsetAsync(G0t, 0, (size_t)M * nn * sizeof(cplx), h->st) != cudaSuccess))
+    rc = DQMC_ERR_CUDA;
   if (rc == DQMC_OK) rc = body();
   cudaStreamSynchronize(h->st);
   for (void* q : owned) cudaFree(q);
@@ -1765,6 +1772,41 @@ int dqmc_calc_boson_action(dqmc_handle* h, double* S) {
   return DQMC_OK;
 }
 
+int dqmc_measure_equal_time(dqmc_handle* h, const double* greens, double* etpc_plus, double* etpc_minus,
+                             double* etcdc_plus, double* etcdc_minus, int32_t device_ptrs) {
+  if (h) cudaSetDevice(h->device);
+  if (!h) return DQMC_ERR_ARG;
+  const int N = h->N;
+  const cplx* src = nullptr;
+  if (greens) {
+    if (device_ptrs) {
+      src = reinterpret_cast<const cplx*>(greens);
+    } else {
+      CU(cudaMemcpyAsync(h->Gtmp, greens, (size_t)h->n * h->n * sizeof(cplx), cudaMemcpyHostToDevice, h->st));
+      src = h->Gtmp;
+    }
+  } else {
+    // the measurement hook's G: wrap_greens(G, current_slice, +1), effective -> true
+    if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
+    if (h->current_slice < 1 || h->current_slice > h->M) return set_err(h, DQMC_ERR_STATE, "no current slice");
+    CHK(copy_nn(h, h->Gtmp, h->G));
+    CHK(wrap_greens(h, h->Gtmp, h->current_slice, 1));
+    CHK(apply_rows(h, h->Gtmp, 0, 1, 1, SLICE_EFF_RIGHT));
+    CHK(apply_cols(h, h->Gtmp, 0, 1, 1, SLICE_EFF_LEFT_INV, nullptr));
+    src = h->Gtmp;
+  }
+  if (!h->etc_d) CU(cudaMalloc(&h->etc_d, (size_t)6 * N * sizeof(double)));
+  LAUNCH(DQMC_K_MISC, 0.0, 0.0, launch_equal_time_corr(src, h->L, h->etc_d, h->st));
+  const cudaMemcpyKind kind = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  double* outs[4] = {etpc_plus, etpc_minus, etcdc_plus, etcdc_minus};
+  const size_t off[4] = {0, (size_t)N, (size_t)2 * N, (size_t)4 * N};
+  const size_t cnt[4] = {(size_t)N, (size_t)N, (size_t)2 * N, (size_t)2 * N};
+  for (int q = 0; q < 4; ++q)
+    if (outs[q]) CU(cudaMemcpyAsync(outs[q], h->etc_d + off[q], cnt[q] * sizeof(double), kind, h->st));
+  CHK(sync(h));
+  return check_device_error(h);
+}
+
 int dqmc_measure(dqmc_handle* h, double* greens_out, double* occupation, double* e_kin) {
   if (h) cudaSetDevice(h->device);
   if (!h) return DQMC_ERR_ARG;
@@ -1876,6 +1918,47 @@ int dqmc_measure_tdgfs(dqmc_handle* h, double* Gt0, double* G0t, int32_t device_
   cudaFree(b);
   if (rc != DQMC_OK) return rc;
   return sync(h);
+}
+
+int dqmc_measure_zfpc(dqmc_handle* h, const double* Gt0, double* zfpc_plus, double* zfpc_minus, int32_t device_ptrs) {
+  if (h) cudaSetDevice(h->device);
+  if (!h) return DQMC_ERR_ARG;
+  const int N = h->N, M = h->M;
+  const size_t bytes = (size_t)M * h->n * h->n * sizeof(cplx);
+  cplx *g = nullptr, *scratch = nullptr;
+  if (Gt0 && device_ptrs) {
+    g = reinterpret_cast<cplx*>(const_cast<double*>(Gt0));
+  } else {
+    if (!Gt0 && !h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
+    CU(cudaMalloc(&g, bytes));
+    int rc = DQMC_OK;
+    if (Gt0) {
+      if (cudaMemcpyAsync(g, Gt0, bytes, cudaMemcpyHostToDevice, h->st) != cudaSuccess) rc = DQMC_ERR_CUDA;
+    } else if (cudaMalloc(&scratch, bytes) != cudaSuccess) {
+      rc = DQMC_ERR_CUDA;
+    } else {
+      rc = tdgf::measure(h, g, scratch);   // G(tau, 0); G(0, tau) is not needed
+    }
+    if (rc != DQMC_OK) {
+      cudaFree(g);
+      cudaFree(scratch);
+      return rc == DQMC_ERR_CUDA ? set_err(h, rc, "device memory for the time-displaced G") : rc;
+    }
+  }
+  if (!h->etc_d) CU(cudaMalloc(&h->etc_d, (size_t)6 * N * sizeof(double)));
+  int rc = DQMC_OK;
+  if (launch_zfpc(g, M, h->L, h->etc_d, h->st) != cudaSuccess) rc = DQMC_ERR_CUDA;
+  ++h->launches;
+  const cudaMemcpyKind kind = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (rc == DQMC_OK && zfpc_plus &&
+      cudaMemcpyAsync(zfpc_plus, h->etc_d, N * sizeof(double), kind, h->st) != cudaSuccess) rc = DQMC_ERR_CUDA;
+  if (rc == DQMC_OK && zfpc_minus &&
+      cudaMemcpyAsync(zfpc_minus, h->etc_d + N, N * sizeof(double), kind, h->st) != cudaSuccess) rc = DQMC_ERR_CUDA;
+  if (rc == DQMC_OK && cudaStreamSynchronize(h->st) != cudaSuccess) rc = DQMC_ERR_CUDA;
+  if (!(Gt0 && device_ptrs)) cudaFree(g);
+  cudaFree(scratch);
+  if (rc != DQMC_OK) return set_err(h, rc, "zfpc");
+  return check_device_error(h);
 }
 
 }  // extern "C"

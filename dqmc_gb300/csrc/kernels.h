@@ -196,6 +196,12 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
 
 // ---- adjoint force (k_force.cu) ----
 // grad[:, :, slice0] = d log|det M| / d phi[:, :, slice0] from G of that slice
+// ---- equal-time correlators (k_measure.cu) ----
+// out (6 L^2 doubles): P+ and P- (L x L real), C+ and C- (L x L complex) of the true G
+cudaError_t launch_equal_time_corr(const cplx* G, int L, double* out, cudaStream_t st);
+// out (2 L^2 doubles): P+ and P- summed over the `slices` matrices of Gt0 (stride n^2)
+cudaError_t launch_zfpc(const cplx* Gt0, int slices, int L, double* out, cudaStream_t st);
+
 cudaError_t launch_force_slice(const cplx* G, const double* phi, double* grad, int N, int slice0, double lambda_dtau,
                                cudaStream_t st);
 // phi[a, :, :] += shift[a] for a = 0..2 (field of N sites x M slices)

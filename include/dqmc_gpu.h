@@ -234,6 +234,16 @@ DQMC_API int dqmc_calc_boson_action(dqmc_handle* h, double* S);
  * occupation (src/fermion_measurements.jl:322) and kinetic energy
  * E_kin = sum_ij T_ij <c_i^dag c_j> (not an observable of the reference). */
 DQMC_API int dqmc_measure(dqmc_handle* h, double* greens_out, double* occupation, double* e_kin);
+/* Equal-time pairing correlators measure_etpc! (src/fermion_measurements.jl:388-427)
+ * and charge-density correlators measure_etcdc! (:580-620) of a true G: the
+ * n x n column-major complex `greens` if not NULL (as the reference's `greens`
+ * argument), else the measurement hook's true G of the current slice.  Outputs
+ * (each may be NULL) are L x L column-major, element (y, x) = displacement
+ * (x, y) averaged over origins: etpc_plus / etpc_minus real (L^2 doubles),
+ * etcdc_plus / etcdc_minus complex (2 L^2 doubles).  device_ptrs != 0: every
+ * pointer is a device address on the handle's device. */
+DQMC_API int dqmc_measure_equal_time(dqmc_handle* h, const double* greens, double* etpc_plus, double* etpc_minus,
+                                     double* etcdc_plus, double* etcdc_minus, int32_t device_ptrs);
 
 /* global_update (src/global_updates.jl:18-58): shift every slice and site of
  * field component k by shift[k] (fixed slot, already in [-box_global,
@@ -263,6 +273,14 @@ DQMC_API int dqmc_force(dqmc_handle* h, double* grad_logdet, double* grad_boson)
  * complex at offset (tau - 1) n^2 (2 M n^2 doubles per array).  device_ptrs != 0: Gt0 and
  * G0t are device addresses on the handle's device; otherwise host buffers. */
 DQMC_API int dqmc_measure_tdgfs(dqmc_handle* h, double* Gt0, double* G0t, int32_t device_ptrs);
+/* measure_zfpc! (src/fermion_measurements.jl:486-530): the pairing correlators of
+ * dqmc_measure_equal_time summed over G(tau, 0), tau = 1..M (not divided by M,
+ * as in the reference).  Gt0: the M blocks that dqmc_measure_tdgfs writes, or
+ * NULL to compute them for the current field on the device.  zfpc_plus /
+ * zfpc_minus: L x L real, element (y, x) at y + L x; each may be NULL.
+ * device_ptrs != 0: Gt0 and the outputs are device addresses. */
+DQMC_API int dqmc_measure_zfpc(dqmc_handle* h, const double* Gt0, double* zfpc_plus, double* zfpc_minus,
+                               int32_t device_ptrs);
 
 /* ---- diagnostics ------------------------------------------------------------- */
 /* Per-group device times (CUDA events on the handle's stream) and the number

@@ -842,8 +842,10 @@ class DQMCRef:
         BBetaT = self.calc_Bchain_udts(False, "right")
         BT0 = self.calc_Bchain_udts(False, "left")
         BBetaTInv = self.calc_Bchain_udts(True, "right")
-        Gt0 = [None] * M
-        G0t = [None] * M
+        # zero blocks as allocate_tdgfs! (:1247-1248): when M/2 is not a multiple
+        # of safe_mult, fill_tdgf! starts from a slice it has not filled yet
+        Gt0 = [np.zeros((self.n, self.n), dtype=np.complex128) for _ in range(M)]
+        G0t = [np.zeros((self.n, self.n), dtype=np.complex128) for _ in range(M)]
         for i, tau in enumerate(range(1, M + 1, s)):
             if i != 0:
                 g1 = inv_sum_udts_scalettar(BT0Inv[0][i - 1], BT0Inv[1][i - 1], BT0Inv[2][i - 1],
@@ -864,6 +866,100 @@ class DQMCRef:
         matrix (src/hoppings.jl:85) and G convention."""
         cdc = np.eye(self.n) - G_true.T
         return float(np.real(np.sum(self.T * cdc)))
+
+
+# ---------------------------------------------------------------------------
+# equal-time fermion correlators (src/fermion_measurements.jl:363-620)
+# ---------------------------------------------------------------------------
+def _site_pbc(L, x, y):
+    """siteidx (src/fermion_measurements.jl:7-12), 0-based: sql[y, x] = y + L x with PBC."""
+    return np.mod(y, L) + L * np.mod(x, L)
+
+
+def _origins(L):
+    x0, y0 = np.meshgrid(np.arange(L), np.arange(L), indexing="ij")
+    return x0.ravel(), y0.ravel()
+
+
+def measure_etpc(L, G):
+    """measure_etpc! (src/fermion_measurements.jl:388-427) with _pc_ev (:436-451)
+    for opdim 3 (G accessed directly, :23-26).  Flavours xu, yd, xd, yu are
+    0, 1, 2, 3 here; index = flavour N + site.  Returns (P_plus, P_minus), each
+    L x L real with [y, x] the displacement, averaged over the origins r0."""
+    N = L * L
+    xu, yd, xd, yu = 0, 1, 2, 3
+    js = ((xd, xu, xu, xd), (xd, xu, yu, yd), (yd, yu, xu, xd), (yd, yu, yu, yd))
+    x0, y0 = _origins(L)
+    r0 = _site_pbc(L, x0, y0)
+    Pp = np.zeros((L, L))
+    Pm = np.zeros((L, L))
+    for x in range(L):
+        for y in range(L):
+            ri = _site_pbc(L, x0 + x, y0 + y)
+            ev = []
+            for j in js:
+                i1, i2, i3, i4 = j[0] * N + ri, j[1] * N + ri, j[2] * N + r0, j[3] * N + r0
+                ev.append(np.real(G[i1, i4] * G[i2, i3] - G[i1, i3] * G[i2, i4]))
+            Pm[y, x] = np.sum(ev[0] - ev[1] - ev[2] + ev[3]) / N
+            Pp[y, x] = np.sum(ev[0] + ev[1] + ev[2] + ev[3]) / N
+    return Pp, Pm
+
+
+def measure_etcdc(L, G):
+    """measure_etcdc! (src/fermion_measurements.jl:580-620) with _etcdc_ev
+    (:630-643): bands X = 1, Y = 2 and spins UP = 0, DOWN = 2 give the 1-based
+    flavour band + spin.  Returns (C_plus, C_minus), L x L complex, [y, x] the
+    displacement, averaged over the origins."""
+    N = L * L
+    X, Y = 1, 2
+    x0, y0 = _origins(L)
+    r0 = _site_pbc(L, x0, y0)
+    Cp = np.zeros((L, L), dtype=np.complex128)
+    Cm = np.zeros((L, L), dtype=np.complex128)
+
+    def ev(ri, j1, j2, j3, j4):
+        i1, i2 = (j1 - 1) * N + ri, (j2 - 1) * N + ri
+        i3, i4 = (j3 - 1) * N + r0, (j4 - 1) * N + r0
+        uncorr = ((i1 == i2) - G[i2, i1]) * ((i3 == i4) - G[i4, i3])
+        return uncorr + ((i1 == i4) - G[i4, i1]) * G[i2, i3]
+
+    for s1 in (0, 2):
+        for s2 in (0, 2):
+            for x in range(L):
+                for y in range(L):
+                    ri = _site_pbc(L, x0 + x, y0 + y)
+                    e1 = ev(ri, X + s1, X + s1, X + s2, X + s2)
+                    e2 = ev(ri, X + s1, X + s1, Y + s2, Y + s2)
+                    e3 = ev(ri, Y + s1, Y + s1, X + s2, X + s2)
+                    e4 = ev(ri, Y + s1, Y + s1, Y + s2, Y + s2)
+                    Cm[y, x] += np.sum(e1 - e2 - e3 + e4)
+                    Cp[y, x] += np.sum(e1 + e2 + e3 + e4)
+    return Cp / N, Cm / N
+
+
+def measure_zfpc(L, Gt0s):
+    """measure_zfpc! (src/fermion_measurements.jl:486-530): the pairing
+    correlators of measure_etpc summed over G(tau, 0), tau = 1..M (origin mean
+    only, no division by M).  Returns (P_plus, P_minus)."""
+    Pp = np.zeros((L, L))
+    Pm = np.zeros((L, L))
+    for g in Gt0s:
+        a, b = measure_etpc(L, g)
+        Pp += a
+        Pm += b
+    return Pp, Pm
+
+
+def is_reflection_symmetric(a, tol=1e-12):
+    """is_reflection_symmetric (src/fermion_measurements.jl:179-201): the inner
+    block a[1:, 1:] equals its reversal along each axis, and the first row and
+    column without their corner equal their reversals, within tol (the
+    reference compares the maximum of the signed difference)."""
+    a = np.asarray(a)
+    inner = a[1:, 1:]
+    parts = [inner - np.flip(inner, axis=0), inner - np.flip(inner, axis=1),
+             a[0, 1:] - a[0, 1:][::-1], a[1:, 0] - a[1:, 0][::-1]]
+    return all(np.max(np.real(d)) < tol and np.max(np.imag(d)) < tol for d in parts)
 
 
 # ---------------------------------------------------------------------------

@@ -411,11 +411,18 @@ def test_batch_matches_single_chains(lib):
     batch.close()
 
 
-@pytest.mark.parametrize("cfg,prec", [("small", "fp64"), ("c0", "fp64"), ("c0", "mixed")])
+def _tdgf_params(cfg, small_params):
+    # ref_test: the reference's test system (M = safe_mult = 10), where fill_tdgf!
+    # propagates slices 6..10 from the not yet filled (zero) slice 5
+    return {"small": dataclasses.replace(small_params, slices=20, safe_mult=5), "ref_test": small_params,
+            "c0": C0}[cfg]
+
+
+@pytest.mark.parametrize("cfg,prec", [("small", "fp64"), ("ref_test", "fp64"), ("c0", "fp64"), ("c0", "mixed")])
 def test_time_displaced_greens(lib, golden, small_params, cfg, prec):
     """measure_tdgfs! (time-displaced G(tau, 0) and -G(0, tau) for every slice)
     against the oracle's restatement; mixed form within 1e-8."""
-    p = dataclasses.replace(small_params, slices=20, safe_mult=5) if cfg == "small" else C0
+    p = _tdgf_params(cfg, small_params)
     phi = R.synthetic_field(p.N, p.slices, 41)
     ref = R.DQMCRef(p, phi)
     gt0_r, g0t_r = ref.measure_tdgfs()
@@ -451,5 +458,47 @@ def test_lu_blocked_and_unblocked(lib, monkeypatch, tune, L, prec):
             Gr, ldr = ref.calc_greens_and_logdet(sl)
             assert relerr(G, Gr) < tol
             assert abs(ld - ldr) < 10 * tol * max(1.0, abs(ldr))
+    finally:
+        gpu.close()
+
+
+@pytest.mark.parametrize("L", [4, 8])
+def test_equal_time_correlators(lib, L):
+    """dqmc_measure_equal_time against the oracle's measure_etpc / measure_etcdc
+    (src/fermion_measurements.jl:388-427, 580-620): on a given true G and on
+    the measurement hook's G of the current slice (1e-12 and 1e-10 relative)."""
+    p = dataclasses.replace(C0, L=L, slices=20)
+    phi = R.synthetic_field(p.N, p.slices, 71 + L)
+    ref = R.DQMCRef(p, phi)
+    ref.init()
+    gpu = lib.DQMC(api_params(p), phi)
+    try:
+        gpu.init()
+        g_true = ref.measured_greens()
+        want = R.measure_etpc(L, g_true) + R.measure_etcdc(L, g_true)
+        # given G: only the summation order differs; hook G: the GPU's own G (TOL)
+        for got, tol in ((gpu.measure_equal_time(g_true), 1e-12), (gpu.measure_equal_time(), TOL)):
+            for a, b in zip(got, want):
+                assert relerr(a, b) < tol
+    finally:
+        gpu.close()
+
+
+@pytest.mark.parametrize("cfg", ["ref_test", "c0"])
+def test_zero_frequency_pairing(lib, small_params, cfg):
+    """dqmc_measure_zfpc (measure_zfpc!, src/fermion_measurements.jl:486-530) on
+    the device's own G(tau, 0) and on the oracle's G(tau, 0) passed in,
+    against the oracle (1e-10 relative)."""
+    p = _tdgf_params(cfg, small_params)
+    phi = R.synthetic_field(p.N, p.slices, 43)
+    ref = R.DQMCRef(p, phi)
+    gt0_r, _ = ref.measure_tdgfs()
+    want = R.measure_zfpc(p.L, gt0_r)
+    gpu = lib.DQMC(api_params(p), phi)
+    try:
+        gpu.init()
+        for got in (gpu.measure_zfpc(), gpu.measure_zfpc(gt0_r)):
+            for a, b in zip(got, want):
+                assert relerr(a, b) < TOL
     finally:
         gpu.close()

@@ -93,3 +93,75 @@ def test_boson_measurements(golden):
     m2, m4 = R.measure_binder_factors(rc)
     assert np.isclose(m2, golden["lit_binder_m2"], rtol=1e-14)
     assert np.isclose(m4, golden["lit_binder_m4"], rtol=1e-14)
+
+
+def _etpc_etcdc_loops(L, G):
+    """Literal transcription of the reference loops (origins outer, then the
+    displacement; src/fermion_measurements.jl:388-427, 580-620), pure Python."""
+    N = L * L
+    site = lambda x, y: (y % L) + L * (x % L)
+    js = ((2, 0, 0, 2), (2, 0, 3, 1), (1, 3, 0, 2), (1, 3, 3, 1))
+    Pp = np.zeros((L, L)); Pm = np.zeros((L, L))
+    Cp = np.zeros((L, L), complex); Cm = np.zeros((L, L), complex)
+    for x in range(L):
+        for y in range(L):
+            for x0 in range(L):
+                for y0 in range(L):
+                    r1 = site(x0 + x, y0 + y); r3 = site(x0, y0)
+                    ev = []
+                    for j in js:
+                        i1, i2, i3, i4 = j[0] * N + r1, j[1] * N + r1, j[2] * N + r3, j[3] * N + r3
+                        ev.append((G[i1, i4] * G[i2, i3] - G[i1, i3] * G[i2, i4]).real)
+                    Pm[y, x] += ev[0] - ev[1] - ev[2] + ev[3]
+                    Pp[y, x] += ev[0] + ev[1] + ev[2] + ev[3]
+    for x0 in range(L):
+        for y0 in range(L):
+            for s1 in (0, 2):
+                for s2 in (0, 2):
+                    for x in range(L):
+                        for y in range(L):
+                            ri = site(x0 + x, y0 + y); r0 = site(x0, y0)
+
+                            def ev(j1, j2, j3, j4):
+                                i1, i2, i3, i4 = (j1 - 1) * N + ri, (j2 - 1) * N + ri, (j3 - 1) * N + r0, (j4 - 1) * N + r0
+                                unc = (float(i1 == i2) - G[i2, i1]) * (float(i3 == i4) - G[i4, i3])
+                                return unc + (float(i1 == i4) - G[i4, i1]) * G[i2, i3]
+                            e1, e2 = ev(1 + s1, 1 + s1, 1 + s2, 1 + s2), ev(1 + s1, 1 + s1, 2 + s2, 2 + s2)
+                            e3, e4 = ev(2 + s1, 2 + s1, 1 + s2, 1 + s2), ev(2 + s1, 2 + s1, 2 + s2, 2 + s2)
+                            Cm[y, x] += e1 - e2 - e3 + e4
+                            Cp[y, x] += e1 + e2 + e3 + e4
+    return Pp / N, Pm / N, Cp / N, Cm / N
+
+
+def test_equal_time_correlators(golden, small_params):
+    """tests_O3_measurements.jl:220-249 on the reference's own G (O3.jld
+    `greens`, made true by effective_greens2greens!): ETPC reflection
+    symmetric within 1e-3, ETCDC imaginary parts below 1e-12 and reflection
+    symmetric within 1e-3; the vectorised restatement equals a literal
+    transcription of the reference loops."""
+    ref = R.DQMCRef(small_params, golden["randconf"])
+    g = ref.effective_greens2greens(golden["greens"])
+    Pp, Pm = R.measure_etpc(4, g)
+    Cp, Cm = R.measure_etcdc(4, g)
+    assert R.is_reflection_symmetric(Pm, tol=1e-3) and R.is_reflection_symmetric(Pp, tol=1e-3)
+    assert np.max(np.imag(Cm)) < 1e-12 and np.max(np.imag(Cp)) < 1e-12
+    assert R.is_reflection_symmetric(Cm, tol=1e-3) and R.is_reflection_symmetric(Cp, tol=1e-3)
+    lp, lm, lcp, lcm = _etpc_etcdc_loops(4, g)
+    for a, b in ((Pp, lp), (Pm, lm), (Cp, lcp), (Cm, lcm)):
+        assert np.max(np.abs(a - b)) < 1e-13
+
+
+def test_zero_frequency_pairing(golden, small_params):
+    """tests_O3_measurements.jl:251-268 for the reference's test configuration:
+    ZFPC of the time-displaced G reflection symmetric within 1e-3, and ZFPC of
+    M copies of the equal-time G equal to M times ETPC."""
+    ref = R.DQMCRef(small_params, golden["randconf"])
+    ref.init()
+    g = ref.effective_greens2greens(ref.greens)
+    Gt0, _ = ref.measure_tdgfs()
+    Pp, Pm = R.measure_zfpc(4, Gt0)
+    assert R.is_reflection_symmetric(Pm, tol=1e-3) and R.is_reflection_symmetric(Pp, tol=1e-3)
+    M = small_params.slices
+    zp, zm = R.measure_zfpc(4, [g] * M)
+    ep, em = R.measure_etpc(4, g)
+    assert np.allclose(zp / M, ep, rtol=1e-12, atol=1e-14) and np.allclose(zm / M, em, rtol=1e-12, atol=1e-14)
