@@ -117,6 +117,7 @@ __device__ double block_sum(double v, double* scratch) {
 // ---------------------------------------------------------------------------
 constexpr int QR_THREADS = 256;
 constexpr int QR_MAXT = 32;   // elements per lane of one column (n <= 1024)
+constexpr int CAND_PER_LANE = 8;   // per-CTA pivot candidates read per lane: grids of at most 256 CTAs
 
 // Candidate of the next pivot: the CTA-local maximum of the partial norms
 // and its logical position (ties: smaller position, as LAPACK's idamax).
@@ -265,13 +266,21 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
   for (int k = 0; k < n; ++k) {
     // ---- pivot: best of the per-CTA candidates (first position of maximal norm), warp 0 ----
     if (wid == 0) {
+      // all candidate loads in flight at once (grid <= 32 * CAND_PER_LANE), then the compares
+      double cvv[CAND_PER_LANE];
+      int cqq[CAND_PER_LANE];
+#pragma unroll
+      for (int u = 0; u < CAND_PER_LANE; ++u) {
+        const int c = lane + 32 * u;
+        cvv[u] = 0.0;
+        cqq[u] = n;
+        if (c < (int)gridDim.x) { cvv[u] = __ldcg(&w.cand_v[c]); cqq[u] = __ldcg(&w.cand_q[c]); }
+      }
       double best = 0.0;
       int bestq = n;
-      for (int c = lane; c < (int)gridDim.x; c += 32) {
-        double val = __ldcg(&w.cand_v[c]);
-        int q = __ldcg(&w.cand_q[c]);
-        if (cand_better(val, q, best, bestq)) { best = val; bestq = q; }
-      }
+#pragma unroll
+      for (int u = 0; u < CAND_PER_LANE; ++u)
+        if (cand_better(cvv[u], cqq[u], best, bestq)) { best = cvv[u]; bestq = cqq[u]; }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         double ob = __shfl_xor_sync(0xffffffffu, best, o);
@@ -597,13 +606,21 @@ __global__ void __launch_bounds__(256) k_lu_panel(cplx* __restrict__ A, int n, i
     const int k = p0 + kk;
     // ---- pivot: best candidate (first row of maximal |Re| + |Im|) ----
     if (wid == 0) {
+      // all candidate loads in flight at once (grid <= 32 * CAND_PER_LANE), then the compares
+      double cvv[CAND_PER_LANE];
+      int crr[CAND_PER_LANE];
+#pragma unroll
+      for (int u = 0; u < CAND_PER_LANE; ++u) {
+        const int c = lane + 32 * u;
+        cvv[u] = 0.0;
+        crr[u] = n;
+        if (c < (int)gridDim.x) { cvv[u] = __ldcg(&w.cand_v[c]); crr[u] = __ldcg(&w.cand_r[c]); }
+      }
       double best = 0.0;
       int brow = n, bc = 0;
-      for (int c = lane; c < (int)gridDim.x; c += 32) {
-        const double v = __ldcg(&w.cand_v[c]);
-        const int r = __ldcg(&w.cand_r[c]);
-        if (piv_better(v, r, best, brow)) { best = v; brow = r; bc = c; }
-      }
+#pragma unroll
+      for (int u = 0; u < CAND_PER_LANE; ++u)
+        if (piv_better(cvv[u], crr[u], best, brow)) { best = cvv[u]; brow = crr[u]; bc = lane + 32 * u; }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const double ob = __shfl_xor_sync(0xffffffffu, best, o);
@@ -1154,6 +1171,7 @@ cudaError_t launch_qrp(cplx* A, int n, QRWork& w, int sm_count, cudaStream_t st,
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   int grid = sm_count;   // one CTA per SM; remaining columns are dealt round-robin over all CTAs
   if (max_grid > 0 && grid > max_grid) grid = max_grid;
+  if (grid > 32 * CAND_PER_LANE) grid = 32 * CAND_PER_LANE;
   QRWork copy = w;
   void* args[] = {&A, &n, &copy};
   return cudaLaunchCooperativeKernel((void*)k_qrp, dim3(grid), dim3(QR_THREADS), args, smem, st);
@@ -1243,7 +1261,7 @@ cudaError_t launch_lu_panel(cplx* A, int n, int p0, int b, LUPanel& w, int sm_co
   int grid = sm_count;
   if (max_grid > 0 && grid > max_grid) grid = max_grid;
   if (grid > n - p0) grid = n - p0;
-  if (grid > 1024) grid = 1024;
+  if (grid > 32 * CAND_PER_LANE) grid = 32 * CAND_PER_LANE;
   const int chunk = (n - p0 + grid - 1) / grid;
   const size_t smem = (size_t)chunk * LU_PB * sizeof(cplx);
   constexpr size_t kMax = 160 * 1024;
