@@ -55,9 +55,11 @@ METRIC = "O(3) L=16 sweeps/s: mixed vs FP64 at G err≤1e-8; batched chain-sweep
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # roofline kernels at L=16 (n = 1024), one ncu capture each of this bench's
-# L=16 mixed workload (None: not captured)
-TRAFFIC = {"qrp": 21.385e6, "lu": 21.337e6, "apply_q": 25.293e6, "trsm": 25.249e6, "flush": None,
-           "ozaki_gemm": 263.785e6}
+# L=16 mixed workload: k_qrp (one QR) and k_oz_gemm (one n x n x n product).
+# None: the kind is several kernels per algorithmic unit (blocked LU, blocked
+# triangular solves, compact-WY Q formation, flush)
+TRAFFIC = {"qrp": 21.351e6, "lu": None, "apply_q": None, "trsm": None, "flush": None,
+           "ozaki_gemm": 333.239e6}
 
 
 def model_params(L, M):
