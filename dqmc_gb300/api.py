@@ -89,6 +89,8 @@ SIGNATURES = {
     "dqmc_measure": ([_P, _D, _D, _D], ctypes.c_int),
     "dqmc_measure_equal_time": ([_P, _D, _D, _D, _D, _D, ctypes.c_int32], ctypes.c_int),
     "dqmc_measure_zfpc": ([_P, _D, _D, _D, ctypes.c_int32], ctypes.c_int),
+    "dqmc_measure_zfcdc": ([_P, _D, _D, _D, _D, _D, ctypes.c_int32], ctypes.c_int),
+    "dqmc_measure_zfccc": ([_P, _D, _D, _D, _D, _D, _D, ctypes.c_int32], ctypes.c_int),
     "dqmc_get_timing": ([_P, ctypes.POINTER(CTiming)], ctypes.c_int),
     "dqmc_reset_timing": ([_P, _I32], ctypes.c_int),
     "dqmc_peak_fp64": ([_I32, _D], ctypes.c_int),
@@ -396,8 +398,8 @@ class DQMC:
         return dict(greens=G, occupation=occ.value, e_kin=ek.value)
 
     def measure_equal_time(self, greens=None):
-        """measure_etpc! and measure_etcdc! (src/fermion_measurements.jl:388-427,
-        580-620) of the true G `greens` (n x n), or of the measurement hook's G
+        """measure_etpc! and measure_etcdc! (src/fermion_measurements.jl:388-424,
+        592-630) of the true G `greens` (n x n), or of the measurement hook's G
         when None.  Returns (etpc_plus, etpc_minus, etcdc_plus, etcdc_minus),
         each L x L indexed [y, x] by the displacement."""
         L = self.p.L
@@ -414,7 +416,7 @@ class DQMC:
         return pp, pm, cp, cm
 
     def measure_zfpc(self, gt0=None):
-        """measure_zfpc! (src/fermion_measurements.jl:486-530) over G(tau, 0)
+        """measure_zfpc! (src/fermion_measurements.jl:500-541) over G(tau, 0)
         given as an (M, n, n) array (as measure_tdgfs returns), or computed on
         the device when None.  Returns (zfpc_plus, zfpc_minus), L x L [y, x]."""
         L = self.p.L
@@ -427,6 +429,47 @@ class DQMC:
         self._check(self.lib.dqmc_measure_zfpc(self.h, g.ctypes.data_as(_D) if g is not None else None,
                                                pp.ctypes.data_as(_D), pm.ctypes.data_as(_D), 0))
         return pp, pm
+
+    def measure_zfcdc(self, greens=None, gt0=None, g0t=None):
+        """measure_zfcdc! (src/fermion_measurements.jl:688-743) from the true
+        equal-time G (None: the hook's G) and the (M, n, n) arrays that
+        measure_tdgfs returns (None: computed on the device).  Returns
+        (zfcdc_plus, zfcdc_minus), L x L complex [y, x]."""
+        L = self.p.L
+        if (gt0 is None) != (g0t is None):
+            raise ValueError("pass both gt0 and g0t or neither")
+
+        def blocks(a):
+            return np.ascontiguousarray(np.asarray(a, dtype=np.complex128).transpose(0, 2, 1))
+        g = None if greens is None else np.asfortranarray(np.asarray(greens, dtype=np.complex128))
+        a = None if gt0 is None else blocks(gt0)
+        b = None if g0t is None else blocks(g0t)
+        cp = np.zeros((L, L), dtype=np.complex128, order="F")
+        cm = np.zeros((L, L), dtype=np.complex128, order="F")
+        ptr = lambda x: x.ctypes.data_as(_D) if x is not None else None
+        self._check(self.lib.dqmc_measure_zfcdc(self.h, ptr(g), ptr(a), ptr(b), ptr(cp), ptr(cm), 0))
+        return cp, cm
+
+    def measure_zfccc(self, greens=None, gt0=None, g0t=None):
+        """measure_zfccc! (src/fermion_measurements.jl:814-888) and
+        measure_sfdensity (:911-920), inputs as measure_zfcdc.  Returns
+        (zfccc_xx, zfccc_yy, sfdensity), the arrays L x L complex [y, x]."""
+        L = self.p.L
+        if (gt0 is None) != (g0t is None):
+            raise ValueError("pass both gt0 and g0t or neither")
+
+        def blocks(a):
+            return np.ascontiguousarray(np.asarray(a, dtype=np.complex128).transpose(0, 2, 1))
+        g = None if greens is None else np.asfortranarray(np.asarray(greens, dtype=np.complex128))
+        a = None if gt0 is None else blocks(gt0)
+        b = None if g0t is None else blocks(g0t)
+        lxx = np.zeros((L, L), dtype=np.complex128, order="F")
+        lyy = np.zeros((L, L), dtype=np.complex128, order="F")
+        rho = ctypes.c_double()
+        ptr = lambda x: x.ctypes.data_as(_D) if x is not None else None
+        self._check(self.lib.dqmc_measure_zfccc(self.h, ptr(g), ptr(a), ptr(b), ptr(lxx), ptr(lyy),
+                                                ctypes.byref(rho), 0))
+        return lxx, lyy, rho.value
 
     def global_update(self, shift, u):
         """global_update (src/global_updates.jl:18-58) with a fixed-slot shift

@@ -1085,6 +1085,18 @@ int measure(dqmc_handle* h, cplx* Gt0, cplx* G0t) {
 
 }  // namespace tdgf
 
+// The measurement hook's true G of the current slice into dst:
+// wrap_greens(G, current_slice, +1), then effective -> true
+// (src/dqmc_framework.jl:378-381, src/fermion_measurements.jl:1125-1142).
+static int hook_true_greens(dqmc_handle* h, cplx* dst) {
+  if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
+  if (h->current_slice < 1 || h->current_slice > h->M) return set_err(h, DQMC_ERR_STATE, "no current slice");
+  CHK(copy_nn(h, dst, h->G));
+  CHK(wrap_greens(h, dst, h->current_slice, 1));
+  CHK(apply_rows(h, dst, 0, 1, 1, SLICE_EFF_RIGHT));
+  return apply_cols(h, dst, 0, 1, 1, SLICE_EFF_LEFT_INV, nullptr);
+}
+
 extern "C" {
 
 const char* dqmc_version(void) { return DQMC_VERSION_STRING; }
@@ -1786,13 +1798,7 @@ int dqmc_measure_equal_time(dqmc_handle* h, const double* greens, double* etpc_p
       src = h->Gtmp;
     }
   } else {
-    // the measurement hook's G: wrap_greens(G, current_slice, +1), effective -> true
-    if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
-    if (h->current_slice < 1 || h->current_slice > h->M) return set_err(h, DQMC_ERR_STATE, "no current slice");
-    CHK(copy_nn(h, h->Gtmp, h->G));
-    CHK(wrap_greens(h, h->Gtmp, h->current_slice, 1));
-    CHK(apply_rows(h, h->Gtmp, 0, 1, 1, SLICE_EFF_RIGHT));
-    CHK(apply_cols(h, h->Gtmp, 0, 1, 1, SLICE_EFF_LEFT_INV, nullptr));
+    CHK(hook_true_greens(h, h->Gtmp));
     src = h->Gtmp;
   }
   if (!h->etc_d) CU(cudaMalloc(&h->etc_d, (size_t)6 * N * sizeof(double)));
@@ -1959,6 +1965,104 @@ int dqmc_measure_zfpc(dqmc_handle* h, const double* Gt0, double* zfpc_plus, doub
   cudaFree(scratch);
   if (rc != DQMC_OK) return set_err(h, rc, "zfpc");
   return check_device_error(h);
+}
+
+// Shared body of the zero-frequency charge-density (which = 0) and
+// current-current (which = 1) measurements: stages the equal-time G and the
+// time-displaced blocks, runs the kernel, copies 2 L^2 complex outputs.
+static int zero_frequency_measure(dqmc_handle* h, int which, const double* greens, const double* Gt0,
+                                  const double* G0t, double* out0, double* out1, double* sfdensity,
+                                  int32_t device_ptrs) {
+  if (h) cudaSetDevice(h->device);
+  if (!h || (Gt0 == nullptr) != (G0t == nullptr)) return DQMC_ERR_ARG;
+  const int N = h->N, M = h->M;
+  const size_t nn = (size_t)h->n * h->n, bytes = (size_t)M * nn * sizeof(cplx);
+  const bool own = !(Gt0 && device_ptrs);   // time-displaced blocks staged in memory of this call
+  cplx *gt0 = nullptr, *g0t = nullptr;
+  int rc = DQMC_OK;
+  if (own) {
+    if (!Gt0 && !h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
+    if (cudaMalloc(&gt0, bytes) != cudaSuccess || cudaMalloc(&g0t, bytes) != cudaSuccess) {
+      rc = DQMC_ERR_CUDA;
+    } else if (Gt0) {
+      if (cudaMemcpyAsync(gt0, Gt0, bytes, cudaMemcpyHostToDevice, h->st) != cudaSuccess ||
+          cudaMemcpyAsync(g0t, G0t, bytes, cudaMemcpyHostToDevice, h->st) != cudaSuccess)
+        rc = DQMC_ERR_CUDA;
+    } else {
+      rc = tdgf::measure(h, gt0, g0t);
+    }
+  } else {
+    gt0 = reinterpret_cast<cplx*>(const_cast<double*>(Gt0));
+    g0t = reinterpret_cast<cplx*>(const_cast<double*>(G0t));
+  }
+  // equal-time G: given (host or device) or the measurement hook's
+  const cplx* g = nullptr;
+  if (rc == DQMC_OK) {
+    if (greens && device_ptrs) {
+      g = reinterpret_cast<const cplx*>(greens);
+    } else if (greens) {
+      if (cudaMemcpyAsync(h->Gtmp, greens, nn * sizeof(cplx), cudaMemcpyHostToDevice, h->st) != cudaSuccess)
+        rc = DQMC_ERR_CUDA;
+      g = h->Gtmp;
+    } else {
+      rc = hook_true_greens(h, h->Gtmp);
+      g = h->Gtmp;
+    }
+  }
+  if (rc == DQMC_OK && !h->etc_d && cudaMalloc(&h->etc_d, (size_t)6 * N * sizeof(double)) != cudaSuccess)
+    rc = DQMC_ERR_CUDA;
+  if (rc == DQMC_OK) {
+    // hopping amplitudes by direction (x, y) and band (X, Y), as the measurement hook's E_kin
+    const double thop[2][2] = {{h->p.hoppings[0], h->p.hoppings[2]}, {h->p.hoppings[1], h->p.hoppings[3]}};
+    const cudaError_t e = which == 0 ? launch_zfcdc(g, gt0, g0t, M, h->L, h->etc_d, h->st)
+                                     : launch_zfccc(g, gt0, g0t, M, h->L, thop, h->etc_d, h->st);
+    if (e != cudaSuccess) rc = DQMC_ERR_CUDA;
+    ++h->launches;
+  }
+  const cudaMemcpyKind kind = device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (rc == DQMC_OK && out0 &&
+      cudaMemcpyAsync(out0, h->etc_d, 2 * N * sizeof(double), kind, h->st) != cudaSuccess) rc = DQMC_ERR_CUDA;
+  if (rc == DQMC_OK && out1 &&
+      cudaMemcpyAsync(out1, h->etc_d + 2 * N, 2 * N * sizeof(double), kind, h->st) != cudaSuccess)
+    rc = DQMC_ERR_CUDA;
+  std::vector<double> lxx;
+  if (rc == DQMC_OK && sfdensity) {
+    lxx.resize((size_t)2 * N);
+    if (cudaMemcpyAsync(lxx.data(), h->etc_d, 2 * N * sizeof(double), cudaMemcpyDeviceToHost, h->st) != cudaSuccess)
+      rc = DQMC_ERR_CUDA;
+  }
+  if (cudaStreamSynchronize(h->st) != cudaSuccess && rc == DQMC_OK) rc = DQMC_ERR_CUDA;
+  if (own) {
+    cudaFree(gt0);
+    cudaFree(g0t);
+  }
+  if (rc == DQMC_ERR_CUDA) return set_err(h, rc, "zero-frequency measurement: device memory or copy");
+  if (rc != DQMC_OK) return rc;
+  if (sfdensity) {
+    // measure_sfdensity (src/fermion_measurements.jl:911-920): with q the real
+    // 2D DFT of Re Lambda_xx (first index y), rho_s = (Re q[0, 1] - Re q[1, 0]) / 4
+    const int L = h->L;
+    const double w = 2.0 * 3.14159265358979323846 / L;
+    double qx = 0.0, qy = 0.0;
+    for (int x = 0; x < L; ++x)
+      for (int y = 0; y < L; ++y) {
+        const double v = lxx[2 * ((size_t)y + (size_t)L * x)];
+        qx += v * std::cos(w * x);
+        qy += v * std::cos(w * y);
+      }
+    *sfdensity = 0.25 * (qx - qy);
+  }
+  return check_device_error(h);
+}
+
+int dqmc_measure_zfcdc(dqmc_handle* h, const double* greens, const double* Gt0, const double* G0t,
+                       double* zfcdc_plus, double* zfcdc_minus, int32_t device_ptrs) {
+  return zero_frequency_measure(h, 0, greens, Gt0, G0t, zfcdc_plus, zfcdc_minus, nullptr, device_ptrs);
+}
+
+int dqmc_measure_zfccc(dqmc_handle* h, const double* greens, const double* Gt0, const double* G0t,
+                       double* zfccc_xx, double* zfccc_yy, double* sfdensity, int32_t device_ptrs) {
+  return zero_frequency_measure(h, 1, greens, Gt0, G0t, zfccc_xx, zfccc_yy, sfdensity, device_ptrs);
 }
 
 }  // extern "C"

@@ -201,6 +201,12 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
 cudaError_t launch_equal_time_corr(const cplx* G, int L, double* out, cudaStream_t st);
 // out (2 L^2 doubles): P+ and P- summed over the `slices` matrices of Gt0 (stride n^2)
 cudaError_t launch_zfpc(const cplx* Gt0, int slices, int L, double* out, cudaStream_t st);
+// out (4 L^2 doubles): C+ and C- (L x L complex) of the equal-time G, G(tau, 0) and -G(0, tau)
+cudaError_t launch_zfcdc(const cplx* G, const cplx* Gt0, const cplx* G0t, int slices, int L, double* out,
+                         cudaStream_t st);
+// out (4 L^2 doubles): Lambda_xx and Lambda_yy (L x L complex); thop[dir][band] hopping amplitudes
+cudaError_t launch_zfccc(const cplx* G, const cplx* Gt0, const cplx* G0t, int slices, int L, const double thop[2][2],
+                         double* out, cudaStream_t st);
 
 cudaError_t launch_force_slice(const cplx* G, const double* phi, double* grad, int N, int slice0, double lambda_dtau,
                                cudaStream_t st);

@@ -234,8 +234,8 @@ DQMC_API int dqmc_calc_boson_action(dqmc_handle* h, double* S);
  * occupation (src/fermion_measurements.jl:322) and kinetic energy
  * E_kin = sum_ij T_ij <c_i^dag c_j> (not an observable of the reference). */
 DQMC_API int dqmc_measure(dqmc_handle* h, double* greens_out, double* occupation, double* e_kin);
-/* Equal-time pairing correlators measure_etpc! (src/fermion_measurements.jl:388-427)
- * and charge-density correlators measure_etcdc! (:580-620) of a true G: the
+/* Equal-time pairing correlators measure_etpc! (src/fermion_measurements.jl:388-424)
+ * and charge-density correlators measure_etcdc! (:592-630) of a true G: the
  * n x n column-major complex `greens` if not NULL (as the reference's `greens`
  * argument), else the measurement hook's true G of the current slice.  Outputs
  * (each may be NULL) are L x L column-major, element (y, x) = displacement
@@ -273,7 +273,7 @@ DQMC_API int dqmc_force(dqmc_handle* h, double* grad_logdet, double* grad_boson)
  * complex at offset (tau - 1) n^2 (2 M n^2 doubles per array).  device_ptrs != 0: Gt0 and
  * G0t are device addresses on the handle's device; otherwise host buffers. */
 DQMC_API int dqmc_measure_tdgfs(dqmc_handle* h, double* Gt0, double* G0t, int32_t device_ptrs);
-/* measure_zfpc! (src/fermion_measurements.jl:486-530): the pairing correlators of
+/* measure_zfpc! (src/fermion_measurements.jl:500-541): the pairing correlators of
  * dqmc_measure_equal_time summed over G(tau, 0), tau = 1..M (not divided by M,
  * as in the reference).  Gt0: the M blocks that dqmc_measure_tdgfs writes, or
  * NULL to compute them for the current field on the device.  zfpc_plus /
@@ -281,6 +281,22 @@ DQMC_API int dqmc_measure_tdgfs(dqmc_handle* h, double* Gt0, double* G0t, int32_
  * device_ptrs != 0: Gt0 and the outputs are device addresses. */
 DQMC_API int dqmc_measure_zfpc(dqmc_handle* h, const double* Gt0, double* zfpc_plus, double* zfpc_minus,
                                int32_t device_ptrs);
+/* measure_zfcdc! (src/fermion_measurements.jl:688-743, _zfcdc_ev :753-766):
+ * zero-frequency charge-density correlators summed over tau = 1..M from the
+ * true equal-time G `greens` (NULL: the measurement hook's G), G(tau, 0) in Gt0
+ * and the stored -G(0, tau) in G0t as dqmc_measure_tdgfs writes them (both
+ * NULL: computed for the current field on the device).  zfcdc_plus /
+ * zfcdc_minus: L x L complex (2 L^2 doubles), element (y, x) at y + L x; each
+ * may be NULL.  device_ptrs != 0: every pointer is a device address. */
+DQMC_API int dqmc_measure_zfcdc(dqmc_handle* h, const double* greens, const double* Gt0, const double* G0t,
+                                double* zfcdc_plus, double* zfcdc_minus, int32_t device_ptrs);
+/* measure_zfccc! (src/fermion_measurements.jl:814-888): zero-frequency
+ * current-current correlators Lambda_xx, Lambda_yy (L x L complex, 2 L^2
+ * doubles each, element (y, x) at y + L x), inputs as dqmc_measure_zfcdc; and
+ * measure_sfdensity (:911-920) of Lambda_xx into *sfdensity (host double, may
+ * be NULL).  device_ptrs != 0: every array pointer is a device address. */
+DQMC_API int dqmc_measure_zfccc(dqmc_handle* h, const double* greens, const double* Gt0, const double* G0t,
+                                double* zfccc_xx, double* zfccc_yy, double* sfdensity, int32_t device_ptrs);
 
 /* ---- diagnostics ------------------------------------------------------------- */
 /* Per-group device times (CUDA events on the handle's stream) and the number

@@ -869,7 +869,7 @@ class DQMCRef:
 
 
 # ---------------------------------------------------------------------------
-# equal-time fermion correlators (src/fermion_measurements.jl:363-620)
+# equal-time fermion correlators (src/fermion_measurements.jl:363-653)
 # ---------------------------------------------------------------------------
 def _site_pbc(L, x, y):
     """siteidx (src/fermion_measurements.jl:7-12), 0-based: sql[y, x] = y + L x with PBC."""
@@ -882,7 +882,7 @@ def _origins(L):
 
 
 def measure_etpc(L, G):
-    """measure_etpc! (src/fermion_measurements.jl:388-427) with _pc_ev (:436-451)
+    """measure_etpc! (src/fermion_measurements.jl:388-424) with _pc_ev (:435-449)
     for opdim 3 (G accessed directly, :23-26).  Flavours xu, yd, xd, yu are
     0, 1, 2, 3 here; index = flavour N + site.  Returns (P_plus, P_minus), each
     L x L real with [y, x] the displacement, averaged over the origins r0."""
@@ -906,8 +906,8 @@ def measure_etpc(L, G):
 
 
 def measure_etcdc(L, G):
-    """measure_etcdc! (src/fermion_measurements.jl:580-620) with _etcdc_ev
-    (:630-643): bands X = 1, Y = 2 and spins UP = 0, DOWN = 2 give the 1-based
+    """measure_etcdc! (src/fermion_measurements.jl:592-630) with _etcdc_ev
+    (:641-653): bands X = 1, Y = 2 and spins UP = 0, DOWN = 2 give the 1-based
     flavour band + spin.  Returns (C_plus, C_minus), L x L complex, [y, x] the
     displacement, averaged over the origins."""
     N = L * L
@@ -938,7 +938,7 @@ def measure_etcdc(L, G):
 
 
 def measure_zfpc(L, Gt0s):
-    """measure_zfpc! (src/fermion_measurements.jl:486-530): the pairing
+    """measure_zfpc! (src/fermion_measurements.jl:500-541): the pairing
     correlators of measure_etpc summed over G(tau, 0), tau = 1..M (origin mean
     only, no division by M).  Returns (P_plus, P_minus)."""
     Pp = np.zeros((L, L))
@@ -948,6 +948,84 @@ def measure_zfpc(L, Gt0s):
         Pp += a
         Pm += b
     return Pp, Pm
+
+
+def measure_zfcdc(L, greens, Gt0s, G0ts):
+    """measure_zfcdc! (src/fermion_measurements.jl:688-743) with _zfcdc_ev
+    (:753-766): greens is one true equal-time G (used as G(tau) and G(0) for
+    every tau), Gt0s[tau] = G(tau, 0) and G0ts[tau] the reference's stored
+    -G(0, tau).  Summed over tau = 1..M and averaged over the origins.
+    Returns (C_plus, C_minus), L x L complex indexed [y, x]."""
+    N = L * L
+    X, Y = 1, 2
+    x0, y0 = _origins(L)
+    r0 = _site_pbc(L, x0, y0)
+    Cp = np.zeros((L, L), dtype=np.complex128)
+    Cm = np.zeros((L, L), dtype=np.complex128)
+    for Gt0, G0t in zip(Gt0s, G0ts):
+        Gtau = G0 = greens
+
+        def ev(ri, j1, j2, j3, j4):
+            i1, i2 = (j1 - 1) * N + ri, (j2 - 1) * N + ri
+            i3, i4 = (j3 - 1) * N + r0, (j4 - 1) * N + r0
+            uncorr = ((i1 == i2) - Gtau[i2, i1]) * ((i3 == i4) - G0[i4, i3])
+            return uncorr + (-G0t[i4, i1]) * Gt0[i2, i3]
+
+        for s1 in (0, 2):
+            for s2 in (0, 2):
+                for x in range(L):
+                    for y in range(L):
+                        ri = _site_pbc(L, x0 + x, y0 + y)
+                        e1 = ev(ri, X + s1, X + s1, X + s2, X + s2)
+                        e2 = ev(ri, X + s1, X + s1, Y + s2, Y + s2)
+                        e3 = ev(ri, Y + s1, Y + s1, X + s2, X + s2)
+                        e4 = ev(ri, Y + s1, Y + s1, Y + s2, Y + s2)
+                        Cm[y, x] += np.sum(e1 - e2 - e3 + e4)
+                        Cp[y, x] += np.sum(e1 + e2 + e3 + e4)
+    return Cp / N, Cm / N
+
+
+def measure_zfccc(L, T, greens, Gt0s, G0ts):
+    """measure_zfccc! (src/fermion_measurements.jl:814-888): zero-frequency
+    current-current correlators from the hopping matrix T (n x n, the
+    reference's mc.l.hopping_matrix), one true equal-time G, G(tau, 0) and the
+    stored -G(0, tau).  Returns (Lambda_xx, Lambda_yy), L x L complex [y, x],
+    summed over tau, averaged over the origins and negated (i^2)."""
+    N = L * L
+    x0, y0 = _origins(L)
+    r0 = _site_pbc(L, x0, y0)
+    out = []
+    for dx, dy in ((1, 0), (0, 1)):
+        lam = np.zeros((L, L), dtype=np.complex128)
+        r0p = _site_pbc(L, x0 + dx, y0 + dy)
+        for Gt0, G0t in zip(Gt0s, G0ts):
+            Gtau = G0 = greens
+            for f1 in range(4):
+                for f2 in range(4):
+                    for x in range(L):
+                        for y in range(L):
+                            ri = _site_pbc(L, x0 + x, y0 + y)
+                            rj = _site_pbc(L, x0 + x + dx, y0 + y + dy)
+                            ais, ajs = f1 * N + ri, f1 * N + rj
+                            a0, a0p = f2 * N + r0, f2 * N + r0p
+                            tij, tji = T[ais, ajs], T[ajs, ais]
+                            t00p, t0p0 = T[a0, a0p], T[a0p, a0]
+                            v = (tij * Gtau[ajs, ais] - tji * Gtau[ais, ajs]) * \
+                                (t00p * G0[a0p, a0] - t0p0 * G0[a0, a0p])
+                            v = v - tij * t00p * G0t[a0p, ais] * Gt0[ajs, a0] \
+                                + tij * t0p0 * G0t[a0, ais] * Gt0[ajs, a0p] \
+                                + tji * t00p * G0t[a0p, ajs] * Gt0[ais, a0] \
+                                - tji * t0p0 * G0t[a0, ajs] * Gt0[ais, a0p]
+                            lam[y, x] += np.sum(v)
+        out.append(lam / -N)
+    return out[0], out[1]
+
+
+def measure_sfdensity(lambda_xx):
+    """measure_sfdensity (src/fermion_measurements.jl:911-920): with q the real
+    2D DFT of Re Lambda_xx (first index y), rho_s = (Re q[0, 1] - Re q[1, 0]) / 4."""
+    q = np.fft.rfft2(np.real(np.asarray(lambda_xx)).T).T   # halve the first (y) axis, as Julia's rfft
+    return 0.25 * (np.real(q[0, 1]) - np.real(q[1, 0]))
 
 
 def is_reflection_symmetric(a, tol=1e-12):

@@ -465,7 +465,7 @@ def test_lu_blocked_and_unblocked(lib, monkeypatch, tune, L, prec):
 @pytest.mark.parametrize("L", [4, 8])
 def test_equal_time_correlators(lib, L):
     """dqmc_measure_equal_time against the oracle's measure_etpc / measure_etcdc
-    (src/fermion_measurements.jl:388-427, 580-620): on a given true G and on
+    (src/fermion_measurements.jl:388-424, 592-630): on a given true G and on
     the measurement hook's G of the current slice (1e-12 and 1e-10 relative)."""
     p = dataclasses.replace(C0, L=L, slices=20)
     phi = R.synthetic_field(p.N, p.slices, 71 + L)
@@ -486,7 +486,7 @@ def test_equal_time_correlators(lib, L):
 
 @pytest.mark.parametrize("cfg", ["ref_test", "c0"])
 def test_zero_frequency_pairing(lib, small_params, cfg):
-    """dqmc_measure_zfpc (measure_zfpc!, src/fermion_measurements.jl:486-530) on
+    """dqmc_measure_zfpc (measure_zfpc!, src/fermion_measurements.jl:500-541) on
     the device's own G(tau, 0) and on the oracle's G(tau, 0) passed in,
     against the oracle (1e-10 relative)."""
     p = _tdgf_params(cfg, small_params)
@@ -500,5 +500,51 @@ def test_zero_frequency_pairing(lib, small_params, cfg):
         for got in (gpu.measure_zfpc(), gpu.measure_zfpc(gt0_r)):
             for a, b in zip(got, want):
                 assert relerr(a, b) < TOL
+    finally:
+        gpu.close()
+
+
+@pytest.mark.parametrize("cfg", ["ref_test", "c0"])
+def test_zero_frequency_charge_density(lib, small_params, cfg):
+    """dqmc_measure_zfcdc (measure_zfcdc!, src/fermion_measurements.jl:688-743):
+    all inputs on the device (hook G, device time-displaced G) against the
+    oracle (1e-10 relative), and the oracle's inputs passed in (1e-12)."""
+    p = _tdgf_params(cfg, small_params)
+    phi = R.synthetic_field(p.N, p.slices, 47)
+    ref = R.DQMCRef(p, phi)
+    ref.init()
+    g = ref.measured_greens()
+    gt0_r, g0t_r = ref.measure_tdgfs()
+    want = R.measure_zfcdc(p.L, g, gt0_r, g0t_r)
+    gpu = lib.DQMC(api_params(p), phi)
+    try:
+        gpu.init()
+        for got, tol in ((gpu.measure_zfcdc(), TOL), (gpu.measure_zfcdc(g, gt0_r, g0t_r), 1e-12)):
+            for a, b in zip(got, want):
+                assert relerr(a, b) < tol
+    finally:
+        gpu.close()
+
+
+@pytest.mark.parametrize("cfg", ["ref_test", "c0"])
+def test_zero_frequency_current_current(lib, small_params, cfg):
+    """dqmc_measure_zfccc (measure_zfccc!, src/fermion_measurements.jl:814-888,
+    and measure_sfdensity :911-920) against the oracle: all inputs on the device
+    (1e-10 relative) and the oracle's inputs passed in (1e-12)."""
+    p = _tdgf_params(cfg, small_params)
+    phi = R.synthetic_field(p.N, p.slices, 53)
+    ref = R.DQMCRef(p, phi)
+    ref.init()
+    g = ref.measured_greens()
+    gt0_r, g0t_r = ref.measure_tdgfs()
+    T = ref.T.toarray() if hasattr(ref.T, "toarray") else np.asarray(ref.T)
+    lxx_r, lyy_r = R.measure_zfccc(p.L, T, g, gt0_r, g0t_r)
+    rho_r = R.measure_sfdensity(lxx_r)
+    gpu = lib.DQMC(api_params(p), phi)
+    try:
+        gpu.init()
+        for (lxx, lyy, rho), tol in ((gpu.measure_zfccc(), TOL), (gpu.measure_zfccc(g, gt0_r, g0t_r), 1e-12)):
+            assert relerr(lxx, lxx_r) < tol and relerr(lyy, lyy_r) < tol
+            assert abs(rho - rho_r) < tol * max(1.0, float(np.max(np.abs(lxx_r))))
     finally:
         gpu.close()

@@ -97,7 +97,7 @@ def test_boson_measurements(golden):
 
 def _etpc_etcdc_loops(L, G):
     """Literal transcription of the reference loops (origins outer, then the
-    displacement; src/fermion_measurements.jl:388-427, 580-620), pure Python."""
+    displacement; src/fermion_measurements.jl:388-424, 592-630), pure Python."""
     N = L * L
     site = lambda x, y: (y % L) + L * (x % L)
     js = ((2, 0, 0, 2), (2, 0, 3, 1), (1, 3, 0, 2), (1, 3, 3, 1))
@@ -165,3 +165,59 @@ def test_zero_frequency_pairing(golden, small_params):
     zp, zm = R.measure_zfpc(4, [g] * M)
     ep, em = R.measure_etpc(4, g)
     assert np.allclose(zp / M, ep, rtol=1e-12, atol=1e-14) and np.allclose(zm / M, em, rtol=1e-12, atol=1e-14)
+
+
+def test_zero_frequency_charge_density(golden, small_params):
+    """tests_O3_measurements.jl:270-282 for the reference's test configuration:
+    ZFCDC imaginary parts below 1e-12, C- reflection symmetric within 1e-3 and
+    C+ within 2e-3; the vectorised restatement equals a literal transcription of
+    the reference loops (tau, origin, spins, displacement)."""
+    ref = R.DQMCRef(small_params, golden["randconf"])
+    ref.init()
+    g = ref.effective_greens2greens(ref.greens)
+    Gt0, G0t = ref.measure_tdgfs()
+    Cp, Cm = R.measure_zfcdc(4, g, Gt0, G0t)
+    assert np.max(np.imag(Cm)) < 1e-12 and np.max(np.imag(Cp)) < 1e-12
+    assert R.is_reflection_symmetric(Cm, tol=1e-3) and R.is_reflection_symmetric(Cp, tol=2e-3)
+    L, N = 4, 16
+    site = lambda x, y: (y % L) + L * (x % L)
+    lp = np.zeros((L, L), complex); lm = np.zeros((L, L), complex)
+    for tau in range(small_params.slices):
+        for x0 in range(L):
+            for y0 in range(L):
+                for s1 in (0, 2):
+                    for s2 in (0, 2):
+                        for x in range(L):
+                            for y in range(L):
+                                ri, r0 = site(x0 + x, y0 + y), site(x0, y0)
+
+                                def ev(j1, j3):
+                                    i1, i3 = (j1 - 1) * N + ri, (j3 - 1) * N + r0
+                                    unc = (1.0 - g[i1, i1]) * (1.0 - g[i3, i3])
+                                    return unc + (-G0t[tau][i3, i1]) * Gt0[tau][i1, i3]
+                                e1, e2 = ev(1 + s1, 1 + s2), ev(1 + s1, 2 + s2)
+                                e3, e4 = ev(2 + s1, 1 + s2), ev(2 + s1, 2 + s2)
+                                lm[y, x] += e1 - e2 - e3 + e4
+                                lp[y, x] += e1 + e2 + e3 + e4
+    assert np.max(np.abs(Cp - lp / N)) < 1e-12 and np.max(np.abs(Cm - lm / N)) < 1e-12
+
+
+def test_zero_frequency_current_current(golden, small_params):
+    """tests_O3_measurements.jl:286-302 for the reference's test system: Lambda_xx
+    and Lambda_yy with imaginary parts below 1e-12, reflection symmetric within
+    2e-3 and 1e-2.  (The superfluid-density literal of that test, 0.0515709...,
+    belongs to the field that init!(mc) draws from Julia's seeded RNG and is not
+    reproducible here.)  Also: rho_s from the real DFT equals the direct cosine
+    sums of its definition."""
+    ref = R.DQMCRef(small_params, golden["randconf"])
+    ref.init()
+    g = ref.effective_greens2greens(ref.greens)
+    Gt0, G0t = ref.measure_tdgfs()
+    T = ref.T.toarray() if hasattr(ref.T, "toarray") else np.asarray(ref.T)
+    lxx, lyy = R.measure_zfccc(4, T, g, Gt0, G0t)
+    assert np.max(np.imag(lxx)) < 1e-12 and np.max(np.imag(lyy)) < 1e-12
+    assert R.is_reflection_symmetric(lxx, tol=2e-3) and R.is_reflection_symmetric(lyy, tol=1e-2)
+    L = 4
+    c = np.cos(2 * np.pi * np.arange(L) / L)
+    direct = 0.25 * (np.sum(np.real(lxx) * c[None, :]) - np.sum(np.real(lxx) * c[:, None]))
+    assert abs(R.measure_sfdensity(lxx) - direct) < 1e-14
