@@ -157,8 +157,8 @@ def test_local_updates_one_slice(lib, golden, small_params):
     assert abs(gpu.boson_action - ref.boson_action_value) < 1e-10 * abs(ref.boson_action_value)
 
 
-@pytest.mark.parametrize("delay,method", [(1, "scales"), (4, "scales"), (16, "scales"), (1, "two_qr"),
-                                          (16, "two_qr")])
+@pytest.mark.parametrize("delay,method", [(1, "scales"), (4, "scales"), (8, "scales"), (16, "scales"),
+                                          (32, "scales"), (1, "two_qr"), (16, "two_qr")])
 def test_sweep_config0_accept_sequence(lib, delay, method):
     """Config 0: one full sweep (M update calls) on shared streams, with
     immediate rank-4 updates (delay 1) and delayed rank-k updates."""
