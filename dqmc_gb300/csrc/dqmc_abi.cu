@@ -13,6 +13,7 @@
 #include <thread>
 #include <utility>
 #include <string>
+#include <initializer_list>
 #include <vector>
 
 #include "../../include/dqmc_gpu.h"
@@ -1088,6 +1089,27 @@ int measure(dqmc_handle* h, cplx* Gt0, cplx* G0t) {
 // The measurement hook's true G of the current slice into dst:
 // wrap_greens(G, current_slice, +1), then effective -> true
 // (src/dqmc_framework.jl:378-381, src/fermion_measurements.jl:1125-1142).
+// Host-side check of an address a kernel will dereference: device or managed
+// memory, or registered host memory mapped at the same address (NULL passes;
+// callers check it).  A pageable host array passed as a device address would
+// otherwise make the kernel fault.
+static bool device_accessible(const void* p) {
+  if (!p) return true;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged ||
+         (at.type == cudaMemoryTypeHost && at.devicePointer == p);
+}
+
+static bool all_device_accessible(std::initializer_list<const void*> ps) {
+  for (const void* p : ps)
+    if (!device_accessible(p)) return false;
+  return true;
+}
+
 static int hook_true_greens(dqmc_handle* h, cplx* dst) {
   if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
   if (h->current_slice < 1 || h->current_slice > h->M) return set_err(h, DQMC_ERR_STATE, "no current slice");
@@ -1452,6 +1474,8 @@ int dqmc_sweep_device(dqmc_handle* h, int32_t n_calls, const double* delta_strea
                       const double* unif_stream_dev, uint8_t* accepted_dev, dqmc_stats* stats) {
   if (h) cudaSetDevice(h->device);
   if (!h || n_calls < 0 || !delta_stream_dev || !unif_stream_dev) return DQMC_ERR_ARG;
+  if (!all_device_accessible({delta_stream_dev, unif_stream_dev, accepted_dev}))
+    return set_err(h, DQMC_ERR_ARG, "stream or accept pointer is not device memory");
   if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
   if (n_calls == 0) return DQMC_OK;
   return sweep_impl(h, n_calls, delta_stream_dev, unif_stream_dev, accepted_dev, stats);
@@ -1520,6 +1544,8 @@ int dqmc_batch_sweep(dqmc_batch* b, int32_t n_calls, const double* const* delta_
     dqmc_handle* h = b->chains[i];
     if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init on every chain first");
     if (!delta_dev[i] || !unif_dev[i]) return DQMC_ERR_ARG;
+    if (!all_device_accessible({delta_dev[i], unif_dev[i]}))
+      return set_err(h, DQMC_ERR_ARG, "stream pointer is not device memory");
   }
   std::vector<int> order(C);
   for (int i = 0; i < C; ++i) order[i] = i;
@@ -1788,6 +1814,8 @@ int dqmc_measure_equal_time(dqmc_handle* h, const double* greens, double* etpc_p
                              double* etcdc_plus, double* etcdc_minus, int32_t device_ptrs) {
   if (h) cudaSetDevice(h->device);
   if (!h) return DQMC_ERR_ARG;
+  if (device_ptrs && !all_device_accessible({greens, etpc_plus, etpc_minus, etcdc_plus, etcdc_minus}))
+    return set_err(h, DQMC_ERR_ARG, "device_ptrs set but an array is not device memory");
   const int N = h->N;
   const cplx* src = nullptr;
   if (greens) {
@@ -1910,6 +1938,8 @@ int dqmc_measure_tdgfs(dqmc_handle* h, double* Gt0, double* G0t, int32_t device_
   if (!h || !Gt0 || !G0t) return DQMC_ERR_ARG;
   if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
   const size_t bytes = (size_t)h->M * h->n * h->n * sizeof(cplx);
+  if (device_ptrs && !all_device_accessible({Gt0, G0t}))
+    return set_err(h, DQMC_ERR_ARG, "device_ptrs set but an array is not device memory");
   if (device_ptrs) {
     CHK(tdgf::measure(h, reinterpret_cast<cplx*>(Gt0), reinterpret_cast<cplx*>(G0t)));
     return sync(h);
@@ -1929,6 +1959,8 @@ int dqmc_measure_tdgfs(dqmc_handle* h, double* Gt0, double* G0t, int32_t device_
 int dqmc_measure_zfpc(dqmc_handle* h, const double* Gt0, double* zfpc_plus, double* zfpc_minus, int32_t device_ptrs) {
   if (h) cudaSetDevice(h->device);
   if (!h) return DQMC_ERR_ARG;
+  if (device_ptrs && !all_device_accessible({Gt0, zfpc_plus, zfpc_minus}))
+    return set_err(h, DQMC_ERR_ARG, "device_ptrs set but an array is not device memory");
   const int N = h->N, M = h->M;
   const size_t bytes = (size_t)M * h->n * h->n * sizeof(cplx);
   cplx *g = nullptr, *scratch = nullptr;
@@ -1975,6 +2007,8 @@ static int zero_frequency_measure(dqmc_handle* h, int which, const double* green
                                   int32_t device_ptrs) {
   if (h) cudaSetDevice(h->device);
   if (!h || (Gt0 == nullptr) != (G0t == nullptr)) return DQMC_ERR_ARG;
+  if (device_ptrs && !all_device_accessible({greens, Gt0, G0t, out0, out1}))
+    return set_err(h, DQMC_ERR_ARG, "device_ptrs set but an array is not device memory");
   const int N = h->N, M = h->M;
   const size_t nn = (size_t)h->n * h->n, bytes = (size_t)M * nn * sizeof(cplx);
   const bool own = !(Gt0 && device_ptrs);   // time-displaced blocks staged in memory of this call
