@@ -7,6 +7,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <mutex>
 
 #define DQMC_HD __host__ __device__ __forceinline__
 
@@ -115,6 +116,30 @@ struct GridBarrierExit {
       }
     }
   }
+};
+
+// Raises a kernel's dynamic shared-memory limit (cudaFuncSetAttribute) once
+// per device: the attribute belongs to the device's context, so a process
+// driving several GPUs sets it on each.  One static instance per kernel
+// launcher; thread-safe.
+class SmemLimit {
+ public:
+  cudaError_t raise(const void* fn, int bytes) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu_);
+    if (set_[dev] >= bytes) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) set_[dev] = bytes;
+    return e;
+  }
+
+ private:
+  static constexpr int kMaxDevices = 64;
+  std::mutex mu_;
+  int set_[kMaxDevices] = {};
 };
 
 // Error bits reported by kernels through a device int.

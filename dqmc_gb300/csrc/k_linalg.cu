@@ -1160,11 +1160,8 @@ cudaError_t launch_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, c
 cudaError_t launch_qrp(cplx* A, int n, QRWork& w, int sm_count, cudaStream_t st, int max_grid) {
   if (n > 32 * QR_MAXT) return cudaErrorInvalidValue;
   size_t smem = (size_t)n * (sizeof(cplx) + sizeof(int));
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_qrp, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-    attr = true;
-  }
+  static SmemLimit smem_limit;
+  if (cudaError_t ea = smem_limit.raise((const void*)k_qrp, 64 * 1024); ea != cudaSuccess) return ea;
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_qrp, QR_THREADS, smem);
   if (e != cudaSuccess) return e;
@@ -1194,11 +1191,8 @@ cudaError_t launch_apply_q_right(cplx* X, int m, int n, const QRWork& w, bool co
 cudaError_t launch_trsm_left_upper(const cplx* T, const int* order, const cplx* rdiag, cplx* Y, int n, int m,
                                    cudaStream_t st) {
   size_t smem = (size_t)4 * n * sizeof(cplx);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_trsm_left_upper, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
+  static SmemLimit smem_limit;
+  if (cudaError_t ea = smem_limit.raise((const void*)k_trsm_left_upper, 200 * 1024); ea != cudaSuccess) return ea;
   k_trsm_left_upper<<<(m + 3) / 4, 128, smem, st>>>(T, order, rdiag, Y, n, m);
   return cudaGetLastError();
 }
@@ -1208,13 +1202,9 @@ cudaError_t launch_trsm_diag_block(const cplx* T, int ldT, const cplx* rdiag, cp
   if (b < 1 || b > 128) return cudaErrorInvalidValue;
   if (!lower && !rdiag) return cudaErrorInvalidValue;
   const size_t smem = ((size_t)b * (b - 1) / 2 + b) * sizeof(cplx);
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_trsm_diag_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)((128 * 127 / 2 + 128) * sizeof(cplx)));
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static SmemLimit smem_limit;
+  constexpr int kMaxTdb = (int)((128 * 127 / 2 + 128) * sizeof(cplx));   // b = 128
+  if (cudaError_t ea = smem_limit.raise((const void*)k_trsm_diag_block, kMaxTdb); ea != cudaSuccess) return ea;
   k_trsm_diag_block<<<(m + TRSM_DB_WARPS - 1) / TRSM_DB_WARPS, 32 * TRSM_DB_WARPS, smem, st>>>(
       T, ldT, rdiag, Y, ldY, j0, b, m, lower ? 1 : 0);
   return cudaGetLastError();
@@ -1222,11 +1212,8 @@ cudaError_t launch_trsm_diag_block(const cplx* T, int ldT, const cplx* rdiag, cp
 
 cudaError_t launch_trsm_left_lower_unit(const cplx* Lc, cplx* Y, int n, int m, cudaStream_t st) {
   size_t smem = (size_t)4 * n * sizeof(cplx);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_trsm_left_lower_unit, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
+  static SmemLimit smem_limit;
+  if (cudaError_t ea = smem_limit.raise((const void*)k_trsm_left_lower_unit, 200 * 1024); ea != cudaSuccess) return ea;
   k_trsm_left_lower_unit<<<(m + 3) / 4, 128, smem, st>>>(Lc, Y, n, m);
   return cudaGetLastError();
 }
@@ -1240,11 +1227,8 @@ cudaError_t launch_wy_prep(const cplx* V, const cplx* tau, int n, int jb, int b,
 cudaError_t launch_lup(cplx* A, cplx* Lb, int n, LUKernel& w, int sm_count, cudaStream_t st, int max_grid) {
   if (n > 32 * QR_MAXT) return cudaErrorInvalidValue;
   size_t smem = (size_t)n * (sizeof(cplx) + sizeof(int));
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_lup, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-    attr = true;
-  }
+  static SmemLimit smem_limit;
+  if (cudaError_t ea = smem_limit.raise((const void*)k_lup, 64 * 1024); ea != cudaSuccess) return ea;
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lup, QR_THREADS, smem);
   if (e != cudaSuccess) return e;
@@ -1266,12 +1250,8 @@ cudaError_t launch_lu_panel(cplx* A, int n, int p0, int b, LUPanel& w, int sm_co
   const size_t smem = (size_t)chunk * LU_PB * sizeof(cplx);
   constexpr size_t kMax = 160 * 1024;
   if (smem > kMax) return cudaErrorInvalidValue;   // grid too small for the panel rows
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_lu_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMax);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static SmemLimit smem_limit;
+  if (cudaError_t ea = smem_limit.raise((const void*)k_lu_panel, (int)kMax); ea != cudaSuccess) return ea;
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lu_panel, 256, smem);
   if (e != cudaSuccess) return e;
@@ -1314,11 +1294,8 @@ cudaError_t launch_lu_logdet(const cplx* udiag, const double* Dl, const double* 
 
 cudaError_t launch_trsm_right_upper(const cplx* T, const int* order, cplx* Y, int m, int n, cudaStream_t st) {
   size_t smem = (size_t)4 * n * sizeof(cplx);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_trsm_right_upper, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
+  static SmemLimit smem_limit;
+  if (cudaError_t ea = smem_limit.raise((const void*)k_trsm_right_upper, 200 * 1024); ea != cudaSuccess) return ea;
   k_trsm_right_upper<<<(m + 3) / 4, 128, smem, st>>>(T, order, Y, m, n);
   return cudaGetLastError();
 }

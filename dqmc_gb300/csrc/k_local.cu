@@ -735,14 +735,11 @@ cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d,
   const bool cache = local_delayed_smem(N, d.k, grid, true) <= kMaxSmem;
   const size_t smem = local_delayed_smem(N, d.k, grid, cache);
   if (smem > kMaxSmem) return cudaErrorInvalidValue;
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_local_delayed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_local_delayed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static SmemLimit limit_cache, limit_plain;
+  if (cudaError_t ea = limit_cache.raise((const void*)k_local_delayed<true>, (int)kMaxSmem); ea != cudaSuccess)
+    return ea;
+  if (cudaError_t ea = limit_plain.raise((const void*)k_local_delayed<false>, (int)kMaxSmem); ea != cudaSuccess)
+    return ea;
   const void* fn = cache ? (const void*)k_local_delayed<true> : (const void*)k_local_delayed<false>;
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, LU_THREADS, smem);
@@ -756,12 +753,8 @@ cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d,
 
 cudaError_t launch_local_updates(const LocalUpdateArgs& a, int sm_count, cudaStream_t st, int max_grid) {
   const size_t smem = local_smem_bytes(a.mc.N);
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_local_updates, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static SmemLimit smem_limit;
+  if (cudaError_t ea = smem_limit.raise((const void*)k_local_updates, 100 * 1024); ea != cudaSuccess) return ea;
   if (smem > 100 * 1024) return cudaErrorInvalidValue;
   int per_sm = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local_updates, LU_THREADS, smem);

@@ -255,11 +255,8 @@ cudaError_t launch_apply_cols(cplx* A, int n, const ModelConst& mc, const void* 
   int cpc = pick_cols_per_cta(n);
   int grid = (n + cpc - 1) / cpc;
   size_t smem = (size_t)cpc * n * sizeof(cplx) + (size_t)mc.N * sizeof(EvEntry);
-  static bool attr_done = false;
-  if (!attr_done) {
-    cudaFuncSetAttribute(k_apply_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_done = true;
-  }
+  static SmemLimit smem_limit;
+  if (cudaError_t ea = smem_limit.raise((const void*)k_apply_cols, 200 * 1024); ea != cudaSuccess) return ea;
   k_apply_cols<<<grid, 256, smem, st>>>(A, n, cpc, mc, (const EvEntry*)evtab, first_slice0, count, step, mode,
                                          colscale);
   return cudaGetLastError();
@@ -270,11 +267,8 @@ cudaError_t launch_apply_rows(cplx* A, int n, const ModelConst& mc, const void* 
   int rpc = pick_cols_per_cta(n);
   int grid = (n + rpc - 1) / rpc;
   size_t smem = (size_t)rpc * n * sizeof(cplx) + (size_t)mc.N * sizeof(EvEntry);
-  static bool attr_done = false;
-  if (!attr_done) {
-    cudaFuncSetAttribute(k_apply_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_done = true;
-  }
+  static SmemLimit smem_limit;
+  if (cudaError_t ea = smem_limit.raise((const void*)k_apply_rows, 200 * 1024); ea != cudaSuccess) return ea;
   k_apply_rows<<<grid, 256, smem, st>>>(A, n, rpc, mc, (const EvEntry*)evtab, first_slice0, count, step, mode);
   return cudaGetLastError();
 }
