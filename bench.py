@@ -296,13 +296,14 @@ def measure_tdgf(args, dev):
     n = rp.n
     out = {"workload": f"O(3) L={L} beta=10 (M={M}): G(tau,0) and -G(0,tau) for all {M} slices"}
     res = {}
+    corr = {}
     for prec in ("fp64", "mixed"):
         chain = _make_chain(api, L, M, rp, args, dev, prec, args.delay if prec == "mixed" else 1, phi)
         a = torch.empty(M * n * n * 2, dtype=torch.float64, device=f"cuda:{dev}")
         b = torch.empty_like(a)
+        D = lambda t: ctypes.cast(t.data_ptr(), api._D)
         def call():
-            chain._check(chain.lib.dqmc_measure_tdgfs(chain.h, ctypes.cast(a.data_ptr(), api._D),
-                                                      ctypes.cast(b.data_ptr(), api._D), 1))
+            chain._check(chain.lib.dqmc_measure_tdgfs(chain.h, D(a), D(b), 1))
         call()   # warm-up (allocations, first launches)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -310,6 +311,29 @@ def measure_tdgf(args, dev):
         torch.cuda.synchronize()
         out[f"seconds_{prec}"] = time.perf_counter() - t0
         res[prec] = (a.clone(), b.clone())
+        if prec == "fp64":
+            # fermion correlators on the device: equal-time ones of the hook G,
+            # zero-frequency ones over the G(tau, 0), G(0, tau) just measured
+            o = [torch.empty(2 * rp.N, dtype=torch.float64, device=f"cuda:{dev}") for _ in range(6)]
+            rho = ctypes.c_double()
+            calls = {
+                "equal_time": lambda: chain.lib.dqmc_measure_equal_time(chain.h, None, D(o[0]), D(o[1]), D(o[2]),
+                                                                          D(o[3]), 1),
+                "zfpc": lambda: chain.lib.dqmc_measure_zfpc(chain.h, D(a), D(o[4]), D(o[5]), 1),
+                "zfcdc": lambda: chain.lib.dqmc_measure_zfcdc(chain.h, None, D(a), D(b), D(o[2]), D(o[3]), 1),
+                "zfccc": lambda: chain.lib.dqmc_measure_zfccc(chain.h, None, D(a), D(b), D(o[2]), D(o[3]),
+                                                             ctypes.byref(rho), 1),
+            }
+            gpu_s = {}
+            for name, fn in calls.items():
+                chain._check(fn())   # warm-up
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                chain._check(fn())
+                torch.cuda.synchronize()
+                gpu_s[name] = time.perf_counter() - t0
+            corr["gpu_seconds"] = gpu_s
+            corr["etpc_plus_gpu"] = o[0][: rp.N].cpu().numpy().reshape(L, L, order="F")
         chain.close()
     ga, gb = res["fp64"]
     ma, mb = res["mixed"]
@@ -323,6 +347,28 @@ def measure_tdgf(args, dev):
         g = ga.view(M, n, n, 2)
         gpu_gt0 = torch.complex(g[..., 0], g[..., 1]).transpose(1, 2).cpu().numpy()
         out["max_abs_diff_fp64_vs_oracle"] = float(np.max(np.abs(gpu_gt0 - gt0)))
+        # oracle correlators: equal-time ones in full, zero-frequency ones on a
+        # sample of slices, extrapolated to all M
+        ref.init()
+        gh = ref.measured_greens()
+        t0 = time.perf_counter()
+        pp, _ = R.measure_etpc(L, gh)
+        R.measure_etcdc(L, gh)
+        cpu_s = {"equal_time": time.perf_counter() - t0}
+        sample = 4
+        T = ref.T.toarray() if hasattr(ref.T, "toarray") else np.asarray(ref.T)
+        for name, fn in (("zfpc", lambda: R.measure_zfpc(L, gt0[:sample])),
+                         ("zfcdc", lambda: R.measure_zfcdc(L, gh, gt0[:sample], g0t[:sample])),
+                         ("zfccc", lambda: R.measure_zfccc(L, T, gh, gt0[:sample], g0t[:sample]))):
+            t0 = time.perf_counter()
+            fn()
+            cpu_s[name] = (time.perf_counter() - t0) * M / sample
+        corr["cpu_oracle_seconds"] = cpu_s
+        corr["cpu_sample"] = (f"equal-time correlators in full; zero-frequency ones on {sample} of {M} slices, "
+                              f"extrapolated (numpy, one thread)")
+        corr["max_abs_diff_etpc_plus_vs_oracle"] = float(np.max(np.abs(corr["etpc_plus_gpu"] - pp)))
+    corr.pop("etpc_plus_gpu", None)
+    out["correlators"] = corr
     return out
 
 
