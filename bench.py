@@ -177,6 +177,26 @@ def cpu_baseline(p, phi, n_calls, seed, threads):
     return (n_calls / p.slices) / dt, dt
 
 
+def cpu_baseline_threads(L, M, n_calls, threads):
+    """cpu_baseline in a fresh interpreter whose BLAS is limited to `threads`
+    threads (the thread count of an already-loaded BLAS cannot be changed
+    portably); returns (sweeps/s, seconds) or None."""
+    code = ("import json, bench\n"
+            "from oracle.dqmc_ref import synthetic_field\n"
+            f"rp = bench.model_params({L}, {M})\n"
+            f"v, s = bench.cpu_baseline(rp, synthetic_field(rp.N, {M}, 1000), {n_calls}, 1002, {threads})\n"
+            "print(json.dumps([v, s]))\n")
+    env = dict(os.environ, OPENBLAS_NUM_THREADS=str(threads), OMP_NUM_THREADS=str(threads),
+               MKL_NUM_THREADS=str(threads))
+    try:
+        out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600,
+                             cwd=os.path.dirname(os.path.abspath(__file__)))
+        v, secs = json.loads(out.stdout.strip().splitlines()[-1])
+        return v, secs
+    except Exception:
+        return None
+
+
 def run_reference(args, world, rank):
     """The reference's own CPU implementation is Julia (not installed on
     either machine); its CPU restatement (the oracle) is timed instead."""
@@ -534,8 +554,29 @@ def run_ours(args, world, rank, local):
         src = "FP64 FMA peak measured live on this GPU (dqmc_peak_fp64)"
     achieved = fl / launches_top / (ms_top / launches_top / 1000.0) / 1e12
     hbm_gbs = by / (ms_top / 1000.0) / 1e9
-    breakdown = {k: {"ms": round(v["ms"], 3), "launches": v["launches"], "share": round(v["ms"] / max(1e-9, tot_ms), 4)}
-                 for k, v in kinds.items() if v["launches"]}
+    # per kind: algorithmic rates of one sweep against the pipe its flops run
+    # on (split-BF16 kinds against the BF16 peak; kinds that mix FP64 panels
+    # with split-BF16 GEMMs get no pipe fraction) and its bytes against HBM
+    fp64_peak = api.peak_fp64_tflops(dev)
+    pipe_of = {"slice_cols": "fp64", "slice_rows": "fp64", "qrp": "fp64", "ozaki_gemm": "tensor",
+               "flush": "tensor" if head == "mixed" else "fp64", "local_updates": "latency",
+               "lu": "fp64" if head == "fp64" else "fp64+tensor", "trsm": "fp64" if head == "fp64" else "fp64+tensor",
+               "apply_q": "fp64" if head == "fp64" else "fp64+tensor", "misc": "hbm"}
+    breakdown = {}
+    for k, v in kinds.items():
+        if not v["launches"]:
+            continue
+        kfl, kby = flops_model(k, tim, n, R["accepted"] / max(1, args.steps))   # one evented sweep
+        secs_k = max(1e-12, v["ms"] / 1000.0)
+        e = {"ms": round(v["ms"], 3), "launches": v["launches"], "share": round(v["ms"] / max(1e-9, tot_ms), 4),
+             "pipe": pipe_of.get(k), "tflops": kfl / secs_k / 1e12, "gbs": kby / secs_k / 1e9}
+        if peaks.get("hbm_gbs"):
+            e["hbm_frac"] = e["gbs"] / peaks["hbm_gbs"]
+        if e["pipe"] == "fp64" and fp64_peak:
+            e["pipe_frac"] = e["tflops"] / fp64_peak
+        elif e["pipe"] == "tensor" and peaks.get("bf16_tflops"):
+            e["pipe_frac"] = e["tflops"] / peaks["bf16_tflops"]
+        breakdown[k] = e
     # time-displaced Green's functions (the measurement step after the sweep)
     tdgf = None
     if not args.no_batch and args.config == "c3" and rank == 0:
@@ -554,7 +595,11 @@ def run_ours(args, world, rank, local):
         if world == 1 and not args.no_cpu:
             threads = os.cpu_count() or 1
             val, secs = cpu_baseline(rp, phi, args.cpu_calls, 1002, threads)
+            one = cpu_baseline_threads(L, M, 3, 1)
             cpu = {"value": val, "unit": "sweeps/s", "cores": threads, "kind": "port",
+                   "value_1_thread": one[0] if one else None,
+                   "sample_1_thread": f"3 of {M} update calls, one BLAS thread, {one[1]:.1f} s, extrapolated"
+                   if one else "failed",
                    "sample": f"{args.cpu_calls} of {M} update calls (numpy/scipy oracle, OpenBLAS "
                              f"{threads} threads), {secs:.1f} s, extrapolated to one sweep"}
         compare = None
