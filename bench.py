@@ -236,20 +236,21 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
-def measure_batch(args, world, rank, dev, warmup, steps, precision):
-    """64 chains of uneven L (config c2) swept concurrently through
-    dqmc_batch_*: delayed-update depth per L from the autotuner (or
-    --batch-delay), device-resident streams; returns the chain-sweeps/s of
-    all ranks (wall clock around the timed sweeps, synchronised) and the
-    details."""
+def measure_batch(args, world, rank, dev, warmup, steps, precision, Ls=None, M=None, desc=None):
+    """64 chains of uneven L (config c2; or the chains of lattice sizes Ls with
+    M slices) swept concurrently through dqmc_batch_*: delayed-update depth
+    per L from the autotuner (or --batch-delay), device-resident streams;
+    returns the chain-sweeps/s of all ranks (wall clock around the timed
+    sweeps, synchronised) and the details."""
     import torch
     from dqmc_gb300 import api
     from oracle.dqmc_ref import synthetic_field, synthetic_streams
 
-    _, M, desc = CONFIGS["c2"]
+    if Ls is None:
+        _, M, desc = CONFIGS["c2"]
+        rng = np.random.default_rng(2000 + rank)
+        Ls = [int(x) for x in rng.choice([6, 8, 10, 12], size=args.chains)]
     torch.cuda.set_device(dev)
-    rng = np.random.default_rng(2000 + rank)
-    Ls = [int(x) for x in rng.choice([6, 8, 10, 12], size=args.chains)]
     auto = precision == "mixed" and args.batch_delay == "auto"
     plist, fields = [], []
     for k, L in enumerate(Ls):
@@ -294,8 +295,8 @@ def measure_batch(args, world, rank, dev, warmup, steps, precision):
     wall = allreduce_max(time.perf_counter() - t0, world)
     clk = clocks.stop()
     batch.close()
-    value = world * args.chains * steps / wall
-    info = {"chains": args.chains, "L_counts": {L: Ls.count(L) for L in (6, 8, 10, 12)}, "slices": M,
+    value = world * len(Ls) * steps / wall
+    info = {"chains": len(Ls), "L_counts": {L: Ls.count(L) for L in sorted(set(Ls))}, "slices": M,
             "precision": precision, "delays": delays, "autotuned": auto, "warmup": warmup, "steps": steps,
             "acc_rate": acc / max(1, prop)}
     return value, wall, clk, info, desc
@@ -589,6 +590,21 @@ def run_ours(args, world, rank, local):
         # warm-up: both start states of a sweep (down and up) captured as graphs
         bval, bwall, bclk, binfo, bdesc = measure_batch(args, world, rank, dev, 3, 2, "mixed")
         batched = dict(value=bval, unit="chain-sweeps/s", workload=bdesc, seconds=bwall, clocks=bclk, **binfo)
+        res_fp64_value = world * args.steps / res["fp64"]["secs"] if "fp64" in res else None
+        wl = desc.replace(" FP64", "")
+        # the headline lattice batched: 8 L=16, beta=20 chains in flight, both forms
+        # (warm-up: the two captured sweep graphs; one timed batch sweep each)
+        b16 = {}
+        for prec in ("mixed", "fp64"):
+            v, w, c, info, _ = measure_batch(args, world, rank, dev, 2, 1, prec, Ls=[L] * 8, M=M,
+                                             desc=f"8 independent chains, {wl}")
+            b16[prec] = dict(value=v, seconds=w, clocks=c, delays=info["delays"], acc_rate=info["acc_rate"])
+        batched["headline_lattice"] = {
+            "workload": f"8 independent chains of {wl} in flight at once", "unit": "chain-sweeps/s",
+            "mixed": b16["mixed"], "fp64": b16["fp64"],
+            "mixed_over_fp64_batched": b16["mixed"]["value"] / b16["fp64"]["value"],
+            "mixed_batched_over_fp64_single_chain": b16["mixed"]["value"] / res_fp64_value
+            if res_fp64_value else None}
 
     if rank == 0:
         cpu = None
