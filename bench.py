@@ -393,6 +393,58 @@ def measure_tdgf(args, dev):
     return out
 
 
+def measure_force(args, dev):
+    """Adjoint force at config-4 sizes (L=12, beta=10, M=100): device time of
+    one dqmc_force, its largest relative deviation from central differences
+    (h=1e-5) of the library's log|det M| on 24 random entries, and 20
+    Langevin steps (eps=1e-3) with a local sweep after every 10th (the full
+    100-step schedule runs in the GPU tests).  Errors are recorded in the
+    result instead of ending the run."""
+    from dqmc_gb300 import api
+    from oracle import dqmc_ref as R
+    L, M = 12, 100
+    rp = model_params(L, M)
+    out = {"workload": f"O(3) L={L} beta=10 (M={M}), FP64 form: force, finite differences, Langevin"}
+    try:
+        phi = R.synthetic_field(rp.N, M, 71)
+        chain = _make_chain(api, L, M, rp, args, dev, "fp64", 1, phi)
+        chain.force()   # warm-up
+        t0 = time.perf_counter()
+        gl, _ = chain.force()
+        out["seconds_force"] = time.perf_counter() - t0
+        rng = np.random.default_rng(72)
+        h, worst = 1e-5, 0.0
+        for _ in range(24):
+            a, i, l = rng.integers(3), rng.integers(rp.N), rng.integers(M)
+            f = []
+            for sgn in (1, -1):
+                ph = phi.copy()
+                ph[a, i, l] += sgn * h
+                chain.set_field(ph)
+                f.append(-chain.calc_greens_and_logdet(1)[1])
+            fd = (f[0] - f[1]) / (2 * h)
+            worst = max(worst, abs(gl[a, i, l] - fd) / max(1.0, abs(fd)))
+        out["fd_entries"] = 24
+        out["max_rel_error_vs_finite_differences"] = worst
+        chain.init(phi)
+        steps = 20
+        delta, unif = R.synthetic_streams(rp.N, (steps // 10) * M, rp.box, 73)
+        t0 = time.perf_counter()
+        for step in range(steps):
+            chain.langevin_step(1e-3, rng)
+            if step % 10 == 9:
+                k = step // 10
+                chain.sweep(M, delta[k * M:(k + 1) * M], unif[k * M:(k + 1) * M])
+                chain.init(chain.get_field())   # back to the state (M, -1) the force needs
+        out["langevin_steps"] = steps
+        out["seconds_langevin_steps_with_sweeps"] = time.perf_counter() - t0
+        out["field_finite_after_langevin"] = bool(np.all(np.isfinite(chain.get_field())))
+        chain.close()
+    except Exception as e:   # keep the bench line
+        out["error"] = f"{type(e).__name__}: {e}"
+    return out
+
+
 def run_batch(args, world, rank, local):
     """Config c2: 64 chains of uneven L swept concurrently (dqmc_batch_*);
     value = chain-sweeps/s of all chains."""
@@ -579,9 +631,10 @@ def run_ours(args, world, rank, local):
             e["pipe_frac"] = e["tflops"] / peaks["bf16_tflops"]
         breakdown[k] = e
     # time-displaced Green's functions (the measurement step after the sweep)
-    tdgf = None
+    tdgf = force = None
     if not args.no_batch and args.config == "c3" and rank == 0:
         tdgf = measure_tdgf(args, dev)
+        force = measure_force(args, dev)
     # the batched part of the metric: 64 chains of L in {6, 8, 10, 12} (config c2), mixed form
     batched = None
     if not args.no_batch and args.config == "c3":
@@ -661,6 +714,7 @@ def run_ours(args, world, rank, local):
             "cpu_baseline": cpu,
             "batched": batched,
             "tdgf": tdgf,
+            "force": force,
         }
         print(json.dumps(line), flush=True)
     if batched is None:
