@@ -1,6 +1,6 @@
 """Benchmark of the GPU DQMC sweep (one JSON line on rank 0).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c3] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config L16] [--impl ours|reference]
 
 A step is one sweep = M `update` calls (propagate + local updates of one
 slice) of the O(3) spin-fermion model on seeded synthetic fields and
@@ -35,6 +35,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -45,11 +46,11 @@ if ROOT not in sys.path:
 
 CONFIGS = {
     # name: (L, M, description)
-    "c0": (4, 40, "O(3) L=4 beta=4 (M=40) dtau=0.1 safe_mult=10 FP64"),
-    "c2": (0, 80, "64 independent O(3) chains, L uniform in {6,8,10,12}, beta=8 (M=80) dtau=0.1 safe_mult=10"),
-    "c1": (10, 100, "O(3) L=10 beta=10 (M=100) dtau=0.1 safe_mult=10 FP64"),
-    "c3": (16, 200, "O(3) L=16 beta=20 (M=200) dtau=0.1 safe_mult=10 FP64"),
-    "c4": (12, 100, "O(3) L=12 beta=10 (M=100) dtau=0.1 safe_mult=10 FP64"),
+    "L4": (4, 40, "O(3) L=4 beta=4 (M=40) dtau=0.1 safe_mult=10 FP64"),
+    "chains64": (0, 80, "64 independent O(3) chains, L uniform in {6,8,10,12}, beta=8 (M=80) dtau=0.1 safe_mult=10"),
+    "L10": (10, 100, "O(3) L=10 beta=10 (M=100) dtau=0.1 safe_mult=10 FP64"),
+    "L16": (16, 200, "O(3) L=16 beta=20 (M=200) dtau=0.1 safe_mult=10 FP64"),
+    "L12": (12, 100, "O(3) L=12 beta=10 (M=100) dtau=0.1 safe_mult=10 FP64"),
 }
 METRIC = "O(3) L=16 sweeps/s: mixed vs FP64 at G err≤1e-8; batched chain-sweeps/s"
 
@@ -108,7 +109,9 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{index}.csv")
+        # raw samples (the summary goes into the JSON line); DQMC_CLOCKS_DIR keeps them elsewhere
+        self.path = os.path.join(os.environ.get("DQMC_CLOCKS_DIR") or tempfile.gettempdir(),
+                                 f"dqmc_clocks_rank{index}.csv")
 
     def start(self):
         try:
@@ -237,7 +240,7 @@ def run_reference(args, world, rank):
 
 
 def measure_batch(args, world, rank, dev, warmup, steps, precision, Ls=None, M=None, desc=None):
-    """64 chains of uneven L (config c2; or the chains of lattice sizes Ls with
+    """64 chains of uneven L (the chains64 workload; or the chains of lattice sizes Ls with
     M slices) swept concurrently through dqmc_batch_*: delayed-update depth
     per L from the autotuner (or --batch-delay), device-resident streams;
     returns the chain-sweeps/s of all ranks (wall clock around the timed
@@ -247,7 +250,7 @@ def measure_batch(args, world, rank, dev, warmup, steps, precision, Ls=None, M=N
     from oracle.dqmc_ref import synthetic_field, synthetic_streams
 
     if Ls is None:
-        _, M, desc = CONFIGS["c2"]
+        _, M, desc = CONFIGS["chains64"]
         rng = np.random.default_rng(2000 + rank)
         Ls = [int(x) for x in rng.choice([6, 8, 10, 12], size=args.chains)]
     torch.cuda.set_device(dev)
@@ -394,7 +397,7 @@ def measure_tdgf(args, dev):
 
 
 def measure_force(args, dev):
-    """Adjoint force at config-4 sizes (L=12, beta=10, M=100): device time of
+    """Adjoint force at L=12, beta=10 (M=100): device time of
     one dqmc_force, its largest relative deviation from central differences
     (h=1e-5) of the library's log|det M| on 24 random entries, and 20
     Langevin steps (eps=1e-3) with a local sweep after every 10th (the full
@@ -446,7 +449,7 @@ def measure_force(args, dev):
 
 
 def run_batch(args, world, rank, local):
-    """Config c2: 64 chains of uneven L swept concurrently (dqmc_batch_*);
+    """The chains64 workload: 64 chains of uneven L swept concurrently (dqmc_batch_*);
     value = chain-sweeps/s of all chains."""
     dev = local if world > 1 else 0
     precision = "mixed" if args.precision in ("mixed", "both") else "fp64"
@@ -632,12 +635,12 @@ def run_ours(args, world, rank, local):
         breakdown[k] = e
     # time-displaced Green's functions (the measurement step after the sweep)
     tdgf = force = None
-    if not args.no_batch and args.config == "c3" and rank == 0:
+    if not args.no_batch and args.config == "L16" and rank == 0:
         tdgf = measure_tdgf(args, dev)
         force = measure_force(args, dev)
-    # the batched part of the metric: 64 chains of L in {6, 8, 10, 12} (config c2), mixed form
+    # the batched part of the metric: 64 chains of L in {6, 8, 10, 12} (chains64), mixed form
     batched = None
-    if not args.no_batch and args.config == "c3":
+    if not args.no_batch and args.config == "L16":
         for r in res.values():
             r["chain"].close()
         # warm-up: both start states of a sweep (down and up) captured as graphs
@@ -728,7 +731,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c3", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="L16", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-checks", action="store_true", help="all_checks off")
     ap.add_argument("--cpu-calls", type=int, default=10)
@@ -739,7 +742,7 @@ def main():
                     help="both: FP64 and mixed forms on the same field and streams; value = mixed")
     ap.add_argument("--delay", type=int, default=16, help="mixed form: delayed-update depth k")
     ap.add_argument("--fp64-delay", type=int, default=1, help="FP64 form: delayed-update depth (1 = rank-4)")
-    ap.add_argument("--chains", type=int, default=64, help="chains of the batched config c2")
+    ap.add_argument("--chains", type=int, default=64, help="chains of the batched chains64 workload")
     ap.add_argument("--batch-delay", default="auto", help="batched chains: delayed-update depth, or 'auto' "
                     "(autotuned per L over 8, 16, 32)")
     ap.add_argument("--no-batch", action="store_true", help="default run: skip the batched-chains measurement")
@@ -747,7 +750,7 @@ def main():
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
-    elif args.config == "c2":
+    elif args.config == "chains64":
         run_batch(args, world, rank, local)
     else:
         run_ours(args, world, rank, local)

@@ -41,8 +41,8 @@ def lib():
     return api
 
 
-# config 0 of the workload list: L=4, beta=4 (M=40), lambda=1, r=c=u=1, box 0.2
-C0 = R.Params(L=4, slices=40, delta_tau=0.1, safe_mult=10, lambda_=1.0, r=1.0, c=1.0, u=1.0, mu1=-0.5, mu2=-0.5,
+# the L=4, beta=4 (M=40) workload: lambda=1, r=c=u=1, box 0.2
+P_L4 = R.Params(L=4, slices=40, delta_tau=0.1, safe_mult=10, lambda_=1.0, r=1.0, c=1.0, u=1.0, mu1=-0.5, mu2=-0.5,
               box=0.2)
 
 
@@ -86,9 +86,9 @@ def test_decompose_udt(lib, small_params):
 
 
 @pytest.mark.parametrize("method", METHODS)
-@pytest.mark.parametrize("cfg", ["small", "c0"])
+@pytest.mark.parametrize("cfg", ["small", "l4"])
 def test_init_and_full_propagation(lib, golden, small_params, cfg, method):
-    p = small_params if cfg == "small" else C0
+    p = small_params if cfg == "small" else P_L4
     phi = golden["randconf"] if cfg == "small" else R.synthetic_field(p.N, p.slices, 100)
     ref = R.DQMCRef(p, phi)
     ref.init()
@@ -107,7 +107,7 @@ def test_init_and_full_propagation(lib, golden, small_params, cfg, method):
 
 @pytest.mark.parametrize("method", METHODS)
 def test_calc_greens_from_scratch(lib, golden, small_params, method):
-    p = C0
+    p = P_L4
     phi = R.synthetic_field(p.N, p.slices, 5)
     ref = R.DQMCRef(p, phi)
     gpu = lib.DQMC(api_params(p, greens_method=method), phi)
@@ -120,7 +120,7 @@ def test_calc_greens_from_scratch(lib, golden, small_params, method):
 
 
 def test_wrap_greens(lib, small_params):
-    p = C0
+    p = P_L4
     phi = R.synthetic_field(p.N, p.slices, 6)
     ref = R.DQMCRef(p, phi)
     gpu = lib.DQMC(api_params(p), phi)
@@ -144,7 +144,7 @@ def _compare_updates(ref, gpu, delta, u, margin=1e-9):
 
 
 def test_local_updates_one_slice(lib, golden, small_params):
-    p = dataclasses.replace(C0)
+    p = dataclasses.replace(P_L4)
     phi = R.synthetic_field(p.N, p.slices, 7)
     ref = R.DQMCRef(p, phi)
     ref.init()
@@ -159,10 +159,10 @@ def test_local_updates_one_slice(lib, golden, small_params):
 
 @pytest.mark.parametrize("delay,method", [(1, "scales"), (4, "scales"), (8, "scales"), (16, "scales"),
                                           (32, "scales"), (1, "two_qr"), (16, "two_qr")])
-def test_sweep_config0_accept_sequence(lib, delay, method):
-    """Config 0: one full sweep (M update calls) on shared streams, with
+def test_sweep_l4_accept_sequence(lib, delay, method):
+    """L=4, beta=4: one full sweep (M update calls) on shared streams, with
     immediate rank-4 updates (delay 1) and delayed rank-k updates."""
-    p = C0
+    p = P_L4
     phi = R.synthetic_field(p.N, p.slices, 2024)
     delta, u = R.synthetic_streams(p.N, p.slices, p.box, 2025)
     ref = R.DQMCRef(p, phi)
@@ -185,8 +185,8 @@ def test_sweep_config0_accept_sequence(lib, delay, method):
 
 
 @pytest.mark.parametrize("delay", [1, 16])
-def test_sweep_config1_shapes(lib, delay):
-    """Config 1 shapes (L=10, M=100): 15 update calls crossing a stabilisation,
+def test_sweep_l10_shapes(lib, delay):
+    """L=10, M=100: 15 update calls crossing a stabilisation,
     immediate and delayed (k = 16) updates."""
     p = R.Params(L=10, slices=100, delta_tau=0.1, safe_mult=10, lambda_=1.0, r=1.0, c=1.0, u=1.0, mu1=-0.5,
                  mu2=-0.5, box=0.2)
@@ -209,7 +209,7 @@ def test_sweep_config1_shapes(lib, delay):
 
 
 def test_measurement_hook(lib):
-    p = C0
+    p = P_L4
     phi = R.synthetic_field(p.N, p.slices, 77)
     ref = R.DQMCRef(p, phi)
     ref.init()
@@ -248,7 +248,7 @@ def test_split_bf16_gemm_accuracy(lib, L):
 
 @pytest.mark.parametrize("delay", [1, 16])
 def test_mixed_sweep_matches_fp64(lib, delay):
-    p = C0
+    p = P_L4
     phi = R.synthetic_field(p.N, p.slices, 555)
     delta, u = R.synthetic_streams(p.N, p.slices, p.box, 556)
     ref = R.DQMCRef(p, phi)
@@ -269,8 +269,8 @@ def test_mixed_sweep_matches_fp64(lib, delay):
         assert relerr(gpu.greens, ref.greens) < MIXED_TOL
 
 
-def test_mixed_config1_greens_error(lib):
-    """Mixed form at config 1 shapes: |G_mixed - G_FP64| after 15 update calls
+def test_mixed_l10_greens_error(lib):
+    """Mixed form at L=10, M=100: |G_mixed - G_FP64| after 15 update calls
     (delayed k = 16) with the accept sequences compared where the margin is
     above the mixed-form error."""
     p = R.Params(L=10, slices=100, delta_tau=0.1, safe_mult=10, lambda_=1.0, r=1.0, c=1.0, u=1.0, mu1=-0.5,
@@ -310,8 +310,8 @@ def test_force_matches_oracle(lib):
     assert np.max(np.abs(gb - gb_r)) < 1e-12 * max(1.0, np.max(np.abs(gb_r)))
 
 
-def test_force_config4_finite_differences(lib):
-    """Config 4 sizes (L=12, beta=10, M=100): the adjoint force against
+def test_force_l12_finite_differences(lib):
+    """L=12, beta=10 (M=100): the adjoint force against
     central differences (h=1e-5) of log|det M| = -log|det G| computed from
     scratch by the library, on 200 random entries (1e-6 relative)."""
     p = R.Params(L=12, slices=100, delta_tau=0.1, safe_mult=10, lambda_=1.0, r=1.0, c=1.0, u=1.0, mu1=-0.5,
@@ -337,9 +337,9 @@ def test_force_config4_finite_differences(lib):
 
 def test_langevin_steps(lib):
     """100 Langevin steps (eps = 1e-3) on S_b - log|det M| with a local sweep
-    after every 10th (config 4's schedule, at config 0 sizes): the field stays
+    after every 10th (the L=12 schedule, here at L=4, M=40): the field stays
     finite and the tracked boson action matches a recomputation."""
-    p = C0
+    p = P_L4
     gpu = lib.DQMC(api_params(p), R.synthetic_field(p.N, p.slices, 81))
     gpu.init()
     rng = np.random.default_rng(82)
@@ -360,7 +360,7 @@ def test_langevin_steps(lib):
 # ---------------------------------------------------------------------------
 @pytest.mark.parametrize("force_accept", [True, False])
 def test_global_update(lib, force_accept):
-    p = C0
+    p = P_L4
     phi = R.synthetic_field(p.N, p.slices, 91)
     shift = np.array([0.05, -0.03, 0.02])
     u = 0.0 if force_accept else 1.0 - 1e-15
@@ -423,10 +423,10 @@ def _tdgf_params(cfg, small_params):
     # ref_test: the reference's test system (M = safe_mult = 10), where fill_tdgf!
     # propagates slices 6..10 from the not yet filled (zero) slice 5
     return {"small": dataclasses.replace(small_params, slices=20, safe_mult=5), "ref_test": small_params,
-            "c0": C0}[cfg]
+            "l4": P_L4}[cfg]
 
 
-@pytest.mark.parametrize("cfg,prec", [("small", "fp64"), ("ref_test", "fp64"), ("c0", "fp64"), ("c0", "mixed")])
+@pytest.mark.parametrize("cfg,prec", [("small", "fp64"), ("ref_test", "fp64"), ("l4", "fp64"), ("l4", "mixed")])
 def test_time_displaced_greens(lib, golden, small_params, cfg, prec):
     """measure_tdgfs! (time-displaced G(tau, 0) and -G(0, tau) for every slice)
     against the oracle's restatement; mixed form within 1e-8."""
@@ -452,7 +452,7 @@ def test_lu_blocked_and_unblocked(lib, monkeypatch, tune, L, prec):
     panel at n = 400) and through the unblocked cooperative LU, selected per
     handle by DQMC_TUNE; both reproduce the oracle (1e-10 FP64, 1e-8 mixed)."""
     monkeypatch.setenv("DQMC_TUNE", tune)
-    p = dataclasses.replace(C0, L=L, slices=20)
+    p = dataclasses.replace(P_L4, L=L, slices=20)
     phi = R.synthetic_field(p.N, p.slices, 31 + L)
     ref = R.DQMCRef(p, phi)
     prm = api_params(p)
@@ -475,7 +475,7 @@ def test_equal_time_correlators(lib, L):
     """dqmc_measure_equal_time against the oracle's measure_etpc / measure_etcdc
     (src/fermion_measurements.jl:388-424, 592-630): on a given true G and on
     the measurement hook's G of the current slice (1e-12 and 1e-10 relative)."""
-    p = dataclasses.replace(C0, L=L, slices=20)
+    p = dataclasses.replace(P_L4, L=L, slices=20)
     phi = R.synthetic_field(p.N, p.slices, 71 + L)
     ref = R.DQMCRef(p, phi)
     ref.init()
@@ -492,7 +492,7 @@ def test_equal_time_correlators(lib, L):
         gpu.close()
 
 
-@pytest.mark.parametrize("cfg", ["ref_test", "c0"])
+@pytest.mark.parametrize("cfg", ["ref_test", "l4"])
 def test_zero_frequency_pairing(lib, small_params, cfg):
     """dqmc_measure_zfpc (measure_zfpc!, src/fermion_measurements.jl:500-541) on
     the device's own G(tau, 0) and on the oracle's G(tau, 0) passed in,
@@ -512,7 +512,7 @@ def test_zero_frequency_pairing(lib, small_params, cfg):
         gpu.close()
 
 
-@pytest.mark.parametrize("cfg", ["ref_test", "c0"])
+@pytest.mark.parametrize("cfg", ["ref_test", "l4"])
 def test_zero_frequency_charge_density(lib, small_params, cfg):
     """dqmc_measure_zfcdc (measure_zfcdc!, src/fermion_measurements.jl:688-743):
     all inputs on the device (hook G, device time-displaced G) against the
@@ -534,7 +534,7 @@ def test_zero_frequency_charge_density(lib, small_params, cfg):
         gpu.close()
 
 
-@pytest.mark.parametrize("cfg", ["ref_test", "c0"])
+@pytest.mark.parametrize("cfg", ["ref_test", "l4"])
 def test_zero_frequency_current_current(lib, small_params, cfg):
     """dqmc_measure_zfccc (measure_zfccc!, src/fermion_measurements.jl:814-888,
     and measure_sfdensity :911-920) against the oracle: all inputs on the device
@@ -565,14 +565,14 @@ def _binned(x, nbins=4):
 
 
 def test_observables_agree_within_binned_errors(lib):
-    """The benchmark spec's observable check: boson susceptibility chi_static
+    """Observable agreement: boson susceptibility chi_static
     (src/boson_measurements.jl:6-32) and the fermion kinetic energy from the
     measurement hook's true G, recorded at the measurement point (slice M,
-    direction -1) after each of 24 up-down sweeps of config 0 from the same
+    direction -1) after each of 24 up-down sweeps at L=4, M=40 from the same
     field and streams on the GPU and in the oracle.  The binned means agree
     within their binned errors; since the accept sequences are identical, the
     series themselves agree to round-off (1e-9 relative)."""
-    p = C0
+    p = P_L4
     phi = R.synthetic_field(p.N, p.slices, 91)
     n_ud, calls = 24, 2 * p.slices
     delta, u = R.synthetic_streams(p.N, n_ud * calls, p.box, 92)

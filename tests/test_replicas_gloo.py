@@ -51,7 +51,7 @@ def test_reference_arm_two_ranks():
     pytest.importorskip("torch")
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), "bench.py", "--impl", "reference",
-           "--config", "c0", "--gpus", "2", "--steps", "1", "--warmup", "0", "--ref-calls", "2"]
+           "--config", "L4", "--gpus", "2", "--steps", "1", "--warmup", "0", "--ref-calls", "2"]
     env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1")
     out = subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stderr[-2000:]
