@@ -11,6 +11,17 @@ golden data (`test/data/O3.jld`, `test/data/linalg.jld`, decoded into
 known answers written in the reference's test files (`test/tests_O3.jl`,
 `test/tests_O3_measurements.jl`, `test/tests_linalg.jl`).
 
+Reference files restated here (paths within carstenbauer/dqmc):
+  * src/stack.jl:251-499 (stack, propagate, calculate_greens);
+  * src/local_updates.jl:1-95, src/action.jl:1-100, src/interactions.jl:35-141;
+  * src/slice_matrices.jl:25-226, src/hoppings.jl:16-95, src/hoppings_checkerboard.jl:4-136,
+    src/lattice.jl:105-153;
+  * src/linalg.jl:20-61, 195-339, 512-567 (UDT, multiply_safely, inverses of UDT sums);
+  * src/fermion_measurements.jl:363-920 (equal-time and zero-frequency correlators),
+    964-1142 (from-scratch G, effective -> true G), 1343-1523 (time-displaced G);
+  * src/boson_measurements.jl:6-32, src/global_updates.jl:18-58,
+    src/dqmc_framework.jl:152-177, 500-517.
+
 Conventions (identical to the reference):
   * sites are 0-based here; site s = y + L*x  (reference: `sql = reshape(1:N, L, L)`,
     src/lattice.jl:109);
