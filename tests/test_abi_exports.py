@@ -52,3 +52,34 @@ def test_version_string_without_gpu(libpath):
 def test_params_struct_layout():
     # dqmc_params: 4 int32, 7 doubles, 4 doubles, 5 int32, 3 int32 -> 112 bytes
     assert ctypes.sizeof(api.CParams) == 4 * 4 + 7 * 8 + 4 * 8 + 5 * 4 + 3 * 4
+
+
+def header_prototypes():
+    """name -> number of parameters of every DQMC_API prototype."""
+    txt = open(os.path.join(ROOT, "include", "dqmc_gpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    out = {}
+    for m in re.finditer(r"DQMC_API\s+[^;(]*?\b(dqmc_\w+)\s*\(([^)]*)\)\s*;", txt, flags=re.S):
+        params = m.group(2).strip()
+        out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_match_header_arity():
+    protos = header_prototypes()
+    assert set(protos) == set(header_functions())
+    wrong = {n: (len(api.SIGNATURES[n][0]), k) for n, k in protos.items() if len(api.SIGNATURES[n][0]) != k}
+    assert not wrong, f"binding argument count differs from the header (binding, header): {wrong}"
+
+
+def test_kernel_kinds_match_header():
+    txt = open(os.path.join(ROOT, "include", "dqmc_gpu.h")).read()
+    ids = {int(v) for v in re.findall(r"#define DQMC_K_\w+\s+(\d+)", txt)}
+    nk = int(re.search(r"#define DQMC_NKINDS\s+(\d+)", txt).group(1))
+    assert ids == set(range(nk)) and len(api.KERNEL_KINDS) == nk
+    # names in the header's order: the comment word after each index matches the binding's name
+    order = [m.group(1).lower() for m in re.finditer(r"#define DQMC_K_(\w+)\s+\d+", txt)]
+    alias = {"slice_cols": "slice_cols", "slice_rows": "slice_rows", "local": "local_updates", "gemm": "zgemm",
+             "qrp": "qrp", "applyq": "apply_q", "trsm": "trsm", "misc": "misc", "ozgemm": "ozaki_gemm",
+             "flush": "flush", "lu": "lu"}
+    assert [alias[o] for o in order] == api.KERNEL_KINDS
