@@ -150,3 +150,35 @@ def test_time_displaced_greens_at_safe_slices(small_params):
         assert np.max(np.abs(Gt0[tau - 1] - want)) < 1e-12
         want0 = m.effective_greens2greens(-(np.eye(n) - G0) @ np.linalg.inv(chain(tau - 1, 1)))
         assert np.max(np.abs(G0t[tau - 1] - want0)) < 1e-10 * max(1.0, np.max(np.abs(want0)))
+
+
+@pytest.mark.parametrize("seed", [1234, 99])
+def test_udt_inversion_identities(seed):
+    """tests_linalg.jl:119-174 ("UDT and UDV inversion business", well-conditioned)
+    restated for the oracle: with X = U D T and Y = Uy Dy Ty from decompose_udt of
+    uniform random complex matrices (the size of the reference's test G, 64 x 64),
+    inv_one_plus_udt_scalettar gives (I + X)^-1 and inv_sum_udts_scalettar gives
+    (X + Y)^-1 to round-off; and, with D spread over 1e-12..1e12 (the regime the
+    scale separation exists for), [1 + U D T]^-1 still matches a 50-digit inverse."""
+    rng = np.random.default_rng(seed)
+    n = 64
+    X = rng.uniform(size=(n, n)) + 1j * rng.uniform(size=(n, n))
+    Y = rng.uniform(size=(n, n)) + 1j * rng.uniform(size=(n, n))
+    u, d, t = R.decompose_udt(X.copy())
+    uy, dy, ty = R.decompose_udt(Y.copy())
+    assert np.allclose(u @ np.diag(d) @ t, X, atol=1e-12)
+    assert np.allclose(R.inv_one_plus_udt_scalettar(u, d, t), np.linalg.inv(np.eye(n) + X), atol=1e-10)
+    assert np.allclose(R.inv_sum_udts_scalettar(u, d, t, uy, dy, ty), np.linalg.inv(X + Y), atol=1e-10)
+    # badly scaled (16 x 16): D from 1e12 to 1e-12, reference inverse in 50-digit arithmetic
+    mpmath = pytest.importorskip("mpmath")
+    m = 16
+    us, _, ts = R.decompose_udt(X[:m, :m].copy())
+    d2 = np.logspace(12, -12, m)
+    mpmath.mp.dps = 50
+    U = mpmath.matrix([[mpmath.mpc(z.real, z.imag) for z in row] for row in us])
+    T = mpmath.matrix([[mpmath.mpc(z.real, z.imag) for z in row] for row in ts])
+    Dm = mpmath.diag([mpmath.mpf(x) for x in d2])
+    inv = (mpmath.eye(m) + U * Dm * T) ** -1
+    want = np.array([[complex(inv[i, j]) for j in range(m)] for i in range(m)])
+    got = R.inv_one_plus_udt_scalettar(us, d2, ts)
+    assert np.max(np.abs(got - want)) / max(1.0, np.max(np.abs(want))) < 1e-10
