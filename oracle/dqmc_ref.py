@@ -1133,6 +1133,13 @@ def measure_chi_static(conf, delta_tau=0.1):
     return float(measure_chi_dynamic(conf, delta_tau)[0, 0, 0])
 
 
+def measure_op(conf):
+    """measure_op (src/boson_measurements.jl:41-45): mean |phi| over all
+    components, sites and slices, and the mean of each component."""
+    conf = np.asarray(conf)
+    return float(np.mean(np.abs(conf))), conf.mean(axis=(1, 2))
+
+
 def measure_binder_factors(conf):
     m = conf.mean(axis=(1, 2))
     m2 = float(m @ m)

@@ -93,6 +93,10 @@ def test_boson_measurements(golden):
     m2, m4 = R.measure_binder_factors(rc)
     assert np.isclose(m2, golden["lit_binder_m2"], rtol=1e-14)
     assert np.isclose(m4, golden["lit_binder_m4"], rtol=1e-14)
+    # measure_op literals of tests_O3_measurements.jl:7-9 (the reference's own tolerances)
+    a, b = R.measure_op(rc)
+    assert np.isclose(a, 0.5080018386458331, rtol=1.5e-8)
+    assert np.allclose(b, [0.514548, 0.536541, 0.472916], atol=1e-4)
 
 
 def _etpc_etcdc_loops(L, G):
