@@ -142,6 +142,21 @@ class SmemLimit {
   int set_[kMaxDevices] = {};
 };
 
+// Host-side check of an address a kernel will dereference: device or managed
+// memory, or registered host memory mapped at the same address (NULL passes;
+// callers check it).  A pageable host array passed as a device address would
+// otherwise make the kernel fault.  Allocates nothing.
+inline bool device_accessible(const void* p) {
+  if (!p) return true;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged ||
+         (at.type == cudaMemoryTypeHost && at.devicePointer == p);
+}
+
 // Error bits reported by kernels through a device int.
 enum {
   DQMC_KERR_BARRIER_TIMEOUT = 2,

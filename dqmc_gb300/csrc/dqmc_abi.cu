@@ -1086,29 +1086,15 @@ int measure(dqmc_handle* h, cplx* Gt0, cplx* G0t) {
 
 }  // namespace tdgf
 
-// The measurement hook's true G of the current slice into dst:
-// wrap_greens(G, current_slice, +1), then effective -> true
-// (src/dqmc_framework.jl:378-381, src/fermion_measurements.jl:1125-1142).
-// Host-side check of an address a kernel will dereference: device or managed
-// memory, or registered host memory mapped at the same address (NULL passes;
-// callers check it).  A pageable host array passed as a device address would
-// otherwise make the kernel fault.
-static bool device_accessible(const void* p) {
-  if (!p) return true;
-  cudaPointerAttributes at;
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged ||
-         (at.type == cudaMemoryTypeHost && at.devicePointer == p);
-}
-
 static bool all_device_accessible(std::initializer_list<const void*> ps) {
   for (const void* p : ps)
     if (!device_accessible(p)) return false;
   return true;
 }
+
+// The measurement hook's true G of the current slice into dst:
+// wrap_greens(G, current_slice, +1), then effective -> true
+// (src/dqmc_framework.jl:378-381, src/fermion_measurements.jl:1125-1142).
 
 static int hook_true_greens(dqmc_handle* h, cplx* dst) {
   if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
@@ -1153,6 +1139,9 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
   if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess) return fail(DQMC_ERR_CUDA);
   h->sm_count = prop.multiProcessorCount;
   if (!prop.cooperativeLaunch) return fail(DQMC_ERR_CUDA);
+  // inflight > 1 on a single chain: cooperative grids capped as for one of
+  // that many chains sharing the GPU (a batch chain's launch shapes)
+  if (p->inflight > 1) h->coop_cap = h->sm_count / p->inflight > 0 ? h->sm_count / p->inflight : 1;
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) return fail(DQMC_ERR_CUDA);
   const size_t n = h->n, N = h->N, M = h->M, ne = h->ne;
   const size_t nn = n * n * sizeof(cplx);

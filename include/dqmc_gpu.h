@@ -66,7 +66,8 @@ typedef struct dqmc_params {
   int32_t ozaki_bits;  /* mixed form: mantissa bits kept per GEMM operand (0 = default 40, max 60) */
   int32_t delay;       /* delayed-update depth k (0 or 1 = immediate rank-4 updates) */
   int32_t greens_method; /* DQMC_GREENS_SCALES (default) or DQMC_GREENS_TWO_QR */
-  int32_t inflight;    /* dqmc_batch_create: chains swept at the same time (0 = min(count, 8)); first chain's value */
+  int32_t inflight;    /* dqmc_batch_create: chains swept at the same time (0 = min(count, 8)); first chain's value.
+                          dqmc_create: > 1 caps the cooperative grids as for one of that many batch chains */
   int32_t reserved[1];
 } dqmc_params;
 
@@ -162,14 +163,18 @@ DQMC_API int dqmc_sweep_device(dqmc_handle* h, int32_t n_calls, const double* de
  * them DEVICE pointers: greens (n x n complex, updated in place), phi
  * (3 x N x M, updated in place), delta[3*N], unif[N], accepted[N] (may be
  * NULL) and action (one double, incremented by each accepted Delta S).
- * `stream` is a cudaStream_t (NULL = legacy default stream); the call returns
- * after the stream has finished the update.
+ * `stream` is a cudaStream_t of the selected device (NULL = legacy default
+ * stream).  The call is synchronous: it returns after the stream has
+ * finished the update, and it returns DQMC_ERR_ARG on a stream that is being
+ * captured, on a stream of another device, and when any array is not device
+ * memory.  The calling thread's current device is restored on return.
  *   - It allocates nothing: its scratch (the rank-4 factors, a grid barrier
  *     and an error flag; 128 KB) is one static device array that every GPU
  *     which loads the library holds until exit.  Limit: n = 4 L^2 <= 1024
  *     (L <= 16); larger sizes return DQMC_ERR_TOO_LARGE.
  *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *     (cudaGetSymbolAddress) and keeps it: do not use the library across a
+ *     cudaDeviceReset of that device.
  *   - All calls share the array: calls that overlap on the GPU (other host
  *     threads, other streams) race and must be serialised by the caller. */
 DQMC_API int dqmc_local_updates_noalloc(const dqmc_params* p, double* greens, double* phi, int32_t slice,

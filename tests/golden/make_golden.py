@@ -1,9 +1,10 @@
 """Generates the golden fixtures of this directory from the reference's own
 test data (carstenbauer/dqmc `test/data/O3.jld` and `test/data/linalg.jld`).
 
-Run in a checkout that has the reference next to it:
+Run with the path of a checkout of the reference, as an argument or in the
+environment variable DQMC_REFERENCE:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path-to-carstenbauer-dqmc>
 
 Only datasets that do not depend on Julia's global RNG stream are kept (the
 reference draws the others after `Random.seed!` with Julia <= 1.6's dSFMT,
@@ -85,4 +86,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DQMC_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py <path-to-carstenbauer-dqmc> (or set DQMC_REFERENCE)")
+    main(ref)

@@ -32,16 +32,22 @@ def test_noalloc_rejects_sizes_beyond_static_scratch():
 
 
 @pytest.mark.gpu
-def test_noalloc_matches_handle_path_two_calls():
+@pytest.mark.parametrize("L,M,steps", [(4, 40, 0), (4, 40, 3), (16, 20, 0), (16, 20, 5)])
+def test_noalloc_matches_handle_path_two_calls(L, M, steps):
+    """Two calls in a row at n = 64 and at the static limit n = 1024, at the
+    slice after init (M) and at a slice `steps` propagations further down."""
     torch = pytest.importorskip("torch")
     from dqmc_gb300 import api, build
     build.build()
     lib = api.load_library()
-    mp = _params(api)
-    N, n, M = mp.N, mp.n, mp.slices
-    chain = api.DQMC(mp, synthetic_field(N, M, 4242))
+    mp = _params(api, L, M)
+    N, n = mp.N, mp.n
+    chain = api.DQMC(mp, synthetic_field(N, M, 4242 + L))
     chain.init()
+    for _ in range(steps):
+        chain.propagate()
     slice1 = chain.current_slice
+    assert slice1 == M - steps
     dev = torch.device("cuda:0")
 
     def to_dev(a):
@@ -52,7 +58,7 @@ def test_noalloc_matches_handle_path_two_calls():
     act_d = torch.tensor([chain.boson_action], dtype=torch.float64, device=dev)
     acc_d = torch.zeros(N, dtype=torch.uint8, device=dev)
     cp = mp.to_c()
-    delta, unif = synthetic_streams(N, 2, mp.box, 4343)
+    delta, unif = synthetic_streams(N, 2, mp.box, 4343 + L)
     for call in range(2):
         # existing entry point (handle owns its memory)
         _, acc_ref, _, _ = chain.local_updates(delta[call], unif[call], return_details=True)
@@ -70,7 +76,35 @@ def test_noalloc_matches_handle_path_two_calls():
         G_ref = chain.greens
         assert np.max(np.abs(G_na - G_ref)) < TOL * max(1.0, np.max(np.abs(G_ref))), f"call {call}"
         assert np.array_equal(acc_d.cpu().numpy().astype(bool), acc_ref), f"call {call}"
+        assert acc_ref.any(), "no acceptance: the update path was not exercised"
         phi_na = phi_d.cpu().numpy().reshape((3, N, M), order="F")
         assert np.allclose(phi_na, chain.get_field(), rtol=0, atol=TOL), f"call {call}"
         assert abs(act_d.item() - chain.boson_action) < TOL * abs(chain.boson_action), f"call {call}"
     chain.close()
+
+
+@pytest.mark.gpu
+def test_noalloc_rejects_host_array():
+    """A host (numpy) array where a device array is expected is an argument
+    error, returned before anything is launched; the device arrays are left
+    untouched."""
+    torch = pytest.importorskip("torch")
+    from dqmc_gb300 import api, build
+    build.build()
+    lib = api.load_library()
+    mp = _params(api, 4, 10)
+    N, n, M = mp.N, mp.n, mp.slices
+    dev = torch.device("cuda:0")
+    G_host = np.zeros(2 * n * n)
+    phi_d = torch.zeros(3 * N * M, dtype=torch.float64, device=dev)
+    d_d = torch.zeros(3 * N, dtype=torch.float64, device=dev)
+    u_d = torch.full((N,), 0.5, dtype=torch.float64, device=dev)
+    act_d = torch.zeros(1, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    cp = mp.to_c()
+    rc = lib.dqmc_local_updates_noalloc(ctypes.byref(cp), ctypes.c_void_p(G_host.ctypes.data),
+                                        ctypes.c_void_p(phi_d.data_ptr()), 1, ctypes.c_void_p(d_d.data_ptr()),
+                                        ctypes.c_void_p(u_d.data_ptr()), None, ctypes.c_void_p(act_d.data_ptr()),
+                                        None)
+    assert rc == -1
+    assert act_d.item() == 0.0
