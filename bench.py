@@ -45,12 +45,12 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 CONFIGS = {
-    # name: (L, M, description)
-    "L4": (4, 40, "O(3) L=4 beta=4 (M=40) dtau=0.1 safe_mult=10 FP64"),
+    # name: (L, M, workload); the arithmetic form is reported in its own key
+    "L4": (4, 40, "O(3) L=4 beta=4 (M=40) dtau=0.1 safe_mult=10"),
     "chains64": (0, 80, "64 independent O(3) chains, L uniform in {6,8,10,12}, beta=8 (M=80) dtau=0.1 safe_mult=10"),
-    "L10": (10, 100, "O(3) L=10 beta=10 (M=100) dtau=0.1 safe_mult=10 FP64"),
-    "L16": (16, 200, "O(3) L=16 beta=20 (M=200) dtau=0.1 safe_mult=10 FP64"),
-    "L12": (12, 100, "O(3) L=12 beta=10 (M=100) dtau=0.1 safe_mult=10 FP64"),
+    "L10": (10, 100, "O(3) L=10 beta=10 (M=100) dtau=0.1 safe_mult=10"),
+    "L16": (16, 200, "O(3) L=16 beta=20 (M=200) dtau=0.1 safe_mult=10"),
+    "L12": (12, 100, "O(3) L=12 beta=10 (M=100) dtau=0.1 safe_mult=10"),
 }
 METRIC = "O(3) L=16 sweeps/s: mixed vs FP64 at G err≤1e-8; batched chain-sweeps/s"
 
@@ -159,11 +159,30 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def flops_model(kind, t, n, accepted):
+def flops_model(kind, t, n, accepted, delay=1, real_flushes=0):
+    """Algorithmic (FP64-equivalent flops, bytes) of one kernel kind over the
+    launches in `t`.  The rank-4 update of an accepted site is 32 n^2 flops
+    and one read + write of G (32 n^2 bytes).  Immediate form (delay 1): the
+    local-update kernel does it.  Delayed form: the decision kernel only
+    decides and forms the new factor rows/columns (its cost is reported per
+    site, not as a rate); the flush does the rank-4k work, 32 n^2 flops per
+    accepted site, and moves G once per flush that carries work."""
     k = t["kinds"][kind]
     if kind == "local_updates":
-        return 32.0 * n * n * accepted, 32.0 * n * n * accepted
+        if delay <= 1:
+            return 32.0 * n * n * accepted, 32.0 * n * n * accepted
+        return 0.0, 0.0
+    if kind == "flush":
+        return 32.0 * n * n * accepted, 32.0 * n * n * real_flushes
     return k["flops"], k["bytes"]
+
+
+def real_flush_count(acc_flags, M, N, delay):
+    """Flushes with work in one sweep of delayed rounds: a round ends after
+    `delay` acceptances or at the end of the slice, so a slice with a
+    acceptances flushes ceil(a / delay) times with work."""
+    a = np.asarray(acc_flags, dtype=np.int64).reshape(M, N).sum(axis=1)
+    return int(np.sum((a + delay - 1) // delay))
 
 
 def cpu_baseline(p, phi, n_calls, seed, threads):
@@ -202,7 +221,11 @@ def cpu_baseline_threads(L, M, n_calls, threads):
 
 def run_reference(args, world, rank):
     """The reference's own CPU implementation is Julia (not installed on
-    either machine); its CPU restatement (the oracle) is timed instead."""
+    either machine); its CPU restatement (the oracle) is timed instead.  A
+    step is a bounded sample of the workload: `ref_calls` consecutive update
+    calls (10 = one safe_mult block, one stabilisation included);
+    ms_per_step is that sample's time, and value extrapolates it to sweeps/s
+    (M update calls per sweep)."""
     if rank != 0:
         return
     L, M, desc = CONFIGS[args.config]
@@ -224,16 +247,19 @@ def run_reference(args, world, rank):
         for _ in range(calls_per_step):
             ref.update(delta[c], u[c]); c += 1
         times.append(time.perf_counter() - t0)
-    per_call = sum(times) / (args.steps * calls_per_step)
-    value = 1.0 / (per_call * p.slices)
+    step_s = sum(times) / args.steps
+    value = (calls_per_step / p.slices) / step_s
+    sample = (f"a step is {calls_per_step} consecutive of the {M} update calls of one sweep; ms_per_step is "
+              f"that sample's time and value extrapolates it to sweeps/s")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * step_s, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform fields/streams)",
-        "config": {"workload": desc, "L": L, "slices": M, "sample": f"{calls_per_step} update calls per step"},
+        "config": {"workload": desc, "form": "fp64 (CPU oracle port of the reference)", "L": L, "slices": M,
+                   "sample": sample},
         "cpu_baseline": {"value": value, "unit": "sweeps/s", "cores": threads, "kind": "port",
-                         "sample": f"{calls_per_step} of {M} update calls per step, extrapolated; "
-                                   "Julia reference unavailable (no Julia toolchain)"},
+                         "sample": sample + f"; numpy/scipy oracle, OpenBLAS {threads} threads; "
+                                            "Julia reference unavailable (no Julia toolchain)"},
         "e2e": {"value": value, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -399,10 +425,10 @@ def measure_tdgf(args, dev):
 def measure_force(args, dev):
     """Adjoint force at L=12, beta=10 (M=100): device time of
     one dqmc_force, its largest relative deviation from central differences
-    (h=1e-5) of the library's log|det M| on 24 random entries, and 20
-    Langevin steps (eps=1e-3) with a local sweep after every 10th (the full
-    100-step schedule runs in the GPU tests).  Errors are recorded in the
-    result instead of ending the run."""
+    (h=1e-5) of the library's log|det M| on 24 random entries, and the full
+    schedule of 100 Langevin steps (eps=1e-3) with a local sweep (M update
+    calls) after every 10th.  Errors are recorded in the result instead of
+    ending the run."""
     from dqmc_gb300 import api
     from oracle import dqmc_ref as R
     L, M = 12, 100
@@ -430,7 +456,7 @@ def measure_force(args, dev):
         out["fd_entries"] = 24
         out["max_rel_error_vs_finite_differences"] = worst
         chain.init(phi)
-        steps = 20
+        steps = 100
         delta, unif = R.synthetic_streams(rp.N, (steps // 10) * M, rp.box, 73)
         t0 = time.perf_counter()
         for step in range(steps):
@@ -440,8 +466,11 @@ def measure_force(args, dev):
                 chain.sweep(M, delta[k * M:(k + 1) * M], unif[k * M:(k + 1) * M])
                 chain.init(chain.get_field())   # back to the state (M, -1) the force needs
         out["langevin_steps"] = steps
+        out["local_sweeps"] = steps // 10
         out["seconds_langevin_steps_with_sweeps"] = time.perf_counter() - t0
-        out["field_finite_after_langevin"] = bool(np.all(np.isfinite(chain.get_field())))
+        fin = chain.get_field()
+        out["field_finite_after_langevin"] = bool(np.all(np.isfinite(fin)))
+        out["boson_action_tracked_minus_recomputed"] = abs(chain.boson_action - R.boson_action(rp, fin))
         chain.close()
     except Exception as e:   # keep the bench line
         out["error"] = f"{type(e).__name__}: {e}"
@@ -485,9 +514,13 @@ def _make_chain(api, L, M, rp, args, dev, precision, delay, phi):
     return chain
 
 
-def _measure_form(api, chain, args, M, N, d_dev, u_dev, acc_dev, flush, world):
-    """W warm-up sweeps (accept flags kept), then K timed sweeps with an L2
-    flush before each; returns (device seconds, accepted, instability, timing)."""
+def _measure_form(api, chain, args, M, N, d_dev, u_dev, acc_dev, flush, world, steps, save_after=()):
+    """W warm-up sweeps, then `steps` timed sweeps with an L2 flush before
+    each, then one evented sweep (kernel breakdown).  Returns a dict: device
+    seconds of the timed sweeps, accepted count, largest stabilisation
+    difference, the evented sweep's timing, accepted count and flags, the
+    accept flags of the warm-up and timed sweeps, and G after the sweeps
+    listed in save_after (downloaded between sweeps, outside the events)."""
     import ctypes
     import torch
     st = api.CStats()
@@ -500,34 +533,84 @@ def _measure_form(api, chain, args, M, N, d_dev, u_dev, acc_dev, flush, world):
         chain._check(rc)
         return st.device_ms, st.accepted, st.max_instability
 
+    saved = {}
     for s in range(args.warmup):
         sweep(s)
+        if s in save_after:
+            saved[s] = chain.greens
     torch.cuda.synchronize()
-    warm_greens = chain.greens
     barrier(world)
     chain.reset_timing(False)
     torch.cuda.synchronize()
     dev_ms, accepted, instab = 0.0, 0, 0.0
-    for s in range(args.warmup, args.warmup + args.steps):
+    for s in range(args.warmup, args.warmup + steps):
         flush.fill_(float(s))
         torch.cuda.synchronize()
         ms, acc, ins = sweep(s)
         dev_ms += ms
         accepted += acc
         instab = max(instab, ins)
+        if s in save_after:
+            saved[s] = chain.greens
     torch.cuda.synchronize()
     barrier(world)
+    flags = acc_dev[:(args.warmup + steps) * M * N].cpu().numpy().reshape(args.warmup + steps, M, N)
     # kernel breakdown: one more sweep with a CUDA-event pair around every
     # launch (the library enqueues launch by launch while timing, instead of
     # replaying its captured sweep graph), on the first timed sweep's streams
     chain.reset_timing(True)
     flush.fill_(-1.0)
     torch.cuda.synchronize()
-    sweep(args.warmup)
+    _, acc_ev, _ = sweep(args.warmup)
     torch.cuda.synchronize()
     tim = chain.timing()
     chain.reset_timing(False)
-    return dev_ms / 1000.0, accepted, instab, tim, warm_greens
+    ev_flags = acc_dev[args.warmup * M * N:(args.warmup + 1) * M * N].cpu().numpy()
+    return dict(secs=dev_ms / 1000.0, accepted=accepted, instab=instab, timing=tim, saved=saved,
+                ev_accepted=acc_ev, ev_flags=ev_flags, flags=flags)
+
+
+def kernel_rooflines(tim, n, N, M, accepted_ev, ev_flags, delay, form, peaks, fp64_peak):
+    """Per kernel kind, over the one evented sweep: device ms, launches, share,
+    and the algorithmic rate against the bound of the kind.  Local updates of
+    the delayed form: microseconds per site and per accepted site (latency
+    bound); flush: algorithmic GB/s against HBM (G read and written once per
+    flush with work) and FP64-equivalent TFLOP/s; split-BF16 GEMMs: tensor
+    TFLOP/s against the BF16 peak; FP64 kinds against the FP64 peak."""
+    kinds = tim["kinds"]
+    tot_ms = sum(x["ms"] for x in kinds.values())
+    flushes = real_flush_count(ev_flags, M, N, delay) if delay > 1 else 0
+    pipe_of = {"slice_cols": "fp64", "slice_rows": "fp64", "qrp": "fp64", "ozaki_gemm": "tensor",
+               "flush": "tensor" if form == "mixed" else "fp64", "local_updates": "latency",
+               "lu": "fp64" if form == "fp64" else "fp64+tensor", "trsm": "fp64" if form == "fp64" else "fp64+tensor",
+               "apply_q": "fp64" if form == "fp64" else "fp64+tensor", "misc": "hbm", "zgemm": "fp64"}
+    out = {}
+    for k, v in kinds.items():
+        if not v["launches"]:
+            continue
+        secs = max(1e-12, v["ms"] / 1000.0)
+        kfl, kby = flops_model(k, tim, n, accepted_ev, delay, flushes)
+        e = {"ms": round(v["ms"], 2), "launches": v["launches"], "share": round(v["ms"] / max(1e-9, tot_ms), 4),
+             "pipe": pipe_of.get(k)}
+        if k == "local_updates" and delay > 1:
+            e["us_per_site"] = round(1e6 * secs / (M * N), 3)
+            e["us_per_accepted_site"] = round(1e6 * secs / max(1, accepted_ev), 3)
+        elif k == "flush":
+            e["flushes_with_work"] = flushes
+            e["us_per_flush_with_work"] = round(1e6 * secs / max(1, flushes), 2)
+            e["hbm_gbs"] = round(kby / secs / 1e9, 1)
+            e["hbm_frac"] = round(kby / secs / 1e9 / peaks["hbm_gbs"], 4) if peaks.get("hbm_gbs") else None
+            e["fp64_equiv_tflops"] = round(kfl / secs / 1e12, 3)
+            e["tensor_tflops"] = round(v["flops"] / secs / 1e12, 1) if form == "mixed" else None
+        else:
+            e["tflops"] = round(kfl / secs / 1e12, 3)
+            e["gbs"] = round(kby / secs / 1e9, 1)
+            if e["pipe"] == "fp64" and fp64_peak:
+                e["pipe_frac"] = round(kfl / secs / 1e12 / fp64_peak, 4)
+            elif e["pipe"] == "tensor" and peaks.get("bf16_tflops"):
+                e["pipe_frac"] = round(kfl / secs / 1e12 / peaks["bf16_tflops"], 4)
+        out[k] = e
+    return out
 
 
 def run_ours(args, world, rank, local):
@@ -551,17 +634,21 @@ def run_ours(args, world, rank, local):
     forms = [("mixed", args.delay)] if args.precision == "mixed" else [("fp64", args.fp64_delay)]
     if args.precision == "both":
         forms = [("fp64", args.fp64_delay), ("mixed", args.delay)]
+    head = forms[-1][0]
+    # the comparison form (FP64 when both run) is timed over at most fp64_steps sweeps
+    k_cmp = min(args.steps, args.fp64_steps) if len(forms) > 1 else args.steps
+    save_after = (args.warmup - 1, args.warmup + k_cmp - 1)
     res = {}
     clocks = ClockSampler(dev)
     clocks.start()
     for prec, delay in forms:
         acc_dev = torch.zeros(sweeps * M * N, dtype=torch.uint8, device=f"cuda:{dev}")
         chain = _make_chain(api, L, M, rp, args, dev, prec, delay, phi)
-        t, acc, ins, tim, wg = _measure_form(api, chain, args, M, N, d_dev, u_dev, acc_dev, flush, world)
-        res[prec] = dict(chain=chain, secs=allreduce_max(t, world), accepted=acc, instab=ins, timing=tim,
-                         warm_greens=wg, warm_acc=acc_dev[: args.warmup * M * N].cpu().numpy())
+        steps = args.steps if prec == head else k_cmp
+        r = _measure_form(api, chain, args, M, N, d_dev, u_dev, acc_dev, flush, world, steps, save_after)
+        r.update(chain=chain, delay=delay, steps=steps, secs=allreduce_max(r["secs"], world))
+        res[prec] = r
     clk = clocks.stop()
-    head = "mixed" if "mixed" in res else "fp64"
     R = res[head]
     value = world * args.steps / R["secs"]
     chain = R["chain"]
@@ -586,54 +673,62 @@ def run_ours(args, world, rank, local):
     e2e_s = allreduce_max(time.perf_counter() - t0, world)
     e2e_value = world * e2e_steps / e2e_s
 
-    # ---- roofline of the dominant kernel of the headline form ----
+    # ---- rooflines of the headline form (one evented sweep) ----
+    peaks, peak_kind = measured_peaks()
+    fp64_peak = api.peak_fp64_tflops(dev)
     tim = R["timing"]
     kinds = tim["kinds"]
     tot_ms = sum(x["ms"] for x in kinds.values())
-    # the local updates are bound by their per-site dependency chain (decision,
-    # then the new factor columns), not by a pipe or by HBM: they are reported
-    # as such, and the roofline is taken on the largest throughput-bound kind
+    per_kind = kernel_rooflines(tim, n, N, M, R["ev_accepted"], R["ev_flags"], R["delay"], head, peaks, fp64_peak)
+    # the `roofline` key: the largest kind with a throughput bound (the
+    # delayed local updates are bound by their per-site dependency chain and
+    # are reported per site in `kernels`)
     dominant = max(kinds, key=lambda k: kinds[k]["ms"])
-    bounded = {k: v for k, v in kinds.items() if k not in ("local_updates", "misc")}
+    bounded = {k: v for k, v in kinds.items() if k not in ("local_updates", "misc") and v["launches"]}
     top = max(bounded, key=lambda k: bounded[k]["ms"])
-    fl, by = flops_model(top, tim, n, R["accepted"])
-    ms_top = kinds[top]["ms"]
-    launches_top = max(1, kinds[top]["launches"])
-    peaks, peak_kind = measured_peaks()
-    if top in ("ozaki_gemm",) or (top == "flush" and head == "mixed"):
-        bound, peak, unit, src = "tensor", peaks.get("bf16_tflops"), "TFLOP/s", f"bf16_tflops ({peak_kind})"
-    elif top in ("slice_cols", "slice_rows"):
-        bound, peak, unit, src = "hbm", peaks.get("hbm_gbs"), "GB/s", f"hbm_gbs ({peak_kind})"
-        fl = by / 1e3   # GB/s below
-    else:
-        bound, peak, unit = "fp64", api.peak_fp64_tflops(dev), "TFLOP/s"
+    e = per_kind[top]
+    if top == "flush":
+        bound, achieved, peak, unit = "hbm", e["hbm_gbs"], peaks.get("hbm_gbs"), "GB/s"
+        src = f"hbm_gbs ({peak_kind})"
+        traffic = TRAFFIC.get("flush")
+    elif e["pipe"] == "tensor":
+        bound, achieved, peak, unit = "tensor", e["tflops"], peaks.get("bf16_tflops"), "TFLOP/s"
+        src = f"bf16_tflops ({peak_kind})"
+        traffic = TRAFFIC.get(top)
+    elif e["pipe"] == "fp64":
+        bound, achieved, peak, unit = "fp64", e["tflops"], fp64_peak, "TFLOP/s"
         src = "FP64 FMA peak measured live on this GPU (dqmc_peak_fp64)"
-    achieved = fl / launches_top / (ms_top / launches_top / 1000.0) / 1e12
-    hbm_gbs = by / (ms_top / 1000.0) / 1e9
-    # per kind: algorithmic rates of one sweep against the pipe its flops run
-    # on (split-BF16 kinds against the BF16 peak; kinds that mix FP64 panels
-    # with split-BF16 GEMMs get no pipe fraction) and its bytes against HBM
-    fp64_peak = api.peak_fp64_tflops(dev)
-    pipe_of = {"slice_cols": "fp64", "slice_rows": "fp64", "qrp": "fp64", "ozaki_gemm": "tensor",
-               "flush": "tensor" if head == "mixed" else "fp64", "local_updates": "latency",
-               "lu": "fp64" if head == "fp64" else "fp64+tensor", "trsm": "fp64" if head == "fp64" else "fp64+tensor",
-               "apply_q": "fp64" if head == "fp64" else "fp64+tensor", "misc": "hbm"}
-    breakdown = {}
-    for k, v in kinds.items():
-        if not v["launches"]:
-            continue
-        kfl, kby = flops_model(k, tim, n, R["accepted"] / max(1, args.steps))   # one evented sweep
-        secs_k = max(1e-12, v["ms"] / 1000.0)
-        e = {"ms": round(v["ms"], 3), "launches": v["launches"], "share": round(v["ms"] / max(1e-9, tot_ms), 4),
-             "pipe": pipe_of.get(k), "tflops": kfl / secs_k / 1e12, "gbs": kby / secs_k / 1e9}
-        if peaks.get("hbm_gbs"):
-            e["hbm_frac"] = e["gbs"] / peaks["hbm_gbs"]
-        if e["pipe"] == "fp64" and fp64_peak:
-            e["pipe_frac"] = e["tflops"] / fp64_peak
-        elif e["pipe"] == "tensor" and peaks.get("bf16_tflops"):
-            e["pipe_frac"] = e["tflops"] / peaks["bf16_tflops"]
-        breakdown[k] = e
-    # time-displaced Green's functions (the measurement step after the sweep)
+        traffic = TRAFFIC.get(top)
+    else:
+        bound, achieved, peak, unit = "fp64+tensor", e["tflops"], fp64_peak, "TFLOP/s (FP64-equivalent)"
+        src = "FP64 FMA peak measured live on this GPU (dqmc_peak_fp64)"
+        traffic = TRAFFIC.get(top)
+    roofline = {"bound": bound, "kernel": top, "achieved": achieved, "peak": peak, "unit": unit,
+                "frac": achieved / peak if peak else None, "traffic": traffic, "peak_source": src,
+                "share": e["share"], "launches_per_sweep": e["launches"],
+                "dominant_kind": {"kernel": dominant, "share": round(kinds[dominant]["ms"] / max(1e-9, tot_ms), 4),
+                                  "bound": "latency" if dominant == "local_updates" else bound}}
+
+    compare = None
+    if "fp64" in res and "mixed" in res:
+        f64, mix = res["fp64"], res["mixed"]
+        nc = args.warmup + k_cmp
+        fa, ma = f64["flags"][:nc], mix["flags"][:nc]
+        flips = int(np.sum(fa != ma))
+        gerr = {}
+        for s_idx, label in ((args.warmup - 1, "after_warmup"), (args.warmup + k_cmp - 1, f"after_{nc}_sweeps")):
+            if s_idx in f64["saved"] and s_idx in mix["saved"]:
+                gerr[label] = float(np.max(np.abs(mix["saved"][s_idx] - f64["saved"][s_idx])))
+        compare = {"fp64_sweeps_per_s": world * f64["steps"] / f64["secs"],
+                   "mixed_sweeps_per_s": world * mix["steps"] / mix["secs"],
+                   "mixed_over_fp64": (mix["steps"] / mix["secs"]) / (f64["steps"] / f64["secs"]),
+                   "fp64_delay": f64["delay"], "mixed_delay": mix["delay"], "fp64_timed_sweeps": f64["steps"],
+                   "sweeps_compared": nc, "accept_flips": flips,
+                   "accept_sequences_identical": flips == 0,
+                   "max_abs_G_mixed_minus_fp64": gerr,
+                   "mixed_max_instability": mix["instab"], "fp64_max_instability": f64["instab"]}
+
+    # time-displaced Green's functions (the measurement step after the sweep) and the force
     tdgf = force = None
     if not args.no_batch and args.config == "L16" and rank == 0:
         tdgf = measure_tdgf(args, dev)
@@ -646,17 +741,16 @@ def run_ours(args, world, rank, local):
         # warm-up: both start states of a sweep (down and up) captured as graphs
         bval, bwall, bclk, binfo, bdesc = measure_batch(args, world, rank, dev, 3, 2, "mixed")
         batched = dict(value=bval, unit="chain-sweeps/s", workload=bdesc, seconds=bwall, clocks=bclk, **binfo)
-        res_fp64_value = world * args.steps / res["fp64"]["secs"] if "fp64" in res else None
-        wl = desc.replace(" FP64", "")
+        res_fp64_value = world * res["fp64"]["steps"] / res["fp64"]["secs"] if "fp64" in res else None
         # the headline lattice batched: 8 L=16, beta=20 chains in flight, both forms
         # (warm-up: the two captured sweep graphs; one timed batch sweep each)
         b16 = {}
         for prec in ("mixed", "fp64"):
             v, w, c, info, _ = measure_batch(args, world, rank, dev, 2, 1, prec, Ls=[L] * 8, M=M,
-                                             desc=f"8 independent chains, {wl}")
+                                             desc=f"8 independent chains, {desc}")
             b16[prec] = dict(value=v, seconds=w, clocks=c, delays=info["delays"], acc_rate=info["acc_rate"])
         batched["headline_lattice"] = {
-            "workload": f"8 independent chains of {wl} in flight at once", "unit": "chain-sweeps/s",
+            "workload": f"8 independent chains of {desc} in flight at once", "unit": "chain-sweeps/s",
             "mixed": b16["mixed"], "fp64": b16["fp64"],
             "mixed_over_fp64_batched": b16["mixed"]["value"] / b16["fp64"]["value"],
             "mixed_batched_over_fp64_single_chain": b16["mixed"]["value"] / res_fp64_value
@@ -674,50 +768,33 @@ def run_ours(args, world, rank, local):
                    if one else "failed",
                    "sample": f"{args.cpu_calls} of {M} update calls (numpy/scipy oracle, OpenBLAS "
                              f"{threads} threads), {secs:.1f} s, extrapolated to one sweep"}
-        compare = None
-        if "fp64" in res and "mixed" in res:
-            f64, mix = res["fp64"], res["mixed"]
-            same = bool(np.array_equal(f64["warm_acc"], mix["warm_acc"]))
-            compare = {"fp64_sweeps_per_s": world * args.steps / f64["secs"],
-                       "mixed_sweeps_per_s": world * args.steps / mix["secs"],
-                       "mixed_over_fp64": f64["secs"] / mix["secs"],
-                       "fp64_delay": args.fp64_delay, "mixed_delay": args.delay,
-                       "warmup_accept_sequences_identical": same,
-                       "max_abs_G_mixed_minus_fp64_after_warmup": float(np.max(np.abs(mix["warm_greens"] - f64["warm_greens"]))) if same else None,
-                       "mixed_max_instability": mix["instab"], "fp64_max_instability": f64["instab"]}
+            if compare:
+                compare["fp64_gpu_over_cpu_oracle"] = compare["fp64_sweeps_per_s"] / val
+        # most important keys first: a reader of the line's head sees the
+        # headline, e2e, roofline, the mixed-form quality and the CPU baseline
         line = {
             "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": R["secs"] * 1000.0 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if head == "fp64" else "f64 + split-bf16 tensor GEMMs",
             "data": "synthetic (seeded uniform[-1,1] fields, uniform proposal/Metropolis streams)",
-            "config": {"workload": desc if head == "fp64" else
-                       desc.replace(" FP64", "") + ", mixed form (FP64 factorisations, split-BF16 GEMMs)", "L": L, "slices": M, "n": n, "safe_mult": 10, "chains_per_gpu": 1,
-                       "form": head, "delay": args.delay if head == "mixed" else args.fp64_delay,
-                       "parallelism": f"replicas x{world}",
+            "config": {"workload": desc, "form": head, "L": L, "slices": M, "n": n, "safe_mult": 10,
+                       "chains_per_gpu": 1, "delay": R["delay"], "parallelism": f"replicas x{world}",
                        "l2": "working set > L2 (stack 2x21x16.8 MB) and 256 MB L2 flush before each sweep"},
-            "mixed_vs_fp64": compare,
             "e2e": {"value": e2e_value, "unit": "sweeps/s", "h2d_bytes_per_step": int(M * 4 * N * 8),
                     "d2h_bytes_per_step": int(M * N), "steps": e2e_steps},
+            "roofline": roofline,
+            "mixed_vs_fp64": compare,
+            "cpu_baseline": cpu,
+            "clocks": clk,
             # launches of the timed region: K sweeps x the launches of one sweep
             "gpu_launches": int(tim["kernel_launches"]) * args.steps,
-            "roofline": {"bound": bound, "kernel": top, "achieved": achieved, "peak": peak, "unit": unit,
-                         "frac": achieved / peak if peak else None, "traffic": TRAFFIC.get(top),
-                         "peak_source": src, "share": round(kinds[top]["ms"] / max(1e-9, tot_ms), 4),
-                         "algorithmic_gbs": hbm_gbs, "hbm_peak_gbs": peaks.get("hbm_gbs"),
-                         "hbm_frac": hbm_gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None,
-                         "bf16_peak_tflops": peaks.get("bf16_tflops"),
-                         "dominant_kind": {"kernel": dominant,
-                                           "share": round(kinds[dominant]["ms"] / max(1e-9, tot_ms), 4),
-                                           "bound": "latency" if dominant == "local_updates" else bound}},
-            "kernel_breakdown": breakdown,
             "acc_rate": R["accepted"] / (args.steps * M * N),
             "max_instability": R["instab"],
-            "clocks": clk,
-            "cpu_baseline": cpu,
+            "kernels": per_kind,
+            "force": force,
             "batched": batched,
             "tdgf": tdgf,
-            "force": force,
         }
         print(json.dumps(line), flush=True)
     if batched is None:
@@ -742,6 +819,8 @@ def main():
                     help="both: FP64 and mixed forms on the same field and streams; value = mixed")
     ap.add_argument("--delay", type=int, default=16, help="mixed form: delayed-update depth k")
     ap.add_argument("--fp64-delay", type=int, default=1, help="FP64 form: delayed-update depth (1 = rank-4)")
+    ap.add_argument("--fp64-steps", type=int, default=5, help="both forms: timed sweeps of the FP64 form "
+                    "(at most --steps)")
     ap.add_argument("--chains", type=int, default=64, help="chains of the batched chains64 workload")
     ap.add_argument("--batch-delay", default="auto", help="batched chains: delayed-update depth, or 'auto' "
                     "(autotuned per L over 8, 16, 32)")

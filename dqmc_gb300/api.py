@@ -98,6 +98,7 @@ SIGNATURES = {
     "dqmc_force": ([_P, _D, _D], ctypes.c_int),
     "dqmc_measure_tdgfs": ([_P, _D, _D, _I32], ctypes.c_int),
     "dqmc_global_update": ([_P, _D, ctypes.c_double, ctypes.POINTER(_I32), _D], ctypes.c_int),
+    "dqmc_hmc_update": ([_P, _D, _I32, ctypes.c_double, ctypes.c_double, ctypes.POINTER(_I32), _D], ctypes.c_int),
     "dqmc_batch_create": ([ctypes.POINTER(CParams), _I32, ctypes.POINTER(_P)], ctypes.c_int),
     "dqmc_batch_destroy": ([_P], ctypes.c_int),
     "dqmc_batch_handle": ([_P, _I32, ctypes.POINTER(_P)], ctypes.c_int),
@@ -478,6 +479,16 @@ class DQMC:
         acc, pa = _I32(), ctypes.c_double()
         self._check(self.lib.dqmc_global_update(self.h, _dptr(sh), float(u), ctypes.byref(acc), ctypes.byref(pa)))
         return bool(acc.value), pa.value
+
+    def hmc_update(self, momenta, n_steps, eps, u):
+        """Hybrid Monte Carlo move on S_b - log|det M| with fixed-slot momenta
+        (3, N, M), n_steps leapfrog steps of size eps and Metropolis uniform u;
+        returns (accepted, dH).  Needs the state (M, -1) and keeps it."""
+        pi = np.asfortranarray(np.asarray(momenta, dtype=np.float64).reshape(3, self.N, self.M))
+        acc, dh = _I32(), ctypes.c_double()
+        self._check(self.lib.dqmc_hmc_update(self.h, _dptr(pi), int(n_steps), float(eps), float(u),
+                                             ctypes.byref(acc), ctypes.byref(dh)))
+        return bool(acc.value), dh.value
 
     def force(self):
         """(d log|det M|/d phi, d S_boson/d phi), each (3, N, M); needs the

@@ -300,7 +300,7 @@ int zgemm_general(dqmc_handle* h, int m, int nn, int k, char opA, char opB, cplx
     LAUNCH(kind >= 0 ? kind : DQMC_K_OZGEMM, ozaki_tensor_flops(m, nn, k, S), gemm_bytes(m, nn, k),
            launch_ozaki_zgemm(m, nn, k, opA, opB, alpha, A, lda, B, ldb, beta, C, ldc, rs, cs, S, bits,
                               h->oz_scratch, h->oz_bytes, h->oz_acc, h->oz_acc_bytes, h->st, active, splitk,
-                              &kernels));
+                              &kernels, h->err_d));
     h->launches += kernels - 1;   // slicing kernels and the split-K finaliser
     return DQMC_OK;
   }
@@ -1695,21 +1695,28 @@ int dqmc_calc_greens(dqmc_handle* h, int32_t slice, double* out, double* logdet)
   return DQMC_OK;
 }
 
+// Backup buffers of the global moves (stack, G, field, interaction table),
+// allocated on first use.
+static int ensure_global_backup(dqmc_handle* h) {
+  if (h->gb_u) return DQMC_OK;
+  const size_t stack_c = (size_t)h->ne * h->n * h->n, NM = (size_t)h->N * h->M;
+  CU(cudaMalloc(&h->gb_u, stack_c * sizeof(cplx)));
+  CU(cudaMalloc(&h->gb_t, stack_c * sizeof(cplx)));
+  CU(cudaMalloc(&h->gb_d, (size_t)h->ne * h->n * sizeof(double)));
+  CU(cudaMalloc(&h->gb_G, nn_bytes(h)));
+  CU(cudaMalloc(&h->gb_phi, 3 * NM * sizeof(double)));
+  CU(cudaMalloc(&h->gb_evtab, NM * evtab_entry_bytes()));
+  return DQMC_OK;
+}
+
 int dqmc_global_update(dqmc_handle* h, const double* shift, double u, int32_t* accepted, double* p_acc) {
   if (h) cudaSetDevice(h->device);
   if (!h || !shift) return DQMC_ERR_ARG;
   if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
   if (h->current_slice != h->M || h->direction != -1)
     return set_err(h, DQMC_ERR_STATE, "dqmc_global_update needs the state (slice M, direction -1)");
-  const size_t stack_c = (size_t)h->ne * h->n * h->n, NM = (size_t)h->N * h->M;
-  if (!h->gb_u) {
-    CU(cudaMalloc(&h->gb_u, stack_c * sizeof(cplx)));
-    CU(cudaMalloc(&h->gb_t, stack_c * sizeof(cplx)));
-    CU(cudaMalloc(&h->gb_d, (size_t)h->ne * h->n * sizeof(double)));
-    CU(cudaMalloc(&h->gb_G, nn_bytes(h)));
-    CU(cudaMalloc(&h->gb_phi, 3 * NM * sizeof(double)));
-    CU(cudaMalloc(&h->gb_evtab, NM * evtab_entry_bytes()));
-  }
+  const size_t NM = (size_t)h->N * h->M;
+  CHK(ensure_global_backup(h));
   double S_old = 0.0, ldsum_old = 0.0;
   CU(cudaMemcpyAsync(&S_old, h->action_d, sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CU(cudaMemcpyAsync(&ldsum_old, h->scal_d + 2, sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -1755,6 +1762,113 @@ int dqmc_global_update(dqmc_handle* h, const double* shift, double u, int32_t* a
   return DQMC_OK;
 }
 
+// d log|det M| / d phi into h->force_d from the per-slice G of one down pass
+// (slices M, M-1, ..., 1) starting at the state (M, -1); the state is left
+// at (1, -1).
+static int force_down_pass(dqmc_handle* h) {
+  const size_t cnt = (size_t)3 * h->N * h->M;
+  if (!h->force_d) CU(cudaMalloc(&h->force_d, cnt * sizeof(double)));
+  const double ld = h->p.lambda * h->p.delta_tau;
+  for (int c = 0; c < h->M; ++c) {
+    if (c > 0) CHK(propagate(h));
+    LAUNCH(DQMC_K_MISC, 0.0, 0.0, launch_force_slice(h->G, h->phi, h->force_d, h->N, h->current_slice - 1, ld, h->st));
+  }
+  return DQMC_OK;
+}
+
+// Hybrid Monte Carlo move on the effective action S_eff = S_b - log|det M|
+// (the log-weight of the reference's global update, src/global_updates.jl:18-58):
+// leapfrog with the adjoint force -dS_eff/dphi = dlog|det M|/dphi - dS_b/dphi,
+// then a Metropolis test on dH.  The field lives on the host between the
+// steps (3 N M doubles); every step uploads it, rebuilds the stack and takes
+// the force from one down pass.
+int dqmc_hmc_update(dqmc_handle* h, const double* momenta, int32_t n_steps, double eps, double u,
+                    int32_t* accepted, double* delta_H) {
+  if (h) cudaSetDevice(h->device);
+  if (!h || !momenta || n_steps < 1 || !(eps > 0.0) || !std::isfinite(eps)) return DQMC_ERR_ARG;
+  if (!h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
+  if (h->current_slice != h->M || h->direction != -1)
+    return set_err(h, DQMC_ERR_STATE, "dqmc_hmc_update needs the state (slice M, direction -1)");
+  const size_t NM = (size_t)h->N * h->M, cnt = 3 * NM;
+  CHK(ensure_global_backup(h));
+  std::vector<double> phi(cnt), pi(momenta, momenta + cnt), gl(cnt), gb(cnt);
+  double S_old = 0.0, ldsum_old = 0.0;
+  CU(cudaMemcpyAsync(phi.data(), h->phi, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaMemcpyAsync(&S_old, h->action_d, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaMemcpyAsync(&ldsum_old, h->scal_d + 2, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CHK(sync(h));
+  // H = |pi|^2 / 2 + S_b - log|det M|, with log|det M| = -log det G = sum log d2
+  double kin_old = 0.0;
+  for (double v : pi) kin_old += 0.5 * v * v;
+  const double H_old = kin_old + S_old - ldsum_old;
+  // back up (stack and G by pointer swap, field and table by copy)
+  clear_graphs(h);
+  std::swap(h->u_stack, h->gb_u);
+  std::swap(h->t_stack, h->gb_t);
+  std::swap(h->d_stack, h->gb_d);
+  std::swap(h->G, h->gb_G);
+  CU(cudaMemcpyAsync(h->gb_phi, h->phi, cnt * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  CU(cudaMemcpyAsync(h->gb_evtab, h->evtab, NM * evtab_entry_bytes(), cudaMemcpyDeviceToDevice, h->st));
+  // the force at the start: the backed-up stack's G is the current one, so
+  // the first down pass runs on a rebuilt copy of the same field
+  auto rebuild = [&]() -> int {
+    CU(cudaMemcpyAsync(h->phi, phi.data(), cnt * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    LAUNCH(DQMC_K_MISC, 0.0, 0.0,
+           launch_build_evtab(h->phi, h->evtab, h->N, h->M, h->p.lambda * h->p.delta_tau, h->st));
+    CHK(build_stack(h));
+    return propagate(h);
+  };
+  auto force = [&]() -> int {   // F = dlog|det M|/dphi - dS_b/dphi at the field `phi`
+    CHK(force_down_pass(h));
+    CU(cudaMemcpyAsync(gl.data(), h->force_d, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CHK(sync(h));
+    boson_gradient_host(h, phi, gb.data());
+    return DQMC_OK;
+  };
+  int rc = rebuild();
+  if (rc == DQMC_OK) rc = force();
+  for (int st = 0; rc == DQMC_OK && st < n_steps; ++st) {
+    for (size_t k = 0; k < cnt; ++k) pi[k] += 0.5 * eps * (gl[k] - gb[k]);
+    for (size_t k = 0; k < cnt; ++k) phi[k] += eps * pi[k];
+    rc = rebuild();
+    if (rc == DQMC_OK) rc = force();
+    if (rc == DQMC_OK)
+      for (size_t k = 0; k < cnt; ++k) pi[k] += 0.5 * eps * (gl[k] - gb[k]);
+  }
+  // the state (M, -1) of the final field, its action and log|det M|
+  if (rc == DQMC_OK) rc = rebuild();
+  double ldsum_new = 0.0;
+  if (rc == DQMC_OK) {
+    CU(cudaMemcpyAsync(&ldsum_new, h->scal_d + 2, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    rc = sync(h);
+  }
+  const double S_new = boson_action_host(h, phi);
+  double kin_new = 0.0;
+  for (double v : pi) kin_new += 0.5 * v * v;
+  const double dH = kin_new + S_new - ldsum_new - H_old;
+  const bool ok = rc == DQMC_OK && std::isfinite(dH);
+  const double p = ok ? std::exp(-dH) : 0.0;
+  const bool acc = ok && (p > 1.0 || u < p);
+  if (acc) {
+    CU(cudaMemcpyAsync(h->action_d, &S_new, sizeof(double), cudaMemcpyHostToDevice, h->st));
+  } else {
+    std::swap(h->u_stack, h->gb_u);
+    std::swap(h->t_stack, h->gb_t);
+    std::swap(h->d_stack, h->gb_d);
+    std::swap(h->G, h->gb_G);
+    CU(cudaMemcpyAsync(h->phi, h->gb_phi, cnt * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    CU(cudaMemcpyAsync(h->evtab, h->gb_evtab, NM * evtab_entry_bytes(), cudaMemcpyDeviceToDevice, h->st));
+    CU(cudaMemcpyAsync(h->scal_d + 2, &ldsum_old, sizeof(double), cudaMemcpyHostToDevice, h->st));
+    h->current_slice = h->M;
+    h->direction = -1;
+  }
+  CHK(sync(h));
+  if (rc != DQMC_OK) return rc;
+  if (accepted) *accepted = acc ? 1 : 0;
+  if (delta_H) *delta_H = dH;
+  return DQMC_OK;
+}
+
 int dqmc_force(dqmc_handle* h, double* grad_logdet, double* grad_boson) {
   if (h) cudaSetDevice(h->device);
   if (!h) return DQMC_ERR_ARG;
@@ -1762,13 +1876,7 @@ int dqmc_force(dqmc_handle* h, double* grad_logdet, double* grad_boson) {
   if (h->current_slice != h->M || h->direction != -1)
     return set_err(h, DQMC_ERR_STATE, "dqmc_force needs the state (slice M, direction -1)");
   const size_t cnt = (size_t)3 * h->N * h->M;
-  if (!h->force_d) CU(cudaMalloc(&h->force_d, cnt * sizeof(double)));
-  const double ld = h->p.lambda * h->p.delta_tau;
-  // down pass: slices M, M-1, ..., 1
-  for (int c = 0; c < h->M; ++c) {
-    if (c > 0) CHK(propagate(h));
-    LAUNCH(DQMC_K_MISC, 0.0, 0.0, launch_force_slice(h->G, h->phi, h->force_d, h->N, h->current_slice - 1, ld, h->st));
-  }
+  CHK(force_down_pass(h));
   // back to (M, -1): turnaround at 0 and the up pass
   while (!(h->current_slice == h->M && h->direction == -1)) CHK(propagate(h));
   if (grad_logdet) CU(cudaMemcpyAsync(grad_logdet, h->force_d, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->st));

@@ -24,8 +24,13 @@
 // The tensor-core products use warp-level mma.sync m16n8k16 (BF16 in, FP32
 // accumulate) fed from shared memory with ldmatrix; operands are staged with
 // cp.async double buffering.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
 #include <type_traits>
 #include "common.cuh"
 #include "kernels.h"
@@ -433,6 +438,315 @@ __global__ void k_oz_finalize(OzArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// tcgen05 engine: TMA-staged slices, tensor-core MMAs into TMEM accumulators
+// ---------------------------------------------------------------------------
+// One CTA computes a 128 x 32 complex tile of C.  Each MMA is
+// M = 128, N = 64, K = 16 (kind::f16, BF16 in, FP32 out): its B operand
+// stacks the 32 columns of B'_re over the 32 of B'_im, so one accumulator
+// holds [Re | Im] of the tile.  Every group t = p + q (2 <= t <= S + 1) has
+// its own accumulator of 64 TMEM columns, all S live at once (S <= 8: 512
+// columns), so one pass over K serves every slice pair and each K block of
+// every slice is staged once:
+//   * warp 0 (one lane) streams, per K block of 64, the S B-slices (double-
+//     buffered) and the S A-slices (a ring of 3) with cp.async.bulk.tensor
+//     (128-byte swizzle) onto mbarriers;
+//   * warp 1 allocates TMEM, and one lane issues tcgen05.mma for every pair
+//     (p, q) with p + q <= S + 1 into group p + q, releasing each A slot and
+//     B buffer with tcgen05.commit;
+//   * warps 2-5 (one per TMEM lane quarter) wait for the final commit, read
+//     the S exact FP32 group sums with tcgen05.ld and combine them exactly in
+//     64-bit integers (Horner in 2^bits), then scale and store as before.
+// Every wait is bounded; on a timeout the kernel sets an error bit, drains
+// what it issued (bounded) and frees its TMEM.
+constexpr int TC_BM = 128;                      // rows of C per CTA (TMEM lanes)
+constexpr int TC_BN = 32;                       // complex columns of C per CTA (MMA N = 64)
+constexpr int TC_BK = 64;                       // BF16 per K block: one 128-byte swizzle row
+constexpr int TC_MAXS = 8;                      // S groups x 64 TMEM columns <= 512
+constexpr int TC_ARING = 3;                     // A-slice stages
+constexpr int TC_THREADS = 192;                 // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr int TC_A_TILE = TC_BM * TC_BK * 2;    // 16 KB
+constexpr int TC_B_HALF = TC_BN * TC_BK * 2;    // 4 KB: 32 rows of B'_re or of B'_im
+constexpr int TC_B_TILE = 2 * TC_B_HALF;        // 8 KB
+// MMA instruction descriptor (kind::f16): D F32 (bits 4-5 = 1), A BF16 (bits
+// 7-9 = 1), B BF16 (bits 10-12 = 1), both K-major (bits 15, 16 = 0),
+// N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(2 * TC_BN) >> 3 << 17) |
+                              ((uint32_t)TC_BM >> 4 << 24);
+
+__host__ __device__ constexpr size_t tc_smem_bytes(int S) {
+  return 1024 + (size_t)2 * S * TC_B_TILE + (size_t)TC_ARING * TC_A_TILE + 256;
+}
+__host__ __device__ constexpr uint32_t tc_tmem_cols(int S) {
+  return S <= 2 ? 128u : (S <= 4 ? 256u : 512u);
+}
+
+// Shared-memory matrix descriptor of a K-major operand tile written by TMA
+// with the 128-byte swizzle: start address >> 4 (bits 0-13), leading byte
+// offset 16 >> 4 (bits 16-29; unused for this layout), stride byte offset
+// 1024 >> 4 between 8-row groups (bits 32-45), descriptor version 1 (bits
+// 46-47), layout SWIZZLE_128B = 2 (bits 61-63).  Tiles start on 1024-byte
+// boundaries; the K step of 16 BF16 (32 bytes) inside the swizzle row adds
+// 2 to the start field.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t smem_addr) {
+  return (uint64_t)((smem_addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Waits until the phase of parity `parity` of the barrier has completed; gives
+// up after ~2^31 SM cycles (about a second), sets the error bit and *abort.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, volatile int* abort) {
+  const long long t0 = clock64();
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_test(bar, parity)) return true;
+    if ((it & 255) == 255) {
+      if (*abort) return false;
+      if (clock64() - t0 > (1ll << 31)) {
+        atomicOr(err, DQMC_KERR_BARRIER_TIMEOUT);
+        *abort = 1;
+        return false;
+      }
+    }
+  }
+}
+// Bounded wait used on the abort path only (about 0.1 s, no error reporting).
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_test(bar, parity) && clock64() - t0 < (1ll << 28)) {}
+}
+// 3-D tiled TMA load (x = K element, y = row, z = slice) into shared memory,
+// completing `bytes` of the barrier's transaction count.
+__device__ __forceinline__ void tma_load3(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], "
+      "[%2];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(TC_IDESC), "r"(accumulate)
+      : "memory");
+}
+// arrives on the barrier once every tcgen05.mma issued so far by this thread has completed
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+// 32 TMEM lanes (this warp's quarter) x 16 consecutive 32-bit columns
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int c = 0; c < 16; ++c) v[c] = __uint_as_float(r[c]);
+}
+
+struct TcMaps {
+  CUtensorMap a, bre, bim;   // (Kp, rows, S) BF16 slices, box (64, 128 | 32, 1), 128-byte swizzle
+};
+
+template <bool INT>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_constant__ TcMaps maps, OzArgs a,
+                                                             int* err) {
+  if (a.active && *a.active == 0) return;   // flush with nothing pending (uniform over the grid)
+  extern __shared__ uint8_t tc_smem_raw[];
+  const uint32_t raw = smem_u32(tc_smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  uint8_t* basep = tc_smem_raw + (base - raw);
+  const int S = a.S;
+  const uint32_t sB = base;                                     // [2][S] B tiles of 8 KB
+  const uint32_t sA = base + 2u * S * TC_B_TILE;                // [TC_ARING] A tiles of 16 KB
+  const uint32_t sBar = sA + TC_ARING * TC_A_TILE;              // barriers
+  uint64_t* bars = reinterpret_cast<uint64_t*>(basep + (sBar - base));
+  // barrier slots: full_b 0-1, empty_b 2-3, full_a 4-6, empty_a 7-9, acc_full 10, drain 11
+  auto bar = [&](int k) { return sBar + 8u * k; };
+  volatile int* s_abort = reinterpret_cast<volatile int*>(bars + 12);
+  uint32_t* s_tmem = reinterpret_cast<uint32_t*>(bars + 13);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i0 = blockIdx.y * TC_BM, j0 = blockIdx.x * TC_BN;
+  const int nkb_all = (a.Kp + TC_BK - 1) / TC_BK;
+  const int kb0 = a.kchunk ? (int)blockIdx.z * a.kchunk : 0;
+  const int kb1 = a.kchunk ? min(nkb_all, kb0 + a.kchunk) : nkb_all;
+  const uint32_t ncols = tc_tmem_cols(S);
+
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 2; ++k) { mbar_init(bar(k), 1); mbar_init(bar(2 + k), 1); }
+    for (int k = 0; k < TC_ARING; ++k) { mbar_init(bar(4 + k), 1); mbar_init(bar(7 + k), 1); }
+    mbar_init(bar(10), 1);
+    mbar_init(bar(11), 1);
+    *s_abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(s_tmem)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *s_tmem;
+
+  int armed[2 + TC_ARING] = {0, 0, 0, 0, 0};   // producer: phases armed per full barrier (B 0-1, A 2-4)
+  if (warp == 0) {
+    // ---- TMA producer ----
+    if (lane == 0 && kb0 < kb1) {
+      int a_use = 0;
+      for (int kb = kb0; kb < kb1 && !*s_abort; ++kb) {
+        const int bu = kb - kb0, bb = bu & 1;
+        if (!mbar_wait(bar(2 + bb), ((bu >> 1) & 1) ^ 1, err, s_abort)) break;
+        armed[bb] = bu + 1;
+        mbar_expect_tx(bar(bb), (uint32_t)(S * TC_B_TILE));
+        for (int q = 0; q < S; ++q) {
+          const uint32_t dst = sB + (uint32_t)(bb * S + q) * TC_B_TILE;
+          tma_load3(dst, &maps.bre, bar(bb), kb * TC_BK, j0, q);
+          tma_load3(dst + TC_B_HALF, &maps.bim, bar(bb), kb * TC_BK, j0, q);
+        }
+        for (int p = 0; p < S; ++p, ++a_use) {
+          const int slot = a_use % TC_ARING;
+          if (!mbar_wait(bar(7 + slot), ((a_use / TC_ARING) & 1) ^ 1, err, s_abort)) break;
+          armed[2 + slot] = a_use / TC_ARING + 1;
+          mbar_expect_tx(bar(4 + slot), (uint32_t)TC_A_TILE);
+          tma_load3(sA + (uint32_t)slot * TC_A_TILE, &maps.a, bar(4 + slot), kb * TC_BK, i0, p);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      int a_use = 0;
+      for (int kb = kb0; kb < kb1 && !*s_abort; ++kb) {
+        const int bu = kb - kb0, bb = bu & 1;
+        if (!mbar_wait(bar(bb), (bu >> 1) & 1, err, s_abort)) break;
+        tc_fence_after();
+        bool ok = true;
+        for (int p = 0; p < S; ++p, ++a_use) {
+          const int slot = a_use % TC_ARING;
+          if (!mbar_wait(bar(4 + slot), (a_use / TC_ARING) & 1, err, s_abort)) { ok = false; break; }
+          tc_fence_after();
+          const uint64_t ad = tc_desc(sA + (uint32_t)slot * TC_A_TILE);
+          for (int q = 0; q + p < S; ++q) {
+            // pair (p + 1, q + 1) belongs to group t = p + q + 2: accumulator columns (p + q) * 64
+            const uint64_t bd = tc_desc(sB + (uint32_t)(bb * S + q) * TC_B_TILE);
+            const uint32_t d = tmem + (uint32_t)(p + q) * (2 * TC_BN);
+#pragma unroll
+            for (int kk = 0; kk < TC_BK / 16; ++kk)
+              tc_mma(d, ad + 2u * kk, bd + 2u * kk, (kb == kb0 && p == 0 && kk == 0) ? 0u : 1u);
+          }
+          tc_commit(bar(7 + slot));   // A slot free once these MMAs have read it
+        }
+        tc_commit(bar(2 + bb));       // B buffer free
+        if (!ok) break;
+      }
+      tc_commit(bar(10));             // all accumulators final (or, on abort, all issued MMAs done)
+    }
+  } else {
+    // ---- epilogue: warps 2-5, TMEM lane quarter (warp % 4) ----
+    const int quarter = warp & 3;
+    const bool waited = mbar_wait(bar(10), 0, err, s_abort);
+    // tcgen05.ld is warp-collective: the decision must be uniform over the warp
+    const bool have = __all_sync(0xffffffffu, waited && kb0 < kb1 && !*s_abort);
+    tc_fence_after();
+    const int row = i0 + 32 * quarter + lane;
+    const uint32_t tq = tmem + ((uint32_t)(32 * quarter) << 16);
+    const double wint = INT ? ldexp(1.0, -a.bits * (S + 1)) : 1.0;
+    const bool plain = oz_plain(a);
+    if (have) {
+#pragma unroll 1
+      for (int h = 0; h < 2; ++h) {
+        typedef typename std::conditional<INT, long long, double>::type acc_t;
+        acc_t ar[16], ai[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) { ar[c] = 0; ai[c] = 0; }
+#pragma unroll 1
+        for (int g = 0; g < S; ++g) {
+          float vr[16], vi[16];
+          tc_ld16(tq + (uint32_t)(g * 2 * TC_BN + 16 * h), vr);
+          tc_ld16(tq + (uint32_t)(g * 2 * TC_BN + TC_BN + 16 * h), vi);
+          if constexpr (INT) {
+            const long long step = 1ll << a.bits;
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+              ar[c] = ar[c] * step + (long long)__float2int_rn(vr[c]);
+              ai[c] = ai[c] * step + (long long)__float2int_rn(vi[c]);
+            }
+          } else {
+            const double wgt = ldexp(1.0, -a.bits * (g + 2));
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+              ar[c] = fma(wgt, (double)vr[c], ar[c]);
+              ai[c] = fma(wgt, (double)vi[c], ai[c]);
+            }
+          }
+        }
+        if (row < a.m) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const int col = j0 + 16 * h + c;
+            if (col < a.n) {
+              if constexpr (INT) {
+                if (a.acc) {
+                  unsigned long long* qa = a.acc + 2 * ((size_t)col * a.m + row);
+                  atomicAdd(qa, (unsigned long long)ar[c]);
+                  atomicAdd(qa + 1, (unsigned long long)ai[c]);
+                } else {
+                  oz_store(a, row, col, __ll2double_rn(ar[c]), __ll2double_rn(ai[c]), wint, plain);
+                }
+              } else {
+                oz_store(a, row, col, ar[c], ai[c], wint, plain);
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  // ---- teardown: on an abort, let issued copies and MMAs finish (bounded) ----
+  __syncthreads();
+  if (*s_abort) {
+    if (threadIdx.x == 32) {
+      mbar_drain(bar(10), 0);   // the MMA thread's final commit: every MMA it issued has completed
+    } else if (threadIdx.x == 0) {
+      for (int k = 0; k < 2; ++k)
+        if (armed[k]) mbar_drain(bar(k), (armed[k] - 1) & 1);
+      for (int k = 0; k < TC_ARING; ++k)
+        if (armed[2 + k]) mbar_drain(bar(4 + k), (armed[2 + k] - 1) & 1);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+  }
+}
+
 }  // namespace
 
 // Slice count S and width `bits` for a product with inner dimension K and a
@@ -461,11 +775,50 @@ size_t ozaki_scratch_bytes(int m, int n, int K, int S) {
   return (size_t)S * Kp * ((size_t)m + 2 * (size_t)n) * sizeof(__nv_bfloat16) + ((size_t)m + n) * sizeof(double) + 256;
 }
 
+// cuTensorMapEncodeTiled from the driver, looked up once (no link against libcuda).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// BF16 slices (Kp, rows, S), K contiguous: box of 64 K elements (128 bytes,
+// the swizzle span) x box_rows rows x 1 slice, 128-byte swizzle.
+static bool encode_slices(CUtensorMap* map, const __nv_bfloat16* base, size_t Kp, int rows, int S, int box_rows) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)S};
+  cuuint64_t strides[2] = {(cuuint64_t)(Kp * 2), (cuuint64_t)(Kp * 2 * rows)};
+  cuuint32_t box[3] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16*>(base), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Engine of the products: the mma.sync kernel, or the tcgen05 kernel with
+// DQMC_OZ_ENGINE=tc (S <= 8).
+static bool use_tc_engine(int S) {
+  static const int forced_tc = [] {
+    const char* e = std::getenv("DQMC_OZ_ENGINE");
+    return e && std::strcmp(e, "tc") == 0 ? 1 : 0;
+  }();
+  return forced_tc && S <= TC_MAXS;
+}
+
 cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
                                const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
                                const double* colscale, int S, int bits, void* scratch, size_t scratch_bytes,
                                unsigned long long* acc, size_t acc_bytes, cudaStream_t st, const int* active,
-                               int splitk, int* kernels) {
+                               int splitk, int* kernels, int* err) {
   if (S < 1 || S > 12 || bits < 1 || bits > 8) return cudaErrorInvalidValue;
   const int Kpad = (k + 15) / 16 * 16;
   const size_t Kp = 2 * (size_t)Kpad;
@@ -488,8 +841,10 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
   a.int_combine = 24 + bits * (S - 1) <= 61 ? 1 : 0;
   a.kchunk = 0;
   a.acc = nullptr;
-  dim3 grid((nn + OZ_BN - 1) / OZ_BN, (m + OZ_BM - 1) / OZ_BM);
-  const int ksteps = (int)(Kp / OZ_BK);
+  const bool tc = use_tc_engine(S) && err;
+  const int bm = tc ? TC_BM : OZ_BM, bn = tc ? TC_BN : OZ_BN, bk = tc ? TC_BK : OZ_BK;
+  dim3 grid((nn + bn - 1) / bn, (m + bm - 1) / bm);
+  const int ksteps = (int)((Kp + bk - 1) / bk);
   if (splitk > 1 && a.int_combine && !active && ksteps > 1 && acc &&
       (size_t)m * nn * 2 * sizeof(unsigned long long) <= acc_bytes) {
     // split K over blockIdx.z: exact 64-bit integer partial sums in acc, which
@@ -500,8 +855,28 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
     a.acc = acc;
   }
   if (kernels) *kernels = a.acc ? 4 : 3;
-  if (a.int_combine) k_oz_gemm<true><<<grid, OZ_THREADS, 0, st>>>(a);
-  else k_oz_gemm<false><<<grid, OZ_THREADS, 0, st>>>(a);
+  if (tc) {
+    TcMaps maps;
+    if (!encode_slices(&maps.a, As, Kp, m, S, TC_BM) || !encode_slices(&maps.bre, Bre, Kp, nn, S, TC_BN) ||
+        !encode_slices(&maps.bim, Bim, Kp, nn, S, TC_BN))
+      return cudaErrorInvalidValue;
+    static SmemLimit limit_int, limit_fp;
+    const size_t smem = tc_smem_bytes(S);
+    if (a.int_combine) {
+      if (cudaError_t e = limit_int.raise((const void*)k_oz_gemm_tc<true>, (int)tc_smem_bytes(TC_MAXS));
+          e != cudaSuccess)
+        return e;
+      k_oz_gemm_tc<true><<<grid, TC_THREADS, smem, st>>>(maps, a, err);
+    } else {
+      if (cudaError_t e = limit_fp.raise((const void*)k_oz_gemm_tc<false>, (int)tc_smem_bytes(TC_MAXS));
+          e != cudaSuccess)
+        return e;
+      k_oz_gemm_tc<false><<<grid, TC_THREADS, smem, st>>>(maps, a, err);
+    }
+  } else {
+    if (a.int_combine) k_oz_gemm<true><<<grid, OZ_THREADS, 0, st>>>(a);
+    else k_oz_gemm<false><<<grid, OZ_THREADS, 0, st>>>(a);
+  }
   if (a.acc) {
     const size_t total = (size_t)m * nn;
     const int blocks = (int)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);

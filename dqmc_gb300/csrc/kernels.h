@@ -192,7 +192,8 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
                                const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
                                const double* colscale, int S, int bits, void* scratch, size_t scratch_bytes,
                                unsigned long long* acc, size_t acc_bytes, cudaStream_t st,
-                               const int* active = nullptr, int splitk = 1, int* kernels = nullptr);
+                               const int* active = nullptr, int splitk = 1, int* kernels = nullptr,
+                               int* err = nullptr);
 
 // ---- adjoint force (k_force.cu) ----
 // grad[:, :, slice0] = d log|det M| / d phi[:, :, slice0] from G of that slice

@@ -258,6 +258,17 @@ DQMC_API int dqmc_measure_equal_time(dqmc_handle* h, const double* greens, doubl
  * (M, -1).  accepted / p_acc may be NULL. */
 DQMC_API int dqmc_global_update(dqmc_handle* h, const double* shift, double u, int32_t* accepted, double* p_acc);
 
+/* Hybrid Monte Carlo move (no counterpart in the reference, which has only the
+ * field-shift global update of src/global_updates.jl:18-58; the acceptance
+ * rule, the restore on rejection and the required state (M, -1) are that
+ * update's).  With momenta pi[3*N*M] (fixed slot, standard normal, layout of
+ * phi) and H = |pi|^2/2 + S_boson - log|det M|, n_steps leapfrog steps of
+ * size eps with the force dlog|det M|/dphi - dS_boson/dphi (dqmc_force),
+ * then accept with p = exp(-dH) if p > 1 or u < p.  A rejection restores
+ * field, stack, G and action.  accepted / delta_H may be NULL. */
+DQMC_API int dqmc_hmc_update(dqmc_handle* h, const double* momenta, int32_t n_steps, double eps, double u,
+                             int32_t* accepted, double* delta_H);
+
 /* ---- adjoint force ----------------------------------------------------------- */
 /* Gradients of the log-weight parts with respect to every field component
  * (double[3*N*M], layout of phi):

@@ -1115,6 +1115,42 @@ def log_weight_parts(mc: "DQMCRef"):
     return -ld, boson_action(mc.p, mc.phi)
 
 
+def hmc_update(mc: "DQMCRef", momenta, n_steps, eps, u):
+    """Hybrid Monte Carlo move on S_eff = S_boson - log|det M| (the
+    log-weight whose ratio src/global_updates.jl:18-58 accepts on):
+    H = |pi|^2/2 + S_eff, n_steps leapfrog steps of size eps with the force
+    -dS_eff/dphi = force_logdetM - force_boson, then accept if p > 1 or
+    u < p with p = exp(-dH); a rejection restores the field.  The state is
+    rebuilt with init() afterwards.  Returns (accepted, dH)."""
+    p = mc.p
+    phi0 = mc.phi.copy()
+    pi = np.array(momenta, dtype=np.float64).reshape(phi0.shape)
+
+    def H(phi, pi):
+        mc.phi = phi
+        ldm, sb = log_weight_parts(mc)
+        return 0.5 * float(np.sum(pi * pi)) + sb - ldm
+
+    def force(phi):
+        mc.phi = phi
+        return force_logdetM(mc) - force_boson(p, phi)
+
+    H0 = H(phi0.copy(), pi)
+    phi = phi0.copy()
+    F = force(phi.copy())
+    for _ in range(n_steps):
+        pi = pi + 0.5 * eps * F
+        phi = phi + eps * pi
+        F = force(phi.copy())
+        pi = pi + 0.5 * eps * F
+    dH = H(phi.copy(), pi) - H0
+    pacc = math.exp(-dH)
+    acc = pacc > 1.0 or u < pacc
+    mc.phi = phi if acc else phi0
+    mc.init()
+    return acc, dH
+
+
 # ---------------------------------------------------------------------------
 # boson measurements  (src/boson_measurements.jl:6-56)
 # ---------------------------------------------------------------------------

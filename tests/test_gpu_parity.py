@@ -598,3 +598,64 @@ def test_observables_agree_within_binned_errors(lib):
             assert np.allclose(a, b, rtol=1e-9, atol=1e-12)
     finally:
         gpu.close()
+
+
+# ---------------------------------------------------------------------------
+# hybrid Monte Carlo move (leapfrog with the adjoint force, Metropolis on dH)
+# ---------------------------------------------------------------------------
+P_HMC = R.Params(L=4, slices=20, delta_tau=0.1, safe_mult=10, lambda_=1.0, r=1.0, c=1.0, u=1.0, mu1=-0.5,
+                 mu2=-0.5, box=0.2)
+
+
+@pytest.mark.parametrize("u", [0.0, 1.0 - 1e-15])
+def test_hmc_update_matches_oracle(lib, u):
+    """One HMC move (3 leapfrog steps, eps = 0.01) from the same field and
+    momenta: dH and the acceptance probability exp(-dH) agree with the
+    oracle's restatement within 1e-9, the decision is the same, and the state
+    after the move (field, G, action) is the oracle's (accepted trajectory or
+    restored field)."""
+    p = P_HMC
+    # a field near equilibrium (|phi| <= 0.2): dH > 0 here, so u = 0 accepts
+    # and u = 1 - 1e-15 rejects (restore path)
+    phi = 0.2 * R.synthetic_field(p.N, p.slices, 95)
+    pi = np.random.default_rng(96).standard_normal((3, p.N, p.slices))
+    ref = R.DQMCRef(p, phi)
+    acc_r, dh_r = R.hmc_update(ref, pi, 3, 0.01, u)
+    assert dh_r > 0 and acc_r == (u == 0.0)
+    gpu = lib.DQMC(api_params(p), phi)
+    try:
+        gpu.init()
+        acc_g, dh_g = gpu.hmc_update(pi, 3, 0.01, u)
+        assert abs(dh_g - dh_r) < 1e-9, (dh_g, dh_r)
+        assert abs(np.exp(-dh_g) - np.exp(-dh_r)) < 1e-9
+        assert acc_g == acc_r
+        assert gpu.state == (p.slices, -1)
+        assert np.allclose(gpu.get_field(), ref.phi, rtol=0, atol=1e-12)
+        assert relerr(gpu.greens, ref.greens) < TOL
+        assert abs(gpu.boson_action - R.boson_action(p, ref.phi)) < 1e-10 * abs(gpu.boson_action)
+        # the chain continues from the state the move left
+        delta, uu = R.synthetic_streams(p.N, 3, p.box, 97)
+        ref.sweep(3, delta, uu)
+        gpu.sweep(3, delta, uu)
+        assert relerr(gpu.greens, ref.greens) < TOL
+    finally:
+        gpu.close()
+
+
+def test_hmc_energy_error_scales_as_eps_squared(lib):
+    """Leapfrog over a fixed trajectory length tau = 0.1: halving the step
+    size divides |dH| by about 4 (second-order integrator)."""
+    p = P_HMC
+    phi = R.synthetic_field(p.N, p.slices, 98)
+    pi = np.random.default_rng(99).standard_normal((3, p.N, p.slices))
+    gpu = lib.DQMC(api_params(p), phi)
+    try:
+        dh = []
+        for eps, steps in ((0.02, 5), (0.01, 10), (0.005, 20)):
+            gpu.init(phi)
+            _, d = gpu.hmc_update(pi, steps, eps, 1.0 - 1e-15)
+            dh.append(abs(d))
+        r1, r2 = dh[0] / dh[1], dh[1] / dh[2]
+        assert 3.0 < r1 < 5.3 and 3.0 < r2 < 5.3, (dh, r1, r2)
+    finally:
+        gpu.close()
