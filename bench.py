@@ -802,6 +802,24 @@ def run_ours(args, world, rank, local):
             r["chain"].close()
 
 
+def run_profile_workload(args):
+    """The small workload of the ncu captures: init (stack build, first G) and
+    `profile_calls` update calls of one chain of the --config lattice in one
+    form, through the same library path as the timed sweeps."""
+    from dqmc_gb300 import api
+    from oracle.dqmc_ref import synthetic_field, synthetic_streams
+    L, M, _ = CONFIGS[args.config]
+    rp = model_params(L, M)
+    prec = "fp64" if args.precision == "fp64" else "mixed"
+    delay = args.fp64_delay if prec == "fp64" else args.delay
+    chain = _make_chain(api, L, M, rp, args, 0, prec, delay, synthetic_field(rp.N, M, 1000))
+    delta, unif = synthetic_streams(rp.N, args.profile_calls, rp.box, 1001)
+    res = chain.sweep(args.profile_calls, delta, unif)
+    print(json.dumps({"profile_workload": f"L={L} M={M} {prec} delay={delay}", "calls": args.profile_calls,
+                      "acc_rate": res["acc_rate"]}), flush=True)
+    chain.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -825,9 +843,14 @@ def main():
     ap.add_argument("--batch-delay", default="auto", help="batched chains: delayed-update depth, or 'auto' "
                     "(autotuned per L over 8, 16, 32)")
     ap.add_argument("--no-batch", action="store_true", help="default run: skip the batched-chains measurement")
+    ap.add_argument("--profile-calls", type=int, default=0, help="profiling workload: init and this many update "
+                    "calls of the chosen form (--precision fp64 or mixed) on the --config lattice, no timing, "
+                    "no JSON line")
     args = ap.parse_args()
     world, rank, local = dist_setup()
-    if args.impl == "reference":
+    if args.profile_calls > 0:
+        run_profile_workload(args)
+    elif args.impl == "reference":
         run_reference(args, world, rank)
     elif args.config == "chains64":
         run_batch(args, world, rank, local)
