@@ -310,6 +310,9 @@ class _Reader:
             return np.frombuffer(raw, dtype=code, count=count)
         if kind == "ref":
             return np.frombuffer(raw, dtype="<u8", count=count)
+        if kind == "string":   # fixed-length strings
+            n = dtype[1]
+            return [raw[k * n:(k + 1) * n].split(b"\0")[0].decode("utf-8") for k in range(count)]
         if kind == "compound":
             names = [m[0] for m in dtype[2]]
             if names in (["re", "im"], ["re_", "im_"]):
@@ -343,6 +346,27 @@ class _Reader:
             return vals[0]
         # HDF5 stores row-major with Julia dims reversed -> column-major view
         return np.asarray(vals).reshape(dims[::-1], order="F") if len(dims) > 1 else np.asarray(vals)
+
+
+def load_tree(path):
+    """Every dataset of an HDF5/JLD file as {"group/.../name": value}, groups
+    walked recursively (JLD's `_types` and `_refs` included)."""
+    r = _Reader(path)
+    out = {}
+
+    def is_group(addr):
+        return any(mtype in (0x02, 0x06, 0x11) for mtype, _, _ in r.messages(addr))
+
+    def walk(addr, prefix):
+        for name, a in r.links(addr).items():
+            full = f"{prefix}{name}"
+            if is_group(a):
+                walk(a, full + "/")
+            else:
+                out[full] = r.read(a)
+
+    walk(r.root, "")
+    return out
 
 
 def load_jld(path):

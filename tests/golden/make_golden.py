@@ -61,6 +61,34 @@ TIME_NEIGHBORS_M10 = np.array([[2, 3, 4, 5, 6, 7, 8, 9, 10, 1],                 
                                [10, 1, 2, 3, 4, 5, 6, 7, 8, 9]])
 
 
+def jld_layout(path):
+    """Encodings of the reference's JLD file that an output writer must match:
+    the 512-byte user block, the superblock's version and size fields, the
+    datatype messages of a Float64 array (`randconf`), an Int64 scalar
+    (`_creator/WORD_SIZE`) and a UInt32 scalar (`_creator/JULIA_MAJOR`), and the
+    member names of `_creator`."""
+    from jld_reader import _Reader
+    r = _Reader(path)
+    root = r.links(r.root)
+    creator = r.links(root["_creator"])
+
+    def dtype_msg(addr):
+        for mtype, _, data in r.messages(addr):
+            if mtype == 0x03:
+                return np.frombuffer(bytes(data), dtype=np.uint8)
+        raise KeyError("no datatype message")
+
+    d = r.d
+    return {
+        "jld_userblock": np.frombuffer(d[:512], dtype=np.uint8),
+        "jld_superblock_head": np.frombuffer(d[r.base:r.base + 24], dtype=np.uint8),
+        "jld_dt_float64_array": dtype_msg(root["randconf"]),
+        "jld_dt_int64_scalar": dtype_msg(creator["WORD_SIZE"]),
+        "jld_dt_uint32_scalar": dtype_msg(creator["JULIA_MAJOR"]),
+        "jld_creator_names": np.array(sorted(creator)),
+    }
+
+
 def main(ref_root):
     o3 = load_jld(os.path.join(ref_root, "test", "data", "O3.jld"))
     la = load_jld(os.path.join(ref_root, "test", "data", "linalg.jld"))
@@ -80,6 +108,7 @@ def main(ref_root):
     out["lit_corners_B"] = CORNERS_B
     out["lit_neighbors_L4"] = NEIGHBORS_L4
     out["lit_time_neighbors_M10"] = TIME_NEIGHBORS_M10
+    out.update(jld_layout(os.path.join(ref_root, "test", "data", "O3.jld")))
     path = os.path.join(HERE, "o3_reference_golden.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, os.path.getsize(path), "bytes")
