@@ -498,6 +498,25 @@ class DQMC:
         self._check(self.lib.dqmc_force(self.h, _dptr(gl), _dptr(gb)))
         return gl, gb
 
+    def log_weight(self):
+        """log|det M| + S_b of the current field (state (M, -1)), with
+        log|det M| = -log|det G| of the fresh G at slice M."""
+        return -self.log_det + self.boson_action
+
+    def rrule_log_weight(self, phi):
+        """Reverse rule of phi -> log|det M(phi)| + S_b(phi), the counterpart
+        of a ChainRulesCore rrule: sets the field and rebuilds the stack, and
+        returns (y, pullback) with pullback(dy) = dy * (dlog|det M|/dphi +
+        dS_b/dphi) from the adjoint force (dqmc_force).  The chain is left in
+        the state (M, -1) of phi."""
+        self.init(phi)
+        y = self.log_weight()
+        gl, gb = self.force()
+
+        def pullback(dy):
+            return float(dy) * (gl + gb)
+        return y, pullback
+
     def langevin_step(self, eps, rng):
         """One Langevin move on the effective action S_b - log|det M|:
         phi <- phi - eps (dS_b - dlog|det M|) + sqrt(2 eps) eta, then the stack

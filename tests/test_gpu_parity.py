@@ -659,3 +659,22 @@ def test_hmc_energy_error_scales_as_eps_squared(lib):
         assert 3.0 < r1 < 5.3 and 3.0 < r2 < 5.3, (dh, r1, r2)
     finally:
         gpu.close()
+
+
+def test_rrule_log_weight(lib):
+    """The reverse rule of phi -> log|det M| + S_b: value against the oracle's
+    log_weight_parts, pullback against the oracle's dense gradient (scaled by
+    the cotangent)."""
+    p = P_HMC
+    phi = R.synthetic_field(p.N, p.slices, 61)
+    gpu = lib.DQMC(api_params(p), phi)
+    try:
+        y, pullback = gpu.rrule_log_weight(phi)
+        ref = R.DQMCRef(p, phi)
+        ldm, sb = R.log_weight_parts(ref)
+        assert abs(y - (ldm + sb)) < 1e-10 * abs(ldm + sb)
+        g = pullback(2.5)
+        want = 2.5 * (R.force_logdetM(ref) + R.force_boson(p, phi))
+        assert np.max(np.abs(g - want)) < 1e-10 * max(1.0, np.max(np.abs(want)))
+    finally:
+        gpu.close()
