@@ -21,9 +21,9 @@
 // The only error is the truncation of the slice expansion (~2^{-B_BITS S}
 // relative to sigma_i tau_j K).
 //
-// The tensor-core products use warp-level mma.sync m16n8k16 (BF16 in, FP32
-// accumulate) fed from shared memory with ldmatrix; operands are staged with
-// cp.async double buffering.
+// The tensor-core products run on tcgen05.mma (kind::f16, BF16 in, FP32
+// accumulators in tensor memory), with every operand tile staged by TMA
+// (cp.async.bulk.tensor) onto mbarriers; see the engine section below.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -36,11 +36,6 @@
 #include "kernels.h"
 
 namespace {
-
-constexpr int OZ_BM = 64, OZ_BN = 64, OZ_BK = 32;
-constexpr int OZ_THREADS = 256;
-constexpr int OZ_LDS = OZ_BK + 8;   // padded shared-memory row (bf16 elements): 80 B, conflict-free ldmatrix
-constexpr int OZ_STAGES = 3;        // cp.async pipeline depth (46 KB of static shared memory)
 
 // ---------------------------------------------------------------------------
 // split: slices of op(X) scaled per row ("row" side = A) or per column (B side)
@@ -172,33 +167,67 @@ __global__ void k_oz_split_cols(const cplx* __restrict__ X, int ld, char op, int
   }
 }
 
-// ---------------------------------------------------------------------------
-// products
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
-__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::); }
-
-__device__ __forceinline__ void ldmatrix_x4(unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3, const void* p) {
-  unsigned s = (unsigned)__cvta_generic_to_shared(p);
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-               : "r"(s));
-}
-__device__ __forceinline__ void ldmatrix_x2(unsigned& r0, unsigned& r1, const void* p) {
-  unsigned s = (unsigned)__cvta_generic_to_shared(p);
-  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n" : "=r"(r0), "=r"(r1) : "r"(s));
-}
-__device__ __forceinline__ void mma_bf16(float* d, const unsigned* a, const unsigned* b) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+// Both sides in one launch when each operand vector is contiguous across
+// vectors (op(A) = A 'N': element k of row i at A[k lda + i]; op(B) = B^T
+// 'T': element k of column j at B[k ldb + j]) and Kpad <= 64, the shape of
+// the delayed-update flush: 32 vectors x Kpad elements are loaded with
+// coalesced reads into shared memory, then one warp per vector finds its
+// scale and cuts its digits (the same digits as k_oz_split_rows/cols).
+// blockIdx.y = 0: rows of A; 1: columns of B.
+constexpr int OZ_TILED_KMAX = 64;
+__global__ void __launch_bounds__(256) k_oz_split_tiled(const cplx* __restrict__ A, int lda, int m,
+                                                        const cplx* __restrict__ B, int ldb, int nn, int K, int Kpad,
+                                                        int S, int bits, __nv_bfloat16* __restrict__ As,
+                                                        __nv_bfloat16* __restrict__ Bre, __nv_bfloat16* __restrict__ Bim,
+                                                        double* __restrict__ sA, double* __restrict__ sB,
+                                                        const int* __restrict__ active) {
+  __shared__ cplx tile[OZ_TILED_KMAX][33];
+  const int side = blockIdx.y;
+  const cplx* X = side ? B : A;
+  const int ld = side ? ldb : lda, cnt = side ? nn : m;
+  const int v0 = blockIdx.x * 32;
+  if (v0 >= cnt) return;
+  if (active) {   // only the first 4p inner indices are live (delayed-update flush)
+    const int kk = 4 * *active;
+    if (kk == 0) return;
+    if (kk < K) K = kk;
+  }
+  for (int idx = threadIdx.x; idx < Kpad * 32; idx += blockDim.x) {
+    const int k = idx >> 5, v = idx & 31;
+    tile[k][v] = (k < K && v0 + v < cnt) ? X[(size_t)k * ld + v0 + v] : cmake(0.0, 0.0);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const size_t Kp = 2 * (size_t)Kpad;
+  for (int v = wid; v < 32; v += blockDim.x >> 5) {
+    const int vec = v0 + v;
+    if (vec >= cnt) break;
+    int me = 0;
+    for (int k = lane; k < K; k += 32) me = max(me, max(expo_field(tile[k][v].x), expo_field(tile[k][v].y)));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) me = max(me, __shfl_xor_sync(0xffffffffu, me, o));
+    const int E = me > 0 ? me - 1022 : 0;   // 2^E > max |.| (frexp exponent)
+    if (lane == 0) (side ? sB : sA)[vec] = ldexp(1.0, E);
+    for (int k = lane; k < Kpad; k += 32) {
+      const cplx x = tile[k][v];
+      long long xr = fixed62(x.x, E), xi = fixed62(x.y, E);
+      for (int p = 0; p < S; ++p) {
+        const int sft = 62 - (p + 1) * bits;
+        const int ar = next_digit(xr, sft), ai = next_digit(xi, sft);
+        if (side == 0) {
+          __nv_bfloat16* o = As + (size_t)p * m * Kp + (size_t)vec * Kp;
+          o[k] = __float2bfloat16_rn((float)ar);
+          o[Kpad + k] = __float2bfloat16_rn((float)ai);
+        } else {
+          const size_t base = (size_t)p * nn * Kp + (size_t)vec * Kp;
+          Bre[base + k] = __float2bfloat16_rn((float)ar);
+          Bre[base + Kpad + k] = __float2bfloat16_rn((float)-ai);
+          Bim[base + k] = __float2bfloat16_rn((float)ai);
+          Bim[base + Kpad + k] = __float2bfloat16_rn((float)ar);
+        }
+      }
+    }
+  }
 }
 
 struct OzArgs {
@@ -219,6 +248,19 @@ struct OzArgs {
   unsigned long long* acc;   // split K: exact integer sums (m x n x {re, im}), finished by k_oz_finalize
                              // (zero on entry; the finaliser zeroes what it read)
 };
+
+// alpha v + beta c_old for one output value (the scaled product v):
+// alpha = +-1, beta in {0, 1} take one multiply and at most one add.
+__device__ __forceinline__ cplx oz_combine(const OzArgs& a, cplx v, cplx c_old, bool plain) {
+  if (plain) {
+    if (a.alpha.x < 0.0) v = cmake(-v.x, -v.y);
+    if (a.beta.x != 0.0) v = cadd(c_old, v);
+    return v;
+  }
+  v = cmul(a.alpha, v);
+  if (a.beta.x != 0.0 || a.beta.y != 0.0) v = cfma(a.beta, c_old, v);
+  return v;
+}
 
 // Final scaling and accumulation of one output value (shared by the GEMM and
 // the split-K finaliser).
@@ -245,186 +287,6 @@ __device__ __forceinline__ bool oz_plain(const OzArgs& a) {
          (a.beta.x == 0.0 || a.beta.x == 1.0);
 }
 
-// One CTA: 64 x 64 output tile; 8 warps in a 2 x 4 grid of 32 x 16 warp tiles.
-template <bool INT>
-__global__ void __launch_bounds__(OZ_THREADS, 2) k_oz_gemm(OzArgs a) {
-  if (a.active && *a.active == 0) return;
-  __shared__ __align__(16) __nv_bfloat16 sA[OZ_STAGES][OZ_BM * OZ_LDS];
-  __shared__ __align__(16) __nv_bfloat16 sBr[OZ_STAGES][OZ_BN * OZ_LDS];
-  __shared__ __align__(16) __nv_bfloat16 sBi[OZ_STAGES][OZ_BN * OZ_LDS];
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int wm = wid >> 2, wn = wid & 3;          // warp tile origin: rows 32*wm, cols 16*wn
-  const int i0 = blockIdx.y * OZ_BM, j0 = blockIdx.x * OZ_BN;
-  const size_t Kp = a.Kp;
-  const size_t sliceA = (size_t)a.m * Kp, sliceB = (size_t)a.n * Kp;
-
-  // accumulators over the groups: 2 (m16) x 2 (n8) mma tiles x 4 values, re
-  // and im; exact 64-bit integers (Horner in 2^bits) or FP64 with weights
-  typedef typename std::conditional<INT, long long, double>::type acc_t;
-  acc_t accr[2][2][4], acci[2][2][4];
-#pragma unroll
-  for (int x = 0; x < 2; ++x)
-#pragma unroll
-    for (int y = 0; y < 2; ++y)
-#pragma unroll
-      for (int z = 0; z < 4; ++z) { accr[x][y][z] = 0; acci[x][y][z] = 0; }
-
-  // staging of one K step of pair (p, q) into buffer `buf`
-  auto stage = [&](int buf, int p, int q, int k0) {
-    // 64 rows x 32 bf16 = 4 chunks of 16 B per row; 256 threads -> 1 chunk each per operand
-    const int r = tid >> 2, ch = tid & 3;
-    {
-      int gi = i0 + r;
-      __nv_bfloat16* dst = &sA[buf][r * OZ_LDS + ch * 8];
-      if (gi < a.m) cp_async16(dst, a.As + (size_t)p * sliceA + (size_t)gi * Kp + k0 + ch * 8);
-      else *reinterpret_cast<uint4*>(dst) = make_uint4(0, 0, 0, 0);
-    }
-    {
-      int gj = j0 + r;
-      __nv_bfloat16* dr = &sBr[buf][r * OZ_LDS + ch * 8];
-      __nv_bfloat16* di = &sBi[buf][r * OZ_LDS + ch * 8];
-      if (gj < a.n) {
-        cp_async16(dr, a.Bre + (size_t)q * sliceB + (size_t)gj * Kp + k0 + ch * 8);
-        cp_async16(di, a.Bim + (size_t)q * sliceB + (size_t)gj * Kp + k0 + ch * 8);
-      } else {
-        *reinterpret_cast<uint4*>(dr) = make_uint4(0, 0, 0, 0);
-        *reinterpret_cast<uint4*>(di) = make_uint4(0, 0, 0, 0);
-      }
-    }
-    cp_async_commit();
-  };
-
-  const int ksteps_all = (int)(Kp / OZ_BK);
-  const int ks0 = a.kchunk ? (int)blockIdx.z * a.kchunk : 0;
-  const int ksteps = a.kchunk ? min(ksteps_all, ks0 + a.kchunk) : ksteps_all;
-  // one stream of (group t, slice pair (p, q = t - p), K step) items, staged
-  // OZ_STAGES - 1 items ahead across pair and group boundaries
-  auto pmin_of = [&](int t) { return t - a.S > 1 ? t - a.S : 1; };
-  auto pmax_of = [&](int t) { return t - 1 < a.S ? t - 1 : a.S; };
-  auto advance = [&](int& t, int& p, int& ks) {
-    if (++ks < ksteps) return;
-    ks = ks0;
-    if (++p <= pmax_of(t)) return;
-    ++t;
-    p = pmin_of(t);
-  };
-  int lt = 2, lp = pmin_of(2), lks = ks0;   // next item to stage
-  int ct = 2, cp = pmin_of(2), cks = ks0;   // item being computed
-  const bool any = ks0 < ksteps;
-  int staged = 0;                           // items staged so far
-  for (int pre = 0; any && pre < OZ_STAGES - 1 && lt <= a.S + 1; ++pre) {
-    stage(staged % OZ_STAGES, lp - 1, lt - lp - 1, lks * OZ_BK);
-    ++staged;
-    advance(lt, lp, lks);
-  }
-  float fr[2][2][4], fi[2][2][4];
-#pragma unroll
-  for (int x = 0; x < 2; ++x)
-#pragma unroll
-    for (int y = 0; y < 2; ++y)
-#pragma unroll
-      for (int z = 0; z < 4; ++z) { fr[x][y][z] = 0.f; fi[x][y][z] = 0.f; }
-  for (int c = 0; any && ct <= a.S + 1; ++c) {
-    const int buf = c % OZ_STAGES;
-    // item c is complete when at most (staged - c - 1) later groups are pending
-    if (staged - c - 1 >= 1) cp_async_wait_one(); else cp_async_wait_all();
-    __syncthreads();
-    if (lt <= a.S + 1) {   // the buffer of item c - 1 is free: stage item c + OZ_STAGES - 1
-      stage(staged % OZ_STAGES, lp - 1, lt - lp - 1, lks * OZ_BK);
-      ++staged;
-      advance(lt, lp, lks);
-    }
-#pragma unroll
-    for (int kk = 0; kk < OZ_BK; kk += 16) {
-      unsigned af[2][4];
-#pragma unroll
-      for (int x = 0; x < 2; ++x) {
-        // rows 32*wm + 16*x + (lane % 16), k columns kk + 8*(lane / 16)
-        const __nv_bfloat16* pa = &sA[buf][(32 * wm + 16 * x + (lane & 15)) * OZ_LDS + kk + 8 * (lane >> 4)];
-        ldmatrix_x4(af[x][0], af[x][1], af[x][2], af[x][3], pa);
-      }
-      unsigned br[2][2], bi[2][2];
-#pragma unroll
-      for (int y = 0; y < 2; ++y) {
-        // columns 16*wn + 8*y + (lane % 8), k rows kk + 8*((lane / 8) % 2)
-        const int rowb = 16 * wn + 8 * y + (lane & 7);
-        const int kof = kk + 8 * ((lane >> 3) & 1);
-        ldmatrix_x2(br[y][0], br[y][1], &sBr[buf][rowb * OZ_LDS + kof]);
-        ldmatrix_x2(bi[y][0], bi[y][1], &sBi[buf][rowb * OZ_LDS + kof]);
-      }
-#pragma unroll
-      for (int x = 0; x < 2; ++x)
-#pragma unroll
-        for (int y = 0; y < 2; ++y) {
-          mma_bf16(fr[x][y], af[x], br[y]);
-          mma_bf16(fi[x][y], af[x], bi[y]);
-        }
-    }
-    const int t_done = ct;
-    advance(ct, cp, cks);
-    if (ct != t_done) {
-      // group t_done complete: fold its exact FP32 sums into the accumulators
-      if constexpr (INT) {
-        const long long step = 1ll << a.bits;
-#pragma unroll
-        for (int x = 0; x < 2; ++x)
-#pragma unroll
-          for (int y = 0; y < 2; ++y)
-#pragma unroll
-            for (int z = 0; z < 4; ++z) {
-              accr[x][y][z] = accr[x][y][z] * step + (long long)__float2int_rn(fr[x][y][z]);
-              acci[x][y][z] = acci[x][y][z] * step + (long long)__float2int_rn(fi[x][y][z]);
-            }
-      } else {
-        const double wgt = ldexp(1.0, -a.bits * t_done);
-#pragma unroll
-        for (int x = 0; x < 2; ++x)
-#pragma unroll
-          for (int y = 0; y < 2; ++y)
-#pragma unroll
-            for (int z = 0; z < 4; ++z) {
-              accr[x][y][z] = fma(wgt, (double)fr[x][y][z], accr[x][y][z]);
-              acci[x][y][z] = fma(wgt, (double)fi[x][y][z], acci[x][y][z]);
-            }
-      }
-#pragma unroll
-      for (int x = 0; x < 2; ++x)
-#pragma unroll
-        for (int y = 0; y < 2; ++y)
-#pragma unroll
-          for (int z = 0; z < 4; ++z) { fr[x][y][z] = 0.f; fi[x][y][z] = 0.f; }
-    }
-  }
-  __syncthreads();
-  // integer form: value = acc * 2^{-bits (S + 1)}
-  const double wint = INT ? ldexp(1.0, -a.bits * (a.S + 1)) : 1.0;
-  const bool plain = oz_plain(a);
-  // epilogue: mma C fragment layout (m16n8): value z of lane -> row (lane/4) + 8*(z/2), col 2*(lane%4) + (z%2)
-#pragma unroll
-  for (int x = 0; x < 2; ++x)
-#pragma unroll
-    for (int y = 0; y < 2; ++y)
-#pragma unroll
-      for (int z = 0; z < 4; ++z) {
-        const int row = i0 + 32 * wm + 16 * x + (lane >> 2) + 8 * (z >> 1);
-        const int col = j0 + 16 * wn + 8 * y + 2 * (lane & 3) + (z & 1);
-        if (row < a.m && col < a.n) {
-          if constexpr (INT) {
-            if (a.acc) {
-              // split K: integer partial sums add exactly (and in any order)
-              unsigned long long* q = a.acc + 2 * ((size_t)col * a.m + row);
-              atomicAdd(q, (unsigned long long)accr[x][y][z]);
-              atomicAdd(q + 1, (unsigned long long)acci[x][y][z]);
-            } else {
-              oz_store(a, row, col, __ll2double_rn(accr[x][y][z]), __ll2double_rn(acci[x][y][z]), wint, plain);
-            }
-          } else {
-            oz_store(a, row, col, accr[x][y][z], acci[x][y][z], wint, plain);
-          }
-        }
-      }
-}
-
 __global__ void k_oz_finalize(OzArgs a) {
   const double wint = ldexp(1.0, -a.bits * (a.S + 1));
   const bool plain = oz_plain(a);
@@ -449,7 +311,7 @@ __global__ void k_oz_finalize(OzArgs a) {
 // columns), so one pass over K serves every slice pair and each K block of
 // every slice is staged once:
 //   * warp 0 (one lane) streams, per K block of 64, the S B-slices (double-
-//     buffered) and the S A-slices (a ring of 3) with cp.async.bulk.tensor
+//     buffered) and the S A-slices (a ring of 4) with cp.async.bulk.tensor
 //     (128-byte swizzle) onto mbarriers;
 //   * warp 1 allocates TMEM, and one lane issues tcgen05.mma for every pair
 //     (p, q) with p + q <= S + 1 into group p + q, releasing each A slot and
@@ -463,7 +325,7 @@ constexpr int TC_BM = 128;                      // rows of C per CTA (TMEM lanes
 constexpr int TC_BN = 32;                       // complex columns of C per CTA (MMA N = 64)
 constexpr int TC_BK = 64;                       // BF16 per K block: one 128-byte swizzle row
 constexpr int TC_MAXS = 8;                      // S groups x 64 TMEM columns <= 512
-constexpr int TC_ARING = 3;                     // A-slice stages
+constexpr int TC_ARING = 4;                     // A-slice stages
 constexpr int TC_THREADS = 192;                 // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr int TC_A_TILE = TC_BM * TC_BK * 2;    // 16 KB
 constexpr int TC_B_HALF = TC_BN * TC_BK * 2;    // 4 KB: 32 rows of B'_re or of B'_im
@@ -583,10 +445,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
   const uint32_t sA = base + 2u * S * TC_B_TILE;                // [TC_ARING] A tiles of 16 KB
   const uint32_t sBar = sA + TC_ARING * TC_A_TILE;              // barriers
   uint64_t* bars = reinterpret_cast<uint64_t*>(basep + (sBar - base));
-  // barrier slots: full_b 0-1, empty_b 2-3, full_a 4-6, empty_a 7-9, acc_full 10, drain 11
+  // barrier slots: full_b 0-1, empty_b 2-3, full_a FA.., empty_a EA.., all accumulators final ACC
+  constexpr int FA = 4, EA = FA + TC_ARING, ACC = EA + TC_ARING, NBAR = ACC + 1;
   auto bar = [&](int k) { return sBar + 8u * k; };
-  volatile int* s_abort = reinterpret_cast<volatile int*>(bars + 12);
-  uint32_t* s_tmem = reinterpret_cast<uint32_t*>(bars + 13);
+  volatile int* s_abort = reinterpret_cast<volatile int*>(bars + NBAR);
+  uint32_t* s_tmem = reinterpret_cast<uint32_t*>(bars + NBAR + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i0 = blockIdx.y * TC_BM, j0 = blockIdx.x * TC_BN;
   const int nkb_all = (a.Kp + TC_BK - 1) / TC_BK;
@@ -596,9 +459,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
 
   if (threadIdx.x == 0) {
     for (int k = 0; k < 2; ++k) { mbar_init(bar(k), 1); mbar_init(bar(2 + k), 1); }
-    for (int k = 0; k < TC_ARING; ++k) { mbar_init(bar(4 + k), 1); mbar_init(bar(7 + k), 1); }
-    mbar_init(bar(10), 1);
-    mbar_init(bar(11), 1);
+    for (int k = 0; k < TC_ARING; ++k) { mbar_init(bar(FA + k), 1); mbar_init(bar(EA + k), 1); }
+    mbar_init(bar(ACC), 1);
     *s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -613,7 +475,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
   tc_fence_after();
   const uint32_t tmem = *s_tmem;
 
-  int armed[2 + TC_ARING] = {0, 0, 0, 0, 0};   // producer: phases armed per full barrier (B 0-1, A 2-4)
+  int armed[2 + TC_ARING] = {};   // producer: phases armed per full barrier (B 0-1, A from 2)
   if (warp == 0) {
     // ---- TMA producer ----
     if (lane == 0 && kb0 < kb1) {
@@ -630,10 +492,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
         }
         for (int p = 0; p < S; ++p, ++a_use) {
           const int slot = a_use % TC_ARING;
-          if (!mbar_wait(bar(7 + slot), ((a_use / TC_ARING) & 1) ^ 1, err, s_abort)) break;
+          if (!mbar_wait(bar(EA + slot), ((a_use / TC_ARING) & 1) ^ 1, err, s_abort)) break;
           armed[2 + slot] = a_use / TC_ARING + 1;
-          mbar_expect_tx(bar(4 + slot), (uint32_t)TC_A_TILE);
-          tma_load3(sA + (uint32_t)slot * TC_A_TILE, &maps.a, bar(4 + slot), kb * TC_BK, i0, p);
+          mbar_expect_tx(bar(FA + slot), (uint32_t)TC_A_TILE);
+          tma_load3(sA + (uint32_t)slot * TC_A_TILE, &maps.a, bar(FA + slot), kb * TC_BK, i0, p);
         }
       }
     }
@@ -648,7 +510,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
         bool ok = true;
         for (int p = 0; p < S; ++p, ++a_use) {
           const int slot = a_use % TC_ARING;
-          if (!mbar_wait(bar(4 + slot), (a_use / TC_ARING) & 1, err, s_abort)) { ok = false; break; }
+          if (!mbar_wait(bar(FA + slot), (a_use / TC_ARING) & 1, err, s_abort)) { ok = false; break; }
           tc_fence_after();
           const uint64_t ad = tc_desc(sA + (uint32_t)slot * TC_A_TILE);
           for (int q = 0; q + p < S; ++q) {
@@ -659,17 +521,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
             for (int kk = 0; kk < TC_BK / 16; ++kk)
               tc_mma(d, ad + 2u * kk, bd + 2u * kk, (kb == kb0 && p == 0 && kk == 0) ? 0u : 1u);
           }
-          tc_commit(bar(7 + slot));   // A slot free once these MMAs have read it
+          tc_commit(bar(EA + slot));  // A slot free once these MMAs have read it
         }
         tc_commit(bar(2 + bb));       // B buffer free
         if (!ok) break;
       }
-      tc_commit(bar(10));             // all accumulators final (or, on abort, all issued MMAs done)
+      tc_commit(bar(ACC));            // all accumulators final (or, on abort, all issued MMAs done)
     }
   } else {
     // ---- epilogue: warps 2-5, TMEM lane quarter (warp % 4) ----
     const int quarter = warp & 3;
-    const bool waited = mbar_wait(bar(10), 0, err, s_abort);
+    const bool waited = mbar_wait(bar(ACC), 0, err, s_abort);
     // tcgen05.ld is warp-collective: the decision must be uniform over the warp
     const bool have = __all_sync(0xffffffffu, waited && kb0 < kb1 && !*s_abort);
     tc_fence_after();
@@ -706,20 +568,44 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
           }
         }
         if (row < a.m) {
+          if (INT && a.acc) {
 #pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            const int col = j0 + 16 * h + c;
-            if (col < a.n) {
-              if constexpr (INT) {
-                if (a.acc) {
-                  unsigned long long* qa = a.acc + 2 * ((size_t)col * a.m + row);
-                  atomicAdd(qa, (unsigned long long)ar[c]);
-                  atomicAdd(qa + 1, (unsigned long long)ai[c]);
-                } else {
-                  oz_store(a, row, col, __ll2double_rn(ar[c]), __ll2double_rn(ai[c]), wint, plain);
-                }
-              } else {
-                oz_store(a, row, col, ar[c], ai[c], wint, plain);
+            for (int c = 0; c < 16; ++c) {
+              const int col = j0 + 16 * h + c;
+              if (col < a.n) {
+                unsigned long long* qa = a.acc + 2 * ((size_t)col * a.m + row);
+                atomicAdd(qa, (unsigned long long)ar[c]);
+                atomicAdd(qa + 1, (unsigned long long)ai[c]);
+              }
+            }
+          } else {
+            // every load (scales, old C) is issued before the first store, so
+            // they are in flight together instead of one memory latency per column
+            double fr = a.sA[row] * wint;
+            if (a.rs) fr *= a.rs[row];
+            double fc[16];
+            cplx cold[16];
+            const bool rd = a.beta.x != 0.0 || a.beta.y != 0.0;
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+              const int col = j0 + 16 * h + c;
+              fc[c] = 0.0;
+              cold[c] = cmake(0.0, 0.0);
+              if (col < a.n) {
+                fc[c] = a.sB[col];
+                if (a.cs) fc[c] *= a.cs[col];
+                if (rd) cold[c] = a.C[(size_t)col * a.ldc + row];
+              }
+            }
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+              const int col = j0 + 16 * h + c;
+              if (col < a.n) {
+                const double f = fr * fc[c];
+                double vr, vi;
+                if constexpr (INT) { vr = __ll2double_rn(ar[c]); vi = __ll2double_rn(ai[c]); }
+                else { vr = ar[c]; vi = ai[c]; }
+                a.C[(size_t)col * a.ldc + row] = oz_combine(a, cmake(vr * f, vi * f), cold[c], plain);
               }
             }
           }
@@ -731,12 +617,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
   __syncthreads();
   if (*s_abort) {
     if (threadIdx.x == 32) {
-      mbar_drain(bar(10), 0);   // the MMA thread's final commit: every MMA it issued has completed
+      mbar_drain(bar(ACC), 0);  // the MMA thread's final commit: every MMA it issued has completed
     } else if (threadIdx.x == 0) {
       for (int k = 0; k < 2; ++k)
         if (armed[k]) mbar_drain(bar(k), (armed[k] - 1) & 1);
       for (int k = 0; k < TC_ARING; ++k)
-        if (armed[2 + k]) mbar_drain(bar(4 + k), (armed[2 + k] - 1) & 1);
+        if (armed[2 + k]) mbar_drain(bar(FA + k), (armed[2 + k] - 1) & 1);
     }
   }
   tc_fence_before();
@@ -752,10 +638,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
 // Slice count S and width `bits` for a product with inner dimension K and a
 // target of `target_bits` mantissa bits: the smallest S whose widest exact
 // width bits = floor((24 - log2(K' S)) / 2) (at most 8, the BF16 integer range)
-// reaches the target.  Returns false when no S <= 12 does.
+// reaches the target.  Returns false when no S <= 8 does (the product keeps one
+// TMEM accumulator of 64 columns per group: 8 groups fill the 512 columns).
 bool ozaki_plan(int K, int target_bits, int* S_out, int* bits_out) {
   const double kp = 2.0 * ((K + 15) / 16 * 16);
-  for (int S = 2; S <= 12; ++S) {
+  for (int S = 2; S <= TC_MAXS; ++S) {
     int bits = (int)std::floor((24.0 - std::log2(kp * S)) / 2.0);
     if (bits > 8) bits = 8;
     if (bits < 1) return false;
@@ -804,22 +691,12 @@ static bool encode_slices(CUtensorMap* map, const __nv_bfloat16* base, size_t Kp
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// Engine of the products: the mma.sync kernel, or the tcgen05 kernel with
-// DQMC_OZ_ENGINE=tc (S <= 8).
-static bool use_tc_engine(int S) {
-  static const int forced_tc = [] {
-    const char* e = std::getenv("DQMC_OZ_ENGINE");
-    return e && std::strcmp(e, "tc") == 0 ? 1 : 0;
-  }();
-  return forced_tc && S <= TC_MAXS;
-}
-
 cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
                                const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
                                const double* colscale, int S, int bits, void* scratch, size_t scratch_bytes,
                                unsigned long long* acc, size_t acc_bytes, cudaStream_t st, const int* active,
                                int splitk, int* kernels, int* err) {
-  if (S < 1 || S > 12 || bits < 1 || bits > 8) return cudaErrorInvalidValue;
+  if (S < 1 || S > TC_MAXS || bits < 1 || bits > 8) return cudaErrorInvalidValue;
   const int Kpad = (k + 15) / 16 * 16;
   const size_t Kp = 2 * (size_t)Kpad;
   // exactness of the FP32 group sums: Kp * S * 2^(2 bits) <= 2^24
@@ -831,8 +708,15 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
   __nv_bfloat16* Bim = Bre + (size_t)S * nn * Kp;
   double* sA = reinterpret_cast<double*>(Bim + (size_t)S * nn * Kp);
   double* sB = sA + m;
-  k_oz_split_rows<<<m, 128, 0, st>>>(A, lda, opA, m, k, Kpad, S, bits, As, sA, active);
-  k_oz_split_cols<<<nn, 128, 0, st>>>(B, ldb, opB, k, nn, Kpad, S, bits, Bre, Bim, sB, active);
+  const bool tiled = opA == 'N' && opB == 'T' && Kpad <= OZ_TILED_KMAX;
+  if (tiled) {
+    const int vecs = m > nn ? m : nn;
+    k_oz_split_tiled<<<dim3((vecs + 31) / 32, 2), 256, 0, st>>>(A, lda, m, B, ldb, nn, k, Kpad, S, bits, As, Bre, Bim,
+                                                               sA, sB, active);
+  } else {
+    k_oz_split_rows<<<m, 128, 0, st>>>(A, lda, opA, m, k, Kpad, S, bits, As, sA, active);
+    k_oz_split_cols<<<nn, 128, 0, st>>>(B, ldb, opB, k, nn, Kpad, S, bits, Bre, Bim, sB, active);
+  }
   OzArgs a;
   a.As = As; a.Bre = Bre; a.Bim = Bim; a.sA = sA; a.sB = sB;
   a.m = m; a.n = nn; a.Kp = (int)Kp; a.S = S; a.bits = bits;
@@ -841,10 +725,9 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
   a.int_combine = 24 + bits * (S - 1) <= 61 ? 1 : 0;
   a.kchunk = 0;
   a.acc = nullptr;
-  const bool tc = use_tc_engine(S) && err;
-  const int bm = tc ? TC_BM : OZ_BM, bn = tc ? TC_BN : OZ_BN, bk = tc ? TC_BK : OZ_BK;
-  dim3 grid((nn + bn - 1) / bn, (m + bm - 1) / bm);
-  const int ksteps = (int)((Kp + bk - 1) / bk);
+  if (S > TC_MAXS || !err) return cudaErrorInvalidValue;
+  dim3 grid((nn + TC_BN - 1) / TC_BN, (m + TC_BM - 1) / TC_BM);
+  const int ksteps = (int)((Kp + TC_BK - 1) / TC_BK);
   if (splitk > 1 && a.int_combine && !active && ksteps > 1 && acc &&
       (size_t)m * nn * 2 * sizeof(unsigned long long) <= acc_bytes) {
     // split K over blockIdx.z: exact 64-bit integer partial sums in acc, which
@@ -854,8 +737,8 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
     grid.z = (ksteps + a.kchunk - 1) / a.kchunk;
     a.acc = acc;
   }
-  if (kernels) *kernels = a.acc ? 4 : 3;
-  if (tc) {
+  if (kernels) *kernels = (a.acc ? 4 : 3) - (tiled ? 1 : 0);
+  {
     TcMaps maps;
     if (!encode_slices(&maps.a, As, Kp, m, S, TC_BM) || !encode_slices(&maps.bre, Bre, Kp, nn, S, TC_BN) ||
         !encode_slices(&maps.bim, Bim, Kp, nn, S, TC_BN))
@@ -873,9 +756,6 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
         return e;
       k_oz_gemm_tc<false><<<grid, TC_THREADS, smem, st>>>(maps, a, err);
     }
-  } else {
-    if (a.int_combine) k_oz_gemm<true><<<grid, OZ_THREADS, 0, st>>>(a);
-    else k_oz_gemm<false><<<grid, OZ_THREADS, 0, st>>>(a);
   }
   if (a.acc) {
     const size_t total = (size_t)m * nn;
