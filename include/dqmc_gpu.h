@@ -63,7 +63,8 @@ typedef struct dqmc_params {
   int32_t all_checks;  /* compare wrapped and fresh G at each stabilisation (src/stack.jl:416-429) */
   int32_t precision;   /* DQMC_PREC_FP64 or DQMC_PREC_MIXED */
   int32_t device;      /* CUDA device ordinal; -1 = the calling thread's current device */
-  int32_t ozaki_bits;  /* mixed form: mantissa bits kept per GEMM operand (0 = default 40, max 60) */
+  int32_t ozaki_bits;  /* mixed form: mantissa bits kept per GEMM operand (0 = default 40); at most what
+                          8 slices reach at the product's inner dimension (40 bits at K = 1024) */
   int32_t delay;       /* delayed-update depth k (0 or 1 = immediate rank-4 updates) */
   int32_t greens_method; /* DQMC_GREENS_SCALES (default) or DQMC_GREENS_TWO_QR */
   int32_t inflight;    /* dqmc_batch_create: chains swept at the same time (0 = min(count, 8)); first chain's value.
