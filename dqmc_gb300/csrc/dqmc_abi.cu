@@ -94,6 +94,12 @@ struct dqmc_handle {
   cplx* wy_z = nullptr;       // (kWyMax x n) T Vb^H W
   cplx* wy_t = nullptr;       // (kWyMax) tau of the block
   double* force_d = nullptr;   // (3, N, M) d log|det M| / d phi
+  // time-displaced measurement: work matrices and B-chain stacks in one block,
+  // and G(tau, 0) / G(0, tau) buffers for host or absent outputs (allocated on
+  // the first measurement and kept until dqmc_destroy)
+  void* tdgf_ws = nullptr;
+  cplx* tdgf_a = nullptr;
+  cplx* tdgf_b = nullptr;
   double* etc_d = nullptr;     // (6 N) equal-time correlators P+, P-, C+, C-
   // global updates: backup of stack, G, field and interaction table (allocated on first use)
   cplx *gb_u = nullptr, *gb_t = nullptr, *gb_G = nullptr;
@@ -813,7 +819,7 @@ void free_all(dqmc_handle* h) {
                   h->Tr, h->Dl, h->Dr, h->W1, h->W2, h->W3, h->W4, h->D1, h->d2, h->ord1, h->qr.vn1,
                   h->qr.vn2, h->qr.order, h->qr.tau, h->qr.beta, h->qr.V, h->qr.bar, h->qr.cand_v, h->qr.cand_q, h->delta_d, h->unif_d,
                   h->acc_d, h->det_d, h->pacc_d, h->action_d, h->nacc_d, h->Acol, h->Brow, h->bar, h->err_d,
-                  h->scal_d, h->oz_scratch, h->oz_acc, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lup.piv, h->lup.cand_rows, h->lup.rowk, h->lu_L, h->lu_pivrow, h->lu_scales, h->wy_v, h->wy_s, h->wy_z, h->wy_t, h->force_d, h->etc_d, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
+                  h->scal_d, h->oz_scratch, h->oz_acc, h->Xd, h->Yd, h->dstate, h->prep, h->blk, h->pub, h->lu.perm, h->lu.udiag, h->lu.rdiag, h->lup.piv, h->lup.cand_rows, h->lup.rowk, h->lu_L, h->lu_pivrow, h->lu_scales, h->wy_v, h->wy_s, h->wy_z, h->wy_t, h->force_d, h->etc_d, h->tdgf_ws, h->tdgf_a, h->tdgf_b, h->gb_u, h->gb_t, h->gb_G, h->gb_d, h->gb_phi, h->gb_evtab};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   clear_graphs(h);
@@ -1006,23 +1012,31 @@ int measure(dqmc_handle* h, cplx* Gt0, cplx* G0t) {
   const int n = h->n, s = h->s, M = h->M, nr = M / s;
   const size_t nn = (size_t)n * n;
   Work w;
-  std::vector<void*> owned;
-  auto alloc = [&](void** p, size_t bytes) -> int {
-    if (cudaMalloc(p, bytes) != cudaSuccess) return DQMC_ERR_CUDA;
-    owned.push_back(*p);
-    return DQMC_OK;
-  };
-  int rc = DQMC_OK;
   cplx* st_u[4] = {}; cplx* st_t[4] = {}; double* st_d[4] = {};
-  for (int k = 0; k < 8 && rc == DQMC_OK; ++k) rc = alloc((void**)&w.m[k], nn * sizeof(cplx));
-  for (int k = 0; k < 4 && rc == DQMC_OK; ++k) rc = alloc((void**)&w.v[k], n * sizeof(double));
-  if (rc == DQMC_OK) rc = alloc((void**)&w.s4, 4 * n * sizeof(double));
-  if (rc == DQMC_OK) rc = alloc((void**)&w.neg, n * sizeof(double));
-  for (int k = 0; k < 4 && rc == DQMC_OK; ++k) {
-    rc = alloc((void**)&st_u[k], nr * nn * sizeof(cplx));
-    if (rc == DQMC_OK) rc = alloc((void**)&st_t[k], nr * nn * sizeof(cplx));
-    if (rc == DQMC_OK) rc = alloc((void**)&st_d[k], (size_t)nr * n * sizeof(double));
+  // one block, carved in the same order on every call: 8 work matrices, 4 + 4 + 1
+  // vectors, and the four B-chain stacks (U, T, D); allocated once per handle
+  size_t off = 0;
+  std::vector<std::pair<void**, size_t>> parts;
+  for (int k = 0; k < 8; ++k) parts.push_back({(void**)&w.m[k], nn * sizeof(cplx)});
+  for (int k = 0; k < 4; ++k) parts.push_back({(void**)&w.v[k], n * sizeof(double)});
+  parts.push_back({(void**)&w.s4, 4 * n * sizeof(double)});
+  parts.push_back({(void**)&w.neg, n * sizeof(double)});
+  for (int k = 0; k < 4; ++k) {
+    parts.push_back({(void**)&st_u[k], nr * nn * sizeof(cplx)});
+    parts.push_back({(void**)&st_t[k], nr * nn * sizeof(cplx)});
+    parts.push_back({(void**)&st_d[k], (size_t)nr * n * sizeof(double)});
   }
+  for (auto& pt : parts) off += (pt.second + 255) / 256 * 256;
+  if (!h->tdgf_ws && cudaMalloc(&h->tdgf_ws, off) != cudaSuccess) {
+    h->tdgf_ws = nullptr;
+    return DQMC_ERR_CUDA;
+  }
+  off = 0;
+  for (auto& pt : parts) {
+    *pt.first = static_cast<char*>(h->tdgf_ws) + off;
+    off += (pt.second + 255) / 256 * 256;
+  }
+  int rc = DQMC_OK;
   auto body = [&]() -> int {
     // stacks: 0 = B(tau,1)^-1 (LEFT, inverse), 1 = B(beta,tau) (RIGHT), 2 = B(tau,1) (LEFT), 3 = B(beta,tau)^-1 (RIGHT, inverse)
     CHK(bchain_udts(h, w, true, false, st_u[0], st_d[0], st_t[0]));
@@ -1079,9 +1093,17 @@ int measure(dqmc_handle* h, cplx* Gt0, cplx* G0t) {
                         cudaMemsetAsync(G0t, 0, (size_t)M * nn * sizeof(cplx), h->st) != cudaSuccess))
     rc = DQMC_ERR_CUDA;
   if (rc == DQMC_OK) rc = body();
-  cudaStreamSynchronize(h->st);
-  for (void* q : owned) cudaFree(q);
   return rc;
+}
+
+// G(tau, 0) and G(0, tau) buffers of the handle for host or absent outputs
+int output_buffers(dqmc_handle* h, cplx** a, cplx** b) {
+  const size_t bytes = (size_t)h->M * h->n * h->n * sizeof(cplx);
+  if (!h->tdgf_a && cudaMalloc(&h->tdgf_a, bytes) != cudaSuccess) { h->tdgf_a = nullptr; return DQMC_ERR_CUDA; }
+  if (!h->tdgf_b && cudaMalloc(&h->tdgf_b, bytes) != cudaSuccess) { h->tdgf_b = nullptr; return DQMC_ERR_CUDA; }
+  *a = h->tdgf_a;
+  *b = h->tdgf_b;
+  return DQMC_OK;
 }
 
 }  // namespace tdgf
@@ -2042,14 +2064,11 @@ int dqmc_measure_tdgfs(dqmc_handle* h, double* Gt0, double* G0t, int32_t device_
     return sync(h);
   }
   cplx *a = nullptr, *b = nullptr;
-  CU(cudaMalloc(&a, bytes));
-  if (cudaMalloc(&b, bytes) != cudaSuccess) { cudaFree(a); return set_err(h, DQMC_ERR_CUDA, "out of device memory"); }
+  if (tdgf::output_buffers(h, &a, &b) != DQMC_OK) return set_err(h, DQMC_ERR_CUDA, "out of device memory");
   int rc = tdgf::measure(h, a, b);
-  if (rc == DQMC_OK && cudaMemcpy(Gt0, a, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) rc = DQMC_ERR_CUDA;
-  if (rc == DQMC_OK && cudaMemcpy(G0t, b, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) rc = DQMC_ERR_CUDA;
-  cudaFree(a);
-  cudaFree(b);
-  if (rc != DQMC_OK) return rc;
+  if (rc == DQMC_OK && cudaMemcpyAsync(Gt0, a, bytes, cudaMemcpyDeviceToHost, h->st) != cudaSuccess) rc = DQMC_ERR_CUDA;
+  if (rc == DQMC_OK && cudaMemcpyAsync(G0t, b, bytes, cudaMemcpyDeviceToHost, h->st) != cudaSuccess) rc = DQMC_ERR_CUDA;
+  if (rc != DQMC_OK) return set_err(h, rc, "time-displaced measurement");
   return sync(h);
 }
 
@@ -2065,20 +2084,15 @@ int dqmc_measure_zfpc(dqmc_handle* h, const double* Gt0, double* zfpc_plus, doub
     g = reinterpret_cast<cplx*>(const_cast<double*>(Gt0));
   } else {
     if (!Gt0 && !h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
-    CU(cudaMalloc(&g, bytes));
-    int rc = DQMC_OK;
-    if (Gt0) {
-      if (cudaMemcpyAsync(g, Gt0, bytes, cudaMemcpyHostToDevice, h->st) != cudaSuccess) rc = DQMC_ERR_CUDA;
-    } else if (cudaMalloc(&scratch, bytes) != cudaSuccess) {
-      rc = DQMC_ERR_CUDA;
-    } else {
-      rc = tdgf::measure(h, g, scratch);   // G(tau, 0); G(0, tau) is not needed
+    int rc = tdgf::output_buffers(h, &g, &scratch);
+    if (rc == DQMC_OK) {
+      if (Gt0) {
+        if (cudaMemcpyAsync(g, Gt0, bytes, cudaMemcpyHostToDevice, h->st) != cudaSuccess) rc = DQMC_ERR_CUDA;
+      } else {
+        rc = tdgf::measure(h, g, scratch);   // G(tau, 0); G(0, tau) is not needed
+      }
     }
-    if (rc != DQMC_OK) {
-      cudaFree(g);
-      cudaFree(scratch);
-      return rc == DQMC_ERR_CUDA ? set_err(h, rc, "device memory for the time-displaced G") : rc;
-    }
+    if (rc != DQMC_OK) return rc == DQMC_ERR_CUDA ? set_err(h, rc, "device memory for the time-displaced G") : rc;
   }
   if (!h->etc_d) CU(cudaMalloc(&h->etc_d, (size_t)6 * N * sizeof(double)));
   int rc = DQMC_OK;
@@ -2090,8 +2104,6 @@ int dqmc_measure_zfpc(dqmc_handle* h, const double* Gt0, double* zfpc_plus, doub
   if (rc == DQMC_OK && zfpc_minus &&
       cudaMemcpyAsync(zfpc_minus, h->etc_d + N, N * sizeof(double), kind, h->st) != cudaSuccess) rc = DQMC_ERR_CUDA;
   if (rc == DQMC_OK && cudaStreamSynchronize(h->st) != cudaSuccess) rc = DQMC_ERR_CUDA;
-  if (!(Gt0 && device_ptrs)) cudaFree(g);
-  cudaFree(scratch);
   if (rc != DQMC_OK) return set_err(h, rc, "zfpc");
   return check_device_error(h);
 }
@@ -2108,12 +2120,12 @@ static int zero_frequency_measure(dqmc_handle* h, int which, const double* green
     return set_err(h, DQMC_ERR_ARG, "device_ptrs set but an array is not device memory");
   const int N = h->N, M = h->M;
   const size_t nn = (size_t)h->n * h->n, bytes = (size_t)M * nn * sizeof(cplx);
-  const bool own = !(Gt0 && device_ptrs);   // time-displaced blocks staged in memory of this call
+  const bool own = !(Gt0 && device_ptrs);   // time-displaced blocks staged in the handle's buffers
   cplx *gt0 = nullptr, *g0t = nullptr;
   int rc = DQMC_OK;
   if (own) {
     if (!Gt0 && !h->initialized) return set_err(h, DQMC_ERR_STATE, "call dqmc_init first");
-    if (cudaMalloc(&gt0, bytes) != cudaSuccess || cudaMalloc(&g0t, bytes) != cudaSuccess) {
+    if (tdgf::output_buffers(h, &gt0, &g0t) != DQMC_OK) {
       rc = DQMC_ERR_CUDA;
     } else if (Gt0) {
       if (cudaMemcpyAsync(gt0, Gt0, bytes, cudaMemcpyHostToDevice, h->st) != cudaSuccess ||
@@ -2163,10 +2175,6 @@ static int zero_frequency_measure(dqmc_handle* h, int which, const double* green
       rc = DQMC_ERR_CUDA;
   }
   if (cudaStreamSynchronize(h->st) != cudaSuccess && rc == DQMC_OK) rc = DQMC_ERR_CUDA;
-  if (own) {
-    cudaFree(gt0);
-    cudaFree(g0t);
-  }
   if (rc == DQMC_ERR_CUDA) return set_err(h, rc, "zero-frequency measurement: device memory or copy");
   if (rc != DQMC_OK) return rc;
   if (sfdensity) {
