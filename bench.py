@@ -743,10 +743,11 @@ def run_ours(args, world, rank, local):
         batched = dict(value=bval, unit="chain-sweeps/s", workload=bdesc, seconds=bwall, clocks=bclk, **binfo)
         res_fp64_value = world * res["fp64"]["steps"] / res["fp64"]["secs"] if "fp64" in res else None
         # the headline lattice batched: 8 L=16, beta=20 chains in flight, both forms
-        # (warm-up: the two captured sweep graphs; one timed batch sweep each)
+        # (warm-up: the two captured sweep graphs; two timed batch sweeps mixed, one FP64)
         b16 = {}
         for prec in ("mixed", "fp64"):
-            v, w, c, info, _ = measure_batch(args, world, rank, dev, 2, 1, prec, Ls=[L] * 8, M=M,
+            v, w, c, info, _ = measure_batch(args, world, rank, dev, 2, 2 if prec == "mixed" else 1, prec,
+                                             Ls=[L] * 8, M=M,
                                              desc=f"8 independent chains, {desc}")
             b16[prec] = dict(value=v, seconds=w, clocks=c, delays=info["delays"], acc_rate=info["acc_rate"])
         batched["headline_lattice"] = {
@@ -832,7 +833,7 @@ def main():
     ap.add_argument("--cpu-calls", type=int, default=10)
     ap.add_argument("--ref-calls", type=int, default=10, help="reference arm: update calls per step "
                     "(10 = one safe_mult block, one stabilisation included)")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"],
                     help="both: FP64 and mixed forms on the same field and streams; value = mixed")
     ap.add_argument("--delay", type=int, default=16, help="mixed form: delayed-update depth k")
