@@ -437,9 +437,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   GridBarrierExit bar_exit(a.bar);
   const ModelConst& mc = a.mc;
   const int N = mc.N, n = mc.n, L = mc.L, K4 = 4 * d.k;
-  __shared__ int s_first, s_ok;
-  __shared__ int s_acc[2];          // decision of the site, by site parity
-  __shared__ int s_specok[2][8];    // per warp: the next site's data were complete (by site parity)
+  __shared__ int s_first, s_ok, s_acc;
   if (threadIdx.x == 0) s_first = __ldcg(&d.state[0]);
   __syncthreads();
   const int first = s_first;
@@ -454,18 +452,15 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   cplx* s_blk = reinterpret_cast<cplx*>(smem_local);                   // (owned, 16) G_cur blocks
   cplx* s_xn = s_blk + (size_t)16 * owned;                              // (4 sites, 4 x 4) new X rows
   cplx* s_yn = s_xn + 64;                                              // (4 sites, 4 x 4) new Y columns
-  cplx* Ysm2 = s_yn + 64;                                              // [2] (4k x 4): Y[j, s + cN]
-  cplx* Xsm2 = Ysm2 + (size_t)2 * K4 * 4;                              // [2] (4 x 4k): X[s + rN, j]
-  cplx* s_xrow = Xsm2 + (size_t)2 * K4 * 4;                            // CACHE: (owned, 4, 4k) X[j', j + rN]
+  cplx* Ysm = s_yn + 64;                                               // (4k x 4): Y[j, i + cN]
+  cplx* Xsm = Ysm + (size_t)K4 * 4;                                    // (4 x 4k): X[i + rN, j]
+  cplx* s_xrow = Xsm + (size_t)K4 * 4;                                 // CACHE: (owned, 4, 4k) X[j', j + rN]
   cplx* s_ycol = s_xrow + (CACHE ? (size_t)owned * 4 * K4 : 0);        // CACHE: (owned, 4, 4k) Y[j', j + cN]
   double* phis = reinterpret_cast<double*>(s_ycol + (CACHE ? (size_t)owned * 4 * K4 : 0));   // (3, N)
-  // per-site values, double-buffered by site parity: the site being decided
-  // and the next one (prepared speculatively, assuming a rejection)
-  __shared__ cplx s_delta[2][16];   // Delta_s
-  __shared__ cplx s_adj[2][16];     // adj(M)[r][c]
+  __shared__ cplx s_delta[16];      // Delta_i
+  __shared__ cplx s_adj[2][16];     // adj(M)[r][c] (double-buffered by site parity)
   __shared__ cplx s_det[2];
   __shared__ double s_expds[2];
-  __shared__ double s_u[2];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int l = a.slice0;
   for (int k = threadIdx.x; k < 3 * N; k += blockDim.x) phis[k] = a.phi[(size_t)3 * N * l + k];
@@ -481,27 +476,52 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   const int sub = lane >> 3, qg = (lane >> 1) & 3, h = lane & 1;
   const bool isX = (wid & 1) == 0;
 
-  // Values of site s into slot b with J pending factor columns, every warp
-  // its role: warps 4 and 6 build M = I + Delta (I - G_cur_ss) and form
-  // det M (warp 4) and adj M (warp 6); warp 5 the action difference and the
-  // uniform; warp 7 Delta_s; warps 0-3 and 7 stage the J pending factor
-  // entries touching s.  G_cur_ss is G itself with nothing pending, else the
-  // block its owner keeps (its publication counter must have reached p).
-  auto site_values = [&](int s, int b, int J) {
-    const SitePrep* sp = d.prep + s;
+  for (int i = first; i < N; ++i) {
+    const int J = 4 * p;   // pending columns of X / rows of Y
+    const int slot = i & 1;
+    const SitePrep* sp = d.prep + i;
+    // ---- wait until the owner of site i has folded in all p acceptances ----
+    if (p > 0) {
+      if (threadIdx.x == 0) {
+        volatile int* f = d.pub + i;
+        int ok = 1;
+        long long spins = 0;
+        while (*f < p) {
+          if ((++spins & 1023) == 0) {
+            if (spins > (1ll << 24)) { atomicOr(a.err, 2); ok = 0; break; }
+            if (*(volatile int*)a.err & 2) { ok = 0; break; }
+          }
+        }
+        __threadfence();
+        s_ok = ok;
+      }
+      __syncthreads();
+      if (!s_ok) return;
+    }
+    // ---- G entries of the first pass's phase 1 (independent of the decision) ----
+    cplx gq_pref = cmake(0.0, 0.0);
+    if ((wid >> 1) < owned) {
+      const int rc = blockIdx.x + (wid >> 1) * gridDim.x + sub * N;
+      if (isX) {
+        gq_pref = ldcg_c(&a.G[(size_t)(i + qg * N) * n + rc]);
+        if (rc == i + qg * N) gq_pref.x -= 1.0;
+      } else {
+        gq_pref = ldcg_c(&a.G[(size_t)rc * n + i + qg * N]);
+      }
+    }
     if (wid == 4 || wid == 6) {
-      // ---- M = I + Delta (I - G_cur_ss), lane 4r+c holds M[r][c] (src/local_updates.jl:49-55) ----
+      // ---- M = I + Delta (I - G_cur_ii), lane 4r+c holds M[r][c] (src/local_updates.jl:49-55) ----
       const int r = (lane >> 2) & 3, c = lane & 3;
       cplx g = cmake(0.0, 0.0), drow[4];
       if (lane < 16) {
-        g = J == 0 ? ldcg_c(&a.G[(size_t)(s + c * N) * n + s + r * N]) : ldcg_c(&d.blk[(size_t)16 * s + lane]);
+        g = p == 0 ? ldcg_c(&a.G[(size_t)(i + c * N) * n + i + r * N]) : ldcg_c(&d.blk[(size_t)16 * i + lane]);
 #pragma unroll
         for (int k = 0; k < 4; ++k) drow[k] = ldcg_c(&sp->delta[4 * r + k]);
       } else {
 #pragma unroll
         for (int k = 0; k < 4; ++k) drow[k] = cmake(0.0, 0.0);
       }
-      const cplx mt = cmake((r == c ? 1.0 : 0.0) - g.x, -g.y);   // (I - G_ss)[r][c]
+      const cplx mt = cmake((r == c ? 1.0 : 0.0) - g.x, -g.y);   // (I - G_ii)[r][c]
       cplx m = cmake(r == c ? 1.0 : 0.0, 0.0);
 #pragma unroll
       for (int k = 0; k < 4; ++k) m = cfma(drow[k], shfl_c(mt, 4 * k + c), m);
@@ -517,15 +537,15 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         cplx det = term;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) det = cadd(det, shfl_c(det, lane ^ o));
-        if (lane == 0) s_det[b] = det;
+        if (lane == 0) s_det[slot] = det;
       } else {
         const cplx adj = adjugate_entry(m, lane);
-        if (lane < 16) s_adj[b][lane] = adj;
+        if (lane < 16) s_adj[slot][lane] = adj;
       }
     } else if (wid == 5) {
       // ---- boson action difference: prepared part + space-neighbour coupling ----
       if (lane == 0) {
-        const int y = s % L, x = s / L;
+        const int y = i % L, x = i / L;
         const int nbs[4] = {(y + 1) % L + L * x, y + L * ((x + 1) % L), (y - 1 + L) % L + L * x,
                             y + L * ((x - 1 + L) % L)};
         double sdot = 0.0;
@@ -537,28 +557,24 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         double dS = __ldcg(&sp->dsA);
         dS += 0.5 * mc.dtau * (__ldcg(&sp->dsQ) - 2.0 * sdot);
         dS += __ldcg(&sp->dsB);
-        s_expds[b] = exp(-dS);
-      } else if (lane == 1) {
-        s_u[b] = __ldg(&a.unif[s]);
+        s_expds[slot] = exp(-dS);
       }
     } else if (wid == 7 && lane < 16) {
-      s_delta[b][lane] = ldcg_c(&sp->delta[lane]);
+      s_delta[lane] = ldcg_c(&sp->delta[lane]);
     }
     if (wid < 4 || wid == 7) {
-      // ---- stage the pending factor entries touching s (160 threads, loads issued together) ----
+      // ---- stage the pending factor entries touching site i (160 threads, loads issued together) ----
       constexpr int kStage = 160;
-      cplx* Ysm = Ysm2 + (size_t)b * K4 * 4;
-      cplx* Xsm = Xsm2 + (size_t)b * K4 * 4;
       const int st = wid < 4 ? threadIdx.x : 128 + lane;
       for (int t = st; t < 4 * J; t += 2 * kStage) {
         const int t2 = t + kStage;
         const int j1 = t >> 2, c1 = t & 3, j2 = t2 >> 2, c2 = t2 & 3;
-        const cplx y1 = ldcg_c(&d.Y[(size_t)j1 * n + s + c1 * N]);
-        const cplx x1 = ldcg_c(&d.X[(size_t)j1 * n + s + c1 * N]);
+        const cplx y1 = ldcg_c(&d.Y[(size_t)j1 * n + i + c1 * N]);
+        const cplx x1 = ldcg_c(&d.X[(size_t)j1 * n + i + c1 * N]);
         cplx y2 = cmake(0.0, 0.0), x2 = cmake(0.0, 0.0);
         if (t2 < 4 * J) {
-          y2 = ldcg_c(&d.Y[(size_t)j2 * n + s + c2 * N]);
-          x2 = ldcg_c(&d.X[(size_t)j2 * n + s + c2 * N]);
+          y2 = ldcg_c(&d.Y[(size_t)j2 * n + i + c2 * N]);
+          x2 = ldcg_c(&d.X[(size_t)j2 * n + i + c2 * N]);
         }
         Ysm[4 * j1 + c1] = y1;
         Xsm[(size_t)c1 * K4 + j1] = x1;
@@ -568,54 +584,16 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         }
       }
     }
-  };
-
-  int spec_ready = 0;   // the values of site i were prepared during site i - 1 (uniform over the CTA)
-  for (int i = first; i < N; ++i) {
-    const int J = 4 * p;   // pending columns of X / rows of Y
-    const int b = i & 1;
-    if (!spec_ready) {
-      // ---- wait until the owner of site i has folded in all p acceptances ----
-      if (p > 0) {
-        if (threadIdx.x == 0) {
-          volatile int* f = d.pub + i;
-          int ok = 1;
-          long long spins = 0;
-          while (*f < p) {
-            if ((++spins & 1023) == 0) {
-              if (spins > (1ll << 24)) { atomicOr(a.err, 2); ok = 0; break; }
-              if (*(volatile int*)a.err & 2) { ok = 0; break; }
-            }
-          }
-          __threadfence();
-          s_ok = ok;
-        }
-        __syncthreads();
-        if (!s_ok) return;
-      }
-      site_values(i, b, J);
-      __syncthreads();
-    }
-    // ---- G entries of the first pass's phase 1 (independent of the decision) ----
-    cplx gq_pref = cmake(0.0, 0.0);
-    if ((wid >> 1) < owned) {
-      const int rc = blockIdx.x + (wid >> 1) * gridDim.x + sub * N;
-      if (isX) {
-        gq_pref = ldcg_c(&a.G[(size_t)(i + qg * N) * n + rc]);
-        if (rc == i + qg * N) gq_pref.x -= 1.0;
-      } else {
-        gq_pref = ldcg_c(&a.G[(size_t)rc * n + i + qg * N]);
-      }
-    }
-    // ---- Metropolis decision of site i (one thread; the same in every CTA) ----
-    if (threadIdx.x == 224) {
-      const cplx det = s_det[b];
-      const double exp_dS = s_expds[b];
+    __syncthreads();
+    // ---- Metropolis decision (thread 0; the same in every CTA) ----
+    if (threadIdx.x == 0) {
+      const cplx det = s_det[slot];
+      const double exp_dS = s_expds[slot];
       const double pacc = exp_dS * det.x;
-      const double u = s_u[b];
+      const double u = __ldg(&a.unif[i]);
       const bool bad = !isfinite(det.x) || !isfinite(det.y) || (det.x == 0.0 && det.y == 0.0);
       const bool acc = !bad && (pacc > 1.0 || u < pacc);
-      s_acc[b] = acc;
+      s_acc = acc;
       if (acc)
         for (int q = 0; q < 3; ++q) phis[3 * i + q] += a.delta[3 * i + q];
       if (blockIdx.x == 0) {
@@ -624,7 +602,6 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         if (a.det_out) a.det_out[i] = det;
         if (a.pacc_out) a.pacc_out[i] = pacc;
         if (acc) {
-          const SitePrep* sp = d.prep + i;
           double* pg = &a.phi[((size_t)N * l + i) * 3];
           pg[0] = phis[3 * i]; pg[1] = phis[3 * i + 1]; pg[2] = phis[3 * i + 2];
           if (a.evtab) reinterpret_cast<EvEntry*>(a.evtab)[(size_t)N * l + i] = sp->ev;
@@ -633,29 +610,9 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         }
       }
     }
-    // ---- meanwhile: the values of site i + 1 assuming site i is rejected
-    //      (same p); usable only if every warp found its data complete ----
-    if (i + 1 < N) {
-      int ok = 1;
-      if (p > 0) {
-        if (lane == 0) ok = ld_acquire_u32(reinterpret_cast<const unsigned*>(d.pub + i + 1)) >= (unsigned)p;
-        ok = __shfl_sync(0xffffffffu, ok, 0);
-        __syncwarp();   // lane 0's acquire orders the warp's loads of the owner's data
-      }
-      if (lane == 0) s_specok[b][wid] = ok;
-      if (ok) site_values(i + 1, b ^ 1, J);
-    }
     __syncthreads();
-    if (!s_acc[b]) {
-      int all = i + 1 < N;
-#pragma unroll
-      for (int w = 0; w < LU_THREADS / 32; ++w) all &= s_specok[b][w];
-      spec_ready = all;
-      continue;
-    }
-    spec_ready = 0;
-    const cplx* Ysm = Ysm2 + (size_t)b * K4 * 4;
-    const cplx* Xsm = Xsm2 + (size_t)b * K4 * 4;
+    // decision slots are double-buffered: a rejected site needs no further barrier
+    if (!s_acc) continue;
     // ---- new factor columns: X[:, J+k] = (G_cur[:, i + qN] - I[:, i + qN]) adj(M),
     //      Y[J+k, :] = Delta G_cur[i + qN, :] / det  (X Y = (G_cur - I) M^-1 Delta G_cur) ----
     // The owned site among the next two (i + 1, i + 2), if any and if the
@@ -664,7 +621,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
     // warps 4-7 its Y column c = wid - 4; lane = 8 q + part sums every 8th
     // pending column, then the parts are added by shuffles.
     int t_pri = -1;
-    if (p + 1 < d.k) {
+    if (d.priority && p + 1 < d.k) {
       for (int jn = i + 1; jn <= i + 2 && jn < N; ++jn)
         if (jn % (int)gridDim.x == (int)blockIdx.x) { t_pri = (jn - (int)blockIdx.x) / (int)gridDim.x; break; }
     }
@@ -704,20 +661,20 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         const int ko = lane;
         cplx prod;
         if (isXp) {
-          prod = cmul(g0, s_adj[b][ko]);
-          prod = cfma(g1, s_adj[b][4 + ko], prod);
-          prod = cfma(g2, s_adj[b][8 + ko], prod);
-          prod = cfma(g3, s_adj[b][12 + ko], prod);
+          prod = cmul(g0, s_adj[slot][ko]);
+          prod = cfma(g1, s_adj[slot][4 + ko], prod);
+          prod = cfma(g2, s_adj[slot][8 + ko], prod);
+          prod = cfma(g3, s_adj[slot][12 + ko], prod);
           d.X[(size_t)(J + ko) * n + rc] = prod;
           s_xn[4 * rcs + ko] = prod;             // X_new[j + rcs N, k]
         } else {
-          const cplx det = s_det[b];
+          const cplx det = s_det[slot];
           const double rd = 1.0 / (det.x * det.x + det.y * det.y);
           const cplx inv = cmake(det.x * rd, -det.y * rd);
-          prod = cmul(s_delta[b][4 * ko], g0);
-          prod = cfma(s_delta[b][4 * ko + 1], g1, prod);
-          prod = cfma(s_delta[b][4 * ko + 2], g2, prod);
-          prod = cfma(s_delta[b][4 * ko + 3], g3, prod);
+          prod = cmul(s_delta[4 * ko], g0);
+          prod = cfma(s_delta[4 * ko + 1], g1, prod);
+          prod = cfma(s_delta[4 * ko + 2], g2, prod);
+          prod = cfma(s_delta[4 * ko + 3], g3, prod);
           prod = cmul(prod, inv);
           d.Y[(size_t)(J + ko) * n + rc] = prod;
           s_yn[4 * ko + rcs] = prod;             // Y_new[k, j + rcs N]
@@ -756,7 +713,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         }
         cplx inv = cmake(0.0, 0.0);
         if (!isX) {
-          const cplx det = s_det[b];
+          const cplx det = s_det[slot];
           const double rd = 1.0 / (det.x * det.x + det.y * det.y);
           inv = cmake(det.x * rd, -det.y * rd);
         }
@@ -781,8 +738,8 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         const int ko = qg;
         const cplx g0 = shfl_c(gcur, 8 * sub + 4 * h), g1 = shfl_c(gcur, 8 * sub + 4 * h + 2);
         cplx prod;
-        if (isX) prod = cfma(g1, s_adj[b][4 * (2 * h + 1) + ko], cmul(g0, s_adj[b][4 * (2 * h) + ko]));
-        else prod = cfma(s_delta[b][4 * ko + 2 * h + 1], g1, cmul(s_delta[b][4 * ko + 2 * h], g0));
+        if (isX) prod = cfma(g1, s_adj[slot][4 * (2 * h + 1) + ko], cmul(g0, s_adj[slot][4 * (2 * h) + ko]));
+        else prod = cfma(s_delta[4 * ko + 2 * h + 1], g1, cmul(s_delta[4 * ko + 2 * h], g0));
         prod = cadd(prod, shfl_c(prod, lane ^ 1));
         if (!isX) prod = cmul(prod, inv);
         if (h == 0) {
@@ -804,11 +761,11 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         const int j = blockIdx.x + tsr * gridDim.x;
         if (tsr < owned && tsr != t_pri && j > i) {
           const int r = lane >> 2, c = lane & 3;
-          cplx bk = s_blk[16 * tsr + lane];
+          cplx b = s_blk[16 * tsr + lane];
 #pragma unroll
-          for (int k = 0; k < 4; ++k) bk = cfma(s_xn[16 * ls + 4 * r + k], s_yn[16 * ls + 4 * k + c], bk);
-          s_blk[16 * tsr + lane] = bk;
-          d.blk[(size_t)16 * j + lane] = bk;
+          for (int k = 0; k < 4; ++k) b = cfma(s_xn[16 * ls + 4 * r + k], s_yn[16 * ls + 4 * k + c], b);
+          s_blk[16 * tsr + lane] = b;
+          d.blk[(size_t)16 * j + lane] = b;
         }
       }
       __syncthreads();   // s_xn / s_yn reused by the next pass; all stores precede the publication
@@ -844,8 +801,7 @@ cudaError_t launch_local_prepare(const LocalUpdateArgs& a, SitePrep* prep, int* 
 
 static size_t local_delayed_smem(int N, int k, int grid, bool cache) {
   const size_t owned = (size_t)(N + grid - 1) / grid;
-  // blocks, new X rows / Y columns, and the staged factor entries of two sites
-  size_t c = 16 * owned + 128 + (size_t)4 * 16 * k;
+  size_t c = 16 * owned + 128 + (size_t)2 * 16 * k;
   if (cache) c += 2 * owned * 4 * 4 * (size_t)k;
   return c * sizeof(cplx) + (size_t)3 * N * sizeof(double);
 }

@@ -170,36 +170,37 @@ __global__ void k_oz_split_cols(const cplx* __restrict__ X, int ld, char op, int
 // Both sides in one launch when each operand vector is contiguous across
 // vectors (op(A) = A 'N': element k of row i at A[k lda + i]; op(B) = B^T
 // 'T': element k of column j at B[k ldb + j]) and Kpad <= 64, the shape of
-// the delayed-update flush: 32 vectors x Kpad elements are loaded with
+// the delayed-update flush: 8 vectors x Kpad elements are loaded with
 // coalesced reads into shared memory, then one warp per vector finds its
 // scale and cuts its digits (the same digits as k_oz_split_rows/cols).
 // blockIdx.y = 0: rows of A; 1: columns of B.
 constexpr int OZ_TILED_KMAX = 64;
+constexpr int OZ_TILED_V = 8;      // vectors per block: one warp each
 __global__ void __launch_bounds__(256) k_oz_split_tiled(const cplx* __restrict__ A, int lda, int m,
                                                         const cplx* __restrict__ B, int ldb, int nn, int K, int Kpad,
                                                         int S, int bits, __nv_bfloat16* __restrict__ As,
                                                         __nv_bfloat16* __restrict__ Bre, __nv_bfloat16* __restrict__ Bim,
                                                         double* __restrict__ sA, double* __restrict__ sB,
                                                         const int* __restrict__ active) {
-  __shared__ cplx tile[OZ_TILED_KMAX][33];
+  __shared__ cplx tile[OZ_TILED_KMAX][OZ_TILED_V + 1];
   const int side = blockIdx.y;
   const cplx* X = side ? B : A;
   const int ld = side ? ldb : lda, cnt = side ? nn : m;
-  const int v0 = blockIdx.x * 32;
+  const int v0 = blockIdx.x * OZ_TILED_V;
   if (v0 >= cnt) return;
   if (active) {   // only the first 4p inner indices are live (delayed-update flush)
     const int kk = 4 * *active;
     if (kk == 0) return;
     if (kk < K) K = kk;
   }
-  for (int idx = threadIdx.x; idx < Kpad * 32; idx += blockDim.x) {
-    const int k = idx >> 5, v = idx & 31;
+  for (int idx = threadIdx.x; idx < Kpad * OZ_TILED_V; idx += blockDim.x) {
+    const int k = idx / OZ_TILED_V, v = idx % OZ_TILED_V;
     tile[k][v] = (k < K && v0 + v < cnt) ? X[(size_t)k * ld + v0 + v] : cmake(0.0, 0.0);
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const size_t Kp = 2 * (size_t)Kpad;
-  for (int v = wid; v < 32; v += blockDim.x >> 5) {
+  for (int v = wid; v < OZ_TILED_V; v += blockDim.x >> 5) {
     const int vec = v0 + v;
     if (vec >= cnt) break;
     int me = 0;
@@ -428,6 +429,31 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
   for (int c = 0; c < 16; ++c) v[c] = __uint_as_float(r[c]);
 }
 
+// (double)v 2^e, rounded to nearest even exactly as __ll2double_rn(v) * 2^e
+// whenever the result is a normal double, computed on the integer units;
+// results outside the normal range take the FP64 route.
+__device__ __forceinline__ double ll_ldexp(long long v, int e) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = v < 0 ? 0x8000000000000000ull : 0ull;
+  unsigned long long m = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  int msb = 63 - __clzll((long long)m);
+  if (msb > 52) {
+    const int sh = msb - 52;
+    unsigned long long q = m >> sh;
+    const unsigned long long r = m & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    if (r > half || (r == half && (q & 1ull))) {
+      ++q;
+      if (q >> 53) { q >>= 1; ++msb; }
+    }
+    m = q;
+  } else {
+    m <<= (52 - msb);
+  }
+  const int be = msb + e + 1023;
+  if (be <= 0 || be >= 2047) return ldexp(__ll2double_rn(v), e);
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | (m & 0xFFFFFFFFFFFFFull)));
+}
+
 struct TcMaps {
   CUtensorMap a, bre, bim;   // (Kp, rows, S) BF16 slices, box (64, 128 | 32, 1), 128-byte swizzle
 };
@@ -578,6 +604,36 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
                 atomicAdd(qa + 1, (unsigned long long)ai[c]);
               }
             }
+          } else if (INT && plain && !a.rs && !a.cs) {
+            // the scale sA sB 2^-bits(S+1) is a power of two: the value is the
+            // exact integer converted with that exponent on the integer units
+            // (GB300 issues FP64 at a small fraction of its integer rate); the
+            // only FP64 operation left is the addition of the old C (beta = 1)
+            const int e_row = expo_field(a.sA[row]) - 1023 - a.bits * (S + 1);
+            const bool neg = a.alpha.x < 0.0, add = a.beta.x != 0.0;
+            int e_col[16];
+            cplx cold[16];
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+              const int col = j0 + 16 * h + c;
+              e_col[c] = 0;
+              cold[c] = cmake(0.0, 0.0);
+              if (col < a.n) {
+                e_col[c] = expo_field(a.sB[col]) - 1023;
+                if (add) cold[c] = a.C[(size_t)col * a.ldc + row];
+              }
+            }
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+              const int col = j0 + 16 * h + c;
+              if (col < a.n) {
+                const long long vr = neg ? -(long long)ar[c] : (long long)ar[c];
+                const long long vi = neg ? -(long long)ai[c] : (long long)ai[c];
+                cplx v = cmake(ll_ldexp(vr, e_row + e_col[c]), ll_ldexp(vi, e_row + e_col[c]));
+                if (add) v = cadd(cold[c], v);
+                a.C[(size_t)col * a.ldc + row] = v;
+              }
+            }
           } else {
             // every load (scales, old C) is issued before the first store, so
             // they are in flight together instead of one memory latency per column
@@ -711,7 +767,7 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
   const bool tiled = opA == 'N' && opB == 'T' && Kpad <= OZ_TILED_KMAX;
   if (tiled) {
     const int vecs = m > nn ? m : nn;
-    k_oz_split_tiled<<<dim3((vecs + 31) / 32, 2), 256, 0, st>>>(A, lda, m, B, ldb, nn, k, Kpad, S, bits, As, Bre, Bim,
+    k_oz_split_tiled<<<dim3((vecs + OZ_TILED_V - 1) / OZ_TILED_V, 2), 32 * OZ_TILED_V, 0, st>>>(A, lda, m, B, ldb, nn, k, Kpad, S, bits, As, Bre, Bim,
                                                                sA, sB, active);
   } else {
     k_oz_split_rows<<<m, 128, 0, st>>>(A, lda, opA, m, k, Kpad, S, bits, As, sA, active);
