@@ -793,11 +793,7 @@ int local_updates_dev(dqmc_handle* h, const double* delta_dev, const double* uni
     return DQMC_OK;
   }
   const int n = h->n, k = h->delay;
-  static const int priority = [] {
-    const char* e = std::getenv("DQMC_LOCAL_PRIORITY");
-    return e && e[0] == '0' ? 0 : 1;
-  }();
-  DelayedArgs d{h->Xd, h->Yd, h->dstate, k, h->prep, h->blk, h->pub, priority};
+  DelayedArgs d{h->Xd, h->Yd, h->dstate, k, h->prep, h->blk, h->pub};
   LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_prepare(a, h->prep, h->dstate, h->st));
   const int rounds = (h->N + k - 1) / k + 1;
   for (int r = 0; r < rounds; ++r) {

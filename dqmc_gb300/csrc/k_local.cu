@@ -615,91 +615,10 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
     if (!s_acc) continue;
     // ---- new factor columns: X[:, J+k] = (G_cur[:, i + qN] - I[:, i + qN]) adj(M),
     //      Y[J+k, :] = Delta G_cur[i + qN, :] / det  (X Y = (G_cur - I) M^-1 Delta G_cur) ----
-    // The owned site among the next two (i + 1, i + 2), if any and if the
-    // round goes on, comes first, on all eight warps, and is published at
-    // once: the next decisions wait on it.  Warps 0-3 form its X row r = wid,
-    // warps 4-7 its Y column c = wid - 4; lane = 8 q + part sums every 8th
-    // pending column, then the parts are added by shuffles.
-    int t_pri = -1;
-    if (d.priority && p + 1 < d.k) {
-      for (int jn = i + 1; jn <= i + 2 && jn < N; ++jn)
-        if (jn % (int)gridDim.x == (int)blockIdx.x) { t_pri = (jn - (int)blockIdx.x) / (int)gridDim.x; break; }
-    }
-    if (t_pri >= 0) {
-      const int j = blockIdx.x + t_pri * gridDim.x;
-      const bool isXp = wid < 4;
-      const int rcs = wid & 3, q = lane >> 3, part = lane & 7;
-      const int rc = j + rcs * N;   // X: row rc; Y: column rc
-      cplx gq;
-      if (isXp) {
-        gq = ldcg_c(&a.G[(size_t)(i + q * N) * n + rc]);
-        if (rc == i + q * N) gq.x -= 1.0;
-      } else {
-        gq = ldcg_c(&a.G[(size_t)rc * n + i + q * N]);
-      }
-      const cplx* own = CACHE ? (isXp ? s_xrow : s_ycol) + (size_t)(4 * t_pri + rcs) * K4 : nullptr;
-      cplx sum = cmake(0.0, 0.0);
-      if (isXp) {
-        if (CACHE) {
-          for (int jj = part; jj < J; jj += 8) sum = cfma(own[jj], Ysm[4 * jj + q], sum);
-        } else {
-          for (int jj = part; jj < J; jj += 8) sum = cfma(ldcg_c(&d.X[(size_t)jj * n + rc]), Ysm[4 * jj + q], sum);
-        }
-      } else {
-        if (CACHE) {
-          for (int jj = part; jj < J; jj += 8) sum = cfma(Xsm[(size_t)q * K4 + jj], own[jj], sum);
-        } else {
-          for (int jj = part; jj < J; jj += 8) sum = cfma(Xsm[(size_t)q * K4 + jj], ldcg_c(&d.Y[(size_t)jj * n + rc]), sum);
-        }
-      }
-      sum = cadd(sum, shfl_c(sum, lane ^ 1));
-      sum = cadd(sum, shfl_c(sum, lane ^ 2));
-      sum = cadd(sum, shfl_c(sum, lane ^ 4));
-      const cplx gcur = cadd(gq, sum);   // G_cur[rc, i + qN] (- delta) or G_cur[i + qN, rc], in lanes 8q..8q+7
-      const cplx g0 = shfl_c(gcur, 0), g1 = shfl_c(gcur, 8), g2 = shfl_c(gcur, 16), g3 = shfl_c(gcur, 24);
-      if (lane < 4) {
-        const int ko = lane;
-        cplx prod;
-        if (isXp) {
-          prod = cmul(g0, s_adj[slot][ko]);
-          prod = cfma(g1, s_adj[slot][4 + ko], prod);
-          prod = cfma(g2, s_adj[slot][8 + ko], prod);
-          prod = cfma(g3, s_adj[slot][12 + ko], prod);
-          d.X[(size_t)(J + ko) * n + rc] = prod;
-          s_xn[4 * rcs + ko] = prod;             // X_new[j + rcs N, k]
-        } else {
-          const cplx det = s_det[slot];
-          const double rd = 1.0 / (det.x * det.x + det.y * det.y);
-          const cplx inv = cmake(det.x * rd, -det.y * rd);
-          prod = cmul(s_delta[4 * ko], g0);
-          prod = cfma(s_delta[4 * ko + 1], g1, prod);
-          prod = cfma(s_delta[4 * ko + 2], g2, prod);
-          prod = cfma(s_delta[4 * ko + 3], g3, prod);
-          prod = cmul(prod, inv);
-          d.Y[(size_t)(J + ko) * n + rc] = prod;
-          s_yn[4 * ko + rcs] = prod;             // Y_new[k, j + rcs N]
-        }
-        if (CACHE) const_cast<cplx*>(own)[J + ko] = prod;
-      }
-      __syncthreads();
-      if (wid == 0 && lane < 16) {
-        const int r = lane >> 2, c = lane & 3;
-        cplx bk = s_blk[16 * t_pri + lane];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) bk = cfma(s_xn[4 * r + k], s_yn[4 * k + c], bk);
-        s_blk[16 * t_pri + lane] = bk;
-        d.blk[(size_t)16 * j + lane] = bk;
-      }
-      __syncthreads();   // every store of the site precedes its publication
-      if (threadIdx.x == 0) {
-        __threadfence();
-        *(volatile int*)(d.pub + j) = p + 1;
-      }
-    }
-    // the other owned sites in passes of 4: site t of a pass -> warps 2t (X rows) and 2t+1 (Y columns)
+    // owned sites in passes of 4: site t of a pass -> warps 2t (X rows) and 2t+1 (Y columns)
     for (int t0 = 0; t0 < owned; t0 += 4) {
       const int ts = t0 + (wid >> 1);
-      if (ts < owned && ts != t_pri) {
+      if (ts < owned) {
         const int j = blockIdx.x + ts * gridDim.x;
         const int rc = j + sub * N;   // X: row rc; Y: column rc
         cplx gq = gq_pref;
@@ -759,7 +678,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
       if (!(wid & 1) && lane < 16) {
         const int ls = wid >> 1, tsr = t0 + ls;
         const int j = blockIdx.x + tsr * gridDim.x;
-        if (tsr < owned && tsr != t_pri && j > i) {
+        if (tsr < owned && j > i) {
           const int r = lane >> 2, c = lane & 3;
           cplx b = s_blk[16 * tsr + lane];
 #pragma unroll

@@ -312,7 +312,7 @@ __global__ void k_oz_finalize(OzArgs a) {
 // columns), so one pass over K serves every slice pair and each K block of
 // every slice is staged once:
 //   * warp 0 (one lane) streams, per K block of 64, the S B-slices (double-
-//     buffered) and the S A-slices (a ring of 4) with cp.async.bulk.tensor
+//     buffered) and the S A-slices (a ring of 6) with cp.async.bulk.tensor
 //     (128-byte swizzle) onto mbarriers;
 //   * warp 1 allocates TMEM, and one lane issues tcgen05.mma for every pair
 //     (p, q) with p + q <= S + 1 into group p + q, releasing each A slot and
@@ -326,7 +326,7 @@ constexpr int TC_BM = 128;                      // rows of C per CTA (TMEM lanes
 constexpr int TC_BN = 32;                       // complex columns of C per CTA (MMA N = 64)
 constexpr int TC_BK = 64;                       // BF16 per K block: one 128-byte swizzle row
 constexpr int TC_MAXS = 8;                      // S groups x 64 TMEM columns <= 512
-constexpr int TC_ARING = 4;                     // A-slice stages
+constexpr int TC_ARING = 6;                     // A-slice stages (S <= 6: one K block of A in flight)
 constexpr int TC_THREADS = 192;                 // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr int TC_A_TILE = TC_BM * TC_BK * 2;    // 16 KB
 constexpr int TC_B_HALF = TC_BN * TC_BK * 2;    // 4 KB: 32 rows of B'_re or of B'_im
@@ -416,18 +416,16 @@ __device__ __forceinline__ void tc_commit(uint32_t bar) {
 }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-// 32 TMEM lanes (this warp's quarter) x 16 consecutive 32-bit columns
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
+// 32 TMEM lanes (this warp's quarter) x 16 consecutive 32-bit columns; the
+// registers are valid after tc_wait_ld
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t* r) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
         "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int c = 0; c < 16; ++c) v[c] = __uint_as_float(r[c]);
 }
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // (double)v 2^e, rounded to nearest even exactly as __ll2double_rn(v) * 2^e
 // whenever the result is a normal double, computed on the integer units;
@@ -506,9 +504,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
     // ---- TMA producer ----
     if (lane == 0 && kb0 < kb1) {
       int a_use = 0;
-      for (int kb = kb0; kb < kb1 && !*s_abort; ++kb) {
+      int b_next = kb0;   // next K block whose B slices are to be issued
+      // the B slices of block kb into buffer (kb - kb0) & 1, once it is free;
+      // block = false only tests whether it is free
+      auto issue_b = [&](int kb, bool block) -> bool {
         const int bu = kb - kb0, bb = bu & 1;
-        if (!mbar_wait(bar(2 + bb), ((bu >> 1) & 1) ^ 1, err, s_abort)) break;
+        const uint32_t parity = ((bu >> 1) & 1) ^ 1;
+        if (block ? !mbar_wait(bar(2 + bb), parity, err, s_abort) : !mbar_test(bar(2 + bb), parity)) return false;
         armed[bb] = bu + 1;
         mbar_expect_tx(bar(bb), (uint32_t)(S * TC_B_TILE));
         for (int q = 0; q < S; ++q) {
@@ -516,7 +518,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
           tma_load3(dst, &maps.bre, bar(bb), kb * TC_BK, j0, q);
           tma_load3(dst + TC_B_HALF, &maps.bim, bar(bb), kb * TC_BK, j0, q);
         }
+        return true;
+      };
+      for (int kb = kb0; kb < kb1 && !*s_abort; ++kb) {
+        if (b_next == kb) {
+          if (!issue_b(kb, true)) break;
+          ++b_next;
+        }
         for (int p = 0; p < S; ++p, ++a_use) {
+          // the next block's B as early as its buffer is free (without waiting)
+          if (b_next == kb + 1 && kb + 1 < kb1 && issue_b(kb + 1, false)) ++b_next;
           const int slot = a_use % TC_ARING;
           if (!mbar_wait(bar(EA + slot), ((a_use / TC_ARING) & 1) ^ 1, err, s_abort)) break;
           armed[2 + slot] = a_use / TC_ARING + 1;
@@ -557,11 +568,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
   } else {
     // ---- epilogue: warps 2-5, TMEM lane quarter (warp % 4) ----
     const int quarter = warp & 3;
+    const int row = i0 + 32 * quarter + lane;
+    // the fast path's old C values, loaded while the MMAs still run
+    const bool fast = INT && oz_plain(a) && !a.rs && !a.cs && !a.acc;
+    const bool add = a.beta.x != 0.0;
+    // (one half of the tile's columns at a time: those of half 0 now, those
+    // of half 1 once half 0 is stored, ahead of half 1's accumulator reads)
+    cplx pre[16];
+    auto prefetch = [&](int h) {
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const int col = j0 + 16 * h + c;
+        pre[c] = (fast && add && row < a.m && col < a.n) ? a.C[(size_t)col * a.ldc + row] : cmake(0.0, 0.0);
+      }
+    };
+    prefetch(0);
     const bool waited = mbar_wait(bar(ACC), 0, err, s_abort);
     // tcgen05.ld is warp-collective: the decision must be uniform over the warp
     const bool have = __all_sync(0xffffffffu, waited && kb0 < kb1 && !*s_abort);
     tc_fence_after();
-    const int row = i0 + 32 * quarter + lane;
     const uint32_t tq = tmem + ((uint32_t)(32 * quarter) << 16);
     const double wint = INT ? ldexp(1.0, -a.bits * (S + 1)) : 1.0;
     const bool plain = oz_plain(a);
@@ -574,9 +599,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
         for (int c = 0; c < 16; ++c) { ar[c] = 0; ai[c] = 0; }
 #pragma unroll 1
         for (int g = 0; g < S; ++g) {
+          uint32_t ur[16], ui[16];
+          tc_ld16(tq + (uint32_t)(g * 2 * TC_BN + 16 * h), ur);
+          tc_ld16(tq + (uint32_t)(g * 2 * TC_BN + TC_BN + 16 * h), ui);
+          tc_wait_ld();
           float vr[16], vi[16];
-          tc_ld16(tq + (uint32_t)(g * 2 * TC_BN + 16 * h), vr);
-          tc_ld16(tq + (uint32_t)(g * 2 * TC_BN + TC_BN + 16 * h), vi);
+#pragma unroll
+          for (int c = 0; c < 16; ++c) { vr[c] = __uint_as_float(ur[c]); vi[c] = __uint_as_float(ui[c]); }
           if constexpr (INT) {
             const long long step = 1ll << a.bits;
 #pragma unroll
@@ -604,24 +633,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
                 atomicAdd(qa + 1, (unsigned long long)ai[c]);
               }
             }
-          } else if (INT && plain && !a.rs && !a.cs) {
+          } else if (fast) {
             // the scale sA sB 2^-bits(S+1) is a power of two: the value is the
             // exact integer converted with that exponent on the integer units
             // (GB300 issues FP64 at a small fraction of its integer rate); the
             // only FP64 operation left is the addition of the old C (beta = 1)
             const int e_row = expo_field(a.sA[row]) - 1023 - a.bits * (S + 1);
-            const bool neg = a.alpha.x < 0.0, add = a.beta.x != 0.0;
+            const bool neg = a.alpha.x < 0.0;
             int e_col[16];
-            cplx cold[16];
 #pragma unroll
             for (int c = 0; c < 16; ++c) {
               const int col = j0 + 16 * h + c;
-              e_col[c] = 0;
-              cold[c] = cmake(0.0, 0.0);
-              if (col < a.n) {
-                e_col[c] = expo_field(a.sB[col]) - 1023;
-                if (add) cold[c] = a.C[(size_t)col * a.ldc + row];
-              }
+              e_col[c] = col < a.n ? expo_field(a.sB[col]) - 1023 : 0;
             }
 #pragma unroll
             for (int c = 0; c < 16; ++c) {
@@ -630,7 +653,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
                 const long long vr = neg ? -(long long)ar[c] : (long long)ar[c];
                 const long long vi = neg ? -(long long)ai[c] : (long long)ai[c];
                 cplx v = cmake(ll_ldexp(vr, e_row + e_col[c]), ll_ldexp(vi, e_row + e_col[c]));
-                if (add) v = cadd(cold[c], v);
+                if (add) v = cadd(pre[c], v);
                 a.C[(size_t)col * a.ldc + row] = v;
               }
             }
@@ -666,6 +689,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
             }
           }
         }
+        if (h == 0) prefetch(1);
       }
     }
   }

@@ -66,7 +66,6 @@ struct DelayedArgs {
   const SitePrep* prep;    // (N) from launch_local_prepare for this slice
   cplx* blk;               // (N, 16) cache of the diagonal blocks G_cur[j + rN, j + cN]
   int* pub;                // (N) acceptances of the current round folded into site j's data
-  int priority;            // form and publish the owned one of the next two sites first
 };
 cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d, int sm_count, cudaStream_t st,
                                  int max_grid = 0);
