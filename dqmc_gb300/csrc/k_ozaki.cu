@@ -573,16 +573,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
     const bool fast = INT && oz_plain(a) && !a.rs && !a.cs && !a.acc;
     const bool add = a.beta.x != 0.0;
     // (one half of the tile's columns at a time: those of half 0 now, those
-    // of half 1 once half 0 is stored, ahead of half 1's accumulator reads)
+    // of half 1 once half 0 is stored, ahead of half 1's accumulator reads;
+    // the array is indexed only by unrolled constants, so it stays in
+    // registers: with most of shared memory carved out, local memory is slow)
     cplx pre[16];
-    auto prefetch = [&](int h) {
 #pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        const int col = j0 + 16 * h + c;
-        pre[c] = (fast && add && row < a.m && col < a.n) ? a.C[(size_t)col * a.ldc + row] : cmake(0.0, 0.0);
-      }
-    };
-    prefetch(0);
+    for (int c = 0; c < 16; ++c) {
+      const int col = j0 + c;
+      pre[c] = (fast && add && row < a.m && col < a.n) ? a.C[(size_t)col * a.ldc + row] : cmake(0.0, 0.0);
+    }
     const bool waited = mbar_wait(bar(ACC), 0, err, s_abort);
     // tcgen05.ld is warp-collective: the decision must be uniform over the warp
     const bool have = __all_sync(0xffffffffu, waited && kb0 < kb1 && !*s_abort);
@@ -689,7 +688,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
             }
           }
         }
-        if (h == 0) prefetch(1);
+        if (h == 0) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const int col = j0 + 16 + c;
+            pre[c] = (fast && add && row < a.m && col < a.n) ? a.C[(size_t)col * a.ldc + row] : cmake(0.0, 0.0);
+          }
+        }
       }
     }
   }
