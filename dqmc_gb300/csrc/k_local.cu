@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   GridBarrierExit bar_exit(a.bar);
   const ModelConst& mc = a.mc;
   const int N = mc.N, n = mc.n, L = mc.L, K4 = 4 * d.k;
-  __shared__ int s_first, s_ok, s_acc;
+  __shared__ int s_first, s_ok;
   if (threadIdx.x == 0) s_first = __ldcg(&d.state[0]);
   __syncthreads();
   const int first = s_first;
@@ -461,6 +461,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   __shared__ cplx s_adj[2][16];     // adj(M)[r][c] (double-buffered by site parity)
   __shared__ cplx s_det[2];
   __shared__ double s_expds[2];
+  __shared__ double s_u[2];         // Metropolis uniform of the site
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int l = a.slice0;
   for (int k = threadIdx.x; k < 3 * N; k += blockDim.x) phis[k] = a.phi[(size_t)3 * N * l + k];
@@ -558,6 +559,8 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         dS += 0.5 * mc.dtau * (__ldcg(&sp->dsQ) - 2.0 * sdot);
         dS += __ldcg(&sp->dsB);
         s_expds[slot] = exp(-dS);
+      } else if (lane == 1) {
+        s_u[slot] = __ldg(&a.unif[i]);
       }
     } else if (wid == 7 && lane < 16) {
       s_delta[lane] = ldcg_c(&sp->delta[lane]);
@@ -585,15 +588,14 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
       }
     }
     __syncthreads();
-    // ---- Metropolis decision (thread 0; the same in every CTA) ----
+    // ---- Metropolis decision: every thread evaluates it from the same shared
+    //      values (the same in every CTA); thread 0 writes its effects ----
+    const cplx det = s_det[slot];
+    const double exp_dS = s_expds[slot];
+    const double pacc = exp_dS * det.x;
+    const bool bad = !isfinite(det.x) || !isfinite(det.y) || (det.x == 0.0 && det.y == 0.0);
+    const bool acc = !bad && (pacc > 1.0 || s_u[slot] < pacc);
     if (threadIdx.x == 0) {
-      const cplx det = s_det[slot];
-      const double exp_dS = s_expds[slot];
-      const double pacc = exp_dS * det.x;
-      const double u = __ldg(&a.unif[i]);
-      const bool bad = !isfinite(det.x) || !isfinite(det.y) || (det.x == 0.0 && det.y == 0.0);
-      const bool acc = !bad && (pacc > 1.0 || u < pacc);
-      s_acc = acc;
       if (acc)
         for (int q = 0; q < 3; ++q) phis[3 * i + q] += a.delta[3 * i + q];
       if (blockIdx.x == 0) {
@@ -610,9 +612,9 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         }
       }
     }
-    __syncthreads();
-    // decision slots are double-buffered: a rejected site needs no further barrier
-    if (!s_acc) continue;
+    // the decision values are double-buffered by site parity: a rejected site
+    // needs no barrier here; an accepted one synchronises in the passes below
+    if (!acc) continue;
     // ---- new factor columns: X[:, J+k] = (G_cur[:, i + qN] - I[:, i + qN]) adj(M),
     //      Y[J+k, :] = Delta G_cur[i + qN, :] / det  (X Y = (G_cur - I) M^-1 Delta G_cur) ----
     // owned sites in passes of 4: site t of a pass -> warps 2t (X rows) and 2t+1 (Y columns)

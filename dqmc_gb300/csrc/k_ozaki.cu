@@ -317,9 +317,11 @@ __global__ void k_oz_finalize(OzArgs a) {
 //   * warp 1 allocates TMEM, and one lane issues tcgen05.mma for every pair
 //     (p, q) with p + q <= S + 1 into group p + q, releasing each A slot and
 //     B buffer with tcgen05.commit;
-//   * warps 2-5 (one per TMEM lane quarter) wait for the final commit, read
-//     the S exact FP32 group sums with tcgen05.ld and combine them exactly in
-//     64-bit integers (Horner in 2^bits), then scale and store as before.
+//   * all 8 warps (two per TMEM lane quarter, one half of the columns each;
+//     warps 0 and 1 once they have issued everything) wait for the final
+//     commit, read the S exact FP32 group sums with tcgen05.ld and combine
+//     them exactly in 64-bit integers (Horner in 2^bits), then scale and
+//     store as before.
 // Every wait is bounded; on a timeout the kernel sets an error bit, drains
 // what it issued (bounded) and frees its TMEM.
 constexpr int TC_BM = 128;                      // rows of C per CTA (TMEM lanes)
@@ -327,7 +329,7 @@ constexpr int TC_BN = 32;                       // complex columns of C per CTA 
 constexpr int TC_BK = 64;                       // BF16 per K block: one 128-byte swizzle row
 constexpr int TC_MAXS = 8;                      // S groups x 64 TMEM columns <= 512
 constexpr int TC_ARING = 6;                     // A-slice stages (S <= 6: one K block of A in flight)
-constexpr int TC_THREADS = 192;                 // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr int TC_THREADS = 256;                 // warp 0 TMA, warp 1 MMA, then all 8 warps the epilogue
 constexpr int TC_A_TILE = TC_BM * TC_BK * 2;    // 16 KB
 constexpr int TC_B_HALF = TC_BN * TC_BK * 2;    // 4 KB: 32 rows of B'_re or of B'_im
 constexpr int TC_B_TILE = 2 * TC_B_HALF;        // 8 KB
@@ -565,21 +567,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
       }
       tc_commit(bar(ACC));            // all accumulators final (or, on abort, all issued MMAs done)
     }
-  } else {
-    // ---- epilogue: warps 2-5, TMEM lane quarter (warp % 4) ----
+  }
+  __syncwarp();   // warps 0 and 1 join the epilogue once their issuing lane is done
+  {
+    // ---- epilogue: all 8 warps, two per TMEM lane quarter (warp % 4); warp w
+    //      takes the 16 columns of half w / 4 of the tile ----
     const int quarter = warp & 3;
+    const int h = warp >> 2;
     const int row = i0 + 32 * quarter + lane;
-    // the fast path's old C values, loaded while the MMAs still run
+    // the fast path's old C values, loaded while the MMAs still run (the array
+    // is indexed only by unrolled constants, so it stays in registers)
     const bool fast = INT && oz_plain(a) && !a.rs && !a.cs && !a.acc;
     const bool add = a.beta.x != 0.0;
-    // (one half of the tile's columns at a time: those of half 0 now, those
-    // of half 1 once half 0 is stored, ahead of half 1's accumulator reads;
-    // the array is indexed only by unrolled constants, so it stays in
-    // registers: with most of shared memory carved out, local memory is slow)
     cplx pre[16];
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
-      const int col = j0 + c;
+      const int col = j0 + 16 * h + c;
       pre[c] = (fast && add && row < a.m && col < a.n) ? a.C[(size_t)col * a.ldc + row] : cmake(0.0, 0.0);
     }
     const bool waited = mbar_wait(bar(ACC), 0, err, s_abort);
@@ -590,8 +593,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
     const double wint = INT ? ldexp(1.0, -a.bits * (S + 1)) : 1.0;
     const bool plain = oz_plain(a);
     if (have) {
-#pragma unroll 1
-      for (int h = 0; h < 2; ++h) {
+      {
         typedef typename std::conditional<INT, long long, double>::type acc_t;
         acc_t ar[16], ai[16];
 #pragma unroll
@@ -686,13 +688,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
                 a.C[(size_t)col * a.ldc + row] = oz_combine(a, cmake(vr * f, vi * f), cold[c], plain);
               }
             }
-          }
-        }
-        if (h == 0) {
-#pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            const int col = j0 + 16 + c;
-            pre[c] = (fast && add && row < a.m && col < a.n) ? a.C[(size_t)col * a.ldc + row] : cmake(0.0, 0.0);
           }
         }
       }
