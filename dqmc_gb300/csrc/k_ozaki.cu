@@ -429,30 +429,25 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t* r) {
 }
 __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// (double)v 2^e, rounded to nearest even exactly as __ll2double_rn(v) * 2^e
-// whenever the result is a normal double, computed on the integer units;
-// results outside the normal range take the FP64 route.
+// (double)v 2^e, rounded to nearest even exactly as __ll2double_rn(v) * 2^e,
+// on the integer units and without branches, for -1022 <= e <= 960 (every
+// |v| < 2^63 then gives a normal double): |v| is shifted so that its leading
+// one sits at bit 63, the 53 high bits are rounded to nearest even at bit 11,
+// and a carry out of the significand steps the biased exponent by addition.
 __device__ __forceinline__ double ll_ldexp(long long v, int e) {
-  if (v == 0) return 0.0;
-  const unsigned long long sgn = v < 0 ? 0x8000000000000000ull : 0ull;
-  unsigned long long m = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
-  int msb = 63 - __clzll((long long)m);
-  if (msb > 52) {
-    const int sh = msb - 52;
-    unsigned long long q = m >> sh;
-    const unsigned long long r = m & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
-    if (r > half || (r == half && (q & 1ull))) {
-      ++q;
-      if (q >> 53) { q >>= 1; ++msb; }
-    }
-    m = q;
-  } else {
-    m <<= (52 - msb);
-  }
-  const int be = msb + e + 1023;
-  if (be <= 0 || be >= 2047) return ldexp(__ll2double_rn(v), e);
-  return __longlong_as_double((long long)(sgn | ((unsigned long long)be << 52) | (m & 0xFFFFFFFFFFFFFull)));
+  const unsigned long long sgn = (unsigned long long)v & 0x8000000000000000ull;
+  const unsigned long long m = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  const int lz = __clzll((long long)m) & 63;   // 64 for m = 0, masked; the select below covers it
+  const unsigned long long mn = m << lz;
+  unsigned long long q = mn >> 11;
+  const unsigned rem = (unsigned)mn & 0x7FFu;
+  q += (rem + (unsigned)(q & 1ull)) > 0x400u ? 1ull : 0ull;
+  const long long be = 63 - lz + e + 1023;
+  const unsigned long long bits = sgn | ((unsigned long long)(be - 1) << 52) + q;
+  return m ? __longlong_as_double((long long)bits) : 0.0;
 }
+// the exponent window in which ll_ldexp is exact for every 64-bit value
+__device__ __forceinline__ bool ll_ldexp_safe(int e) { return e >= -1022 && e <= 960; }
 
 struct TcMaps {
   CUtensorMap a, bre, bim;   // (Kp, rows, S) BF16 slices, box (64, 128 | 32, 1), 128-byte swizzle
@@ -647,15 +642,34 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
               const int col = j0 + 16 * h + c;
               e_col[c] = col < a.n ? expo_field(a.sB[col]) - 1023 : 0;
             }
+            bool safe = true;
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
-              const int col = j0 + 16 * h + c;
-              if (col < a.n) {
-                const long long vr = neg ? -(long long)ar[c] : (long long)ar[c];
-                const long long vi = neg ? -(long long)ai[c] : (long long)ai[c];
-                cplx v = cmake(ll_ldexp(vr, e_row + e_col[c]), ll_ldexp(vi, e_row + e_col[c]));
-                if (add) v = cadd(pre[c], v);
-                a.C[(size_t)col * a.ldc + row] = v;
+            for (int c = 0; c < 16; ++c) safe = safe && ll_ldexp_safe(e_row + e_col[c]);
+            if (safe) {
+#pragma unroll
+              for (int c = 0; c < 16; ++c) {
+                const int col = j0 + 16 * h + c;
+                if (col < a.n) {
+                  const long long vr = neg ? -(long long)ar[c] : (long long)ar[c];
+                  const long long vi = neg ? -(long long)ai[c] : (long long)ai[c];
+                  cplx v = cmake(ll_ldexp(vr, e_row + e_col[c]), ll_ldexp(vi, e_row + e_col[c]));
+                  if (add) v = cadd(pre[c], v);
+                  a.C[(size_t)col * a.ldc + row] = v;
+                }
+              }
+            } else {
+              // results that may leave the normal range: the FP64 route (unrolled,
+              // so that the arrays keep constant indices and stay in registers)
+#pragma unroll
+              for (int c = 0; c < 16; ++c) {
+                const int col = j0 + 16 * h + c;
+                if (col < a.n) {
+                  const long long vr = neg ? -(long long)ar[c] : (long long)ar[c];
+                  const long long vi = neg ? -(long long)ai[c] : (long long)ai[c];
+                  cplx v = cmake(ldexp(__ll2double_rn(vr), e_row + e_col[c]), ldexp(__ll2double_rn(vi), e_row + e_col[c]));
+                  if (add) v = cadd(pre[c], v);
+                  a.C[(size_t)col * a.ldc + row] = v;
+                }
               }
             }
           } else {
