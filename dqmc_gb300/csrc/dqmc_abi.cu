@@ -125,9 +125,20 @@ struct dqmc_handle {
     int64_t cnt[DQMC_NKINDS] = {};
     double flops[DQMC_NKINDS] = {}, bytes[DQMC_NKINDS] = {};
     int64_t launches = 0;
+    int while_nodes = 0;      // captured round loops (one body each in the counts above)
   };
   std::vector<SweepGraph> graphs;
   bool graphs_off = false;    // capture refused once: direct launches from then on
+  // delayed rounds inside a captured sweep: a WHILE node repeats [round, flush]
+  // only while sites remain; its body is captured on st_body
+  cudaStream_t st_body = nullptr;
+  bool while_off = false;     // conditional nodes refused once: fixed round count from then on
+  int capture_while = 0;      // WHILE nodes added in the capture in progress
+  int pending_while = 0;      // WHILE nodes of the enqueued sweep
+  unsigned long long rounds_seen = 0;   // device round counter at the last sweep_finish
+  int64_t body_cnt[DQMC_NKINDS] = {};   // launches, flops and bytes of one round body
+  double body_flops[DQMC_NKINDS] = {}, body_bytes[DQMC_NKINDS] = {};
+  int64_t body_launches = 0;
   cudaEvent_t done = nullptr; // end of the last enqueued sweep (batch pipelining)
   std::vector<TimedSpan> spans;
   std::vector<cudaEvent_t> event_pool;
@@ -759,6 +770,72 @@ int ensure_out_capacity(dqmc_handle* h, int calls) {
   return DQMC_OK;
 }
 
+// Inside a stream capture: appends a WHILE node whose body is one delayed
+// round and its flush followed by k_round_cond, which continues the loop while
+// sites of the slice remain (at most max_rounds times).  A slice then runs
+// only the rounds that carry work instead of the fixed bound.  Returns
+// kWhileRefused, with the capture untouched, when the runtime refuses
+// conditional nodes; the caller then captures the fixed round count.
+constexpr int kWhileRefused = 1;   // internal: conditional nodes refused (never returned by the ABI)
+
+template <class Round>
+int capture_round_loop(dqmc_handle* h, int max_rounds, Round&& round) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  if (cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess || !g) {
+    cudaGetLastError();
+    h->while_off = true;
+    return kWhileRefused;
+  }
+  cudaGraphConditionalHandle hc;
+  if (cudaGraphConditionalHandleCreate(&hc, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+    cudaGetLastError();
+    h->while_off = true;
+    return kWhileRefused;
+  }
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = hc;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp) != cudaSuccess) {
+    cudaGetLastError();
+    h->while_off = true;
+    return kWhileRefused;
+  }
+  CU(cudaStreamUpdateCaptureDependencies(h->st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  if (!h->st_body) CU(cudaStreamCreateWithFlags(&h->st_body, cudaStreamNonBlocking));
+  CU(cudaStreamBeginCaptureToGraph(h->st_body, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                   cudaStreamCaptureModeThreadLocal));
+  // the body's launches go to st_body; its counts are those of one round
+  int64_t c0[DQMC_NKINDS]; double f0[DQMC_NKINDS], b0[DQMC_NKINDS];
+  for (int q = 0; q < DQMC_NKINDS; ++q) { c0[q] = h->cnt[q]; f0[q] = h->flops[q]; b0[q] = h->bytes[q]; }
+  const int64_t l0 = h->launches;
+  cudaStream_t main_st = h->st;
+  h->st = h->st_body;
+  int rc = round();
+  if (rc == DQMC_OK) {
+    KSpan ks_(h, DQMC_K_LOCAL, 0.0, 0.0);
+    if (launch_round_cond(hc, h->dstate, h->N, max_rounds, h->err_d,
+                          reinterpret_cast<unsigned long long*>(h->dstate + 4), h->st) != cudaSuccess)
+      rc = set_err(h, DQMC_ERR_CUDA, "round condition launch failed");
+  }
+  h->st = main_st;
+  cudaGraph_t body = nullptr;
+  const bool ended = cudaStreamEndCapture(h->st_body, &body) == cudaSuccess;
+  if (rc != DQMC_OK) return rc;
+  if (!ended) return set_err(h, DQMC_ERR_CUDA, "capture of the round loop body failed");
+  for (int q = 0; q < DQMC_NKINDS; ++q) {
+    h->body_cnt[q] = h->cnt[q] - c0[q]; h->body_flops[q] = h->flops[q] - f0[q]; h->body_bytes[q] = h->bytes[q] - b0[q];
+  }
+  h->body_launches = h->launches - l0;
+  ++h->capture_while;
+  return DQMC_OK;
+}
+
 // local_updates (src/local_updates.jl:1-38) on device streams; outputs to
 // device arrays (may be null).  delay <= 1: immediate rank-4 updates in one
 // cooperative launch.  delay = k > 1: rounds of [local kernel until k accepts
@@ -796,13 +873,20 @@ int local_updates_dev(dqmc_handle* h, const double* delta_dev, const double* uni
   DelayedArgs d{h->Xd, h->Yd, h->dstate, k, h->prep, h->blk, h->pub};
   LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_prepare(a, h->prep, h->dstate, h->st));
   const int rounds = (h->N + k - 1) / k + 1;
-  for (int r = 0; r < rounds; ++r) {
+  auto round = [&]() -> int {
     LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_delayed(a, d, h->sm_count, h->st, h->coop_cap));
     // flush G += X Y over the 4p pending columns (p read on the device; no
     // work when p = 0); the next round clears p
-    CHK(zgemm_general(h, n, n, 4 * k, 'N', 'T', cmake(1, 0), h->Xd, n, h->Yd, n, cmake(1, 0), h->G, n, nullptr,
-                      nullptr, true, DQMC_K_FLUSH, h->dstate + 1));
+    return zgemm_general(h, n, n, 4 * k, 'N', 'T', cmake(1, 0), h->Xd, n, h->Yd, n, cmake(1, 0), h->G, n, nullptr,
+                         nullptr, true, DQMC_K_FLUSH, h->dstate + 1);
+  };
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CU(cudaStreamIsCapturing(h->st, &cs));
+  if (cs == cudaStreamCaptureStatusActive && !h->while_off) {
+    const int r = capture_round_loop(h, rounds, round);
+    if (r != kWhileRefused) return r;
   }
+  for (int r = 0; r < rounds; ++r) CHK(round());
   return DQMC_OK;
 }
 
@@ -827,6 +911,7 @@ void free_all(dqmc_handle* h) {
   for (auto e : h->event_pool) cudaEventDestroy(e);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->st_body) cudaStreamDestroy(h->st_body);
   if (h->st) cudaStreamDestroy(h->st);
 }
 
@@ -1207,7 +1292,7 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
   if (h->delay > 1) {
     A((void**)&h->Xd, (size_t)4 * h->delay * n * sizeof(cplx));
     A((void**)&h->Yd, (size_t)4 * h->delay * n * sizeof(cplx));
-    A((void**)&h->dstate, 2 * sizeof(int));
+    A((void**)&h->dstate, 8 * sizeof(int));   // [0] next site, [1] pending, [2] rounds, [4..5] u64 rounds run
     A((void**)&h->prep, (size_t)h->N * sizeof(SitePrep));
     A((void**)&h->blk, (size_t)16 * h->N * sizeof(cplx));
     A((void**)&h->pub, (size_t)h->N * sizeof(int));
@@ -1362,6 +1447,7 @@ static dqmc_handle::SweepGraph* capture_sweep(dqmc_handle* h, int n_calls, bool 
   for (int k = 0; k < DQMC_NKINDS; ++k) { cnt0[k] = h->cnt[k]; fl0[k] = h->flops[k]; by0[k] = h->bytes[k]; }
   const int64_t l0 = h->launches;
   cudaGetLastError();
+  h->capture_while = 0;
   bool ok = cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
   int rc = DQMC_OK;
   cudaGraph_t graph = nullptr;
@@ -1377,6 +1463,7 @@ static dqmc_handle::SweepGraph* capture_sweep(dqmc_handle* h, int n_calls, bool 
     h->cnt[k] = cnt0[k]; h->flops[k] = fl0[k]; h->bytes[k] = by0[k];
   }
   g.launches = h->launches - l0;
+  g.while_nodes = h->capture_while;
   h->launches = l0;
   h->current_slice = g.slice0; h->direction = g.dir0;
   cudaGetLastError();
@@ -1420,8 +1507,10 @@ static int sweep_enqueue(dqmc_handle* h, int n_calls, const double* delta_dev, c
         g = &x;
     if (!g) g = capture_sweep(h, n_calls, acc_dev != nullptr);
   }
+  h->pending_while = 0;
   if (g) {
     CU(cudaGraphLaunch(g->exec, h->st));
+    h->pending_while = g->while_nodes;
     h->current_slice = g->slice1;
     h->direction = g->dir1;
     for (int k = 0; k < DQMC_NKINDS; ++k) { h->cnt[k] += g->cnt[k]; h->flops[k] += g->flops[k]; h->bytes[k] += g->bytes[k]; }
@@ -1442,8 +1531,24 @@ static int sweep_finish(dqmc_handle* h, dqmc_stats* stats) {
   float ms = 0.f;
   cudaEventElapsedTime(&ms, h->ev0, h->ev1);
   int cnt[2] = {0, 0};
+  unsigned long long rounds = 0;
   CU(cudaMemcpyAsync(cnt, h->nacc_d, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  if (h->pending_while > 0)
+    CU(cudaMemcpyAsync(&rounds, h->dstate + 4, sizeof(rounds), cudaMemcpyDeviceToHost, h->st));
   CU(cudaStreamSynchronize(h->st));
+  if (h->pending_while > 0) {
+    // the graph's counts hold one round body per WHILE node (a WHILE node
+    // runs its body at least once): add the rounds that ran beyond those
+    const int64_t extra = (int64_t)(rounds - h->rounds_seen) - h->pending_while;
+    h->rounds_seen = rounds;
+    for (int q = 0; q < DQMC_NKINDS; ++q) {
+      h->cnt[q] += extra * h->body_cnt[q];
+      h->flops[q] += (double)extra * h->body_flops[q];
+      h->bytes[q] += (double)extra * h->body_bytes[q];
+    }
+    h->launches += extra * h->body_launches;
+    h->pending_while = 0;
+  }
   if (stats) {
     stats->proposals = (int64_t)h->pending_calls * h->N;
     stats->accepted = cnt[0] - cnt[1];

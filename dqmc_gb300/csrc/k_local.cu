@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(128) k_local_prepare(LocalUpdateArgs a, SitePr
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * 4 + (threadIdx.x >> 5);
   // delayed rounds of this slice start from site 0 with nothing pending
-  if (state && blockIdx.x == 0 && threadIdx.x == 0) { state[0] = 0; state[1] = 0; }
+  if (state && blockIdx.x == 0 && threadIdx.x == 0) { state[0] = 0; state[1] = 0; state[2] = 0; }
   if (i >= N) return;
   const double* po = &a.phi[((size_t)N * l + i) * 3];
   const double old[3] = {po[0], po[1], po[2]};
@@ -709,7 +709,28 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   if (blockIdx.x == 0 && threadIdx.x == 0) { d.state[0] = N; d.state[1] = p; }
 }
 
+// Condition of the graph's WHILE node that repeats [delayed round, flush]:
+// one more round while sites of the slice remain, at most max_rounds rounds
+// per slice (state[2] counts them from the prepare kernel on), and none after
+// an error bit is set.  rounds_total counts every round run this way.
+__global__ void k_round_cond(cudaGraphConditionalHandle hc, int* state, int N, int max_rounds, const int* err,
+                             unsigned long long* rounds_total) {
+  if (threadIdx.x == 0) {
+    const int it = state[2] + 1;
+    state[2] = it;
+    const bool more = it < max_rounds && __ldcg(&state[0]) < N && __ldcg(err) == 0;
+    cudaGraphSetConditional(hc, more ? 1u : 0u);
+    *rounds_total += 1ull;
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_round_cond(cudaGraphConditionalHandle hc, int* state, int N, int max_rounds, const int* err,
+                              unsigned long long* rounds_total, cudaStream_t st) {
+  k_round_cond<<<1, 32, 0, st>>>(hc, state, N, max_rounds, err, rounds_total);
+  return cudaGetLastError();
+}
 
 static size_t local_smem_bytes(int N) {
   return (size_t)N * (16 * sizeof(cplx) + sizeof(EvEntry)) + (size_t)3 * N * sizeof(double);

@@ -304,24 +304,27 @@ __global__ void k_oz_finalize(OzArgs a) {
 // ---------------------------------------------------------------------------
 // tcgen05 engine: TMA-staged slices, tensor-core MMAs into TMEM accumulators
 // ---------------------------------------------------------------------------
-// One CTA computes a 128 x 32 complex tile of C.  Each MMA is
+// A CTA computes 128 x 32 complex tiles of C, persistently: one CTA per SM
+// takes tiles x, x + grid, ... and the MMAs of a tile run while the epilogue
+// of the previous one converts and stores.  Each MMA is
 // M = 128, N = 64, K = 16 (kind::f16, BF16 in, FP32 out): its B operand
 // stacks the 32 columns of B'_re over the 32 of B'_im, so one accumulator
 // holds [Re | Im] of the tile.  Every group t = p + q (2 <= t <= S + 1) has
 // its own accumulator of 64 TMEM columns, all S live at once (S <= 8: 512
 // columns), so one pass over K serves every slice pair and each K block of
 // every slice is staged once:
-//   * warp 0 (one lane) streams, per K block of 64, the S B-slices (double-
-//     buffered) and the S A-slices (a ring of 6) with cp.async.bulk.tensor
-//     (128-byte swizzle) onto mbarriers;
+//   * warp 0 (one lane) streams, per K block of 64 of every tile, the S
+//     B-slices (double-buffered) and the S A-slices (a ring of 6) with
+//     cp.async.bulk.tensor (128-byte swizzle) onto mbarriers;
 //   * warp 1 allocates TMEM, and one lane issues tcgen05.mma for every pair
 //     (p, q) with p + q <= S + 1 into group p + q, releasing each A slot and
-//     B buffer with tcgen05.commit;
-//   * all 8 warps (two per TMEM lane quarter, one half of the columns each;
-//     warps 0 and 1 once they have issued everything) wait for the final
-//     commit, read the S exact FP32 group sums with tcgen05.ld and combine
-//     them exactly in 64-bit integers (Horner in 2^bits), then scale and
-//     store as before.
+//     B buffer with tcgen05.commit and marking a tile's accumulators final
+//     with a commit; before the first MMA of the next tile it waits until
+//     the epilogue has read the accumulators out of TMEM;
+//   * warps 2-9 (two per TMEM lane quarter, one half of the columns each)
+//     read the S exact FP32 group sums of a tile with tcgen05.ld, release
+//     TMEM, combine the sums exactly in 64-bit integers (Horner in 2^bits),
+//     then scale and store as before.
 // Every wait is bounded; on a timeout the kernel sets an error bit, drains
 // what it issued (bounded) and frees its TMEM.
 constexpr int TC_BM = 128;                      // rows of C per CTA (TMEM lanes)
@@ -329,7 +332,8 @@ constexpr int TC_BN = 32;                       // complex columns of C per CTA 
 constexpr int TC_BK = 64;                       // BF16 per K block: one 128-byte swizzle row
 constexpr int TC_MAXS = 8;                      // S groups x 64 TMEM columns <= 512
 constexpr int TC_ARING = 6;                     // A-slice stages (S <= 6: one K block of A in flight)
-constexpr int TC_THREADS = 256;                 // warp 0 TMA, warp 1 MMA, then all 8 warps the epilogue
+constexpr int TC_EPI_WARPS = 8;                 // epilogue warps 2-9: two per TMEM lane quarter
+constexpr int TC_THREADS = 32 * (2 + TC_EPI_WARPS);   // warp 0 TMA, warp 1 MMA (and TMEM allocation)
 constexpr int TC_A_TILE = TC_BM * TC_BK * 2;    // 16 KB
 constexpr int TC_B_HALF = TC_BN * TC_BK * 2;    // 4 KB: 32 rows of B'_re or of B'_im
 constexpr int TC_B_TILE = 2 * TC_B_HALF;        // 8 KB
@@ -365,6 +369,9 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 }
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 __device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
   uint32_t done;
@@ -466,22 +473,36 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
   const uint32_t sA = base + 2u * S * TC_B_TILE;                // [TC_ARING] A tiles of 16 KB
   const uint32_t sBar = sA + TC_ARING * TC_A_TILE;              // barriers
   uint64_t* bars = reinterpret_cast<uint64_t*>(basep + (sBar - base));
-  // barrier slots: full_b 0-1, empty_b 2-3, full_a FA.., empty_a EA.., all accumulators final ACC
-  constexpr int FA = 4, EA = FA + TC_ARING, ACC = EA + TC_ARING, NBAR = ACC + 1;
+  // barrier slots: full_b 0-1, empty_b 2-3, full_a FA.., empty_a EA.., a tile's
+  // accumulators final ACC, TMEM drained by the epilogue TE, MMA thread done DONE
+  constexpr int FA = 4, EA = FA + TC_ARING, ACC = EA + TC_ARING, TE = ACC + 1, DONE = TE + 1, NBAR = DONE + 1;
   auto bar = [&](int k) { return sBar + 8u * k; };
   volatile int* s_abort = reinterpret_cast<volatile int*>(bars + NBAR);
   uint32_t* s_tmem = reinterpret_cast<uint32_t*>(bars + NBAR + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i0 = blockIdx.y * TC_BM, j0 = blockIdx.x * TC_BN;
+  // output tiles, taken persistently: CTA x handles tiles x, x + gridDim.x, ...
+  // (tile t: row block t / tiles_x, column block t % tiles_x)
+  const int tiles_x = (a.n + TC_BN - 1) / TC_BN;
+  const int ntiles = tiles_x * ((a.m + TC_BM - 1) / TC_BM);
+  const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
   const int nkb_all = (a.Kp + TC_BK - 1) / TC_BK;
   const int kb0 = a.kchunk ? (int)blockIdx.z * a.kchunk : 0;
   const int kb1 = a.kchunk ? min(nkb_all, kb0 + a.kchunk) : nkb_all;
+  const int nkb = kb1 > kb0 ? kb1 - kb0 : 0;
+  const int U = my_tiles * nkb;                                 // K blocks this CTA streams, all tiles
+  auto tile_of = [&](int tt, int& i0, int& j0) {
+    const int t = (int)blockIdx.x + tt * (int)gridDim.x;
+    i0 = (t / tiles_x) * TC_BM;
+    j0 = (t % tiles_x) * TC_BN;
+  };
   const uint32_t ncols = tc_tmem_cols(S);
 
   if (threadIdx.x == 0) {
     for (int k = 0; k < 2; ++k) { mbar_init(bar(k), 1); mbar_init(bar(2 + k), 1); }
     for (int k = 0; k < TC_ARING; ++k) { mbar_init(bar(FA + k), 1); mbar_init(bar(EA + k), 1); }
     mbar_init(bar(ACC), 1);
+    mbar_init(bar(TE), TC_EPI_WARPS);
+    mbar_init(bar(DONE), 1);
     *s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -498,17 +519,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
 
   int armed[2 + TC_ARING] = {};   // producer: phases armed per full barrier (B 0-1, A from 2)
   if (warp == 0) {
-    // ---- TMA producer ----
-    if (lane == 0 && kb0 < kb1) {
+    // ---- TMA producer: K block u = (tile u / nkb, kb0 + u % nkb) ----
+    if (lane == 0 && U > 0) {
       int a_use = 0;
-      int b_next = kb0;   // next K block whose B slices are to be issued
-      // the B slices of block kb into buffer (kb - kb0) & 1, once it is free;
+      int b_next = 0;   // next K block whose B slices are to be issued
+      // the B slices of block u into buffer u & 1, once it is free;
       // block = false only tests whether it is free
-      auto issue_b = [&](int kb, bool block) -> bool {
-        const int bu = kb - kb0, bb = bu & 1;
-        const uint32_t parity = ((bu >> 1) & 1) ^ 1;
+      auto issue_b = [&](int u, bool block) -> bool {
+        const int bb = u & 1;
+        const uint32_t parity = ((u >> 1) & 1) ^ 1;
         if (block ? !mbar_wait(bar(2 + bb), parity, err, s_abort) : !mbar_test(bar(2 + bb), parity)) return false;
-        armed[bb] = bu + 1;
+        armed[bb] = u + 1;
+        int i0, j0;
+        tile_of(u / nkb, i0, j0);
+        const int kb = kb0 + u % nkb;
         mbar_expect_tx(bar(bb), (uint32_t)(S * TC_B_TILE));
         for (int q = 0; q < S; ++q) {
           const uint32_t dst = sB + (uint32_t)(bb * S + q) * TC_B_TILE;
@@ -517,14 +541,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
         }
         return true;
       };
-      for (int kb = kb0; kb < kb1 && !*s_abort; ++kb) {
-        if (b_next == kb) {
-          if (!issue_b(kb, true)) break;
+      for (int u = 0; u < U && !*s_abort; ++u) {
+        if (b_next == u) {
+          if (!issue_b(u, true)) break;
           ++b_next;
         }
+        int i0, j0;
+        tile_of(u / nkb, i0, j0);
+        const int kb = kb0 + u % nkb;
         for (int p = 0; p < S; ++p, ++a_use) {
           // the next block's B as early as its buffer is free (without waiting)
-          if (b_next == kb + 1 && kb + 1 < kb1 && issue_b(kb + 1, false)) ++b_next;
+          if (b_next == u + 1 && u + 1 < U && issue_b(u + 1, false)) ++b_next;
           const int slot = a_use % TC_ARING;
           if (!mbar_wait(bar(EA + slot), ((a_use / TC_ARING) & 1) ^ 1, err, s_abort)) break;
           armed[2 + slot] = a_use / TC_ARING + 1;
@@ -537,9 +564,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
     // ---- MMA issuer ----
     if (lane == 0) {
       int a_use = 0;
-      for (int kb = kb0; kb < kb1 && !*s_abort; ++kb) {
-        const int bu = kb - kb0, bb = bu & 1;
-        if (!mbar_wait(bar(bb), (bu >> 1) & 1, err, s_abort)) break;
+      for (int u = 0; u < U && !*s_abort; ++u) {
+        const int tt = u / nkb, kbi = u % nkb, bb = u & 1;
+        if (kbi == 0 && tt > 0) {
+          // the epilogue has read tile tt - 1's accumulators out of TMEM
+          if (!mbar_wait(bar(TE), (tt - 1) & 1, err, s_abort)) break;
+          tc_fence_after();
+        }
+        if (!mbar_wait(bar(bb), (u >> 1) & 1, err, s_abort)) break;
         tc_fence_after();
         bool ok = true;
         for (int p = 0; p < S; ++p, ++a_use) {
@@ -553,41 +585,35 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
             const uint32_t d = tmem + (uint32_t)(p + q) * (2 * TC_BN);
 #pragma unroll
             for (int kk = 0; kk < TC_BK / 16; ++kk)
-              tc_mma(d, ad + 2u * kk, bd + 2u * kk, (kb == kb0 && p == 0 && kk == 0) ? 0u : 1u);
+              tc_mma(d, ad + 2u * kk, bd + 2u * kk, (kbi == 0 && p == 0 && kk == 0) ? 0u : 1u);
           }
           tc_commit(bar(EA + slot));  // A slot free once these MMAs have read it
         }
         tc_commit(bar(2 + bb));       // B buffer free
         if (!ok) break;
+        if (kbi == nkb - 1) tc_commit(bar(ACC));   // tile tt's accumulators final
       }
-      tc_commit(bar(ACC));            // all accumulators final (or, on abort, all issued MMAs done)
+      tc_commit(bar(DONE));           // every MMA issued has completed (the abort path waits on it)
     }
-  }
-  __syncwarp();   // warps 0 and 1 join the epilogue once their issuing lane is done
-  {
-    // ---- epilogue: all 8 warps, two per TMEM lane quarter (warp % 4); warp w
-    //      takes the 16 columns of half w / 4 of the tile ----
+  } else if (U > 0) {
+    // ---- epilogue: warps 2-9, two per TMEM lane quarter (warp % 4); warp w
+    //      takes the 16 columns of half (w - 2) / 4 of each tile ----
     const int quarter = warp & 3;
-    const int h = warp >> 2;
-    const int row = i0 + 32 * quarter + lane;
-    // the fast path's old C values, loaded while the MMAs still run (the array
-    // is indexed only by unrolled constants, so it stays in registers)
+    const int h = (warp - 2) >> 2;
     const bool fast = INT && oz_plain(a) && !a.rs && !a.cs && !a.acc;
     const bool add = a.beta.x != 0.0;
-    cplx pre[16];
-#pragma unroll
-    for (int c = 0; c < 16; ++c) {
-      const int col = j0 + 16 * h + c;
-      pre[c] = (fast && add && row < a.m && col < a.n) ? a.C[(size_t)col * a.ldc + row] : cmake(0.0, 0.0);
-    }
-    const bool waited = mbar_wait(bar(ACC), 0, err, s_abort);
-    // tcgen05.ld is warp-collective: the decision must be uniform over the warp
-    const bool have = __all_sync(0xffffffffu, waited && kb0 < kb1 && !*s_abort);
-    tc_fence_after();
     const uint32_t tq = tmem + ((uint32_t)(32 * quarter) << 16);
     const double wint = INT ? ldexp(1.0, -a.bits * (S + 1)) : 1.0;
     const bool plain = oz_plain(a);
-    if (have) {
+    for (int tt = 0; tt < my_tiles; ++tt) {
+      int i0, j0;
+      tile_of(tt, i0, j0);
+      const int row = i0 + 32 * quarter + lane;
+      const bool waited = mbar_wait(bar(ACC), tt & 1, err, s_abort);
+      // tcgen05.ld is warp-collective: the decision must be uniform over the warp
+      const bool have = __all_sync(0xffffffffu, waited && !*s_abort);
+      if (!have) break;
+      tc_fence_after();
       {
         typedef typename std::conditional<INT, long long, double>::type acc_t;
         acc_t ar[16], ai[16];
@@ -618,6 +644,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
             }
           }
         }
+        // this tile's accumulators are all in registers: TMEM may take the next tile
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar(TE));
         if (row < a.m) {
           if (INT && a.acc) {
 #pragma unroll
@@ -636,70 +666,81 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
             // only FP64 operation left is the addition of the old C (beta = 1)
             const int e_row = expo_field(a.sA[row]) - 1023 - a.bits * (S + 1);
             const bool neg = a.alpha.x < 0.0;
-            int e_col[16];
+            // two passes of 8 columns: the old C values of a pass are loaded
+            // together while the next tile's MMAs run (the arrays are indexed
+            // only by unrolled constants, so they stay in registers)
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
-              const int col = j0 + 16 * h + c;
-              e_col[c] = col < a.n ? expo_field(a.sB[col]) - 1023 : 0;
-            }
-            bool safe = true;
+            for (int hh = 0; hh < 2; ++hh) {
+              cplx pre[8];
+              int e_col[8];
 #pragma unroll
-            for (int c = 0; c < 16; ++c) safe = safe && ll_ldexp_safe(e_row + e_col[c]);
-            if (safe) {
-#pragma unroll
-              for (int c = 0; c < 16; ++c) {
-                const int col = j0 + 16 * h + c;
-                if (col < a.n) {
-                  const long long vr = neg ? -(long long)ar[c] : (long long)ar[c];
-                  const long long vi = neg ? -(long long)ai[c] : (long long)ai[c];
-                  cplx v = cmake(ll_ldexp(vr, e_row + e_col[c]), ll_ldexp(vi, e_row + e_col[c]));
-                  if (add) v = cadd(pre[c], v);
-                  a.C[(size_t)col * a.ldc + row] = v;
-                }
+              for (int c = 0; c < 8; ++c) {
+                const int col = j0 + 16 * h + 8 * hh + c;
+                pre[c] = (add && col < a.n) ? a.C[(size_t)col * a.ldc + row] : cmake(0.0, 0.0);
+                e_col[c] = col < a.n ? expo_field(a.sB[col]) - 1023 : 0;
               }
-            } else {
-              // results that may leave the normal range: the FP64 route (unrolled,
-              // so that the arrays keep constant indices and stay in registers)
+              bool safe = true;
 #pragma unroll
-              for (int c = 0; c < 16; ++c) {
-                const int col = j0 + 16 * h + c;
-                if (col < a.n) {
-                  const long long vr = neg ? -(long long)ar[c] : (long long)ar[c];
-                  const long long vi = neg ? -(long long)ai[c] : (long long)ai[c];
-                  cplx v = cmake(ldexp(__ll2double_rn(vr), e_row + e_col[c]), ldexp(__ll2double_rn(vi), e_row + e_col[c]));
-                  if (add) v = cadd(pre[c], v);
-                  a.C[(size_t)col * a.ldc + row] = v;
+              for (int c = 0; c < 8; ++c) safe = safe && ll_ldexp_safe(e_row + e_col[c]);
+              if (safe) {
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                  const int col = j0 + 16 * h + 8 * hh + c;
+                  if (col < a.n) {
+                    const long long vr = neg ? -(long long)ar[8 * hh + c] : (long long)ar[8 * hh + c];
+                    const long long vi = neg ? -(long long)ai[8 * hh + c] : (long long)ai[8 * hh + c];
+                    cplx v = cmake(ll_ldexp(vr, e_row + e_col[c]), ll_ldexp(vi, e_row + e_col[c]));
+                    if (add) v = cadd(pre[c], v);
+                    a.C[(size_t)col * a.ldc + row] = v;
+                  }
+                }
+              } else {
+                // results that may leave the normal range: the FP64 route
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                  const int col = j0 + 16 * h + 8 * hh + c;
+                  if (col < a.n) {
+                    const long long vr = neg ? -(long long)ar[8 * hh + c] : (long long)ar[8 * hh + c];
+                    const long long vi = neg ? -(long long)ai[8 * hh + c] : (long long)ai[8 * hh + c];
+                    cplx v = cmake(ldexp(__ll2double_rn(vr), e_row + e_col[c]),
+                                   ldexp(__ll2double_rn(vi), e_row + e_col[c]));
+                    if (add) v = cadd(pre[c], v);
+                    a.C[(size_t)col * a.ldc + row] = v;
+                  }
                 }
               }
             }
           } else {
-            // every load (scales, old C) is issued before the first store, so
-            // they are in flight together instead of one memory latency per column
+            // per pass of 8 columns every load (scales, old C) is issued before
+            // the first store, so they are in flight together
             double fr = a.sA[row] * wint;
             if (a.rs) fr *= a.rs[row];
-            double fc[16];
-            cplx cold[16];
             const bool rd = a.beta.x != 0.0 || a.beta.y != 0.0;
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
-              const int col = j0 + 16 * h + c;
-              fc[c] = 0.0;
-              cold[c] = cmake(0.0, 0.0);
-              if (col < a.n) {
-                fc[c] = a.sB[col];
-                if (a.cs) fc[c] *= a.cs[col];
-                if (rd) cold[c] = a.C[(size_t)col * a.ldc + row];
-              }
-            }
+            for (int hh = 0; hh < 2; ++hh) {
+              double fc[8];
+              cplx cold[8];
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
-              const int col = j0 + 16 * h + c;
-              if (col < a.n) {
-                const double f = fr * fc[c];
-                double vr, vi;
-                if constexpr (INT) { vr = __ll2double_rn(ar[c]); vi = __ll2double_rn(ai[c]); }
-                else { vr = ar[c]; vi = ai[c]; }
-                a.C[(size_t)col * a.ldc + row] = oz_combine(a, cmake(vr * f, vi * f), cold[c], plain);
+              for (int c = 0; c < 8; ++c) {
+                const int col = j0 + 16 * h + 8 * hh + c;
+                fc[c] = 0.0;
+                cold[c] = cmake(0.0, 0.0);
+                if (col < a.n) {
+                  fc[c] = a.sB[col];
+                  if (a.cs) fc[c] *= a.cs[col];
+                  if (rd) cold[c] = a.C[(size_t)col * a.ldc + row];
+                }
+              }
+#pragma unroll
+              for (int c = 0; c < 8; ++c) {
+                const int col = j0 + 16 * h + 8 * hh + c;
+                if (col < a.n) {
+                  const double f = fr * fc[c];
+                  double vr, vi;
+                  if constexpr (INT) { vr = __ll2double_rn(ar[8 * hh + c]); vi = __ll2double_rn(ai[8 * hh + c]); }
+                  else { vr = ar[8 * hh + c]; vi = ai[8 * hh + c]; }
+                  a.C[(size_t)col * a.ldc + row] = oz_combine(a, cmake(vr * f, vi * f), cold[c], plain);
+                }
               }
             }
           }
@@ -711,7 +752,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_oz_gemm_tc(const __grid_const
   __syncthreads();
   if (*s_abort) {
     if (threadIdx.x == 32) {
-      mbar_drain(bar(ACC), 0);  // the MMA thread's final commit: every MMA it issued has completed
+      mbar_drain(bar(DONE), 0);  // the MMA thread's final commit: every MMA it issued has completed
     } else if (threadIdx.x == 0) {
       for (int k = 0; k < 2; ++k)
         if (armed[k]) mbar_drain(bar(k), (armed[k] - 1) & 1);
@@ -771,6 +812,19 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   return fn;
 }
 
+// SMs of the current device, looked up once per device.
+static int sm_count_of_current_device() {
+  static int cached[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+  if (!cached[dev]) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v < 1) return 148;
+    cached[dev] = v;
+  }
+  return cached[dev];
+}
+
 // BF16 slices (Kp, rows, S), K contiguous: box of 64 K elements (128 bytes,
 // the swizzle span) x box_rows rows x 1 slice, 128-byte swizzle.
 static bool encode_slices(CUtensorMap* map, const __nv_bfloat16* base, size_t Kp, int rows, int S, int box_rows) {
@@ -820,7 +874,11 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
   a.kchunk = 0;
   a.acc = nullptr;
   if (S > TC_MAXS || !err) return cudaErrorInvalidValue;
-  dim3 grid((nn + TC_BN - 1) / TC_BN, (m + TC_BM - 1) / TC_BM);
+  // persistent CTAs: one per SM (each holds the whole TMEM), every CTA takes
+  // tiles x, x + grid, ... and overlaps a tile's epilogue with the next tile's MMAs
+  const int ntiles = ((nn + TC_BN - 1) / TC_BN) * ((m + TC_BM - 1) / TC_BM);
+  const int sms = sm_count_of_current_device();
+  dim3 grid(ntiles < sms ? ntiles : sms);
   const int ksteps = (int)((Kp + TC_BK - 1) / TC_BK);
   if (splitk > 1 && a.int_combine && !active && ksteps > 1 && acc &&
       (size_t)m * nn * 2 * sizeof(unsigned long long) <= acc_bytes) {

@@ -69,6 +69,10 @@ struct DelayedArgs {
 };
 cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d, int sm_count, cudaStream_t st,
                                  int max_grid = 0);
+// Sets the WHILE condition of a captured round loop (see local_updates_dev):
+// another round while state[0] < N, state[2] < max_rounds and *err == 0.
+cudaError_t launch_round_cond(cudaGraphConditionalHandle hc, int* state, int N, int max_rounds, const int* err,
+                              unsigned long long* rounds_total, cudaStream_t st);
 
 
 // ---- dense linear algebra (k_linalg.cu) ----

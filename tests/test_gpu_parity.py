@@ -678,3 +678,50 @@ def test_rrule_log_weight(lib):
         assert np.max(np.abs(g - want)) < 1e-10 * max(1.0, np.max(np.abs(want)))
     finally:
         gpu.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_round_loop_graph_matches_fixed_rounds(lib, prec):
+    """Delayed rounds (k = 16, L = 8, one sweep of M = 40 calls): the captured
+    sweep, whose WHILE node repeats [round, flush] only while sites remain,
+    against the launch-by-launch path with the fixed bound of N/k + 1 rounds
+    per slice.  Same accept mask, field and G bit for bit; the graph runs
+    fewer rounds, and its launch counts follow the rounds that ran: per call
+    one prepare plus a delayed kernel and a condition kernel per round (local
+    kind), and the same flush launches per round as the fixed path."""
+    p = R.Params(L=8, slices=40, delta_tau=0.1, safe_mult=10, lambda_=1.0, r=1.0, c=1.0, u=1.0, mu1=-0.5,
+                 mu2=-0.5, box=0.2)
+    calls = p.slices
+    phi = R.synthetic_field(p.N, p.slices, 4040)
+    delta, u = R.synthetic_streams(p.N, calls, p.box, 4041)
+    chains = []
+    try:
+        for timed in (True, False):
+            mp = api_params(p)
+            mp.precision, mp.delay = prec, 16
+            c = lib.DQMC(mp, phi)
+            chains.append(c)
+            c.init()
+            c.reset_timing(timed)        # timing on: launch by launch, fixed rounds; off: graph replay
+            res = c.sweep(calls, delta, u, return_accepted=True)
+            kinds = c.timing()["kinds"]
+            c.reset_timing(False)
+            c.res, c.kinds = res, kinds
+        fixed, graph = chains
+        assert np.array_equal(graph.res["accepted_mask"], fixed.res["accepted_mask"])
+        assert np.array_equal(graph.get_field(), fixed.get_field())
+        assert np.array_equal(graph.greens, fixed.greens)
+        r_fixed = (p.N + 15) // 16 + 1
+        loc_f, fl_f = fixed.kinds["local_updates"]["launches"], fixed.kinds["flush"]["launches"]
+        loc_g, fl_g = graph.kinds["local_updates"]["launches"], graph.kinds["flush"]["launches"]
+        assert loc_f == calls * (1 + r_fixed)
+        per_round = fl_f // (calls * r_fixed)
+        assert per_round * calls * r_fixed == fl_f and per_round >= 1
+        rounds = (loc_g - calls) // 2
+        assert loc_g == calls + 2 * rounds
+        assert fl_g == rounds * per_round
+        assert calls <= rounds < calls * r_fixed
+        print(f"{prec}: {rounds} rounds run against {calls * r_fixed} fixed")
+    finally:
+        for c in chains:
+            c.close()
