@@ -810,7 +810,9 @@ def run_ours(args, world, rank, local):
 def run_profile_workload(args):
     """The small workload of the ncu captures: init (stack build, first G) and
     `profile_calls` update calls of one chain of the --config lattice in one
-    form, through the same library path as the timed sweeps."""
+    form, through the same library path as the timed sweeps, launch by launch
+    (the evented path of the kernel breakdown, with the fixed round count:
+    kernels inside a graph's conditional node are not captured by ncu)."""
     from dqmc_gb300 import api
     from oracle.dqmc_ref import synthetic_field, synthetic_streams
     L, M, _ = CONFIGS[args.config]
@@ -819,6 +821,7 @@ def run_profile_workload(args):
     delay = args.fp64_delay if prec == "fp64" else args.delay
     chain = _make_chain(api, L, M, rp, args, 0, prec, delay, synthetic_field(rp.N, M, 1000))
     delta, unif = synthetic_streams(rp.N, args.profile_calls, rp.box, 1001)
+    chain.reset_timing(True)
     res = chain.sweep(args.profile_calls, delta, unif)
     print(json.dumps({"profile_workload": f"L={L} M={M} {prec} delay={delay}", "calls": args.profile_calls,
                       "acc_rate": res["acc_rate"]}), flush=True)

@@ -418,6 +418,20 @@ __device__ __forceinline__ cplx adjugate_entry(cplx m, int lane) {
   return d3;
 }
 
+// The words of site i that the delayed kernel keeps in shared memory: the
+// SitePrep (Delta_i, the proposed eV entries, the field difference and the
+// prepared action parts), then the Metropolis uniform and the proposal delta.
+constexpr int kSiteEv = 32, kSiteDiff = 36, kSiteUnif = 44, kSiteProp = 45, kSiteWords = 48;
+static_assert(sizeof(SitePrep) == 44 * sizeof(double), "SitePrep is read as 44 words");
+static_assert(offsetof(SitePrep, ev) == kSiteEv * sizeof(double), "SitePrep.ev");
+static_assert(offsetof(SitePrep, diff) == kSiteDiff * sizeof(double), "SitePrep.diff");
+static_assert(offsetof(SitePrep, dsA) == (kSiteDiff + 3) * sizeof(double), "SitePrep.dsA");
+__device__ __forceinline__ double site_word(const LocalUpdateArgs& a, const DelayedArgs& d, int i, int k) {
+  if (k < 44) return __ldcg(reinterpret_cast<const double*>(d.prep + i) + k);
+  if (k == kSiteUnif) return __ldg(&a.unif[i]);
+  return __ldg(&a.delta[3 * i + (k - kSiteProp)]);
+}
+
 // Processes sites state[0] .. N-1 until k accepted updates are pending or the
 // slice ends; state[0] is left at the next site and state[1] at the number of
 // pending factors.  The flush G += X Y (a separate GEMM launch over the first
@@ -457,11 +471,16 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   cplx* s_xrow = Xsm + (size_t)K4 * 4;                                 // CACHE: (owned, 4, 4k) X[j', j + rN]
   cplx* s_ycol = s_xrow + (CACHE ? (size_t)owned * 4 * K4 : 0);        // CACHE: (owned, 4, 4k) Y[j', j + cN]
   double* phis = reinterpret_cast<double*>(s_ycol + (CACHE ? (size_t)owned * 4 * K4 : 0));   // (3, N)
-  __shared__ cplx s_delta[16];      // Delta_i
   __shared__ cplx s_adj[2][16];     // adj(M)[r][c] (double-buffered by site parity)
   __shared__ cplx s_det[2];
   __shared__ double s_expds[2];
-  __shared__ double s_u[2];         // Metropolis uniform of the site
+  // per site (slot i & 1), read during the previous site's decision: the
+  // SitePrep words, the Metropolis uniform and the proposal (site_word), and
+  // the site's G_cur block, current if no acceptance came in between
+  // (s_gp[slot] = the pending count it was read at, -1 if not read)
+  __shared__ double s_site[2][kSiteWords];
+  __shared__ cplx s_gblk[2][16];
+  __shared__ int s_gp[2];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int l = a.slice0;
   for (int k = threadIdx.x; k < 3 * N; k += blockDim.x) phis[k] = a.phi[(size_t)3 * N * l + k];
@@ -471,6 +490,13 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   }
   // publication counters of the owned sites start the round at 0
   for (int t = threadIdx.x; t < owned; t += blockDim.x) d.pub[blockIdx.x + t * gridDim.x] = 0;
+  // the first site's words and G block (nothing is pending at the round's start)
+  if (threadIdx.x < kSiteWords) s_site[first & 1][threadIdx.x] = site_word(a, d, first, threadIdx.x);
+  if (threadIdx.x >= 64 && threadIdx.x < 80) {
+    const int e = threadIdx.x - 64, r = e >> 2, c = e & 3;
+    s_gblk[first & 1][e] = ldcg_c(&a.G[(size_t)(first + c * N) * n + first + r * N]);
+  }
+  if (threadIdx.x == 0) s_gp[first & 1] = 0;
   if (!grid_barrier(a.bar, a.err, bar_epoch)) return;
 
   // phase-1 role of this warp in the first pass of owned sites
@@ -479,10 +505,13 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
 
   for (int i = first; i < N; ++i) {
     const int J = 4 * p;   // pending columns of X / rows of Y
-    const int slot = i & 1;
-    const SitePrep* sp = d.prep + i;
-    // ---- wait until the owner of site i has folded in all p acceptances ----
-    if (p > 0) {
+    const int slot = i & 1, nslot = slot ^ 1;
+    const double* sw = s_site[slot];                              // this site's words
+    const cplx* sdelta = reinterpret_cast<const cplx*>(sw);      // Delta_i, row-major
+    // the block read ahead is current unless an acceptance came in between
+    const bool have_g = s_gp[slot] == p;
+    // ---- otherwise wait until the owner of site i has folded in all p acceptances ----
+    if (p > 0 && !have_g) {
       if (threadIdx.x == 0) {
         volatile int* f = d.pub + i;
         int ok = 1;
@@ -515,9 +544,9 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
       const int r = (lane >> 2) & 3, c = lane & 3;
       cplx g = cmake(0.0, 0.0), drow[4];
       if (lane < 16) {
-        g = p == 0 ? ldcg_c(&a.G[(size_t)(i + c * N) * n + i + r * N]) : ldcg_c(&d.blk[(size_t)16 * i + lane]);
+        g = have_g ? s_gblk[slot][lane] : ldcg_c(&d.blk[(size_t)16 * i + lane]);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) drow[k] = ldcg_c(&sp->delta[4 * r + k]);
+        for (int k = 0; k < 4; ++k) drow[k] = sdelta[4 * r + k];
       } else {
 #pragma unroll
         for (int k = 0; k < 4; ++k) drow[k] = cmake(0.0, 0.0);
@@ -553,23 +582,39 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         for (int c = 0; c < 3; ++c) {
           double os = 0.0;
           for (int q = 0; q < 4; ++q) os = os + phis[3 * nbs[q] + c];
-          sdot += os * __ldcg(&sp->diff[c]);
+          sdot += os * sw[kSiteDiff + c];
         }
-        double dS = __ldcg(&sp->dsA);
-        dS += 0.5 * mc.dtau * (__ldcg(&sp->dsQ) - 2.0 * sdot);
-        dS += __ldcg(&sp->dsB);
+        double dS = sw[kSiteDiff + 3];
+        dS += 0.5 * mc.dtau * (sw[kSiteDiff + 4] - 2.0 * sdot);
+        dS += sw[kSiteDiff + 5];
         s_expds[slot] = exp(-dS);
-      } else if (lane == 1) {
-        s_u[slot] = __ldg(&a.unif[i]);
       }
-    } else if (wid == 7 && lane < 16) {
-      s_delta[lane] = ldcg_c(&sp->delta[lane]);
+    } else if (wid == 7 && i + 1 < N) {
+      // ---- site i + 1's G_cur block, ahead of time: current if site i is
+      //      rejected and its owner has folded in all p acceptances by now ----
+      int v = p;   // nothing pending: G itself is current
+      if (p > 0) {
+        if (lane == 0) v = (int)ld_acquire_u32(reinterpret_cast<const unsigned*>(d.pub + i + 1));
+        v = __shfl_sync(0xffffffffu, v, 0);
+      }
+      if (v >= p && lane < 16) {
+        const int r = lane >> 2, c = lane & 3, j = i + 1;
+        s_gblk[nslot][lane] = p == 0 ? ldcg_c(&a.G[(size_t)(j + c * N) * n + j + r * N])
+                                     : ldcg_c(&d.blk[(size_t)16 * j + lane]);
+      }
+      if (lane == 0) s_gp[nslot] = v >= p ? p : -1;
     }
-    if (wid < 4 || wid == 7) {
-      // ---- stage the pending factor entries touching site i (160 threads, loads issued together) ----
-      constexpr int kStage = 160;
-      const int st = wid < 4 ? threadIdx.x : 128 + lane;
-      for (int t = st; t < 4 * J; t += 2 * kStage) {
+    if (wid < 4) {
+      // ---- site i + 1's words (warp 3), then the pending factor entries
+      //      touching site i (128 threads, loads issued together) ----
+      if (wid == 3 && i + 1 < N) {
+        const double w0 = site_word(a, d, i + 1, lane);
+        const double w1 = lane + 32 < kSiteWords ? site_word(a, d, i + 1, lane + 32) : 0.0;
+        s_site[nslot][lane] = w0;
+        if (lane + 32 < kSiteWords) s_site[nslot][lane + 32] = w1;
+      }
+      constexpr int kStage = 128;
+      for (int t = threadIdx.x; t < 4 * J; t += 2 * kStage) {
         const int t2 = t + kStage;
         const int j1 = t >> 2, c1 = t & 3, j2 = t2 >> 2, c2 = t2 & 3;
         const cplx y1 = ldcg_c(&d.Y[(size_t)j1 * n + i + c1 * N]);
@@ -594,10 +639,10 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
     const double exp_dS = s_expds[slot];
     const double pacc = exp_dS * det.x;
     const bool bad = !isfinite(det.x) || !isfinite(det.y) || (det.x == 0.0 && det.y == 0.0);
-    const bool acc = !bad && (pacc > 1.0 || s_u[slot] < pacc);
+    const bool acc = !bad && (pacc > 1.0 || sw[kSiteUnif] < pacc);
     if (threadIdx.x == 0) {
       if (acc)
-        for (int q = 0; q < 3; ++q) phis[3 * i + q] += a.delta[3 * i + q];
+        for (int q = 0; q < 3; ++q) phis[3 * i + q] += sw[kSiteProp + q];
       if (blockIdx.x == 0) {
         if (bad) atomicOr(a.err, DQMC_KERR_NONFINITE);
         if (a.acc_out) a.acc_out[i] = (uint8_t)acc;
@@ -606,7 +651,11 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         if (acc) {
           double* pg = &a.phi[((size_t)N * l + i) * 3];
           pg[0] = phis[3 * i]; pg[1] = phis[3 * i + 1]; pg[2] = phis[3 * i + 2];
-          if (a.evtab) reinterpret_cast<EvEntry*>(a.evtab)[(size_t)N * l + i] = sp->ev;
+          if (a.evtab) {
+            EvEntry ev;
+            ev.C = sw[kSiteEv]; ev.Sr = sw[kSiteEv + 1]; ev.Si = sw[kSiteEv + 2]; ev.R = sw[kSiteEv + 3];
+            reinterpret_cast<EvEntry*>(a.evtab)[(size_t)N * l + i] = ev;
+          }
           *a.action += -log(exp_dS);
           *a.n_acc += 1;
         }
@@ -660,7 +709,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         const cplx g0 = shfl_c(gcur, 8 * sub + 4 * h), g1 = shfl_c(gcur, 8 * sub + 4 * h + 2);
         cplx prod;
         if (isX) prod = cfma(g1, s_adj[slot][4 * (2 * h + 1) + ko], cmul(g0, s_adj[slot][4 * (2 * h) + ko]));
-        else prod = cfma(s_delta[4 * ko + 2 * h + 1], g1, cmul(s_delta[4 * ko + 2 * h], g0));
+        else prod = cfma(sdelta[4 * ko + 2 * h + 1], g1, cmul(sdelta[4 * ko + 2 * h], g0));
         prod = cadd(prod, shfl_c(prod, lane ^ 1));
         if (!isX) prod = cmul(prod, inv);
         if (h == 0) {
@@ -677,16 +726,21 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
       }
       __syncthreads();
       // ---- refresh the cached blocks of the pass's sites (needed by later sites only) ----
-      if (!(wid & 1) && lane < 16) {
+      if (!(wid & 1)) {
         const int ls = wid >> 1, tsr = t0 + ls;
         const int j = blockIdx.x + tsr * gridDim.x;
         if (tsr < owned && j > i) {
-          const int r = lane >> 2, c = lane & 3;
-          cplx b = s_blk[16 * tsr + lane];
-#pragma unroll
-          for (int k = 0; k < 4; ++k) b = cfma(s_xn[16 * ls + 4 * r + k], s_yn[16 * ls + 4 * k + c], b);
-          s_blk[16 * tsr + lane] = b;
-          d.blk[(size_t)16 * j + lane] = b;
+          // entry e = 4r + c of the block: lanes e and e + 16 take k = 0, 1 and
+          // k = 2, 3 of X_new[r, k] Y_new[k, c], then add the halves
+          const int e = lane & 15, r = e >> 2, c = e & 3, k0 = (lane >> 4) * 2;
+          cplx b = lane < 16 ? s_blk[16 * tsr + e] : cmake(0.0, 0.0);
+          b = cfma(s_xn[16 * ls + 4 * r + k0], s_yn[16 * ls + 4 * k0 + c], b);
+          b = cfma(s_xn[16 * ls + 4 * r + k0 + 1], s_yn[16 * ls + 4 * (k0 + 1) + c], b);
+          b = cadd(b, shfl_c(b, lane ^ 16));
+          if (lane < 16) {
+            s_blk[16 * tsr + e] = b;
+            d.blk[(size_t)16 * j + e] = b;
+          }
         }
       }
       __syncthreads();   // s_xn / s_yn reused by the next pass; all stores precede the publication
