@@ -89,6 +89,9 @@ struct dqmc_handle {
   // 186/184/194 ms; LU per sweep blocked/unblocked: n = 144 9.0/5.8 ms,
   // n = 576 39.8/33.9 ms, n = 1024 184/232 ms.
   int wy_block = 128, trsm_block = 64, lu_grid = 64, lu_small = 576;
+  // LU panels on one thread-block cluster of this many CTAs (16 or 8; 0: the
+  // cooperative grid of lu_grid CTAs; DQMC_TUNE "lu_cluster=")
+  int lu_cluster = 16;
   cplx* wy_v = nullptr;       // mixed form: (n x kWyMax) reflector block
   cplx* wy_s = nullptr;       // (kWyMax^2) Vb^H Vb
   cplx* wy_z = nullptr;       // (kWyMax x n) T Vb^H W
@@ -502,7 +505,7 @@ int lu_blocked(dqmc_handle* h, cplx* A, const cplx** Lm) {
     int lu_cap = h->coop_cap;
     if (h->lu_grid > 0 && (lu_cap == 0 || h->lu_grid < lu_cap)) lu_cap = h->lu_grid;
     LAUNCH(DQMC_K_LU, 8.0 * (n - p0) * b * b / 2.0, 32.0 * (n - p0) * b,
-           launch_lu_panel(A, n, p0, b, h->lup, h->sm_count, h->st, lu_cap));
+           launch_lu_panel(A, n, p0, b, h->lup, h->sm_count, h->st, lu_cap, h->lu_cluster));
     LAUNCH(DQMC_K_LU, 0.0, 64.0 * b * n, launch_lu_apply_swaps(A, n, p0, b, h->lup.piv, h->lu.perm, h->st));
     if (m > 0) {
       LAUNCH(DQMC_K_LU, 4.0 * b * b * m, 32.0 * b * m,
@@ -1236,6 +1239,7 @@ int dqmc_create(const dqmc_params* p, dqmc_handle** out) {
     if (const char* q = std::strstr(tune, "trsm=")) if (std::sscanf(q + 5, "%d", &v) == 1 && v >= 16 && v <= 128) h->trsm_block = v;
     if (const char* q = std::strstr(tune, "lu_grid=")) if (std::sscanf(q + 8, "%d", &v) == 1 && v >= 0) h->lu_grid = v;
     if (const char* q = std::strstr(tune, "lu_small=")) if (std::sscanf(q + 9, "%d", &v) == 1 && v >= 0) h->lu_small = v;
+    if (const char* q = std::strstr(tune, "lu_cluster=")) if (std::sscanf(q + 11, "%d", &v) == 1 && (v == 0 || v == 8 || v == 16)) h->lu_cluster = v;
   }
   h->L = p->L; h->N = p->L * p->L; h->n = 4 * h->N; h->M = p->slices; h->s = p->safe_mult;
   h->ne = h->M / h->s + 1;

@@ -10,6 +10,7 @@
 // factor comes out directly in the un-permuted ("T = R[:, invperm(p)]")
 // layout that the UDT decomposition needs.
 #include <cfloat>
+#include <cooperative_groups.h>
 #include "common.cuh"
 #include "kernels.h"
 
@@ -685,6 +686,149 @@ __global__ void __launch_bounds__(256) k_lu_panel(cplx* __restrict__ A, int n, i
   }
 }
 
+// The same panel factorisation on one thread-block cluster of cs CTAs (8 or
+// 16, the rows dealt in contiguous chunks): each CTA keeps its candidate (value,
+// row and the row's panel values) and, when it holds it, the step's row k in
+// its own shared memory, double-buffered by step parity; the others read them
+// through distributed shared memory after one cluster barrier per column, in
+// place of the grid barrier and the round trips through L2.  Every CTA runs
+// the same loop, so every cluster barrier is met by all of them; the last
+// barrier of the loop also keeps each CTA's shared memory alive until the
+// others have read it.
+__global__ void __launch_bounds__(256) k_lu_panel_cluster(cplx* __restrict__ A, int n, int p0, int b, LUPanel w) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const int cs = (int)cl.num_blocks(), q = (int)cl.block_rank();
+  extern __shared__ double4_16a smem_panel[];
+  cplx* prow = reinterpret_cast<cplx*>(smem_panel);   // (own rows, LU_PB): this CTA's rows of the panel
+  const int rows = n - p0;
+  const int chunk = (rows + cs - 1) / cs;
+  const int r0 = p0 + q * chunk;
+  const int r1 = r0 + chunk < n ? r0 + chunk : n;
+  const int nrw = r1 > r0 ? r1 - r0 : 0;
+  __shared__ cplx urow[LU_PB], krow[LU_PB];
+  __shared__ cplx c_row[2][LU_PB], k_row[2][LU_PB];
+  __shared__ double c_val[2];
+  __shared__ int c_r[2];
+  __shared__ double s_v[8];
+  __shared__ int s_r[8];
+  __shared__ int s_p, s_wc;
+  __shared__ cplx s_rinv;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int e = threadIdx.x; e < nrw * b; e += blockDim.x) {
+    const int rr = e / b, j = e - rr * b;
+    prow[rr * LU_PB + j] = ldcg_c(&A[(size_t)(p0 + j) * n + r0 + rr]);
+  }
+  __syncthreads();
+
+  // candidate of this CTA for panel column jc over its rows >= k (value, row,
+  // row values), and row k itself if this CTA holds it, into buffers par
+  auto publish = [&](int jc, int k, int par) {
+    double best = 0.0;
+    int brow = n;
+    for (int r = (r0 > k ? r0 : k) + threadIdx.x; r < r1; r += blockDim.x) {
+      const cplx x = prow[(r - r0) * LU_PB + jc];
+      const double a = fabs(x.x) + fabs(x.y);
+      if (piv_better(a, r, best, brow)) { best = a; brow = r; }
+    }
+    warp_argmax(best, brow);
+    if (lane == 0) { s_v[wid] = best; s_r[wid] = brow; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double bv = s_v[0]; int br = s_r[0];
+      for (int u = 1; u < (int)(blockDim.x >> 5); ++u)
+        if (piv_better(s_v[u], s_r[u], bv, br)) { bv = s_v[u]; br = s_r[u]; }
+      c_val[par] = bv;
+      c_r[par] = br;
+      s_r[0] = br;
+    }
+    __syncthreads();
+    const int br = s_r[0];
+    if (br < n)
+      for (int j = threadIdx.x; j < b; j += blockDim.x) c_row[par][j] = prow[(br - r0) * LU_PB + j];
+    if (r0 <= k && k < r1)
+      for (int j = threadIdx.x; j < b; j += blockDim.x) k_row[par][j] = prow[(k - r0) * LU_PB + j];
+  };
+
+  publish(0, p0, 0);
+  cl.sync();
+
+  for (int kk = 0; kk < b; ++kk) {
+    const int k = p0 + kk, par = kk & 1;
+    // ---- pivot: best of the cs candidates (first row of maximal |Re| + |Im|) ----
+    if (wid == 0) {
+      double best = 0.0;
+      int brow = n, bc = 0;
+      if (lane < cs) {
+        best = *cl.map_shared_rank(&c_val[par], lane);
+        brow = *cl.map_shared_rank(&c_r[par], lane);
+        bc = lane;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int orow = __shfl_xor_sync(0xffffffffu, brow, o), oc = __shfl_xor_sync(0xffffffffu, bc, o);
+        if (piv_better(ob, orow, best, brow)) { best = ob; brow = orow; bc = oc; }
+      }
+      if (lane == 0) { s_p = brow; s_wc = bc; }
+    }
+    __syncthreads();
+    const bool none = s_p >= n;   // all candidates zero: no exchange, singular pivot
+    const int p = none ? k : s_p;
+    {
+      const cplx* kr = cl.map_shared_rank(&k_row[par][0], (unsigned)((k - p0) / chunk));
+      const cplx* ur = cl.map_shared_rank(&c_row[par][0], (unsigned)s_wc);
+      for (int j = threadIdx.x; j < b; j += blockDim.x) {
+        const cplx kv = kr[j];
+        krow[j] = kv;
+        urow[j] = none ? kv : ur[j];
+      }
+    }
+    __syncthreads();
+    if (wid == 0) {
+      // 1 / pivot = conj(pv) / |pv|^2 (the D-scale separated matrix has no large scales)
+      const cplx pv = urow[kk];
+      const double d2 = pv.x * pv.x + pv.y * pv.y;
+      const bool zero = d2 == 0.0;
+      const double rd = zero ? 0.0 : 1.0 / d2;
+      if (lane == 0) {
+        s_rinv = cmake(pv.x * rd, -pv.y * rd);
+        if (zero) atomicOr(w.err, DQMC_KERR_SINGULAR);
+        if (q == 0) w.piv[k] = p;
+      }
+    }
+    // the exchanged rows: row k <- pivot row (U), row p <- old row k
+    if (r0 <= k && k < r1)
+      for (int j = threadIdx.x; j < b; j += blockDim.x) prow[(k - r0) * LU_PB + j] = urow[j];
+    if (p != k && r0 <= p && p < r1)
+      for (int j = threadIdx.x; j < b; j += blockDim.x) prow[(p - r0) * LU_PB + j] = krow[j];
+    __syncthreads();
+    const cplx rinv = s_rinv;
+    // ---- multipliers of the own rows below k, then the rank-1 update of the panel ----
+    const int ra = r0 > k + 1 ? r0 : k + 1;
+    const int nr = r1 > ra ? r1 - ra : 0;
+    for (int t = threadIdx.x; t < nr; t += blockDim.x) {
+      cplx* e = &prow[(ra + t - r0) * LU_PB + kk];
+      *e = cmul(*e, rinv);
+    }
+    __syncthreads();
+    const int nc = b - kk - 1;
+    for (int t = threadIdx.x; t < nr * nc; t += blockDim.x) {
+      const int rr = t % nr, jj = kk + 1 + t / nr;
+      cplx* rowp = &prow[(ra + rr - r0) * LU_PB];
+      const cplx l = rowp[kk], u = urow[jj], x = rowp[jj];
+      rowp[jj] = cmake(fma(-l.x, u.x, fma(l.y, u.y, x.x)), fma(-l.x, u.y, fma(-l.y, u.x, x.y)));
+    }
+    __syncthreads();
+    if (kk + 1 < b) publish(kk + 1, k + 1, (kk + 1) & 1);
+    cl.sync();
+  }
+  for (int e = threadIdx.x; e < nrw * b; e += blockDim.x) {
+    const int rr = e / b, j = e - rr * b;
+    A[(size_t)(p0 + j) * n + r0 + rr] = prow[rr * LU_PB + j];
+  }
+}
+
 // Row exchanges of one panel applied to the columns outside it, and to the
 // running permutation: the b exchanges (k, piv[k]) touch at most 2b rows,
 // whose net permutation warp 0 works out (panel rows indexed directly, rows
@@ -1240,8 +1384,56 @@ cudaError_t launch_lup(cplx* A, cplx* Lb, int n, LUKernel& w, int sm_count, cuda
   return cudaLaunchCooperativeKernel((void*)k_lup, dim3(grid), dim3(QR_THREADS), args, smem, st);
 }
 
-cudaError_t launch_lu_panel(cplx* A, int n, int p0, int b, LUPanel& w, int sm_count, cudaStream_t st, int max_grid) {
+// One cluster of cs CTAs (16, else 8 when 16 cannot be scheduled); returns
+// cudaErrorNotSupported, with nothing launched, when neither fits.
+static cudaError_t launch_lu_panel_cluster(cplx* A, int n, int p0, int b, LUPanel& w, int cs, cudaStream_t st) {
+  constexpr size_t kMax = 160 * 1024;
+  static SmemLimit smem_limit;
+  static bool nonportable_set[64] = {};
+  int dev = 0;
+  if (cudaError_t e = cudaGetDevice(&dev); e != cudaSuccess) return e;
+  if (cudaError_t ea = smem_limit.raise((const void*)k_lu_panel_cluster, (int)kMax); ea != cudaSuccess) return ea;
+  if (dev >= 0 && dev < 64 && !nonportable_set[dev]) {
+    if (cudaError_t e = cudaFuncSetAttribute((const void*)k_lu_panel_cluster,
+                                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        e != cudaSuccess)
+      return e;
+    nonportable_set[dev] = true;
+  }
+  for (int c = cs; c >= 8; c /= 2) {
+    const int chunk = (n - p0 + c - 1) / c;
+    const size_t smem = (size_t)chunk * LU_PB * sizeof(cplx);
+    if (smem > kMax) return cudaErrorNotSupported;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(c);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = c;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, (const void*)k_lu_panel_cluster, &cfg) != cudaSuccess) {
+      cudaGetLastError();
+      clusters = 0;
+    }
+    if (clusters < 1) continue;
+    return cudaLaunchKernelEx(&cfg, k_lu_panel_cluster, A, n, p0, b, w);
+  }
+  return cudaErrorNotSupported;
+}
+
+cudaError_t launch_lu_panel(cplx* A, int n, int p0, int b, LUPanel& w, int sm_count, cudaStream_t st, int max_grid,
+                            int cluster) {
   if (b < 1 || b > LU_PB) return cudaErrorInvalidValue;
+  if (cluster >= 8) {
+    const cudaError_t e = launch_lu_panel_cluster(A, n, p0, b, w, cluster, st);
+    if (e != cudaErrorNotSupported) return e;
+  }
   int grid = sm_count;
   if (max_grid > 0 && grid > max_grid) grid = max_grid;
   if (grid > n - p0) grid = n - p0;

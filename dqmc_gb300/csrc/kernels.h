@@ -153,8 +153,10 @@ struct LUPanel {
   GridBarrier* bar;
   int* err;
 };
+// cluster >= 8: the panel on one thread-block cluster of that many CTAs (16 or
+// 8; the cooperative grid when no cluster can be scheduled); 0: the grid
 cudaError_t launch_lu_panel(cplx* A, int n, int p0, int b, LUPanel& w, int sm_count, cudaStream_t st,
-                            int max_grid = 0);
+                            int max_grid = 0, int cluster = 0);
 // the panel's row exchanges applied to the columns outside [p0, p0+b) and to perm
 cudaError_t launch_lu_apply_swaps(cplx* A, int n, int p0, int b, const int* piv, int* perm, cudaStream_t st);
 cudaError_t launch_lu_diag(const cplx* A, int n, cplx* udiag, cplx* rdiag, cudaStream_t st);

@@ -447,12 +447,14 @@ def test_time_displaced_greens(lib, golden, small_params, cfg, prec):
         assert relerr(g0t[tau], g0t_r[tau]) < tol, (tau, relerr(g0t[tau], g0t_r[tau]))
 
 
-@pytest.mark.parametrize("tune", ["lu_small=0", "lu_small=4096"])
+@pytest.mark.parametrize("tune", ["lu_small=0", "lu_small=0,lu_cluster=8", "lu_small=0,lu_cluster=0",
+                                  "lu_small=4096"])
 @pytest.mark.parametrize("L,prec", [(6, "fp64"), (10, "fp64"), (10, "mixed")])
 def test_lu_blocked_and_unblocked(lib, monkeypatch, tune, L, prec):
     """calculate_greens through the blocked LU (panels of 64 columns, ragged last
-    panel at n = 400) and through the unblocked cooperative LU, selected per
-    handle by DQMC_TUNE; both reproduce the oracle (1e-10 FP64, 1e-8 mixed)."""
+    panel at n = 400; the panels on a cluster of 16 or 8 CTAs, or on the
+    cooperative grid) and through the unblocked cooperative LU, selected per
+    handle by DQMC_TUNE; all reproduce the oracle (1e-10 FP64, 1e-8 mixed)."""
     monkeypatch.setenv("DQMC_TUNE", tune)
     p = dataclasses.replace(P_L4, L=L, slices=20)
     phi = R.synthetic_field(p.N, p.slices, 31 + L)
