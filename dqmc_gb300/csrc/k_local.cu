@@ -481,6 +481,18 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   __shared__ double s_site[2][kSiteWords];
   __shared__ cplx s_gblk[2][16];
   __shared__ int s_gp[2];
+  // CTA 0: exp(-dS) of the round's accepted sites in order; the tracked action
+  // gets the same additions -log(exp(-dS)) in the same order once the round
+  // ends, off the per-site chain (no read-modify-write of global memory per site)
+  __shared__ double s_expq[64];
+  auto finish_round = [&](int pend) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && pend > 0) {
+      double act = *a.action;
+      for (int t = 0; t < pend; ++t) act += -log(s_expq[t]);
+      *a.action = act;
+      *a.n_acc += pend;
+    }
+  };
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int l = a.slice0;
   for (int k = threadIdx.x; k < 3 * N; k += blockDim.x) phis[k] = a.phi[(size_t)3 * N * l + k];
@@ -656,8 +668,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
             ev.C = sw[kSiteEv]; ev.Sr = sw[kSiteEv + 1]; ev.Si = sw[kSiteEv + 2]; ev.R = sw[kSiteEv + 3];
             reinterpret_cast<EvEntry*>(a.evtab)[(size_t)N * l + i] = ev;
           }
-          *a.action += -log(exp_dS);
-          *a.n_acc += 1;
+          s_expq[p] = exp_dS;   // the action and the count are updated at the round's end
         }
       }
     }
@@ -748,6 +759,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
     ++p;
     if (p == d.k || i == N - 1) {
       if (blockIdx.x == 0 && threadIdx.x == 0) { d.state[0] = i + 1; d.state[1] = p; }
+      finish_round(p);
       return;   // the flush follows as its own launch
     }
     // ---- publish: the owned later sites now include p acceptances (the CTA
@@ -761,6 +773,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) { d.state[0] = N; d.state[1] = p; }
+  finish_round(p);
 }
 
 // Condition of the graph's WHILE node that repeats [delayed round, flush]:
