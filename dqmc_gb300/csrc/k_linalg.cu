@@ -181,6 +181,29 @@ __device__ __forceinline__ cplx qr_load_dot(cplx (&x)[QR_MAXT], const cplx* __re
   return warp_sum_c(sp);
 }
 
+// loads one lane's slots of a column into x (as qr_load_dot, without the dot)
+__device__ __forceinline__ void qr_load(cplx (&x)[QR_MAXT], const cplx* __restrict__ col, int k, int n, int nq,
+                                        int lane) {
+#pragma unroll
+  for (int q = 0; q < QR_MAXT; ++q) {
+    if (q >= nq) break;
+    const int r = k + lane + 32 * q;
+    x[q] = r < n ? ldcg_c(&col[r]) : cmake(0.0, 0.0);
+  }
+}
+
+// sum_{r > k} conj(x_r) a_r over one lane's slots already in x (the order of qr_load_dot)
+__device__ __forceinline__ cplx qr_dot(const cplx (&x)[QR_MAXT], const cplx* v, int k, int n, int nq, int lane) {
+  cplx sp = cmake(0.0, 0.0);
+#pragma unroll
+  for (int q = 0; q < QR_MAXT; ++q) {
+    if (q >= nq) break;
+    const int r = k + lane + 32 * q;
+    if (r < n && r > k) sp = cfma_conj(v[r], x[q], sp);
+  }
+  return warp_sum_c(sp);
+}
+
 // One column step after the dot product s0 = sum_{r>k} conj(x_r) a_r:
 // a -= tau^H (v^H a) v with v = (1, scal x_{k+1..n}), then the partial norm
 // downdate of zlaqp2 with stored reciprocals (vn1, vn2 at [j], 1/vn1, 1/vn2
@@ -265,6 +288,17 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
 
   const int chunk = (n + gridDim.x - 1) / gridDim.x;   // rows of V written by this CTA
   for (int k = 0; k < n; ++k) {
+    const int rem = n - k - 1;
+    const int nq = (n - k + 31) >> 5;   // warp-uniform: no FP64 work on fully masked slots
+    const int t_first = blockIdx.x + gridDim.x * wid;
+    // the first column of this warp, read while the pivot is chosen; if the
+    // pivot exchange moves another column to its position, it is read again
+    cplx x[QR_MAXT];
+    int j_pre = -1;
+    if (t_first < rem && wid != scal_warp) {
+      j_pre = order[k + 1 + t_first];
+      qr_load(x, A + (size_t)j_pre * n, k, n, nq, lane);
+    }
     // ---- pivot: best of the per-CTA candidates (first position of maximal norm), warp 0 ----
     if (wid == 0) {
       // all candidate loads in flight at once (grid <= 32 * CAND_PER_LANE), then the compares
@@ -342,17 +376,14 @@ __global__ void __launch_bounds__(QR_THREADS) k_qrp(cplx* __restrict__ A, int n,
     // ---- apply H_k^H to the remaining columns, downdate their norms ----
     // remaining logical positions k+1..n-1 are dealt round-robin over the CTAs
     // first, so every SM keeps an equal share of the columns as k grows
-    const int rem = n - k - 1;
-    const int nq = (n - k + 31) >> 5;   // warp-uniform: no FP64 work on fully masked slots
     double cbest = 0.0;
     int cbq = n;
-    const int t_first = blockIdx.x + gridDim.x * wid;
-    cplx x[QR_MAXT];
     cplx s_first = cmake(0.0, 0.0);
     int j_first = -1;
     if (t_first < rem && wid != scal_warp) {
       j_first = order[k + 1 + t_first];
-      s_first = qr_load_dot(x, A + (size_t)j_first * n, v, k, n, nq, lane);
+      if (j_first != j_pre) qr_load(x, A + (size_t)j_first * n, k, n, nq, lane);
+      s_first = qr_dot(x, v, k, n, nq, lane);
     }
     __syncthreads();   // tau, scal visible
     const cplx ctau = cconj(s_tau), scal = s_scal;
