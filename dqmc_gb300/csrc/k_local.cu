@@ -477,10 +477,13 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   // per site (slot i & 1), read during the previous site's decision: the
   // SitePrep words, the Metropolis uniform and the proposal (site_word), and
   // the site's G_cur block, current if no acceptance came in between
-  // (s_gp[slot] = the pending count it was read at, -1 if not read)
-  __shared__ double s_site[2][kSiteWords];
-  __shared__ cplx s_gblk[2][16];
-  __shared__ int s_gp[2];
+  // (s_gp = the pending count it was read at, -1 if not read).  Three buffers
+  // by site (i mod 3): while site i is decided, site i + 1's are written, and
+  // a thread still finishing site i - 1 (after its decision barrier, before
+  // site i's) reads that site's words, so the three must be distinct.
+  __shared__ double s_site[3][kSiteWords];
+  __shared__ cplx s_gblk[3][16];
+  __shared__ int s_gp[3];
   // CTA 0: exp(-dS) of the round's accepted sites in order; the tracked action
   // gets the same additions -log(exp(-dS)) in the same order once the round
   // ends, off the per-site chain (no read-modify-write of global memory per site)
@@ -503,12 +506,12 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   // publication counters of the owned sites start the round at 0
   for (int t = threadIdx.x; t < owned; t += blockDim.x) d.pub[blockIdx.x + t * gridDim.x] = 0;
   // the first site's words and G block (nothing is pending at the round's start)
-  if (threadIdx.x < kSiteWords) s_site[first & 1][threadIdx.x] = site_word(a, d, first, threadIdx.x);
+  if (threadIdx.x < kSiteWords) s_site[first % 3][threadIdx.x] = site_word(a, d, first, threadIdx.x);
   if (threadIdx.x >= 64 && threadIdx.x < 80) {
     const int e = threadIdx.x - 64, r = e >> 2, c = e & 3;
-    s_gblk[first & 1][e] = ldcg_c(&a.G[(size_t)(first + c * N) * n + first + r * N]);
+    s_gblk[first % 3][e] = ldcg_c(&a.G[(size_t)(first + c * N) * n + first + r * N]);
   }
-  if (threadIdx.x == 0) s_gp[first & 1] = 0;
+  if (threadIdx.x == 0) s_gp[first % 3] = 0;
   if (!grid_barrier(a.bar, a.err, bar_epoch)) return;
 
   // phase-1 role of this warp in the first pass of owned sites
@@ -517,11 +520,12 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
 
   for (int i = first; i < N; ++i) {
     const int J = 4 * p;   // pending columns of X / rows of Y
-    const int slot = i & 1, nslot = slot ^ 1;
-    const double* sw = s_site[slot];                              // this site's words
+    const int slot = i & 1;                                       // decision values
+    const int rs = i % 3, nrs = rs == 2 ? 0 : rs + 1;             // read-ahead buffers of sites i, i + 1
+    const double* sw = s_site[rs];                                // this site's words
     const cplx* sdelta = reinterpret_cast<const cplx*>(sw);      // Delta_i, row-major
     // the block read ahead is current unless an acceptance came in between
-    const bool have_g = s_gp[slot] == p;
+    const bool have_g = s_gp[rs] == p;
     // ---- otherwise wait until the owner of site i has folded in all p acceptances ----
     if (p > 0 && !have_g) {
       if (threadIdx.x == 0) {
@@ -556,7 +560,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
       const int r = (lane >> 2) & 3, c = lane & 3;
       cplx g = cmake(0.0, 0.0), drow[4];
       if (lane < 16) {
-        g = have_g ? s_gblk[slot][lane] : ldcg_c(&d.blk[(size_t)16 * i + lane]);
+        g = have_g ? s_gblk[rs][lane] : ldcg_c(&d.blk[(size_t)16 * i + lane]);
 #pragma unroll
         for (int k = 0; k < 4; ++k) drow[k] = sdelta[4 * r + k];
       } else {
@@ -611,10 +615,10 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
       }
       if (v >= p && lane < 16) {
         const int r = lane >> 2, c = lane & 3, j = i + 1;
-        s_gblk[nslot][lane] = p == 0 ? ldcg_c(&a.G[(size_t)(j + c * N) * n + j + r * N])
+        s_gblk[nrs][lane] = p == 0 ? ldcg_c(&a.G[(size_t)(j + c * N) * n + j + r * N])
                                      : ldcg_c(&d.blk[(size_t)16 * j + lane]);
       }
-      if (lane == 0) s_gp[nslot] = v >= p ? p : -1;
+      if (lane == 0) s_gp[nrs] = v >= p ? p : -1;
     }
     if (wid < 4) {
       // ---- site i + 1's words (warp 3), then the pending factor entries
@@ -622,8 +626,8 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
       if (wid == 3 && i + 1 < N) {
         const double w0 = site_word(a, d, i + 1, lane);
         const double w1 = lane + 32 < kSiteWords ? site_word(a, d, i + 1, lane + 32) : 0.0;
-        s_site[nslot][lane] = w0;
-        if (lane + 32 < kSiteWords) s_site[nslot][lane + 32] = w1;
+        s_site[nrs][lane] = w0;
+        if (lane + 32 < kSiteWords) s_site[nrs][lane + 32] = w1;
       }
       constexpr int kStage = 128;
       for (int t = threadIdx.x; t < 4 * J; t += 2 * kStage) {
