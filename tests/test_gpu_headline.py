@@ -128,10 +128,11 @@ def test_l16_mixed_ten_sweeps_match_fp64(lib):
 def test_batched_benchmark_config(lib):
     """The batched configuration the benchmark runs: mixed form, delay picked
     by the autotuner, L in {6, 8, 10, 12}, M = 80, 8 chains in flight with
-    capped cooperative grids.  Every chain is bit-identical to the same chain
-    swept alone on the same grid shapes; the L=12 chain matches the oracle
-    (FP64) across a stabilisation within the mixed-form tolerance, with an
-    identical field (hence accept sequence)."""
+    capped cooperative grids, over one full sweep of M calls.  Every chain is
+    bit-identical to the same chain swept alone on the same grid shapes,
+    after the first 12 calls and after the sweep; after 12 calls the L=12
+    chain matches the oracle (FP64) across a stabilisation within the
+    mixed-form tolerance, with an identical field (hence accept sequence)."""
     torch = pytest.importorskip("torch")
     sizes = [12, 10, 8, 6, 12, 10, 8, 6]
     M, calls, inflight = 80, 12, 8
@@ -141,9 +142,10 @@ def test_batched_benchmark_config(lib):
                      mu2=-0.5, box=0.2)
         plist.append(p)
         fields.append(R.synthetic_field(p.N, M, 700 + k))
-        streams.append(R.synthetic_streams(p.N, calls, p.box, 800 + k))
+        streams.append(R.synthetic_streams(p.N, M, p.box, 800 + k))
     mps = [api_params(p, precision="mixed", inflight=inflight) for p in plist]
     batch = lib.Batch(mps, fields, autotune=True)
+    singles = []
     try:
         assert all(batch.params[i].delay in (8, 16, 32) for i in range(len(sizes)))
         batch.init()
@@ -155,20 +157,30 @@ def test_batched_benchmark_config(lib):
         stats = batch.sweep_device(calls, [t.data_ptr() for t in dev_d], [t.data_ptr() for t in dev_u])
         for k, p in enumerate(plist):
             single = lib.DQMC(batch.params[k], fields[k])
-            try:
-                single.init()
-                res = single.sweep(calls, streams[k][0], streams[k][1])
-                assert stats[k]["accepted"] == res["accepted"], k
-                assert np.array_equal(batch.chains[k].greens, single.greens), k
-                assert np.array_equal(batch.chains[k].get_field(), single.get_field()), k
-            finally:
-                single.close()
+            singles.append(single)
+            single.init()
+            res = single.sweep(calls, streams[k][0][:calls], streams[k][1][:calls])
+            assert stats[k]["accepted"] == res["accepted"], k
+            assert np.array_equal(batch.chains[k].greens, single.greens), k
+            assert np.array_equal(batch.chains[k].get_field(), single.get_field()), k
         ref = R.DQMCRef(plist[0], fields[0])
         ref.init()
-        ref.sweep(calls, streams[0][0], streams[0][1])
+        ref.sweep(calls, streams[0][0][:calls], streams[0][1][:calls])
         assert np.array_equal(batch.chains[0].get_field(), ref.phi)
         assert relerr(batch.chains[0].greens, ref.greens) < MIXED_TOL
+        # the rest of the sweep (M - 12 more calls, through the stabilisations
+        # and the turn at slice 1): still bit-identical to the chains alone
+        rest = M - calls
+        stats = batch.sweep_device(rest, [t.data_ptr() + calls * t.shape[1] * t.shape[2] * 8 for t in dev_d],
+                                   [t.data_ptr() + calls * t.shape[1] * 8 for t in dev_u])
+        for k, single in enumerate(singles):
+            res = single.sweep(rest, streams[k][0][calls:], streams[k][1][calls:])
+            assert stats[k]["accepted"] == res["accepted"], k
+            assert np.array_equal(batch.chains[k].greens, singles[k].greens), k
+            assert np.array_equal(batch.chains[k].get_field(), singles[k].get_field()), k
     finally:
+        for single in singles:
+            single.close()
         batch.close()
 
 
