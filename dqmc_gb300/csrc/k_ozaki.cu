@@ -843,7 +843,7 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
                                const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
                                const double* colscale, int S, int bits, void* scratch, size_t scratch_bytes,
                                unsigned long long* acc, size_t acc_bytes, cudaStream_t st, const int* active,
-                               int splitk, int* kernels, int* err) {
+                               int splitk, int* kernels, int* err, bool persistent) {
   if (S < 1 || S > TC_MAXS || bits < 1 || bits > 8) return cudaErrorInvalidValue;
   const int Kpad = (k + 15) / 16 * 16;
   const size_t Kp = 2 * (size_t)Kpad;
@@ -875,10 +875,12 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
   a.acc = nullptr;
   if (S > TC_MAXS || !err) return cudaErrorInvalidValue;
   // persistent CTAs: one per SM (each holds the whole TMEM), every CTA takes
-  // tiles x, x + grid, ... and overlaps a tile's epilogue with the next tile's MMAs
+  // tiles x, x + grid, ... and overlaps a tile's epilogue with the next tile's
+  // MMAs; otherwise one CTA per tile (chains sharing the GPU: short CTAs let
+  // the other chains' kernels in between)
   const int ntiles = ((nn + TC_BN - 1) / TC_BN) * ((m + TC_BM - 1) / TC_BM);
   const int sms = sm_count_of_current_device();
-  dim3 grid(ntiles < sms ? ntiles : sms);
+  dim3 grid(persistent && ntiles > sms ? sms : ntiles);
   const int ksteps = (int)((Kp + TC_BK - 1) / TC_BK);
   if (splitk > 1 && a.int_combine && !active && ksteps > 1 && acc &&
       (size_t)m * nn * 2 * sizeof(unsigned long long) <= acc_bytes) {

@@ -199,7 +199,7 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
                                const double* colscale, int S, int bits, void* scratch, size_t scratch_bytes,
                                unsigned long long* acc, size_t acc_bytes, cudaStream_t st,
                                const int* active = nullptr, int splitk = 1, int* kernels = nullptr,
-                               int* err = nullptr);
+                               int* err = nullptr, bool persistent = true);
 
 // ---- adjoint force (k_force.cu) ----
 // grad[:, :, slice0] = d log|det M| / d phi[:, :, slice0] from G of that slice
