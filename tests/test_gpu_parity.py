@@ -447,7 +447,7 @@ def test_time_displaced_greens(lib, golden, small_params, cfg, prec):
         assert relerr(g0t[tau], g0t_r[tau]) < tol, (tau, relerr(g0t[tau], g0t_r[tau]))
 
 
-@pytest.mark.parametrize("tune", ["lu_small=0", "lu_small=0,lu_cluster=8", "lu_small=0,lu_cluster=0",
+@pytest.mark.parametrize("tune", ["lu_small=0", "lu_small=0,lu_cluster=16", "lu_small=0,lu_cluster=8",
                                   "lu_small=4096"])
 @pytest.mark.parametrize("L,prec", [(6, "fp64"), (10, "fp64"), (10, "mixed")])
 def test_lu_blocked_and_unblocked(lib, monkeypatch, tune, L, prec):
