@@ -91,8 +91,8 @@ struct dqmc_handle {
   int wy_block = 128, trsm_block = 64, lu_grid = 64, lu_small = 576;
   // LU panels on one thread-block cluster of this many CTAs (16 or 8; 0: the
   // cooperative grid of lu_grid CTAs; DQMC_TUNE "lu_cluster=").  The grid is
-  // the default: at n = 1024 a panel took 320 us on 64 CTAs against 400 us on
-  // a cluster of 16 (FP64 on 16 SMs and the per-column steps bound it)
+  // the default: at n = 1024 both took about 0.3 ms per panel (the cluster's
+  // FP64 work on 16 SMs offsets its cheaper barriers) and 141 ms of LU per sweep
   int lu_cluster = 0;
   cplx* wy_v = nullptr;       // mixed form: (n x kWyMax) reflector block
   cplx* wy_s = nullptr;       // (kWyMax^2) Vb^H Vb
