@@ -56,11 +56,12 @@ METRIC = "O(3) L=16 sweeps/s: mixed vs FP64 at G err≤1e-8; batched chain-sweep
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # roofline kernels at L=16 (n = 1024), one ncu capture each of this bench's
-# L=16 mixed workload: k_qrp (one QR) and k_oz_gemm (one n x n x n product).
-# None: the kind is several kernels per algorithmic unit (blocked LU, blocked
+# L=16 mixed profiling workload (--profile-calls 12): k_qrp (one QR: 16.86 +
+# 4.16 MB) and k_oz_gemm_tc (one n x n x n product: 170.9 + 14.0 MB).  None:
+# the kind is several kernels per algorithmic unit (blocked LU, blocked
 # triangular solves, compact-WY Q formation, flush)
-TRAFFIC = {"qrp": 21.351e6, "lu": None, "apply_q": None, "trsm": None, "flush": None,
-           "ozaki_gemm": 333.239e6}
+TRAFFIC = {"qrp": 21.022e6, "lu": None, "apply_q": None, "trsm": None, "flush": None,
+           "ozaki_gemm": 184.852e6}
 
 
 def model_params(L, M):
