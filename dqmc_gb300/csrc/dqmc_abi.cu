@@ -14,7 +14,9 @@
 #include <utility>
 #include <string>
 #include <initializer_list>
+#include <array>
 #include <vector>
+#include <array>
 
 #include "../../include/dqmc_gpu.h"
 #include "common.cuh"
@@ -138,6 +140,7 @@ struct dqmc_handle {
   // only while sites remain; its body is captured on st_body
   cudaStream_t st_body = nullptr;
   bool while_off = false;     // conditional nodes refused once: fixed round count from then on
+  int64_t graph_epoch = 0;    // advanced whenever the captured launches may have gone stale
   int capture_while = 0;      // WHILE nodes added in the capture in progress
   int pending_while = 0;      // WHILE nodes of the enqueued sweep
   unsigned long long rounds_seen = 0;   // device round counter at the last sweep_finish
@@ -744,6 +747,7 @@ void clear_graphs(dqmc_handle* h) {
   for (auto& g : h->graphs)
     if (g.exec) cudaGraphExecDestroy(g.exec);
   h->graphs.clear();
+  ++h->graph_epoch;   // graphs of a batch that hold this chain's launches are stale too
 }
 
 int ensure_stream_capacity(dqmc_handle* h, int calls) {
@@ -1610,6 +1614,22 @@ int dqmc_sweep_device(dqmc_handle* h, int32_t n_calls, const double* delta_strea
 struct dqmc_batch {
   std::vector<dqmc_handle*> chains;
   int inflight = 1;   // chains swept at the same time
+  // the whole batch sweep as one CUDA graph: every chain's launches on its
+  // own stream, chain q after chain q - inflight, forked from and joined
+  // into st0; one graph per (calls, start state of every chain)
+  struct BatchGraph {
+    int n_calls = 0;
+    std::vector<int> slice0, dir0, slice1, dir1;
+    std::vector<std::array<int64_t, DQMC_NKINDS>> cnt;
+    std::vector<std::array<double, DQMC_NKINDS>> flops, bytes;
+    std::vector<int64_t> launches;
+    std::vector<int64_t> epoch;   // every chain's graph_epoch at the capture
+    cudaGraphExec_t exec = nullptr;
+  };
+  std::vector<BatchGraph> graphs;
+  bool graphs_off = false;
+  cudaStream_t st0 = nullptr;
+  cudaEvent_t fork = nullptr;
 };
 
 // Chains in flight per batch: enough to fill the SMs while each chain's
@@ -1646,8 +1666,140 @@ int dqmc_batch_create(const dqmc_params* params, int32_t count, dqmc_batch** out
 
 int dqmc_batch_destroy(dqmc_batch* b) {
   if (!b) return DQMC_ERR_ARG;
+  if (!b->chains.empty()) cudaSetDevice(b->chains[0]->device);
+  for (auto& g : b->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->st0) cudaStreamDestroy(b->st0);
   for (auto c : b->chains) dqmc_destroy(c);
   delete b;
+  return DQMC_OK;
+}
+
+// Captures the batch sweep from the chains' current states into one graph
+// (order: the launch order of the chains).  The chains' host states are left
+// as before (nothing has run).  Returns null, and stops trying for this
+// batch, if the capture is refused.
+static dqmc_batch::BatchGraph* batch_capture(dqmc_batch* b, int n_calls, const std::vector<int>& order) {
+  const int C = (int)b->chains.size();
+  dqmc_batch::BatchGraph g;
+  g.n_calls = n_calls;
+  g.slice0.resize(C); g.dir0.resize(C); g.slice1.resize(C); g.dir1.resize(C);
+  g.cnt.resize(C); g.flops.resize(C); g.bytes.resize(C); g.launches.resize(C); g.epoch.resize(C);
+  std::vector<std::array<int64_t, DQMC_NKINDS>> c0(C);
+  std::vector<std::array<double, DQMC_NKINDS>> f0(C), b0(C);
+  std::vector<int64_t> l0(C);
+  for (int i = 0; i < C; ++i) {
+    dqmc_handle* h = b->chains[i];
+    g.slice0[i] = h->current_slice; g.dir0[i] = h->direction; g.epoch[i] = h->graph_epoch;
+    for (int k = 0; k < DQMC_NKINDS; ++k) { c0[i][k] = h->cnt[k]; f0[i][k] = h->flops[k]; b0[i][k] = h->bytes[k]; }
+    l0[i] = h->launches;
+    h->capture_while = 0;
+  }
+  cudaGetLastError();
+  bool ok = cudaStreamBeginCapture(b->st0, cudaStreamCaptureModeThreadLocal) == cudaSuccess &&
+            cudaEventRecord(b->fork, b->st0) == cudaSuccess;
+  int rc = DQMC_OK;
+  for (int q = 0; ok && q < C; ++q) {
+    dqmc_handle* h = b->chains[order[q]];
+    ok = cudaStreamWaitEvent(h->st, b->fork, 0) == cudaSuccess;
+    if (ok && q >= b->inflight)
+      ok = cudaStreamWaitEvent(h->st, b->chains[order[q - b->inflight]]->done, 0) == cudaSuccess;
+    if (ok) rc = sweep_body(h, n_calls, h->delta_d, h->unif_d, nullptr);
+    ok = ok && rc == DQMC_OK && h->capture_while == 0 && cudaEventRecord(h->done, h->st) == cudaSuccess;
+  }
+  for (int q = 0; ok && q < C; ++q) ok = cudaStreamWaitEvent(b->st0, b->chains[order[q]]->done, 0) == cudaSuccess;
+  cudaGraph_t graph = nullptr;
+  const bool ended = cudaStreamEndCapture(b->st0, &graph) == cudaSuccess;
+  ok = ok && ended && graph;
+  if (ok) ok = cudaGraphInstantiate(&g.exec, graph, 0) == cudaSuccess;
+  if (graph) cudaGraphDestroy(graph);
+  for (int i = 0; i < C; ++i) {
+    dqmc_handle* h = b->chains[i];
+    g.slice1[i] = h->current_slice; g.dir1[i] = h->direction;
+    for (int k = 0; k < DQMC_NKINDS; ++k) {
+      g.cnt[i][k] = h->cnt[k] - c0[i][k]; g.flops[i][k] = h->flops[k] - f0[i][k]; g.bytes[i][k] = h->bytes[k] - b0[i][k];
+      h->cnt[k] = c0[i][k]; h->flops[k] = f0[i][k]; h->bytes[k] = b0[i][k];
+    }
+    g.launches[i] = h->launches - l0[i];
+    h->launches = l0[i];
+    h->current_slice = g.slice0[i]; h->direction = g.dir0[i];
+    h->last_error.clear();
+  }
+  cudaGetLastError();
+  if (!ok) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    b->graphs_off = true;
+    return nullptr;
+  }
+  b->graphs.push_back(std::move(g));
+  return &b->graphs.back();
+}
+
+// The batch sweep as one graph launch on st0 (streams copied into each
+// chain's own buffers first).  Returns kBatchUngraphed, with nothing
+// enqueued, when the chains are not graphed (timing on, capture refused).
+constexpr int kBatchUngraphed = 1;
+static int batch_graph_sweep(dqmc_batch* b, int n_calls, const std::vector<int>& order,
+                             const double* const* delta_dev, const double* const* unif_dev) {
+  const int C = (int)b->chains.size();
+  dqmc_handle* h = b->chains[0];   // error reports (CU, CHK) go to the first chain
+  if (b->graphs_off) return kBatchUngraphed;
+  for (auto c : b->chains)
+    if (c->timing || c->graphs_off || c->device != h->device) return kBatchUngraphed;
+  cudaSetDevice(h->device);
+  if (!b->st0) CU(cudaStreamCreateWithFlags(&b->st0, cudaStreamNonBlocking));
+  if (!b->fork) CU(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  for (auto c : b->chains) {
+    CHK(ensure_stream_capacity(c, n_calls));
+    if (!c->done) CU(cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming));
+    if (!c->ev0) {
+      CU(cudaEventCreate(&c->ev0));
+      CU(cudaEventCreate(&c->ev1));
+    }
+    CU(cudaStreamSynchronize(c->st));   // work queued on a chain's own stream ends before the graph
+  }
+  dqmc_batch::BatchGraph* g = nullptr;
+  for (auto& x : b->graphs) {
+    if (x.n_calls != n_calls) continue;
+    bool same = true;
+    for (int i = 0; i < C && same; ++i)
+      same = x.slice0[i] == b->chains[i]->current_slice && x.dir0[i] == b->chains[i]->direction &&
+             x.epoch[i] == b->chains[i]->graph_epoch;
+    if (same) { g = &x; break; }
+  }
+  if (!g) g = batch_capture(b, n_calls, order);
+  if (!g) return kBatchUngraphed;
+  // per chain, on st0 before the graph: the streams into the chain's buffers,
+  // the acceptance counter snapshot, the instability maximum reset
+  for (int i = 0; i < C; ++i) {
+    dqmc_handle* c = b->chains[i];
+    const size_t N = c->N;
+    if (delta_dev[i] != c->delta_d)
+      CU(cudaMemcpyAsync(c->delta_d, delta_dev[i], (size_t)n_calls * 3 * N * sizeof(double), cudaMemcpyDeviceToDevice,
+                         b->st0));
+    if (unif_dev[i] != c->unif_d)
+      CU(cudaMemcpyAsync(c->unif_d, unif_dev[i], (size_t)n_calls * N * sizeof(double), cudaMemcpyDeviceToDevice,
+                         b->st0));
+    CU(cudaMemcpyAsync(c->nacc_d + 1, c->nacc_d, sizeof(int), cudaMemcpyDeviceToDevice, b->st0));
+    CU(cudaMemsetAsync(c->scal_d + 3, 0, sizeof(double), b->st0));
+    c->max_instability = 0.0;
+    CU(cudaEventRecord(c->ev0, b->st0));
+  }
+  CU(cudaGraphLaunch(g->exec, b->st0));
+  for (int i = 0; i < C; ++i) {
+    dqmc_handle* c = b->chains[i];
+    CU(cudaEventRecord(c->ev1, b->st0));
+    c->current_slice = g->slice1[i];
+    c->direction = g->dir1[i];
+    for (int k = 0; k < DQMC_NKINDS; ++k) {
+      c->cnt[k] += g->cnt[i][k]; c->flops[k] += g->flops[i][k]; c->bytes[k] += g->bytes[i][k];
+    }
+    c->launches += g->launches[i];
+    c->pending_calls = n_calls;
+    c->pending_while = 0;
+  }
+  CU(cudaStreamSynchronize(b->st0));
   return DQMC_OK;
 }
 
@@ -1657,10 +1809,10 @@ int dqmc_batch_handle(dqmc_batch* b, int32_t i, dqmc_handle** h) {
   return DQMC_OK;
 }
 
-// Largest chains first, in waves of `inflight` chains of similar size; within
-// a wave the update calls are issued round-robin over the chains (one call of
-// each chain in turn), so the launch queue always holds work of every chain
-// of the wave and their streams run side by side.
+// Largest chains first; chain q starts once chain q - inflight has finished,
+// so `inflight` chains run at a time, each with its capped cooperative grids.
+// The whole batch sweep is one graph launch (batch_graph_sweep); launch by
+// launch (timing on) every chain's sweep is enqueued on its own stream.
 int dqmc_batch_sweep(dqmc_batch* b, int32_t n_calls, const double* const* delta_dev, const double* const* unif_dev,
                      dqmc_stats* stats) {
   if (!b || n_calls < 0 || !delta_dev || !unif_dev) return DQMC_ERR_ARG;
@@ -1676,9 +1828,17 @@ int dqmc_batch_sweep(dqmc_batch* b, int32_t n_calls, const double* const* delta_
   for (int i = 0; i < C; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->chains[x]->n > b->chains[y]->n; });
   int rc = DQMC_OK;
-  // largest chains first; chain q starts once chain q - inflight has finished
-  // (a stream wait on its end event), so `inflight` chains run at a time, each
-  // with its capped cooperative grids; every chain's sweep is one graph launch
+  const int gr = batch_graph_sweep(b, n_calls, order, delta_dev, unif_dev);
+  if (gr != kBatchUngraphed) {
+    if (gr != DQMC_OK) return gr;
+    for (int q = 0; q < C; ++q) {
+      dqmc_handle* h = b->chains[order[q]];
+      int r = sweep_finish(h, stats ? &stats[order[q]] : nullptr);
+      if (r != DQMC_OK && rc == DQMC_OK) rc = r;
+    }
+    return rc;
+  }
+  // launch by launch: chain q's stream waits on the end event of chain q - inflight
   for (int q = 0; q < C; ++q) {
     dqmc_handle* h = b->chains[order[q]];
     cudaSetDevice(h->device);
