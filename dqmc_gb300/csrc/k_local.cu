@@ -589,17 +589,20 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         if (lane < 16) s_adj[slot][lane] = adj;
       }
     } else if (wid == 5) {
-      // ---- boson action difference: prepared part + space-neighbour coupling ----
+      // ---- boson action difference: prepared part + space-neighbour coupling;
+      //      lanes 0-2 sum the neighbours' component c = lane (the same four
+      //      additions in the same order), lane 0 takes the rest ----
+      const int y = i % L, x = i / L;
+      const int nbs[4] = {(y + 1) % L + L * x, y + L * ((x + 1) % L), (y - 1 + L) % L + L * x,
+                          y + L * ((x - 1 + L) % L)};
+      double os = 0.0;
+      if (lane < 3)
+        for (int q = 0; q < 4; ++q) os = os + phis[3 * nbs[q] + lane];
+      const double os1 = __shfl_sync(0xffffffffu, os, 1), os2 = __shfl_sync(0xffffffffu, os, 2);
       if (lane == 0) {
-        const int y = i % L, x = i / L;
-        const int nbs[4] = {(y + 1) % L + L * x, y + L * ((x + 1) % L), (y - 1 + L) % L + L * x,
-                            y + L * ((x - 1 + L) % L)};
+        const double osc[3] = {os, os1, os2};
         double sdot = 0.0;
-        for (int c = 0; c < 3; ++c) {
-          double os = 0.0;
-          for (int q = 0; q < 4; ++q) os = os + phis[3 * nbs[q] + c];
-          sdot += os * sw[kSiteDiff + c];
-        }
+        for (int c = 0; c < 3; ++c) sdot += osc[c] * sw[kSiteDiff + c];
         double dS = sw[kSiteDiff + 3];
         dS += 0.5 * mc.dtau * (sw[kSiteDiff + 4] - 2.0 * sdot);
         dS += sw[kSiteDiff + 5];
