@@ -474,6 +474,11 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   __shared__ cplx s_adj[2][16];     // adj(M)[r][c] (double-buffered by site parity)
   __shared__ cplx s_det[2];
   __shared__ double s_expds[2];
+  // the decision, taken by whichever of the det lane and the exp(-dS) lane
+  // finishes second (s_dcnt counts their arrivals), read by all after the
+  // barrier: bit 0 accepted, bit 1 non-finite determinant
+  __shared__ int s_dcnt[2], s_dec[2];
+  __shared__ double s_pacc[2];
   // per site (slot i & 1), read during the previous site's decision: the
   // SitePrep words, the Metropolis uniform and the proposal (site_word), and
   // the site's G_cur block, current if no acceptance came in between
@@ -511,7 +516,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
     const int e = threadIdx.x - 64, r = e >> 2, c = e & 3;
     s_gblk[first % 3][e] = ldcg_c(&a.G[(size_t)(first + c * N) * n + first + r * N]);
   }
-  if (threadIdx.x == 0) s_gp[first % 3] = 0;
+  if (threadIdx.x == 0) { s_gp[first % 3] = 0; s_dcnt[0] = 0; s_dcnt[1] = 0; }
   if (!grid_barrier(a.bar, a.err, bar_epoch)) return;
 
   // phase-1 role of this warp in the first pass of owned sites
@@ -526,6 +531,21 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
     const cplx* sdelta = reinterpret_cast<const cplx*>(sw);      // Delta_i, row-major
     // the block read ahead is current unless an acceptance came in between
     const bool have_g = s_gp[rs] == p;
+    // the Metropolis decision from det M and exp(-dS) (src/local_updates.jl:20-30),
+    // by the second of the two lanes that produce them
+    auto arrive_decide = [&]() {
+      __threadfence_block();
+      if (atomicAdd(&s_dcnt[slot], 1) == 1) {
+        __threadfence_block();
+        const cplx dt = s_det[slot];
+        const double pa = s_expds[slot] * dt.x;
+        const bool bad = !isfinite(dt.x) || !isfinite(dt.y) || (dt.x == 0.0 && dt.y == 0.0);
+        const bool ac = !bad && (pa > 1.0 || sw[kSiteUnif] < pa);
+        s_pacc[slot] = pa;
+        s_dec[slot] = (ac ? 1 : 0) | (bad ? 2 : 0);
+        s_dcnt[slot] = 0;
+      }
+    };
     // ---- otherwise wait until the owner of site i has folded in all p acceptances ----
     if (p > 0 && !have_g) {
       if (threadIdx.x == 0) {
@@ -583,7 +603,10 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         cplx det = term;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) det = cadd(det, shfl_c(det, lane ^ o));
-        if (lane == 0) s_det[slot] = det;
+        if (lane == 0) {
+          s_det[slot] = det;
+          arrive_decide();
+        }
       } else {
         const cplx adj = adjugate_entry(m, lane);
         if (lane < 16) s_adj[slot][lane] = adj;
@@ -607,6 +630,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         dS += 0.5 * mc.dtau * (sw[kSiteDiff + 4] - 2.0 * sdot);
         dS += sw[kSiteDiff + 5];
         s_expds[slot] = exp(-dS);
+        arrive_decide();
       }
     } else if (wid == 7 && i + 1 < N) {
       // ---- site i + 1's G_cur block, ahead of time: current if site i is
@@ -652,13 +676,12 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
       }
     }
     __syncthreads();
-    // ---- Metropolis decision: every thread evaluates it from the same shared
-    //      values (the same in every CTA); thread 0 writes its effects ----
+    // ---- Metropolis decision (the same in every CTA); thread 0 writes its effects ----
+    const int dec = s_dec[slot];
+    const bool acc = (dec & 1) != 0, bad = (dec & 2) != 0;
     const cplx det = s_det[slot];
     const double exp_dS = s_expds[slot];
-    const double pacc = exp_dS * det.x;
-    const bool bad = !isfinite(det.x) || !isfinite(det.y) || (det.x == 0.0 && det.y == 0.0);
-    const bool acc = !bad && (pacc > 1.0 || sw[kSiteUnif] < pacc);
+    const double pacc = s_pacc[slot];
     if (threadIdx.x == 0) {
       if (acc)
         for (int q = 0; q < 3; ++q) phis[3 * i + q] += sw[kSiteProp + q];
