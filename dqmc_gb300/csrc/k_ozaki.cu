@@ -16,8 +16,9 @@
 //    A' = [Re A, Im A] and B'_re = [Re B; -Im B], B'_im = [Im B; Re B];
 //  * slice pairs (p, q) with p + q = t <= S + 1 are accumulated into one FP32
 //    accumulator per t; with K' * S * 2^{2 B_BITS} <= 2^24 every partial sum is
-//    an integer below 2^24, so the FP32 accumulation is exact; the groups are
-//    combined in FP64 with their weights 2^{-B_BITS t} and the scales.
+//    an integer below 2^24, so the FP32 accumulation is exact; the group sums
+//    are combined exactly in 64-bit integers (Horner in 2^B_BITS) and the
+//    result converted once with its power-of-two weight and the scales.
 // The only error is the truncation of the slice expansion (~2^{-B_BITS S}
 // relative to sigma_i tau_j K).
 //
