@@ -650,11 +650,13 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
     if (wid < 4) {
       // ---- site i + 1's words (warp 3), then the pending factor entries
       //      touching site i (128 threads, loads issued together) ----
-      if (wid == 3 && i + 1 < N) {
-        const double w0 = site_word(a, d, i + 1, lane);
-        const double w1 = lane + 32 < kSiteWords ? site_word(a, d, i + 1, lane + 32) : 0.0;
-        s_site[nrs][lane] = w0;
-        if (lane + 32 < kSiteWords) s_site[nrs][lane + 32] = w1;
+      // (the words are loaded first and stored last, so that their latency
+      // overlaps the staging loads)
+      const bool words = wid == 3 && i + 1 < N;
+      double w0 = 0.0, w1 = 0.0;
+      if (words) {
+        w0 = site_word(a, d, i + 1, lane);
+        if (lane + 32 < kSiteWords) w1 = site_word(a, d, i + 1, lane + 32);
       }
       constexpr int kStage = 128;
       for (int t = threadIdx.x; t < 4 * J; t += 2 * kStage) {
@@ -673,6 +675,10 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
           Ysm[4 * j2 + c2] = y2;
           Xsm[(size_t)c2 * K4 + j2] = x2;
         }
+      }
+      if (words) {
+        s_site[nrs][lane] = w0;
+        if (lane + 32 < kSiteWords) s_site[nrs][lane + 32] = w1;
       }
     }
     __syncthreads();
