@@ -384,6 +384,30 @@ __global__ void __launch_bounds__(128) k_local_prepare(LocalUpdateArgs a, SitePr
   }
 }
 
+// det M by the Laplace expansion along rows {0, 1}: the 2x2 minors T_ab of
+// rows {0, 1} (lanes 0-5) and B_ab of rows {2, 3} (lanes 6-11), pairs (a, b)
+// in the order (0,1) (0,2) (0,3) (1,2) (1,3) (2,3), and
+// det = sum_ab (-1)^(a+b+1) T_ab B_(complement of ab); m[r][c] in lane 4r+c.
+// The sum is complete in lane 0 (lanes 0-7 take part in it).
+__device__ __forceinline__ cplx det_laplace(cplx m, int lane) {
+  const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {1, 2, 3, 2, 3, 3};
+  const int mi = lane < 12 ? lane : 0;
+  const int pr = mi < 6 ? 0 : 2, pp = mi < 6 ? mi : mi - 6;
+  const cplx e00 = shfl_c(m, 4 * pr + pa[pp]), e01 = shfl_c(m, 4 * pr + pb[pp]);
+  const cplx e10 = shfl_c(m, 4 * (pr + 1) + pa[pp]), e11 = shfl_c(m, 4 * (pr + 1) + pb[pp]);
+  const cplx minor = csub(cmul(e00, e11), cmul(e01, e10));
+  // lane pp < 6: T_pp times B of the complementary pair (index 5 - pp, in lane 11 - pp)
+  const cplx bc = shfl_c(minor, lane < 6 ? 11 - lane : 0);
+  cplx term = cmake(0.0, 0.0);
+  if (lane < 6) {
+    term = cmul(minor, bc);
+    if (lane == 1 || lane == 4) term = cmake(-term.x, -term.y);   // (a + b) even: (0,2), (1,3)
+  }
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) term = cadd(term, shfl_c(term, lane ^ o));
+  return term;
+}
+
 // adj(M)[r][c] = cofactor C[c][r] for lane 4r+c (lanes < 16), from the 2x2
 // minors of rows {0,1} and {2,3} (Laplace expansion of each 3x3 minor along
 // its single row from the other pair); m[r][c] in lane 4r+c.
@@ -588,21 +612,15 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
         for (int k = 0; k < 4; ++k) drow[k] = cmake(0.0, 0.0);
       }
       const cplx mt = cmake((r == c ? 1.0 : 0.0) - g.x, -g.y);   // (I - G_ii)[r][c]
-      cplx m = cmake(r == c ? 1.0 : 0.0, 0.0);
-#pragma unroll
-      for (int k = 0; k < 4; ++k) m = cfma(drow[k], shfl_c(mt, 4 * k + c), m);
+      // M[r][c] = I + sum_k Delta[r][k] (I - G_ii)[k][c], as two independent pairs
+      const cplx m01 = cfma(drow[1], shfl_c(mt, 4 + c), cmul(drow[0], shfl_c(mt, c)));
+      const cplx m23 = cfma(drow[3], shfl_c(mt, 12 + c), cmul(drow[2], shfl_c(mt, 8 + c)));
+      cplx m = cadd(m01, m23);
+      if (r == c) m.x += 1.0;
       if (wid == 4) {
-        // det M by the permutation expansion (24 lanes); lane 0's sum is the
-        // one used everywhere, so every CTA decides bit for bit alike
-        const int jp = lane < 24 ? lane : 0;
-        cplx pr = shfl_c(m, c_perm[jp][0]);
-#pragma unroll
-        for (int rr = 1; rr < 4; ++rr) pr = cmul(pr, shfl_c(m, 4 * rr + c_perm[jp][rr]));
-        cplx term = cmake(0.0, 0.0);
-        if (lane < 24) term = c_psign[jp] > 0 ? pr : cmake(-pr.x, -pr.y);
-        cplx det = term;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) det = cadd(det, shfl_c(det, lane ^ o));
+        // det M (Laplace expansion by 2x2 minors); lane 0's sum is the one
+        // used everywhere, so every CTA decides bit for bit alike
+        const cplx det = det_laplace(m, lane);
         if (lane == 0) {
           s_det[slot] = det;
           arrive_decide();
