@@ -310,7 +310,7 @@ double ozaki_tensor_flops(double m, double nn, double k, int S) {
 }
 int zgemm_general(dqmc_handle* h, int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
                   const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rs, const double* cs,
-                  bool allow_split, int kind = -1, const int* active = nullptr) {
+                  bool allow_split, int kind = -1, const int* active = nullptr, bool presliced = false) {
   if (allow_split && h->p.precision == DQMC_PREC_MIXED) {
     int S = 0, bits = 0;
     if (!ozaki_plan(k, h->oz_target, &S, &bits)) return set_err(h, DQMC_ERR_ARG, "no exact slicing for this K");
@@ -325,7 +325,7 @@ int zgemm_general(dqmc_handle* h, int m, int nn, int k, char opA, char opB, cplx
     LAUNCH(kind >= 0 ? kind : DQMC_K_OZGEMM, ozaki_tensor_flops(m, nn, k, S), gemm_bytes(m, nn, k),
            launch_ozaki_zgemm(m, nn, k, opA, opB, alpha, A, lda, B, ldb, beta, C, ldc, rs, cs, S, bits,
                               h->oz_scratch, h->oz_bytes, h->oz_acc, h->oz_acc_bytes, h->st, active, splitk,
-                              &kernels, h->err_d, h->coop_cap == 0));
+                              &kernels, h->err_d, h->coop_cap == 0, presliced));
     h->launches += kernels - 1;   // slicing kernels and the split-K finaliser
     return DQMC_OK;
   }
@@ -879,7 +879,16 @@ int local_updates_dev(dqmc_handle* h, const double* delta_dev, const double* uni
     return DQMC_OK;
   }
   const int n = h->n, k = h->delay;
-  DelayedArgs d{h->Xd, h->Yd, h->dstate, k, h->prep, h->blk, h->pub};
+  DelayedArgs d{h->Xd, h->Yd, h->dstate, k, h->prep, h->blk, h->pub, {}};
+  // mixed form: the delayed kernel cuts the flush's slices at the round's end
+  bool presliced = false;
+  if (h->p.precision == DQMC_PREC_MIXED) {
+    int S = 0, bits = 0;
+    if (ozaki_plan(4 * k, h->oz_target, &S, &bits) && ozaki_scratch_bytes(n, n, 4 * k, S) <= h->oz_bytes) {
+      d.sl = ozaki_slices(h->oz_scratch, n, n, 4 * k, S, bits);
+      presliced = true;
+    }
+  }
   LAUNCH(DQMC_K_LOCAL, 0.0, 0.0, launch_local_prepare(a, h->prep, h->dstate, h->st));
   const int rounds = (h->N + k - 1) / k + 1;
   auto round = [&]() -> int {
@@ -887,7 +896,7 @@ int local_updates_dev(dqmc_handle* h, const double* delta_dev, const double* uni
     // flush G += X Y over the 4p pending columns (p read on the device; no
     // work when p = 0); the next round clears p
     return zgemm_general(h, n, n, 4 * k, 'N', 'T', cmake(1, 0), h->Xd, n, h->Yd, n, cmake(1, 0), h->G, n, nullptr,
-                         nullptr, true, DQMC_K_FLUSH, h->dstate + 1);
+                         nullptr, true, DQMC_K_FLUSH, h->dstate + 1, presliced);
   };
   // the WHILE node only for a chain that has the GPU to itself: with chains
   // in flight together (coop_cap > 0) it cost a batch of 64 chains 28% of its

@@ -25,6 +25,7 @@
 // `p_acc > 1.0 || rand() < p_acc`.
 #include "common.cuh"
 #include "kernels.h"
+#include "oz_slice.cuh"
 
 namespace {
 
@@ -517,6 +518,20 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   // gets the same additions -log(exp(-dS)) in the same order once the round
   // ends, off the per-site chain (no read-modify-write of global memory per site)
   __shared__ double s_expq[64];
+  // mixed form: every CTA cuts the BF16 slices of its own rows of X and
+  // columns of Y (K = 4 pend entries each, zeros up to Kpad) for the flush
+  // that follows, so the flush needs no slicing launch
+  auto slice_round = [&](int pend) {
+    if (d.sl.As == nullptr || pend == 0) return;
+    __syncthreads();   // every thread's X / Y entries of the round are stored
+    const int K = 4 * pend, ln = threadIdx.x & 31;
+    for (int t = threadIdx.x >> 5; t < 8 * owned; t += blockDim.x >> 5) {
+      const int ts = t >> 3, sub = (t >> 1) & 3, side = t & 1;
+      const int rc = blockIdx.x + ts * gridDim.x + sub * N;
+      const cplx* src = side ? d.Y : d.X;
+      oz_slice_vec(d.sl, side, rc, K, [&](int jj) { return ldcg_c(&src[(size_t)jj * n + rc]); }, ln);
+    }
+  };
   auto finish_round = [&](int pend) {
     if (blockIdx.x == 0 && threadIdx.x == 0 && pend > 0) {
       double act = *a.action;
@@ -814,6 +829,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
     if (p == d.k || i == N - 1) {
       if (blockIdx.x == 0 && threadIdx.x == 0) { d.state[0] = i + 1; d.state[1] = p; }
       finish_round(p);
+      slice_round(p);
       return;   // the flush follows as its own launch
     }
     // ---- publish: the owned later sites now include p acceptances (the CTA
@@ -828,6 +844,7 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) { d.state[0] = N; d.state[1] = p; }
   finish_round(p);
+  slice_round(p);
 }
 
 // Condition of the graph's WHILE node that repeats [delayed round, flush]:

@@ -35,6 +35,7 @@
 #include <type_traits>
 #include "common.cuh"
 #include "kernels.h"
+#include "oz_slice.cuh"
 
 namespace {
 
@@ -48,44 +49,7 @@ __device__ __forceinline__ cplx op_elem(const cplx* X, int ld, int r, int c, cha
   return op == 'C' ? cconj(v) : v;
 }
 
-// The slicing runs on the integer units.  A row (column) scale is 2^E with
-// E the frexp exponent of its largest |Re|/|Im|, taken from the exponent
-// fields; x 2^-E (|.| < 1) becomes a 62-bit fixed-point integer built from
-// the mantissa, and the S signed digits are cut off it by shifts, each
-// rounded half to even: the same digits as rint on the FP64 value, which is
-// exact at every step.
-__device__ __forceinline__ int expo_field(double x) {
-  return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
-}
-
-// x 2^(62 - E) as an integer (|x| < 2^E); values below 2^(E-62) are dropped
-__device__ __forceinline__ long long fixed62(double x, int E) {
-  const long long b = __double_as_longlong(x);
-  const int ef = (int)((b >> 52) & 0x7FF);
-  if (ef == 0) return 0;
-  const long long m = (b & 0xFFFFFFFFFFFFFll) | 0x10000000000000ll;   // x = m 2^(ef - 1075)
-  const int sh = ef - 1075 - E + 62;                                   // <= 9
-  long long X = 0;
-  if (sh >= 0) X = m << sh;
-  else if (sh > -63) X = m >> (-sh);
-  return b < 0 ? -X : X;
-}
-
-// next digit: round(X / 2^s) half to even, X <- X - digit 2^s
-__device__ __forceinline__ int next_digit(long long& X, int s) {
-  if (s <= 0) {
-    const long long d = s == 0 ? X : X * (1ll << -s);
-    X = 0;
-    return (int)d;
-  }
-  long long q = X >> s;                        // floor
-  const long long r = X - (q << s);            // in [0, 2^s)
-  const long long half = 1ll << (s - 1);
-  if (r > half || (r == half && (q & 1))) ++q;
-  X -= q << s;
-  return (int)q;
-}
-
+// (the digit helpers expo_field, fixed62 and next_digit are in oz_slice.cuh)
 __device__ __forceinline__ int block_max_int(int v, int* red) {
   for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
@@ -200,35 +164,11 @@ __global__ void __launch_bounds__(256) k_oz_split_tiled(const cplx* __restrict__
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const size_t Kp = 2 * (size_t)Kpad;
+  const OzSlices o{As, Bre, Bim, sA, sB, m, nn, Kpad, S, bits};
   for (int v = wid; v < OZ_TILED_V; v += blockDim.x >> 5) {
     const int vec = v0 + v;
     if (vec >= cnt) break;
-    int me = 0;
-    for (int k = lane; k < K; k += 32) me = max(me, max(expo_field(tile[k][v].x), expo_field(tile[k][v].y)));
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) me = max(me, __shfl_xor_sync(0xffffffffu, me, o));
-    const int E = me > 0 ? me - 1022 : 0;   // 2^E > max |.| (frexp exponent)
-    if (lane == 0) (side ? sB : sA)[vec] = ldexp(1.0, E);
-    for (int k = lane; k < Kpad; k += 32) {
-      const cplx x = tile[k][v];
-      long long xr = fixed62(x.x, E), xi = fixed62(x.y, E);
-      for (int p = 0; p < S; ++p) {
-        const int sft = 62 - (p + 1) * bits;
-        const int ar = next_digit(xr, sft), ai = next_digit(xi, sft);
-        if (side == 0) {
-          __nv_bfloat16* o = As + (size_t)p * m * Kp + (size_t)vec * Kp;
-          o[k] = __float2bfloat16_rn((float)ar);
-          o[Kpad + k] = __float2bfloat16_rn((float)ai);
-        } else {
-          const size_t base = (size_t)p * nn * Kp + (size_t)vec * Kp;
-          Bre[base + k] = __float2bfloat16_rn((float)ar);
-          Bre[base + Kpad + k] = __float2bfloat16_rn((float)-ai);
-          Bim[base + k] = __float2bfloat16_rn((float)ai);
-          Bim[base + Kpad + k] = __float2bfloat16_rn((float)ar);
-        }
-      }
-    }
+    oz_slice_vec(o, side, vec, K, [&](int k) { return tile[k][v]; }, lane);
   }
 }
 
@@ -791,6 +731,19 @@ bool ozaki_plan(int K, int target_bits, int* S_out, int* bits_out) {
   return false;
 }
 
+OzSlices ozaki_slices(void* scratch, int m, int n, int K, int S, int bits) {
+  const int Kpad = (K + 15) / 16 * 16;
+  const size_t Kp = 2 * (size_t)Kpad;
+  OzSlices o;
+  o.As = reinterpret_cast<__nv_bfloat16*>(scratch);
+  o.Bre = o.As + (size_t)S * m * Kp;
+  o.Bim = o.Bre + (size_t)S * n * Kp;
+  o.sA = reinterpret_cast<double*>(o.Bim + (size_t)S * n * Kp);
+  o.sB = o.sA + m;
+  o.m = m; o.n = n; o.Kpad = Kpad; o.S = S; o.bits = bits;
+  return o;
+}
+
 // Scratch: As S*m*Kp, Bre/Bim S*n*Kp bf16, scales m + n doubles.
 size_t ozaki_scratch_bytes(int m, int n, int K, int S) {
   const size_t Kpad = ((size_t)K + 15) / 16 * 16;
@@ -844,21 +797,20 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
                                const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
                                const double* colscale, int S, int bits, void* scratch, size_t scratch_bytes,
                                unsigned long long* acc, size_t acc_bytes, cudaStream_t st, const int* active,
-                               int splitk, int* kernels, int* err, bool persistent) {
+                               int splitk, int* kernels, int* err, bool persistent, bool presliced) {
   if (S < 1 || S > TC_MAXS || bits < 1 || bits > 8) return cudaErrorInvalidValue;
   const int Kpad = (k + 15) / 16 * 16;
   const size_t Kp = 2 * (size_t)Kpad;
   // exactness of the FP32 group sums: Kp * S * 2^(2 bits) <= 2^24
   if ((double)Kp * S * ldexp(1.0, 2 * bits) > 16777216.0) return cudaErrorInvalidValue;
   if (ozaki_scratch_bytes(m, nn, k, S) > scratch_bytes) return cudaErrorInvalidValue;
-  char* base = static_cast<char*>(scratch);
-  __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(base);
-  __nv_bfloat16* Bre = As + (size_t)S * m * Kp;
-  __nv_bfloat16* Bim = Bre + (size_t)S * nn * Kp;
-  double* sA = reinterpret_cast<double*>(Bim + (size_t)S * nn * Kp);
-  double* sB = sA + m;
+  const OzSlices sl = ozaki_slices(scratch, m, nn, k, S, bits);
+  __nv_bfloat16 *As = sl.As, *Bre = sl.Bre, *Bim = sl.Bim;
+  double *sA = sl.sA, *sB = sl.sB;
   const bool tiled = opA == 'N' && opB == 'T' && Kpad <= OZ_TILED_KMAX;
-  if (tiled) {
+  if (presliced) {
+    // the slices are already in scratch (cut by the delayed local-update kernel)
+  } else if (tiled) {
     const int vecs = m > nn ? m : nn;
     k_oz_split_tiled<<<dim3((vecs + OZ_TILED_V - 1) / OZ_TILED_V, 2), 32 * OZ_TILED_V, 0, st>>>(A, lda, m, B, ldb, nn, k, Kpad, S, bits, As, Bre, Bim,
                                                                sA, sB, active);
@@ -892,7 +844,7 @@ cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx al
     grid.z = (ksteps + a.kchunk - 1) / a.kchunk;
     a.acc = acc;
   }
-  if (kernels) *kernels = (a.acc ? 4 : 3) - (tiled ? 1 : 0);
+  if (kernels) *kernels = (a.acc ? 4 : 3) - (presliced ? 2 : tiled ? 1 : 0);
   {
     TcMaps maps;
     if (!encode_slices(&maps.a, As, Kp, m, S, TC_BM) || !encode_slices(&maps.bre, Bre, Kp, nn, S, TC_BN) ||

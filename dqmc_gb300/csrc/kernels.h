@@ -1,6 +1,7 @@
 // Host-side launch interface of the device kernels (internal to the library).
 #pragma once
 #include <cuda_runtime.h>
+#include <cuda_bf16.h>
 #include <stdint.h>
 #include "common.cuh"
 
@@ -58,6 +59,14 @@ struct SitePrep {
 };
 // state (2 ints, nullable): delayed-round state of the slice, zeroed here
 cudaError_t launch_local_prepare(const LocalUpdateArgs& a, SitePrep* prep, int* state, cudaStream_t st);
+// BF16 slices of the operands of an m x n x K split-BF16 product in its
+// scratch block: As S x (m x Kp), Bre / Bim S x (n x Kp) (K contiguous, Kp =
+// 2 Kpad), row scales sA (m), column scales sB (n)
+struct OzSlices {
+  __nv_bfloat16 *As, *Bre, *Bim;
+  double *sA, *sB;
+  int m, n, Kpad, S, bits;
+};
 struct DelayedArgs {
   cplx* X;
   cplx* Y;
@@ -66,6 +75,8 @@ struct DelayedArgs {
   const SitePrep* prep;    // (N) from launch_local_prepare for this slice
   cplx* blk;               // (N, 16) cache of the diagonal blocks G_cur[j + rN, j + cN]
   int* pub;                // (N) acceptances of the current round folded into site j's data
+  OzSlices sl;             // mixed form: the flush's slices, cut by the owners at the round's end
+                           // (sl.As null: the flush slices X and Y itself)
 };
 cudaError_t launch_local_delayed(const LocalUpdateArgs& a, const DelayedArgs& d, int sm_count, cudaStream_t st,
                                  int max_grid = 0);
@@ -194,12 +205,14 @@ cudaError_t measure_peak_fp64(int device, double* tflops);
 // ---- split-precision complex GEMM (k_ozaki.cu) ----
 bool ozaki_plan(int K, int target_bits, int* S, int* bits);
 size_t ozaki_scratch_bytes(int m, int n, int K, int S);
+// where launch_ozaki_zgemm keeps the slices of an m x n x K product in scratch
+OzSlices ozaki_slices(void* scratch, int m, int n, int K, int S, int bits);
 cudaError_t launch_ozaki_zgemm(int m, int nn, int k, char opA, char opB, cplx alpha, const cplx* A, int lda,
                                const cplx* B, int ldb, cplx beta, cplx* C, int ldc, const double* rowscale,
                                const double* colscale, int S, int bits, void* scratch, size_t scratch_bytes,
                                unsigned long long* acc, size_t acc_bytes, cudaStream_t st,
                                const int* active = nullptr, int splitk = 1, int* kernels = nullptr,
-                               int* err = nullptr, bool persistent = true);
+                               int* err = nullptr, bool persistent = true, bool presliced = false);
 
 // ---- adjoint force (k_force.cu) ----
 // grad[:, :, slice0] = d log|det M| / d phi[:, :, slice0] from G of that slice
