@@ -529,7 +529,10 @@ __global__ void __launch_bounds__(LU_THREADS, 1) k_local_delayed(LocalUpdateArgs
       const int ts = t >> 3, sub = (t >> 1) & 3, side = t & 1;
       const int rc = blockIdx.x + ts * gridDim.x + sub * N;
       const cplx* src = side ? d.Y : d.X;
-      oz_slice_vec(d.sl, side, rc, K, [&](int jj) { return ldcg_c(&src[(size_t)jj * n + rc]); }, ln);
+      // with CACHE the entries come from this CTA's shared-memory copies (no L2 round trip)
+      const cplx* own = CACHE ? (side ? s_ycol : s_xrow) + (size_t)(4 * ts + sub) * K4 : nullptr;
+      oz_slice_vec(d.sl, side, rc, K, [&](int jj) { return CACHE ? own[jj] : ldcg_c(&src[(size_t)jj * n + rc]); },
+                   ln);
     }
   };
   auto finish_round = [&](int pend) {
